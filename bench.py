@@ -1,0 +1,370 @@
+"""Benchmark: Kaiser-Bessel degrid + grid throughput (Mvis/s) on one GB300.
+
+Workload (the full-size single-operator configuration): 1024^2 image at 0.02" pixels,
+2x-padded 2048 x 2048 uv grid (r2c half plane 2048 x 1025, complex64), KB width W = 8
+(w = 4, beta = 2.34*W), 1e7 visibilities: 90% with areal density ~ 1/|uv| out to 0.48 of the
+grid's Nyquist extent, 10% in 50 Gaussian blobs of width 0.005 Nyquist. Synthetic, seeded.
+
+One step = one degrid (grid -> visibilities) + one grid (visibilities -> zeroed grid) over
+all 1e7 visibilities, plan-ordered and resident in HBM (`value`). Per step the kernels stream
+coordinates, visibilities and outputs (~240 MB) -- more than the 129 MB L2 -- so no L2
+flush is inserted between steps. `e2e` runs the same pair through the C ABI's host-buffer
+entry points (lentils_degrid_host / lentils_grid_host) on pinned complex128 host buffers in
+the reference's row order, host<->device copies and conversions inside the timed region.
+
+`--impl reference` times the reference's CPU gridder (the compiled reference C from
+oracle/_ref when present, else the oracle's C port of it) with all host threads on a bounded
+sample of the same workload.
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+
+REPO = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, REPO)
+
+METRIC = "degrid+grid Mvis/s"
+UNIT = "Mvis/s"
+NVIS = 10_000_000
+IMG = 1024
+PIX = 0.02
+WSUP = 4
+BETA = 2.34 * 2 * WSUP
+SEED = 1234
+
+
+def workload_config():
+    return {"workload": "KB degrid+grid, 1024^2 image -> 2048x2048 grid (half plane "
+                        "2048x1025 c64), W=8, 1e7 vis (10% in 50 blobs)",
+            "nvis": NVIS, "grid": [2 * IMG, 2 * IMG], "kernel_width": 2 * WSUP,
+            "kb_beta": BETA, "pixel_arcsec": PIX, "seed": SEED,
+            "l2": "per-step inputs (~240 MB) exceed the 129 MB L2; no flush",
+            "parallelism": "replicas"}
+
+
+def make_uv():
+    import numpy as np
+    sys.path.insert(0, os.path.join(REPO, "oracle"))
+    import oracle as O  # synthetic-input generator only (not the measured path)
+    rng = np.random.default_rng(SEED)
+    half = 0.5 * IMG * PIX
+    img = O.ImageGeom((IMG, IMG), [(-half, half), (-half, half)])
+    padded, _, _ = O.padded_geom(img, 2)
+    four = O.FourierGeom(padded)
+    uvw = O.synth_uv_blobs(rng, NVIS, four, 0.48, WSUP)
+    return four, uvw
+
+
+class ClockSampler:
+    """nvidia-smi clock / throttle sampling during the timed region."""
+
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device_index=0):
+        self.proc = None
+        self.f = tempfile.NamedTemporaryFile("w+", delete=False, suffix=".csv")
+        self.dev = device_index
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.dev}", f"--query-gpu={self.QUERY}",
+                 "--format=csv,noheader,nounits", "-lms", "100"], stdout=self.f,
+                stderr=subprocess.DEVNULL)
+            time.sleep(0.6)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        time.sleep(0.25)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self.f.flush()
+        self.f.seek(0)
+        rows = [ln.strip().split(",") for ln in self.f.read().splitlines() if ln.strip()]
+        os.unlink(self.f.name)
+        sm, smax, reasons = [], 0.0, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in rows:
+            try:
+                sm.append(float(r[1]))
+                smax = max(smax, float(r[2]))
+                for k, nm in enumerate(names):
+                    if r[5 + k].strip().lower() == "active":
+                        reasons.add(nm)
+            except (ValueError, IndexError):
+                continue
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": smax, "samples": len(sm),
+                "reasons": sorted(reasons)}
+
+
+def load_peaks():
+    p = os.path.join(REPO, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def load_traffic():
+    p = os.path.join(REPO, "profiles", "traffic.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            return json.load(f)
+    return {}
+
+
+def cpu_reference_lib():
+    """The compiled reference gridder when present (oracle/_ref), else the oracle C port."""
+    sys.path.insert(0, os.path.join(REPO, "oracle"))
+    import oracle as O
+    if O.ref_available():
+        try:
+            O.ref_lib("nufft")
+            return O, True
+        except OSError:
+            pass
+    O.build_port()
+    O.port_lib()
+    return O, False
+
+
+def time_cpu_gridder(O, use_ref, four, uvw, nsample, reps=1):
+    import numpy as np
+    rng = np.random.default_rng(SEED + 1)
+    idx = rng.choice(uvw.shape[0], nsample, replace=False)
+    vis = O.VisGeom(uvw[idx], [1.0])
+    g = (rng.normal(size=four.shape) + 1j * rng.normal(size=four.shape))
+    y = O.complex_normal(rng, vis.nvis)
+    times = []
+    for _ in range(reps):
+        t0 = time.perf_counter()
+        O.degrid(vis, four, g, WSUP, BETA, use_ref=use_ref)
+        O.grid(vis, four, y, WSUP, BETA, use_ref=use_ref)
+        times.append(time.perf_counter() - t0)
+    return times
+
+
+def run_reference(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return 0
+    cores = os.cpu_count() or 1
+    os.environ.setdefault("OMP_NUM_THREADS", str(cores))
+    O, use_ref = cpu_reference_lib()
+    four, uvw = make_uv()
+    # calibrate, then size each step's sample so the whole run stays within ~2-3 minutes
+    cal = 20000
+    t = time_cpu_gridder(O, use_ref, four, uvw, cal)[0]
+    rate = cal / t
+    per_step = min(10.0, 150.0 / max(1, args.steps + args.warmup))
+    nsample = int(max(5000, min(2_000_000, rate * per_step)))
+    time_cpu_gridder(O, use_ref, four, uvw, nsample, reps=args.warmup)
+    ts = time_cpu_gridder(O, use_ref, four, uvw, nsample, reps=args.steps)
+    total = sum(ts)
+    value = nsample * args.steps / total / 1e6
+    kind = "reference" if use_ref else "port"
+    sample = (f"{nsample} of the 1e7 visibilities (random subset incl. blobs), full 2048x1025 "
+              f"grid, degrid+grid per step, OMP_NUM_THREADS={os.environ['OMP_NUM_THREADS']}")
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": 1e3 * total / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": workload_config(), "impl": "reference",
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": int(os.environ["OMP_NUM_THREADS"]),
+                             "kind": kind, "sample": sample},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+    return 0
+
+
+def run_ours(args):
+    import numpy as np
+    import torch
+    import torch.distributed as dist
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        dist.init_process_group("nccl", init_method="env://")
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+
+    from lentils_gb300 import _native as N
+    from lentils_gb300.gridding import GriddingPlan
+
+    four, uvw = make_uv()
+    plan_t0 = time.perf_counter()
+    plan = GriddingPlan(uvw, [1.0], four.nu, four.nv, four.du, four.dv, four.gcx, four.gcy,
+                        WSUP, BETA)
+    torch.cuda.synchronize()
+    plan_s = time.perf_counter() - plan_t0
+    st = plan.stats
+    nvis = plan.nvis
+
+    gen = torch.Generator(device=dev).manual_seed(SEED)
+    grid_in = torch.complex(torch.randn((four.nu, four.half_nv), generator=gen, device=dev),
+                            torch.randn((four.nu, four.half_nv), generator=gen, device=dev))
+    vis_in = torch.complex(torch.randn(nvis, generator=gen, device=dev),
+                           torch.randn(nvis, generator=gen, device=dev))
+    vis_out = torch.empty(nvis, dtype=torch.complex64, device=dev)
+    grid_out = torch.zeros((four.nu, four.half_nv), dtype=torch.complex64, device=dev)
+    stream = torch.cuda.current_stream()
+
+    def step(ev=None):
+        if ev is not None:
+            ev[0].record(stream)
+        plan.degrid(grid_in, out=vis_out)
+        if ev is not None:
+            ev[1].record(stream)
+        plan.grid(vis_in, out=grid_out, accumulate=False)
+        if ev is not None:
+            ev[2].record(stream)
+
+    for _ in range(max(3, args.warmup)):
+        step()
+    torch.cuda.synchronize()
+
+    # per-kernel timing (events on the launching stream)
+    evs = [[torch.cuda.Event(enable_timing=True) for _ in range(3)] for _ in range(args.steps)]
+    clocks = ClockSampler(local)
+    clocks.start()
+    if world > 1:
+        dist.barrier()
+    torch.cuda.synchronize()
+    t_start = torch.cuda.Event(enable_timing=True)
+    t_end = torch.cuda.Event(enable_timing=True)
+    t_start.record(stream)
+    for k in range(args.steps):
+        step(evs[k])
+    t_end.record(stream)
+    torch.cuda.synchronize()
+    if world > 1:
+        dist.barrier()
+    clk = clocks.stop()
+    total_ms = t_start.elapsed_time(t_end)
+    deg_ms = sum(e[0].elapsed_time(e[1]) for e in evs) / args.steps
+    grd_ms = sum(e[1].elapsed_time(e[2]) for e in evs) / args.steps
+    if world > 1:
+        t = torch.tensor([total_ms], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        total_ms = float(t.item())
+    ms_per_step = total_ms / args.steps
+    value = world * nvis / (ms_per_step * 1e-3) / 1e6
+
+    # roofline of the dominant kernel: algorithmic bytes = N*(8 B coords + 8 B vis) + G
+    G = four.nu * four.half_nv * 8
+    alg_bytes = nvis * 16 + G
+    dominant = "grid_kernel" if grd_ms >= deg_ms else "degrid_kernel"
+    dom_ms = max(grd_ms, deg_ms)
+    peak, peak_kind = load_peaks()
+    achieved = alg_bytes / (dom_ms * 1e-3) / 1e9
+    traffic = load_traffic().get(dominant)
+
+    # end to end through the C ABI host-buffer entry points, pinned complex128 host buffers
+    grid_h = torch.empty((four.nu, four.half_nv), dtype=torch.complex128, pin_memory=True)
+    grid_h.copy_(grid_in.cpu().to(torch.complex128))
+    vis_h = torch.empty(nvis, dtype=torch.complex128, pin_memory=True)
+    vis_h.copy_(vis_in.cpu().to(torch.complex128))
+    vis_o = torch.empty(nvis, dtype=torch.complex128, pin_memory=True)
+    grid_o = torch.empty((four.nu, four.half_nv), dtype=torch.complex128, pin_memory=True)
+    L = N.lib()
+    sp = ctypes.c_void_p(stream.cuda_stream)
+
+    def e2e_step():
+        N.check(L.lentils_degrid_host(plan.handle, ctypes.c_void_p(grid_h.data_ptr()),
+                                      ctypes.c_void_p(vis_o.data_ptr()), 0, sp))
+        N.check(L.lentils_grid_host(plan.handle, ctypes.c_void_p(vis_h.data_ptr()),
+                                    ctypes.c_void_p(grid_o.data_ptr()), 0, sp))
+
+    for _ in range(2):
+        e2e_step()
+    e2e_steps = max(3, min(args.steps, 20))
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        e2e_step()
+    torch.cuda.synchronize()
+    e2e_s = (time.perf_counter() - t0) / e2e_steps
+    e2e_value = world * nvis / e2e_s / 1e6
+    h2d = G * 2 + nvis * 16
+    d2h = nvis * 16 + G * 2
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_per_step,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic", "config": workload_config(),
+            "gpu_launches": 2 * args.steps,
+            "kernels_ms": {"degrid_kernel": deg_ms, "grid_kernel": grd_ms},
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak, "traffic": traffic, "kernel": dominant,
+                         "peak_source": peak_kind,
+                         "algorithmic_bytes_per_launch": alg_bytes,
+                         "pair_frac": 2 * alg_bytes / ((deg_ms + grd_ms) * 1e-3) / 1e9 / peak},
+            "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d,
+                    "d2h_bytes_per_step": d2h, "ms_per_step": e2e_s * 1e3,
+                    "api": "lentils_degrid_host + lentils_grid_host (pinned c128, row order)"},
+            "plan": {"build_s": plan_s, "items": st["nitems"], "tile": st["tile"],
+                     "heaviest_tile_vis": st["heaviest_tile_vis"]},
+            "clocks": clk,
+        }
+        if not args.no_cpu_baseline:
+            line["cpu_baseline"] = cpu_baseline(four, uvw)
+        print(json.dumps(line))
+    if world > 1:
+        dist.destroy_process_group()
+    return 0
+
+
+def cpu_baseline(four, uvw):
+    """The reference's CPU gridder on all host cores over a bounded sample (~10 s)."""
+    O, use_ref = cpu_reference_lib()
+    cores = int(os.environ.get("OMP_NUM_THREADS", os.cpu_count() or 1))
+    cal = 20000
+    rate = cal / time_cpu_gridder(O, use_ref, four, uvw, cal)[0]
+    nsample = int(max(20000, min(2_000_000, rate * 10.0)))
+    t = time_cpu_gridder(O, use_ref, four, uvw, nsample)[0]
+    return {"value": nsample / t / 1e6, "unit": UNIT, "cores": cores,
+            "kind": "reference" if use_ref else "port",
+            "sample": f"{nsample} random visibilities of the 1e7 set, full grid, degrid+grid"}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    os.environ.setdefault("OMP_NUM_THREADS", str(os.cpu_count() or 1))
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_ours(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -1,0 +1,239 @@
+/*
+ * lentils_gb300 -- C ABI of the GB300 (sm_103a) lensed visibility-operator library.
+ *
+ * Two families of entry points:
+ *
+ *  1. Drop-in replacements with the exact signatures and by-value struct ABI of the
+ *     reference's C backend, so the reference's ctypes layer can bind this library in place
+ *     of libnufft / libdeflect:
+ *        grid_cpu                 <- lentils/backend/nufft.c:42-43   (bound at load_backend.py:95-97)
+ *        deflect_points           <- lentils/backend/deflect.c:60    (bound at load_backend.py:59-61)
+ *        grad_matrix_findiff_csr  <- lentils/backend/nufft.c:163     (bound at load_backend.py:107-109)
+ *     They take HOST pointers, keep the reference's accumulate (+=) semantics and FP64 in/out,
+ *     compute in FP32 on the GPU, and return void like the reference. Their status is
+ *     available afterwards from lentils_last_error().
+ *
+ *  2. Device-resident entry points (prefix lentils_): device pointers, an explicit CUDA
+ *     stream (cudaStream_t passed as void*; NULL = legacy default stream), an int status
+ *     (LENTILS_OK on success), and no hidden host synchronisation unless stated.
+ *
+ * All arrays of complex numbers are interleaved (re, im). "c64" = two float32 per element,
+ * "c128" = two float64 per element. Grids are the r2c half-plane, row-major, shape
+ * (nu, nv/2+1), flat index (nv/2+1)*i_u + i_v (reference nufft.c:96).
+ */
+#ifndef LENTILS_GB300_H
+#define LENTILS_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ------------------------------------------------------------------------------------------
+ * By-value structs. Field order, types and padding are the reference's C ABI, so a ctypes
+ * Structure built for the reference passes unchanged.
+ * ---------------------------------------------------------------------------------------- */
+
+/* lentils/backend/common.h:13-23 */
+typedef struct {
+    int nx, ny;
+    int nchannels;
+    int nstokes;
+    double xmin, xmax, ymin, ymax;
+    double dx, dy;
+    double *channels;
+    char *mask;
+} lentils_image_space;
+
+/* lentils/backend/common.h:39-49 */
+typedef struct {
+    int nu, nv;
+    int half_nv;
+    int nchannels;
+    int nstokes;
+    double du, dv;
+    double gcx, gcy;
+    double *channels;
+} lentils_fourier_space;
+
+/* lentils/backend/common.h:52-61 */
+typedef struct {
+    int nrows;
+    int nchannels;
+    int nstokes;
+    double *uv;       /* (nrows, 3) u, v, w in wavelengths */
+    double *channels; /* (nchannels) scale factors applied to u and v */
+} lentils_visibility_space;
+
+/* lentils/backend/deflect.h:8-17 (320 bytes). Mass-model parameters live in fpars; the
+ * per-type packing is documented at lentils_deflect below. */
+typedef struct {
+    unsigned int type;
+    unsigned int _pad;
+    double z_l, z_s, d_l, d_s, d_ls, sigma_c, beta;
+    double fpars[24];
+    int ipars[8];
+    unsigned char flags[32];
+} lentils_mass_model;
+
+/* lentils/backend/deflect.h:20-26 */
+typedef struct {
+    int num_lenses;
+    int num_zplanes;
+    lentils_mass_model *lenses;
+} lentils_global_lens_model;
+
+/* ------------------------------------------------------------------------------------------
+ * Status codes
+ * ---------------------------------------------------------------------------------------- */
+enum {
+    LENTILS_OK = 0,
+    LENTILS_ERR_INVALID = 1,      /* null pointer, negative size, unknown direction/type   */
+    LENTILS_ERR_NYQUIST = 2,      /* a visibility lies beyond the grid's Nyquist guard     */
+    LENTILS_ERR_ALLOC = 3,        /* device or pinned-host allocation failed               */
+    LENTILS_ERR_CUDA = 4,         /* a CUDA runtime / cuFFT call failed                    */
+    LENTILS_ERR_UNSUPPORTED = 5,  /* valid request this build does not implement           */
+    LENTILS_ERR_TIMEOUT = 6,      /* a bounded device-side wait gave up                    */
+    LENTILS_ERR_NONFINITE = 7,    /* NaN/Inf detected where the caller asked for a check   */
+    LENTILS_ERR_NO_DEVICE = 8     /* no CUDA device visible                                */
+};
+
+/* Status of the most recent call made on this host thread (drop-in functions return void). */
+int lentils_last_error(void);
+/* Human-readable text of the most recent failure on this host thread ("" if none). */
+const char *lentils_last_error_message(void);
+/* Library version as major*10000 + minor*100 + patch. */
+int lentils_version(void);
+
+/* Host-only (no GPU needed): the per-tap Kaiser-Bessel polynomial table the gridding kernels
+ * evaluate, 2w taps x lentils_kb_poly_ncoef() coefficients in t = 2*frac - 1 (highest degree
+ * first, checkerboard sign and 1/(2w) folded in), and the FP64 fit error relative to the
+ * kernel peak. Tap i of a visibility with fractional cell offset frac sits at kernel argument
+ * frac + w - 1 - i; the weight is I0(beta*sqrt(1-(a/w)^2))/(2w) as in kb_g,
+ * lentils/backend/nufft.c:11-21. */
+int lentils_kb_poly_table(int w, double beta, float *coef, int ncoef_capacity, double *fit_err);
+int lentils_kb_poly_ncoef(void);
+
+/* ------------------------------------------------------------------------------------------
+ * Drop-in entry points (host pointers, reference semantics)
+ * ---------------------------------------------------------------------------------------- */
+
+/* Kaiser-Bessel gridding (direction 1, ADJOINT: visibilities -> half-plane grid) and
+ * degridding (direction 0, FORWARD: grid -> visibilities). Replaces grid_cpu,
+ * lentils/backend/nufft.c:42-122. vis is (nchannels, 1, nrows) c128, grid is (nu, nv/2+1)
+ * c128; the output is ACCUMULATED (+=) like the reference. wsup is the kernel half-width w
+ * (the reference loops over 2w+1 taps per axis). */
+void grid_cpu(lentils_visibility_space visspace, double *vis, lentils_fourier_space gspace,
+              double *grid, int wsup, double kb_beta, int direction);
+
+/* Lens equation beta = theta - sum_l alpha_l(theta) for npoints interleaved (x, y) points.
+ * Replaces deflect_points, lentils/backend/deflect.c:60-66. want_deriv must be 0 in this
+ * build (the reference's Python never requests derivatives; lentils_last_error() reports
+ * LENTILS_ERR_UNSUPPORTED otherwise and p_out is left untouched). */
+void deflect_points(lentils_global_lens_model glm, double *p_in, int npoints, double *p_out,
+                    int want_deriv, double *deriv);
+
+/* Forward-difference gradient operator as CSR with 2*nx*ny rows and 2 entries per interior
+ * row. Replaces grad_matrix_findiff_csr, lentils/backend/nufft.c:163-194. Arrays are host
+ * buffers sized as the reference's PriorCovarianceOperator allocates them
+ * (lentils/operators/operator_base.py:226-228). */
+void grad_matrix_findiff_csr(lentils_image_space imspace, int *row_inds, int *cols,
+                             double *vals);
+
+/* ------------------------------------------------------------------------------------------
+ * Gridding plan: visibilities binned by grid tile once per uv set.
+ *
+ * A plan re-orders the visibilities (plan order = sorted by tile and cell) and stores each as
+ * two 32-bit fixed-point tile-relative coordinates. The degrid/grid kernels read and write
+ * visibilities in plan order and in the plan frame (phase centre and Hermitian mirroring
+ * removed). lentils_vis_to_plan / lentils_vis_from_plan convert to and from the reference's
+ * row order and frame. In the normal-equation product F^T C^-1 F the frame factors cancel, so
+ * an iterative solver stays in plan order throughout.
+ * ---------------------------------------------------------------------------------------- */
+typedef struct lentils_plan lentils_plan;
+
+typedef struct {
+    int nu, nv;          /* full uv grid; the stored half-plane is nu x (nv/2+1)            */
+    double du, dv;       /* cell size (wavelengths)                                          */
+    double gcx, gcy;     /* phase centre (radians)                                           */
+    int wsup;            /* kernel half-width w, 1 <= w <= 8                                 */
+    double kb_beta;      /* Kaiser-Bessel shape parameter                                    */
+    int tile;            /* tile edge in cells (16, 32 or 64), 0 = choose automatically      */
+    int chunk;           /* max visibilities per work item, 0 = choose automatically         */
+} lentils_grid_desc;
+
+enum {
+    LENTILS_PLAN_UVW_ON_DEVICE = 1, /* uvw/channels pointers are device memory            */
+    LENTILS_PLAN_NYQUIST_GUARD = 2  /* reject uv beyond the guard of
+                                       lentils/operators/fourier_operators.py:77-80           */
+};
+
+typedef struct {
+    long long nvis;          /* nrows * nchannels                                           */
+    int ntiles_u, ntiles_v;  /* tile grid over the canonical half plane                     */
+    int tile;                /* tile edge (cells)                                           */
+    int nitems;              /* work items (tile, visibility range)                         */
+    int max_item_vis;        /* largest work item                                           */
+    int heaviest_tile_vis;   /* visibilities in the most populated tile                     */
+    int wsup;
+    int has_phase;           /* 1 if the phase centre is off the origin                     */
+    long long device_bytes;  /* device memory held by the plan                              */
+} lentils_plan_stats;
+
+/* Build a plan from uvw (nrows x 3, f64) and channel scale factors (nchannels, f64).
+ * Pointers are host memory unless LENTILS_PLAN_UVW_ON_DEVICE is set. Synchronises stream
+ * once at the end (the work-item count must reach the host). */
+int lentils_plan_create(lentils_plan **plan, const lentils_grid_desc *grid, const double *uvw,
+                        int nrows, const double *channels, int nchannels, int flags,
+                        void *stream);
+int lentils_plan_destroy(lentils_plan *plan);
+int lentils_plan_get_stats(const lentils_plan *plan, lentils_plan_stats *stats);
+
+/* Degrid: half-plane grid (c64, device) -> visibilities (c64, device, plan order, plan frame).
+ * vis_plan is OVERWRITTEN. */
+int lentils_degrid(const lentils_plan *plan, const float *grid, float *vis_plan, void *stream);
+
+/* Grid: visibilities (c64, device, plan order, plan frame) -> half-plane grid (c64, device).
+ * The grid is ACCUMULATED (+=); zero it first for a fresh result. */
+int lentils_grid(const lentils_plan *plan, const float *vis_plan, float *grid, void *stream);
+
+/* Reference row order/frame (c128 or c64 by `user_is_c128`) -> plan order/frame (c64). */
+int lentils_vis_to_plan(const lentils_plan *plan, const void *vis_user, int user_is_c128,
+                        float *vis_plan, void *stream);
+/* Plan order/frame (c64) -> reference row order/frame. accumulate != 0 adds into vis_user. */
+int lentils_vis_from_plan(const lentils_plan *plan, const float *vis_plan, void *vis_user,
+                          int user_is_c128, int accumulate, void *stream);
+
+/* Host-buffer forms: the same operators on HOST c128 buffers in reference row order, with the
+ * host<->device copies and precision conversions done inside (staging buffers are owned by
+ * the plan and allocated on first use). accumulate != 0 adds into the output like grid_cpu
+ * (the output is then also copied host->device); accumulate == 0 overwrites it, which is what
+ * the reference's GriddingOperator gets from its fresh zero buffers
+ * (lentils/operators/fourier_operators.py:85-93). Pinned host buffers give full-rate copies.
+ * Synchronise stream before returning. */
+int lentils_degrid_host(lentils_plan *plan, const double *grid_host, double *vis_host,
+                        int accumulate, void *stream);
+int lentils_grid_host(lentils_plan *plan, const double *vis_host, double *grid_host,
+                      int accumulate, void *stream);
+
+/* ------------------------------------------------------------------------------------------
+ * PEMD + external-shear deflection (device)
+ *
+ * lenses: HOST array of nlenses mass models packed as the reference packs them
+ * (lentils/models/lens_models.py:102-147); types 0 (PEMD, 2F1 series), 1 (external
+ * potential) and 2 (internal multipoles) are supported. points/out: device arrays of
+ * interleaved (x, y). All lenses deflect the same input position (single plane,
+ * lentils/backend/deflect.c:43).
+ * ---------------------------------------------------------------------------------------- */
+int lentils_deflect_f32(const lentils_mass_model *lenses, int nlenses, const float *points,
+                        float *out, long long npoints, void *stream);
+int lentils_deflect_f64io(const lentils_mass_model *lenses, int nlenses, const double *points,
+                          double *out, long long npoints, void *stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* LENTILS_GB300_H */

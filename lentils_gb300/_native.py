@@ -1,0 +1,142 @@
+"""ctypes binding of liblentils_gb300.so (the C ABI declared in include/lentils_gb300.h).
+
+The library is built in-tree by ``lentils_gb300.build``. Loading fails loudly when it is
+missing: there is no CPU fallback anywhere in this package.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+from ctypes import (POINTER, Structure, c_char, c_char_p, c_double, c_float, c_int,
+                    c_longlong, c_void_p)
+
+import numpy as np
+
+PKG = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(PKG, "liblentils_gb300.so")
+
+LENTILS_OK = 0
+ERROR_NAMES = {0: "OK", 1: "INVALID", 2: "NYQUIST", 3: "ALLOC", 4: "CUDA", 5: "UNSUPPORTED",
+               6: "TIMEOUT", 7: "NONFINITE", 8: "NO_DEVICE"}
+
+PLAN_UVW_ON_DEVICE = 1
+PLAN_NYQUIST_GUARD = 2
+
+
+class LentilsError(RuntimeError):
+    def __init__(self, code, message):
+        self.code = code
+        super().__init__(f"lentils_gb300 error {ERROR_NAMES.get(code, code)}: {message}")
+
+
+# --- by-value structs (reference ABI: lentils/backend/common.h, deflect.h) -----------------
+class ImageSpaceC(Structure):
+    _fields_ = [("nx", c_int), ("ny", c_int), ("num_channels", c_int), ("num_stokes", c_int),
+                ("xmin", c_double), ("xmax", c_double), ("ymin", c_double), ("ymax", c_double),
+                ("dx", c_double), ("dy", c_double), ("_c_channels", POINTER(c_double)),
+                ("_c_mask", POINTER(c_char))]
+
+
+class FourierSpaceC(Structure):
+    _fields_ = [("nu", c_int), ("nv", c_int), ("half_nv", c_int), ("num_channels", c_int),
+                ("num_stokes", c_int), ("du", c_double), ("dv", c_double), ("gcx", c_double),
+                ("gcy", c_double), ("_c_channels", POINTER(c_double))]
+
+
+class VisibilitySpaceC(Structure):
+    _fields_ = [("num_rows", c_int), ("num_channels", c_int), ("num_stokes", c_int),
+                ("_c_uvw", POINTER(c_double)), ("_c_channels", POINTER(c_double))]
+
+
+class GlobalLensModelC(Structure):
+    _fields_ = [("num_lenses", c_int), ("num_zplanes", c_int), ("lenses", c_void_p)]
+
+
+class GridDescC(Structure):
+    _fields_ = [("nu", c_int), ("nv", c_int), ("du", c_double), ("dv", c_double),
+                ("gcx", c_double), ("gcy", c_double), ("wsup", c_int), ("kb_beta", c_double),
+                ("tile", c_int), ("chunk", c_int)]
+
+
+class PlanStatsC(Structure):
+    _fields_ = [("nvis", c_longlong), ("ntiles_u", c_int), ("ntiles_v", c_int), ("tile", c_int),
+                ("nitems", c_int), ("max_item_vis", c_int), ("heaviest_tile_vis", c_int),
+                ("wsup", c_int), ("has_phase", c_int), ("device_bytes", c_longlong)]
+
+
+# (name, restype, argtypes) for every function in include/lentils_gb300.h
+_SIGNATURES = [
+    ("lentils_last_error", c_int, []),
+    ("lentils_last_error_message", c_char_p, []),
+    ("lentils_version", c_int, []),
+    ("lentils_kb_poly_table", c_int, [c_int, c_double, c_void_p, c_int, POINTER(c_double)]),
+    ("lentils_kb_poly_ncoef", c_int, []),
+    ("grid_cpu", None, [VisibilitySpaceC, c_void_p, FourierSpaceC, c_void_p, c_int, c_double,
+                        c_int]),
+    ("deflect_points", None, [GlobalLensModelC, c_void_p, c_int, c_void_p, c_int, c_void_p]),
+    ("grad_matrix_findiff_csr", None, [ImageSpaceC, c_void_p, c_void_p, c_void_p]),
+    ("lentils_plan_create", c_int, [POINTER(c_void_p), POINTER(GridDescC), c_void_p, c_int,
+                                    c_void_p, c_int, c_int, c_void_p]),
+    ("lentils_plan_destroy", c_int, [c_void_p]),
+    ("lentils_plan_get_stats", c_int, [c_void_p, POINTER(PlanStatsC)]),
+    ("lentils_degrid", c_int, [c_void_p, c_void_p, c_void_p, c_void_p]),
+    ("lentils_grid", c_int, [c_void_p, c_void_p, c_void_p, c_void_p]),
+    ("lentils_vis_to_plan", c_int, [c_void_p, c_void_p, c_int, c_void_p, c_void_p]),
+    ("lentils_vis_from_plan", c_int, [c_void_p, c_void_p, c_void_p, c_int, c_int, c_void_p]),
+    ("lentils_degrid_host", c_int, [c_void_p, c_void_p, c_void_p, c_int, c_void_p]),
+    ("lentils_grid_host", c_int, [c_void_p, c_void_p, c_void_p, c_int, c_void_p]),
+    ("lentils_deflect_f32", c_int, [c_void_p, c_int, c_void_p, c_void_p, c_longlong, c_void_p]),
+    ("lentils_deflect_f64io", c_int, [c_void_p, c_int, c_void_p, c_void_p, c_longlong,
+                                      c_void_p]),
+]
+
+_LIB = None
+
+
+def lib():
+    """The loaded library (raises if it has not been built)."""
+    global _LIB
+    if _LIB is None:
+        if not os.path.exists(LIB_PATH):
+            raise LentilsError(8, f"{LIB_PATH} is missing; run lentils_gb300.build.build()")
+        L = ctypes.CDLL(LIB_PATH)
+        for name, res, args in _SIGNATURES:
+            fn = getattr(L, name, None)
+            if fn is None:
+                continue
+            fn.restype = res
+            fn.argtypes = args
+        _LIB = L
+    return _LIB
+
+
+def declared_functions():
+    return [n for n, _, _ in _SIGNATURES]
+
+
+def check(status):
+    """Raise LentilsError for a non-zero status."""
+    if status != LENTILS_OK:
+        L = lib()
+        msg = L.lentils_last_error_message()
+        raise LentilsError(status, msg.decode() if msg else "")
+    return status
+
+
+def check_last():
+    """Raise if the most recent call on this thread (a void drop-in entry) failed."""
+    L = lib()
+    code = L.lentils_last_error()
+    if code != LENTILS_OK:
+        raise LentilsError(code, L.lentils_last_error_message().decode())
+
+
+def kb_poly_table(w, beta):
+    """Per-tap polynomial table (2w x ncoef) and its FP64 fit error (host only)."""
+    L = lib()
+    ncoef = L.lentils_kb_poly_ncoef()
+    out = np.zeros((2 * w, ncoef), dtype=np.float32)
+    err = c_double(0.0)
+    check(L.lentils_kb_poly_table(int(w), float(beta), out.ctypes.data, out.size,
+                                  ctypes.byref(err)))
+    return out, err.value

@@ -1,0 +1,108 @@
+// Shared definitions of the lentils_gb300 CUDA library (sm_103a).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <stdio.h>
+#include <string.h>
+
+#include "lentils_gb300.h"
+
+namespace lentils {
+
+// Constants as the reference defines them (lentils/backend/common.h:8-11); the phase uses
+// the truncated 2*pi so that phases match the reference's to the last bit of FP64.
+constexpr double kArcsecToRad = 4.8481368111e-6;
+constexpr double kTwoPiTrunc = 6.28318530718;
+
+// Kaiser-Bessel weights are evaluated as per-tap polynomials in t = 2*frac - 1.
+constexpr int kMaxW = 8;            // largest supported half-width
+constexpr int kMaxTaps = 2 * kMaxW;  // 2w taps per axis (plus a rare edge tap)
+constexpr int kPolyCoef = 10;        // degree-9 polynomials (FP32 round-off for 1 <= w <= 8)
+constexpr int kFracBits = 24;        // fixed-point fraction bits of plan coordinates
+constexpr uint32_t kFracMask = (1u << kFracBits) - 1u;
+
+// ---------------------------------------------------------------------------------------
+// Error state (per host thread)
+// ---------------------------------------------------------------------------------------
+int set_error(int code, const char *fmt, ...);
+int clear_error();
+int cuda_status(cudaError_t e, const char *what);
+
+#define LENTILS_CUDA_TRY(expr)                                                    \
+    do {                                                                          \
+        cudaError_t _e = (expr);                                                  \
+        if (_e != cudaSuccess) return ::lentils::cuda_status(_e, #expr);          \
+    } while (0)
+
+#define LENTILS_CHECK_LAUNCH(what)                                                \
+    do {                                                                          \
+        cudaError_t _e = cudaGetLastError();                                      \
+        if (_e != cudaSuccess) return ::lentils::cuda_status(_e, what);           \
+    } while (0)
+
+// ---------------------------------------------------------------------------------------
+// Kaiser-Bessel polynomial table, passed to kernels by value.
+// cp[k][p] = (c_{2p,k}, c_{2p+1,k}): coefficient k of taps 2p and 2p+1, highest degree
+// first, with the tap's checkerboard sign (-1)^i and the per-axis 1/(2w) normalisation
+// folded in. Tap i (0 <= i < 2w) of a visibility with fractional offset f in [0,1) sits at
+// kernel argument f + w - 1 - i.
+// ---------------------------------------------------------------------------------------
+struct KBPoly {
+    float2 cp[kPolyCoef][kMaxW];
+    float edge;  // weight of the extra tap at argument +w (only when f == 0): -1/(2w)
+};
+
+// Host: fit the table for (w, beta). Returns max abs fit error relative to the peak
+// (evaluated in FP64) through *fit_err when non-null.
+void kb_poly_build(int w, double beta, KBPoly *out, double *fit_err);
+double host_bessel_i0(double x);
+
+// ---------------------------------------------------------------------------------------
+// Canonical grid geometry used by the kernels. The full uv plane is tiled with T x T tiles;
+// canonical cell indices a in [-Hu, nu-Hu), b in [-Hv, nv-Hv); tile (tu, tv) covers
+// a in [tu*T - Hu, (tu+1)*T - Hu).
+// ---------------------------------------------------------------------------------------
+struct GridGeom {
+    int nu, nv, half_nv;
+    int w;       // kernel half-width
+    int T;       // tile edge
+    int logT;
+    int E;       // extended tile edge T + 2w
+    int stride;  // shared-memory row stride (float2 units, odd)
+    int Hu, Hv;  // nu/2, nv/2
+    int ntu, ntv;
+};
+
+struct WorkItem {
+    int tu, tv;   // tile coordinates
+    int begin;    // first visibility (plan order)
+    int count;    // number of visibilities
+};
+
+}  // namespace lentils
+
+// The opaque plan (device-resident arrays + geometry).
+struct lentils_plan {
+    lentils_grid_desc desc;
+    lentils::GridGeom geom;
+    lentils::KBPoly kb;
+    int device;
+    long long nvis;
+    int nrows, nchannels;
+    int nitems;
+    int max_item;
+    int heaviest_tile;
+    int has_phase;
+    // plan-order arrays
+    uint2 *coords;        // fixed-point tile-relative (u, v)
+    int *perm;            // plan index -> user index (channel*nrows + row)
+    float2 *phase;        // s * e^{-i phi} per visibility (plan order)
+    lentils::WorkItem *items;
+    long long device_bytes;
+    // staging for the host-buffer forms (allocated on first use)
+    void *stage_vis64;    // nvis c128
+    void *stage_grid64;   // grid c128
+    float2 *stage_vis32;  // nvis c64
+    float2 *stage_grid32; // grid c64
+};

@@ -1,0 +1,174 @@
+// Drop-in entry points with the reference's exact C signatures (host pointers, by-value
+// structs, void return). Each stages its inputs on the current CUDA device, runs the GPU
+// kernels and copies the results back; failures are reported through lentils_last_error()
+// and printed to stderr, since the reference's signatures have no error channel.
+#include <stdio.h>
+
+#include "common.cuh"
+
+using namespace lentils;
+
+namespace {
+
+void report(const char *fn)
+{
+    fprintf(stderr, "lentils_gb300 %s failed (status %d): %s\n", fn, lentils_last_error(),
+            lentils_last_error_message());
+}
+
+// Forward-difference gradient CSR, closed form per row (so rows fill in parallel):
+// x-rows r < nx*ny have entries iff ix < nx-1; y-rows have entries iff iy < ny-1.
+// Same layout and values as grad_matrix_findiff_csr, lentils/backend/nufft.c:163-194.
+__global__ void grad_csr_kernel(int nx, int ny, double dx, double dy, int *rows, int *cols,
+                                double *vals)
+{
+    const long long n = (long long)nx * ny;
+    const long long nx_entries = 2LL * (nx - 1) * ny;
+    for (long long r = blockIdx.x * (long long)blockDim.x + threadIdx.x; r <= 2 * n;
+         r += (long long)gridDim.x * blockDim.x) {
+        if (r == 2 * n) {
+            rows[r] = (int)(nx_entries + 2LL * nx * (ny - 1));
+            continue;
+        }
+        if (r < n) {
+            const int ix = (int)(r / ny), iy = (int)(r % ny);
+            const long long k = 2LL * std::min<long long>(r, (long long)(nx - 1) * ny);
+            rows[r] = (int)k;
+            if (ix < nx - 1) {
+                vals[k] = -1.0 / dx;
+                cols[k] = ny * ix + iy;
+                vals[k + 1] = 1.0 / dx;
+                cols[k + 1] = ny * (ix + 1) + iy;
+            }
+        } else {
+            const long long rr = r - n;
+            const int ix = (int)(rr / ny), iy = (int)(rr % ny);
+            const long long k = nx_entries + 2LL * ((long long)ix * (ny - 1) + std::min(iy, ny - 1));
+            rows[r] = (int)k;
+            if (iy < ny - 1) {
+                vals[k] = -1.0 / dy;
+                cols[k] = ny * ix + iy;
+                vals[k + 1] = 1.0 / dy;
+                cols[k + 1] = ny * ix + iy + 1;
+            }
+        }
+    }
+}
+
+int grid_cpu_impl(lentils_visibility_space vs, double *vis, lentils_fourier_space gs,
+                  double *grid, int wsup, double beta, int direction)
+{
+    if (direction != 0 && direction != 1)
+        return set_error(LENTILS_ERR_INVALID, "grid_cpu: direction %d (0 or 1)", direction);
+    if (vs.nrows < 0 || vs.nchannels < 1 || !vis || !grid)
+        return set_error(LENTILS_ERR_INVALID, "grid_cpu: bad visibility space or buffers");
+    if (gs.half_nv != gs.nv / 2 + 1)
+        return set_error(LENTILS_ERR_UNSUPPORTED, "grid_cpu: half_nv=%d, expected nv/2+1",
+                         gs.half_nv);
+    if (vs.nrows == 0) return LENTILS_OK;
+    lentils_grid_desc gd;
+    memset(&gd, 0, sizeof(gd));
+    gd.nu = gs.nu;
+    gd.nv = gs.nv;
+    gd.du = gs.du;
+    gd.dv = gs.dv;
+    gd.gcx = gs.gcx;
+    gd.gcy = gs.gcy;
+    gd.wsup = wsup;
+    gd.kb_beta = beta;
+    lentils_plan *plan = nullptr;
+    int st = lentils_plan_create(&plan, &gd, vs.uv, vs.nrows, vs.channels, vs.nchannels, 0,
+                                 nullptr);
+    if (st) return st;
+    if (direction == 0) st = lentils_degrid_host(plan, grid, vis, 1, nullptr);
+    else st = lentils_grid_host(plan, vis, grid, 1, nullptr);
+    const int code = st ? lentils_last_error() : LENTILS_OK;
+    char msg[512] = {0};
+    if (st) strncpy(msg, lentils_last_error_message(), sizeof(msg) - 1);
+    lentils_plan_destroy(plan);
+    if (st) return set_error(code, "%s", msg);
+    return LENTILS_OK;
+}
+
+int deflect_points_impl(lentils_global_lens_model glm, double *pin, int n, double *pout,
+                        int want_deriv)
+{
+    if (want_deriv)
+        return set_error(LENTILS_ERR_UNSUPPORTED,
+                         "deflect_points: parameter derivatives (want_deriv) are not built");
+    if (n < 0 || (n > 0 && (!pin || !pout)) || glm.num_lenses < 0 ||
+        (glm.num_lenses > 0 && !glm.lenses))
+        return set_error(LENTILS_ERR_INVALID, "deflect_points: bad arguments");
+    if (n == 0) return LENTILS_OK;
+    double *din = nullptr, *dout = nullptr;
+    const size_t bytes = sizeof(double) * 2 * (size_t)n;
+    int st = LENTILS_OK;
+    cudaError_t e = cudaMalloc(&din, bytes);
+    if (e == cudaSuccess) e = cudaMalloc(&dout, bytes);
+    if (e == cudaSuccess) e = cudaMemcpy(din, pin, bytes, cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) st = cuda_status(e, "deflect_points staging");
+    if (!st) st = lentils_deflect_f64io(glm.lenses, glm.num_lenses, din, dout, n, nullptr);
+    if (!st) {
+        e = cudaMemcpy(pout, dout, bytes, cudaMemcpyDeviceToHost);
+        if (e != cudaSuccess) st = cuda_status(e, "deflect_points copy back");
+    }
+    cudaFree(din);
+    cudaFree(dout);
+    return st;
+}
+
+int grad_csr_impl(lentils_image_space im, int *rows, int *cols, double *vals)
+{
+    if (im.nx < 1 || im.ny < 1 || !rows || !cols || !vals)
+        return set_error(LENTILS_ERR_INVALID, "grad_matrix_findiff_csr: bad arguments");
+    const long long n = (long long)im.nx * im.ny;
+    const long long nnz = 2LL * (im.nx - 1) * im.ny + 2LL * im.nx * (im.ny - 1);
+    int *drows = nullptr, *dcols = nullptr;
+    double *dvals = nullptr;
+    int st = LENTILS_OK;
+    cudaError_t e = cudaMalloc(&drows, sizeof(int) * (2 * n + 1));
+    if (e == cudaSuccess) e = cudaMalloc(&dcols, sizeof(int) * std::max(nnz, 1LL));
+    if (e == cudaSuccess) e = cudaMalloc(&dvals, sizeof(double) * std::max(nnz, 1LL));
+    if (e != cudaSuccess) st = cuda_status(e, "grad_matrix_findiff_csr alloc");
+    if (!st) {
+        long long blocks = (2 * n + 1 + 255) / 256;
+        if (blocks > 152 * 32) blocks = 152 * 32;
+        grad_csr_kernel<<<(int)blocks, 256>>>(im.nx, im.ny, im.dx, im.dy, drows, dcols, dvals);
+        e = cudaGetLastError();
+        if (e == cudaSuccess) e = cudaMemcpy(rows, drows, sizeof(int) * (2 * n + 1), cudaMemcpyDeviceToHost);
+        if (e == cudaSuccess && nnz > 0) e = cudaMemcpy(cols, dcols, sizeof(int) * nnz, cudaMemcpyDeviceToHost);
+        if (e == cudaSuccess && nnz > 0) e = cudaMemcpy(vals, dvals, sizeof(double) * nnz, cudaMemcpyDeviceToHost);
+        if (e != cudaSuccess) st = cuda_status(e, "grad_matrix_findiff_csr");
+    }
+    cudaFree(drows);
+    cudaFree(dcols);
+    cudaFree(dvals);
+    return st;
+}
+
+}  // namespace
+
+extern "C" {
+
+void grid_cpu(lentils_visibility_space vs, double *vis, lentils_fourier_space gs, double *grid,
+              int wsup, double kb_beta, int direction)
+{
+    clear_error();
+    if (grid_cpu_impl(vs, vis, gs, grid, wsup, kb_beta, direction)) report("grid_cpu");
+}
+
+void deflect_points(lentils_global_lens_model glm, double *p_in, int npoints, double *p_out,
+                    int want_deriv, double *deriv)
+{
+    (void)deriv;
+    clear_error();
+    if (deflect_points_impl(glm, p_in, npoints, p_out, want_deriv)) report("deflect_points");
+}
+
+void grad_matrix_findiff_csr(lentils_image_space imspace, int *row_inds, int *cols, double *vals)
+{
+    clear_error();
+    if (grad_csr_impl(imspace, row_inds, cols, vals)) report("grad_matrix_findiff_csr");
+}
+
+}  // extern "C"

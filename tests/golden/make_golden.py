@@ -1,0 +1,105 @@
+"""Generate the golden fixtures in tests/golden/ from the reference's own C code.
+
+The reference's ``nufft.c`` and ``deflect.c`` are compiled unmodified by ``oracle/Makefile``
+(target ``ref``) into ``oracle/_ref/`` (GSL's I0 replaced by the power-series shim in
+``oracle/shim``); this script calls them through ctypes with one OpenMP thread on seeded
+inputs and stores inputs and outputs as small ``.npz`` files. The fixtures pin the oracle port
+(tests/test_oracle.py) and the GPU drop-ins (tests/test_dropin_gpu.py) wherever the
+reference sources are absent.
+
+Run from the repository root:  OMP_NUM_THREADS=1 python tests/golden/make_golden.py
+"""
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+REPO = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, os.path.join(REPO, "oracle"))
+import oracle as O  # noqa: E402
+
+
+def nufft_case(name, shape, bounds, chans, wsup, nvis, frac, seed, extra_uv=None):
+    rng = np.random.default_rng(seed)
+    img = O.ImageGeom(shape, bounds)
+    padded, _, _ = O.padded_geom(img, 2)
+    four = O.FourierGeom(padded)
+    uvw = O.synth_uv(rng, nvis, four, frac, wsup) / max(chans)
+    if extra_uv is not None:
+        uvw = np.concatenate([uvw, extra_uv(four, chans)])
+    vis = O.VisGeom(uvw, chans)
+    beta = O.kb_beta(wsup)
+    grid_in = (rng.normal(size=four.shape) + 1j * rng.normal(size=four.shape))
+    vis_in = O.complex_normal(rng, vis.nvis)
+    # accumulate onto non-zero outputs to pin the += semantics
+    vis_acc0 = O.complex_normal(rng, vis.nvis) * 0.1
+    grid_acc0 = (rng.normal(size=four.shape) + 1j * rng.normal(size=four.shape)) * 0.1
+    vis_out = vis_acc0.copy()
+    O.grid_cpu(vis, vis_out, four, grid_in.copy(), wsup, beta, 0, use_ref=True)
+    grid_out = grid_acc0.copy()
+    O.grid_cpu(vis, vis_in.copy(), four, grid_out, wsup, beta, 1, use_ref=True)
+    np.savez_compressed(
+        os.path.join(HERE, f"{name}.npz"), uvw=uvw, channels=np.asarray(chans, float),
+        nu=four.nu, nv=four.nv, du=four.du, dv=four.dv, gcx=four.gcx, gcy=four.gcy,
+        wsup=wsup, beta=beta, grid_in=grid_in, vis_in=vis_in, vis_acc0=vis_acc0,
+        grid_acc0=grid_acc0, vis_out=vis_out, grid_out=grid_out)
+    print(name, vis.nvis, four.shape)
+
+
+def integer_points(four, chans):
+    # uv exactly on grid cells (edge taps), the origin, and two points beyond the Nyquist
+    # guard (exercise the wrap, nufft.c:83-86)
+    pts = np.array([[0.0, 0.0, 0.0], [3 * four.du, -5 * four.dv, 0.0],
+                    [-7 * four.du, 2 * four.dv, 0.0],
+                    [0.49 * four.nu * four.du, 0.3 * four.nv * four.dv, 0.0],
+                    [-0.6 * four.nu * four.du, -0.55 * four.nv * four.dv, 0.0]])
+    pts[:, :2] /= chans[0]
+    return pts
+
+
+def deflect_case():
+    rng = np.random.default_rng(11)
+    img = O.ImageGeom((48, 40), [(-1.3, 1.1), (-1.0, 1.2)])
+    pts = img.points().reshape(-1, 2)
+    pts = np.concatenate([pts, rng.uniform(-2, 2, (200, 2)), [[0.05, -0.03]]])
+    cases = {
+        "pemd_shear": O.lens_array([O.pemd_cpars(1.0, 30.0, 0.8, 0.05, -0.03, 0.55),
+                                    O.shear_cpars(0.05, -0.03, 0.05, 20.0)]),
+        "pemd_lowq": O.lens_array([O.pemd_cpars(1.2, -40.0, 0.45, 0.1, 0.2, 0.45)]),
+        "shear_grad": O.lens_array([O.shear_cpars(-0.1, 0.2, 0.07, 75.0, gks=0.02, gka=10.0,
+                                                  gss=0.01, gsa=-30.0)]),
+        "multipoles": O.lens_array([O.multipole_cpars(0.0, 0.1, 0.5, 4,
+                                                      [[0.01, -0.02], [0.005, 0.003]])]),
+    }
+    out = {"points": pts}
+    for k, lenses in cases.items():
+        out[f"{k}_lenses"] = lenses.view(np.uint8).reshape(len(lenses), -1)
+        out[f"{k}_out"] = O.deflect(lenses, pts, use_ref=True)
+    np.savez_compressed(os.path.join(HERE, "deflect.npz"), **out)
+    print("deflect", pts.shape)
+
+
+def grad_case():
+    img = O.ImageGeom((13, 17), [(-0.4, 0.9), (-0.2, 0.6)])
+    rows, cols, vals = O.grad_csr(img, use_ref=True)
+    np.savez_compressed(os.path.join(HERE, "grad_csr.npz"), nx=img.nx, ny=img.ny,
+                        bounds=img.bounds, rows=rows, cols=cols, vals=vals)
+    print("grad_csr", img.shape)
+
+
+if __name__ == "__main__":
+    if not O.build_ref():
+        sys.exit("the reference's C sources could not be compiled (oracle/_ref)")
+    O.build_port()
+    # config-0 geometry (128^2 image, 0.02" pixels, W=6), reduced visibility count
+    nufft_case("nufft_cfg0_w3", (128, 128), [(-1.28, 1.28), (-1.28, 1.28)], [1.0], 3, 3000,
+               0.45, 1)
+    # odd, non-square, off-centre image with two channels and special points (W=8)
+    nufft_case("nufft_odd_w4", (59, 64), [(-0.5, 0.7), (-0.7, 0.5)], [0.5, 0.8], 4, 400, 0.4,
+               2, extra_uv=integer_points)
+    # narrow kernel on a tiny grid (W=2)
+    nufft_case("nufft_tiny_w1", (12, 9), [(-0.2, 0.3), (-0.1, 0.2)], [1.0], 1, 60, 0.5, 3,
+               extra_uv=integer_points)
+    deflect_case()
+    grad_case()
