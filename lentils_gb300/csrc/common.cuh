@@ -19,8 +19,18 @@ constexpr double kTwoPiTrunc = 6.28318530718;
 constexpr int kMaxW = 8;            // largest supported half-width
 constexpr int kMaxTaps = 2 * kMaxW;  // 2w taps per axis (plus a rare edge tap)
 constexpr int kPolyCoef = 10;        // degree-9 polynomials (FP32 round-off for 1 <= w <= 8)
-constexpr int kFracBits = 24;        // fixed-point fraction bits of plan coordinates
+// Plan coordinate word, per axis:
+//   bits  0..23  fraction of the cell (fixed point, 2^-24 cells)
+//   bits 24..29  cell within the tile (tiles up to 64 cells)
+//   bit  30      the reference includes the extra tap floor - w (argument +w)
+//   bit  31      the reference excludes the top tap floor + w (argument below -w)
+// The two flags are decided in FP64 exactly as kb_g tests |arg| <= w (nufft.c:12), so the tap
+// set matches the reference even when the fixed-point rounding lands on a cell boundary.
+constexpr int kFracBits = 24;
 constexpr uint32_t kFracMask = (1u << kFracBits) - 1u;
+constexpr uint32_t kCellMask = 63u;
+constexpr uint32_t kExtraTapBit = 1u << 30;
+constexpr uint32_t kTopOffBit = 1u << 31;
 
 // ---------------------------------------------------------------------------------------
 // Error state (per host thread)

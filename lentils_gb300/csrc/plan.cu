@@ -33,9 +33,14 @@ struct CanonParams {
 constexpr int kFlagGuard = 1;
 constexpr int kFlagNonFinite = 2;
 
-__device__ __forceinline__ void canon_axis(double g, int n, int H, int logT, int T,
-                                           long long &k, int &tile, int &cell, uint32_t &frac)
+// Canonical tile / cell / fraction of one axis, and the reference's edge-tap membership.
+// g is the reference's grid coordinate u/du (unwrapped). Tap i is in the reference's set iff
+// |g - i| <= w evaluated in FP64 (kb_g, nufft.c:12); with b the floor of the quantised
+// coordinate (in the unwrapped frame) the candidates are b-w .. b+w.
+__device__ __forceinline__ void canon_axis(double g, int n, int H, int logT, int T, int w,
+                                           long long &k, int &tile, int &cell, uint32_t &word)
 {
+    const double g0 = g;
     k = (long long)floor((g + (double)H) / (double)n);
     g -= (double)k * (double)n;
     long long q = llrint(ldexp(g, kFracBits));
@@ -49,9 +54,14 @@ __device__ __forceinline__ void canon_axis(double g, int n, int H, int logT, int
         k += 1;
         c -= n;
     }
-    frac = (uint32_t)(q & (long long)kFracMask);
+    const uint32_t frac = (uint32_t)(q & (long long)kFracMask);
     tile = (int)(c >> logT);
     cell = (int)(c & (T - 1));
+    const double b = (double)((q >> kFracBits) + k * (long long)n);  // floor, unwrapped frame
+    const bool extra = (g0 - (b - w)) <= (double)w;
+    const bool top_off = !((g0 - (b + w)) >= -(double)w);
+    word = ((uint32_t)cell << kFracBits) | frac | (extra ? kExtraTapBit : 0u) |
+           (top_off ? kTopOffBit : 0u);
 }
 
 __global__ void canon_kernel(const double *__restrict__ uvw, const double *__restrict__ chans,
@@ -80,13 +90,13 @@ __global__ void canon_kernel(const double *__restrict__ uvw, const double *__res
             atomicOr(flags, kFlagGuard);
         long long ku, kv;
         int tu, tv, lu, lv;
-        uint32_t fu, fv;
-        canon_axis(ug, p.nu, p.Hu, p.logT, p.T, ku, tu, lu, fu);
-        canon_axis(vg, p.nv, p.Hv, p.logT, p.T, kv, tv, lv, fv);
+        uint32_t wu, wv;
+        canon_axis(ug, p.nu, p.Hu, p.logT, p.T, p.w, ku, tu, lu, wu);
+        canon_axis(vg, p.nv, p.Hv, p.logT, p.T, p.w, kv, tv, lv, wv);
         const int tile = tu * p.ntv + tv;
         keys[n] = ((unsigned)tile << (2 * p.logT)) | ((unsigned)lu << p.logT) | (unsigned)lv;
         idx[n] = (int)n;
-        coords[n] = make_uint2(((uint32_t)lu << kFracBits) | fu, ((uint32_t)lv << kFracBits) | fv);
+        coords[n] = make_uint2(wu, wv);
         const long long par = (ku * (long long)p.nu + kv * (long long)p.nv) & 1LL;
         double sn, cs;
         sincos(kTwoPiTrunc * (u * p.gcx + v * p.gcy), &sn, &cs);

@@ -97,8 +97,8 @@ class GriddingPlan:
 
     def degrid(self, grid, out=None, stream=None):
         """Half-plane grid (nu, nv//2+1) complex64 -> plan-order visibilities (overwrites)."""
-        assert grid.dtype == torch.complex64 and grid.is_contiguous()
-        assert grid.numel() == self.nu * self.half_nv
+        assert grid.dtype == torch.complex64 and grid.numel() == self.nu * self.half_nv
+        grid = grid.contiguous()
         if out is None:
             out = torch.empty(self.nvis, dtype=torch.complex64, device=grid.device)
         N.check(N.lib().lentils_degrid(self._handle, _ptr(grid), _ptr(out), _stream_ptr(stream)))
@@ -107,7 +107,8 @@ class GriddingPlan:
     def grid(self, vis, out=None, accumulate=False, stream=None):
         """Plan-order visibilities complex64 -> half-plane grid (accumulates into `out` when
         accumulate=True, else returns a fresh grid)."""
-        assert vis.dtype == torch.complex64 and vis.is_contiguous() and vis.numel() == self.nvis
+        assert vis.dtype == torch.complex64 and vis.numel() == self.nvis
+        vis = vis.contiguous()
         if out is None:
             out = torch.zeros((self.nu, self.half_nv), dtype=torch.complex64, device=vis.device)
         elif not accumulate:
