@@ -147,8 +147,8 @@ void grad_matrix_findiff_csr(lentils_image_space imspace, int *row_inds, int *co
  *
  * A plan re-orders the visibilities (plan order = sorted by tile and cell) and stores each as
  * two 32-bit fixed-point tile-relative coordinates. The degrid/grid kernels read and write
- * visibilities in plan order and in the plan frame (phase centre and Hermitian mirroring
- * removed). lentils_vis_to_plan / lentils_vis_from_plan convert to and from the reference's
+ * visibilities in plan order and in the plan frame (phase-centre factor and the sign of a
+ * wrap by an odd grid size removed). lentils_vis_to_plan / lentils_vis_from_plan convert to and from the reference's
  * row order and frame. In the normal-equation product F^T C^-1 F the frame factors cancel, so
  * an iterative solver stays in plan order throughout.
  * ---------------------------------------------------------------------------------------- */
