@@ -219,6 +219,32 @@ int lentils_grid_host(lentils_plan *plan, const double *vis_host, double *grid_h
                       int accumulate, void *stream);
 
 /* ------------------------------------------------------------------------------------------
+ * Gridding without device allocation. No counterpart in the reference: it exists for callers
+ * that cannot call cudaMalloc -- code running where allocation is forbidden or impossible
+ * (host callbacks and stream-ordered sections that must not synchronise, a memory budget that
+ * another framework's pool has already claimed, real-time pipelines that do not allocate after
+ * start-up).
+ *
+ * Grids up to lentils_noalloc_max_vis() visibilities (nrows * nchannels, 65536) per call from
+ * caller-owned DEVICE buffers: uvw (nrows x 3 f64), channels (nchannels f64), vis (row order,
+ * c64), grid (half plane c64, ACCUMULATED). Same result as lentils_plan_create +
+ * lentils_vis_to_plan + lentils_grid, without the plan: all working memory (binning keys,
+ * permutation, plan-frame data, work items, radix-sort storage) is one static device array of
+ * lentils_noalloc_scratch_bytes() (about 7.3 MB) that every GPU loading this library holds
+ * until the process exits. Larger batches are rejected with LENTILS_ERR_INVALID; grid them in
+ * several calls. The first call on a device looks the array's address up (set-up, once per
+ * device); make that first call before any stream capture. Calls share the array: calls whose
+ * GPU work overlaps race and corrupt each other's results, so order them on one stream. The
+ * call does not synchronise the stream; the guard of fourier_operators.py:77-80 is not applied
+ * (as grid_cpu), and non-finite coordinates are skipped.
+ * ---------------------------------------------------------------------------------------- */
+int lentils_grid_noalloc(const lentils_grid_desc *grid, const double *uvw, int nrows,
+                         const double *channels, int nchannels, const float *vis, float *grid_out,
+                         void *stream);
+int lentils_noalloc_max_vis(void);
+long long lentils_noalloc_scratch_bytes(void);
+
+/* ------------------------------------------------------------------------------------------
  * PEMD + external-shear deflection (device)
  *
  * lenses: HOST array of nlenses mass models packed as the reference packs them

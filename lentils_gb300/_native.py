@@ -85,6 +85,10 @@ _SIGNATURES = [
     ("lentils_vis_from_plan", c_int, [c_void_p, c_void_p, c_void_p, c_int, c_int, c_void_p]),
     ("lentils_degrid_host", c_int, [c_void_p, c_void_p, c_void_p, c_int, c_void_p]),
     ("lentils_grid_host", c_int, [c_void_p, c_void_p, c_void_p, c_int, c_void_p]),
+    ("lentils_grid_noalloc", c_int, [POINTER(GridDescC), c_void_p, c_int, c_void_p, c_int,
+                                     c_void_p, c_void_p, c_void_p]),
+    ("lentils_noalloc_max_vis", c_int, []),
+    ("lentils_noalloc_scratch_bytes", c_longlong, []),
     ("lentils_deflect_f32", c_int, [c_void_p, c_int, c_void_p, c_void_p, c_longlong, c_void_p]),
     ("lentils_deflect_f64io", c_int, [c_void_p, c_int, c_void_p, c_void_p, c_longlong,
                                       c_void_p]),

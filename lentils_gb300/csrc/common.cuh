@@ -84,6 +84,14 @@ struct GridGeom {
     int ntu, ntv;
 };
 
+// Parameters of the binning kernel (plan construction).
+struct CanonParams {
+    int nu, nv, T, logT, Hu, Hv, ntu, ntv, w;
+    int nrows, nch;
+    int guard;
+    double du, dv, gcx, gcy;
+};
+
 struct WorkItem {
     int tu, tv;   // tile coordinates
     int begin;    // first visibility (plan order)

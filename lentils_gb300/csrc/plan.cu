@@ -22,13 +22,6 @@
 
 namespace lentils {
 
-struct CanonParams {
-    int nu, nv, T, logT, Hu, Hv, ntu, ntv, w;
-    int nrows, nch;
-    int guard;
-    double du, dv, gcx, gcy;
-};
-
 // flags bits
 constexpr int kFlagGuard = 1;
 constexpr int kFlagNonFinite = 2;
@@ -204,6 +197,36 @@ int launch_c64_to_c128(const float2 *in, void *out, long long n, int accumulate,
     if (n <= 0) return LENTILS_OK;
     c64_to_c128_kernel<<<grid_blocks(n), 256, 0, s>>>(in, (double2 *)out, n, accumulate);
     LENTILS_CHECK_LAUNCH("c64_to_c128");
+    return LENTILS_OK;
+}
+
+// Launchers of the binning kernels for callers that own their buffers.
+int launch_canon(const double *uvw, const double *chans, const CanonParams &p, unsigned *keys,
+                 int *idx, uint2 *coords, float2 *phase, int *tile_counts, int *flags,
+                 long long nvis, cudaStream_t s)
+{
+    if (nvis <= 0) return LENTILS_OK;
+    canon_kernel<<<grid_blocks(nvis), 256, 0, s>>>(uvw, chans, p, keys, idx, coords, phase,
+                                                   tile_counts, flags);
+    LENTILS_CHECK_LAUNCH("canon_kernel");
+    return LENTILS_OK;
+}
+
+int launch_gather_plan(const int *perm, const uint2 *cin, const float2 *pin, uint2 *cout,
+                       float2 *pout, long long n, cudaStream_t s)
+{
+    if (n <= 0) return LENTILS_OK;
+    gather_plan_kernel<<<grid_blocks(n), 256, 0, s>>>(perm, cin, pin, cout, pout, n);
+    LENTILS_CHECK_LAUNCH("gather_plan_kernel");
+    return LENTILS_OK;
+}
+
+int launch_to_plan_c64(const int *perm, const float2 *phase, const float2 *vu, float2 *vp,
+                       long long n, cudaStream_t s)
+{
+    if (n <= 0) return LENTILS_OK;
+    to_plan_kernel<float2><<<grid_blocks(n), 256, 0, s>>>(perm, phase, vu, vp, n);
+    LENTILS_CHECK_LAUNCH("to_plan_kernel");
     return LENTILS_OK;
 }
 
