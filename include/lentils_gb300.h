@@ -218,6 +218,115 @@ int lentils_degrid_host(lentils_plan *plan, const double *grid_host, double *vis
 int lentils_grid_host(lentils_plan *plan, const double *vis_host, double *grid_host,
                       int accumulate, void *stream);
 
+/* FP64 forms of the plan operators (the double-precision operator used for refinement
+ * residuals): c128 plan-order visibilities and c128 half-plane grids. The phase-centre factor
+ * of the plan frame is stored in FP32 (exact for a centred image, 1e-7 otherwise). */
+int lentils_degrid64(const lentils_plan *plan, const double *grid, double *vis_plan, void *stream);
+int lentils_grid64(const lentils_plan *plan, const double *vis_plan, double *grid, void *stream);
+int lentils_vis_to_plan64(const lentils_plan *plan, const double *vis_user, double *vis_plan,
+                          void *stream);
+int lentils_vis_from_plan64(const lentils_plan *plan, const double *vis_plan, double *vis_user,
+                            int accumulate, void *stream);
+/* Real per-visibility values (e.g. inverse variances) from row order to plan order. */
+int lentils_plan_gather_real(const lentils_plan *plan, const double *user, double *plan_out,
+                             void *stream);
+
+/* ------------------------------------------------------------------------------------------
+ * NUFFT operator F = Degrid . rFFT2 . ZeroPad . Apod (NUFFTOperator,
+ * lentils/operators/fourier_operators.py:96-126) and its transpose, on device buffers.
+ * The image is (nx, ny) row-major real; it is zero-padded by (padx, pady) on each side to the
+ * plan's (nu, nv) grid; apod_x (nx) and apod_y (ny) are the two separable factors of the
+ * apodisation correction (fourier_operators.py:54-68). precisions: bit 0 = build the FP32
+ * operator, bit 1 = the FP64 operator. Visibilities are plan-order, plan-frame; the adjoint
+ * OVERWRITES the image.
+ * ---------------------------------------------------------------------------------------- */
+typedef struct lentils_nufft lentils_nufft;
+int lentils_nufft_create(lentils_nufft **op, const lentils_plan *plan, int nx, int ny, int padx,
+                         int pady, const double *apod_x, const double *apod_y, int precisions,
+                         void *stream);
+int lentils_nufft_destroy(lentils_nufft *op);
+int lentils_nufft_forward(lentils_nufft *op, const float *image, float *vis_plan, void *stream);
+int lentils_nufft_adjoint(lentils_nufft *op, const float *vis_plan, float *image, void *stream);
+int lentils_nufft_forward64(lentils_nufft *op, const double *image, double *vis_plan,
+                            void *stream);
+int lentils_nufft_adjoint64(lentils_nufft *op, const double *vis_plan, double *image,
+                            void *stream);
+
+/* ------------------------------------------------------------------------------------------
+ * Bilinear lens operator L: image pixels <- regular source grid (nsx x nsy nodes at
+ * (sxmin + j*sdx, symin + k*sdy)). src_points: deflected image-pixel positions (nimg x 2, f64,
+ * device), mask: nimg bytes (device, NULL = all pixels). No reference counterpart (the
+ * reference interpolates on Delaunay meshes, lentils/backend/triangles.c:105-140); a pixel
+ * outside the node lattice or masked has an empty row. apply: img = L src; apply_t:
+ * src = L^T img (both overwrite).
+ * ---------------------------------------------------------------------------------------- */
+typedef struct lentils_lensop lentils_lensop;
+int lentils_lensop_create(lentils_lensop **op, const double *src_points,
+                          const unsigned char *mask, int nimg, int nsx, int nsy, double sxmin,
+                          double symin, double sdx, double sdy, void *stream);
+int lentils_lensop_destroy(lentils_lensop *op);
+int lentils_lensop_nnz(const lentils_lensop *op);
+int lentils_lensop_apply(const lentils_lensop *op, const float *src, float *img, void *stream);
+int lentils_lensop_apply_t(const lentils_lensop *op, const float *img, float *src, void *stream);
+int lentils_lensop_apply64(const lentils_lensop *op, const double *src, double *img,
+                           void *stream);
+int lentils_lensop_apply_t64(const lentils_lensop *op, const double *img, double *src,
+                             void *stream);
+int lentils_lensop_diag_ltl(const lentils_lensop *op, double *diag, void *stream);
+
+/* ------------------------------------------------------------------------------------------
+ * Normal-equation operator A = L^T F^T C^-1 F L + lambda R^T R of the CG source inversion
+ * (the pattern of lentils/tests/solver_tests.py:97-114 with the 'gradient' prior of
+ * lentils/operators/operator_base.py:225-242) and its mixed-precision CG solver.
+ * weights_plan: C^-1 per visibility in plan order (f64, device); src_dx/src_dy: source pixel
+ * size (the R of grad_matrix_findiff_csr uses +-1/dx, +-1/dy). apply overwrites out.
+ * ---------------------------------------------------------------------------------------- */
+typedef struct lentils_normal_op lentils_normal_op;
+int lentils_normal_op_create(lentils_normal_op **op, lentils_lensop *L, lentils_nufft *F,
+                             const double *weights_plan, long long nvis, int nimg, int nsx,
+                             int nsy, double src_dx, double src_dy, double lambda, void *stream);
+int lentils_normal_op_destroy(lentils_normal_op *op);
+int lentils_normal_op_apply(lentils_normal_op *op, const float *s, float *out, void *stream);
+int lentils_normal_op_apply64(lentils_normal_op *op, const double *s, double *out, void *stream);
+/* b = L^T F^T C^-1 d in FP64 (d: plan-order, plan-frame c128 visibilities). */
+int lentils_normal_op_rhs64(lentils_normal_op *op, const double *d_plan, double *b, void *stream);
+/* Inverse Jacobi diagonal 1 / (sum(C^-1) * diag(L^T L) + lambda * diag(R^T R)). */
+int lentils_normal_op_jacobi(lentils_normal_op *op, double *inv_diag, float *inv_diag32,
+                             void *stream);
+double lentils_normal_op_weight_sum(const lentils_normal_op *op);
+
+typedef struct {
+    double tol;        /* target true relative residual ||b - A x|| / ||b|| (FP64 operator) */
+    double inner_tol;  /* relative residual reduction of each inner FP32 solve              */
+    int max_outer;
+    int max_inner;
+    int check_every;   /* inner iterations between host reads of the residual norm         */
+    int use_graph;     /* capture one inner iteration in a CUDA graph and replay it        */
+} lentils_cg_options;
+
+typedef struct {
+    int converged;
+    int outer;
+    int inner_total;
+    double rel_residual; /* final true FP64 relative residual */
+    double seconds;      /* wall time of the solve            */
+} lentils_cg_result;
+
+/* Iterative refinement: outer FP64 residuals r = b - A x, inner Jacobi-preconditioned CG with
+ * the FP32 operator (inv_diag32 may be NULL for no preconditioner). x (f64, device) holds the
+ * initial guess and receives the solution. */
+int lentils_cg_solve(lentils_normal_op *op, const double *b, double *x, const float *inv_diag32,
+                     const lentils_cg_options *opt, lentils_cg_result *res, void *stream);
+/* lambda R^T R s of the 'gradient' prior (R = forward differences of
+ * grad_matrix_findiff_csr, lentils/backend/nufft.c:163-194) on an (nx, ny) x-major grid,
+ * matrix-free; overwrites out. */
+int lentils_prior_gradient_apply(const float *s, float *out, int nx, int ny, double dx, double dy,
+                                 double lambda, void *stream);
+int lentils_prior_gradient_apply64(const double *s, double *out, int nx, int ny, double dx,
+                                   double dy, double lambda, void *stream);
+/* FP64 dot product of two device vectors (synchronises the stream). */
+int lentils_dot64(const double *a, const double *b, int n, double *out, void *stream);
+
 /* ------------------------------------------------------------------------------------------
  * Gridding without device allocation. No counterpart in the reference: it exists for callers
  * that cannot call cudaMalloc -- code running where allocation is forbidden or impossible

@@ -58,6 +58,16 @@ class GridDescC(Structure):
                 ("tile", c_int), ("chunk", c_int)]
 
 
+class CGOptionsC(Structure):
+    _fields_ = [("tol", c_double), ("inner_tol", c_double), ("max_outer", c_int),
+                ("max_inner", c_int), ("check_every", c_int), ("use_graph", c_int)]
+
+
+class CGResultC(Structure):
+    _fields_ = [("converged", c_int), ("outer", c_int), ("inner_total", c_int),
+                ("rel_residual", c_double), ("seconds", c_double)]
+
+
 class PlanStatsC(Structure):
     _fields_ = [("nvis", c_longlong), ("ntiles_u", c_int), ("ntiles_v", c_int), ("tile", c_int),
                 ("nitems", c_int), ("max_item_vis", c_int), ("heaviest_tile_vis", c_int),
@@ -85,6 +95,43 @@ _SIGNATURES = [
     ("lentils_vis_from_plan", c_int, [c_void_p, c_void_p, c_void_p, c_int, c_int, c_void_p]),
     ("lentils_degrid_host", c_int, [c_void_p, c_void_p, c_void_p, c_int, c_void_p]),
     ("lentils_grid_host", c_int, [c_void_p, c_void_p, c_void_p, c_int, c_void_p]),
+    ("lentils_degrid64", c_int, [c_void_p, c_void_p, c_void_p, c_void_p]),
+    ("lentils_grid64", c_int, [c_void_p, c_void_p, c_void_p, c_void_p]),
+    ("lentils_vis_to_plan64", c_int, [c_void_p, c_void_p, c_void_p, c_void_p]),
+    ("lentils_vis_from_plan64", c_int, [c_void_p, c_void_p, c_void_p, c_int, c_void_p]),
+    ("lentils_plan_gather_real", c_int, [c_void_p, c_void_p, c_void_p, c_void_p]),
+    ("lentils_nufft_create", c_int, [POINTER(c_void_p), c_void_p, c_int, c_int, c_int, c_int,
+                                     c_void_p, c_void_p, c_int, c_void_p]),
+    ("lentils_nufft_destroy", c_int, [c_void_p]),
+    ("lentils_nufft_forward", c_int, [c_void_p, c_void_p, c_void_p, c_void_p]),
+    ("lentils_nufft_adjoint", c_int, [c_void_p, c_void_p, c_void_p, c_void_p]),
+    ("lentils_nufft_forward64", c_int, [c_void_p, c_void_p, c_void_p, c_void_p]),
+    ("lentils_nufft_adjoint64", c_int, [c_void_p, c_void_p, c_void_p, c_void_p]),
+    ("lentils_lensop_create", c_int, [POINTER(c_void_p), c_void_p, c_void_p, c_int, c_int, c_int,
+                                      c_double, c_double, c_double, c_double, c_void_p]),
+    ("lentils_lensop_destroy", c_int, [c_void_p]),
+    ("lentils_lensop_nnz", c_int, [c_void_p]),
+    ("lentils_lensop_apply", c_int, [c_void_p, c_void_p, c_void_p, c_void_p]),
+    ("lentils_lensop_apply_t", c_int, [c_void_p, c_void_p, c_void_p, c_void_p]),
+    ("lentils_lensop_apply64", c_int, [c_void_p, c_void_p, c_void_p, c_void_p]),
+    ("lentils_lensop_apply_t64", c_int, [c_void_p, c_void_p, c_void_p, c_void_p]),
+    ("lentils_lensop_diag_ltl", c_int, [c_void_p, c_void_p, c_void_p]),
+    ("lentils_normal_op_create", c_int, [POINTER(c_void_p), c_void_p, c_void_p, c_void_p,
+                                         c_longlong, c_int, c_int, c_int, c_double, c_double,
+                                         c_double, c_void_p]),
+    ("lentils_normal_op_destroy", c_int, [c_void_p]),
+    ("lentils_normal_op_apply", c_int, [c_void_p, c_void_p, c_void_p, c_void_p]),
+    ("lentils_normal_op_apply64", c_int, [c_void_p, c_void_p, c_void_p, c_void_p]),
+    ("lentils_normal_op_rhs64", c_int, [c_void_p, c_void_p, c_void_p, c_void_p]),
+    ("lentils_normal_op_jacobi", c_int, [c_void_p, c_void_p, c_void_p, c_void_p]),
+    ("lentils_normal_op_weight_sum", c_double, [c_void_p]),
+    ("lentils_cg_solve", c_int, [c_void_p, c_void_p, c_void_p, c_void_p, POINTER(CGOptionsC),
+                                 POINTER(CGResultC), c_void_p]),
+    ("lentils_prior_gradient_apply", c_int, [c_void_p, c_void_p, c_int, c_int, c_double,
+                                             c_double, c_double, c_void_p]),
+    ("lentils_prior_gradient_apply64", c_int, [c_void_p, c_void_p, c_int, c_int, c_double,
+                                               c_double, c_double, c_void_p]),
+    ("lentils_dot64", c_int, [c_void_p, c_void_p, c_int, POINTER(c_double), c_void_p]),
     ("lentils_grid_noalloc", c_int, [POINTER(GridDescC), c_void_p, c_int, c_void_p, c_int,
                                      c_void_p, c_void_p, c_void_p]),
     ("lentils_noalloc_max_vis", c_int, []),

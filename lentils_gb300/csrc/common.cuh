@@ -63,9 +63,16 @@ struct KBPoly {
     float edge;  // weight of the extra tap at argument +w (only when f == 0): -1/(2w)
 };
 
+// The same table in FP64 (for the double-precision operator used by the refinement residual):
+// cd[k][i] is coefficient k (highest degree first) of tap i.
+struct KBPoly64 {
+    double cd[kPolyCoef][kMaxTaps];
+    double edge;
+};
+
 // Host: fit the table for (w, beta). Returns max abs fit error relative to the peak
-// (evaluated in FP64) through *fit_err when non-null.
-void kb_poly_build(int w, double beta, KBPoly *out, double *fit_err);
+// (evaluated in FP64) through *fit_err when non-null. `out64` may be null.
+void kb_poly_build(int w, double beta, KBPoly *out, double *fit_err, KBPoly64 *out64 = nullptr);
 double host_bessel_i0(double x);
 
 // ---------------------------------------------------------------------------------------
@@ -105,6 +112,7 @@ struct lentils_plan {
     lentils_grid_desc desc;
     lentils::GridGeom geom;
     lentils::KBPoly kb;
+    lentils::KBPoly64 kb64;
     int device;
     long long nvis;
     int nrows, nchannels;
@@ -114,6 +122,7 @@ struct lentils_plan {
     int has_phase;
     // plan-order arrays
     uint2 *coords;        // fixed-point tile-relative (u, v)
+    float2 *coords_res;   // g - q*2^-24 per axis (exact in FP64, stored FP32): FP64 kernels only
     int *perm;            // plan index -> user index (channel*nrows + row)
     float2 *phase;        // s * e^{-i phi} per visibility (plan order)
     lentils::WorkItem *items;

@@ -31,7 +31,8 @@ constexpr int kFlagNonFinite = 2;
 // |g - i| <= w evaluated in FP64 (kb_g, nufft.c:12); with b the floor of the quantised
 // coordinate (in the unwrapped frame) the candidates are b-w .. b+w.
 __device__ __forceinline__ void canon_axis(double g, int n, int H, int logT, int T, int w,
-                                           long long &k, int &tile, int &cell, uint32_t &word)
+                                           long long &k, int &tile, int &cell, uint32_t &word,
+                                           float &res)
 {
     const double g0 = g;
     k = (long long)floor((g + (double)H) / (double)n);
@@ -48,6 +49,7 @@ __device__ __forceinline__ void canon_axis(double g, int n, int H, int logT, int
         c -= n;
     }
     const uint32_t frac = (uint32_t)(q & (long long)kFracMask);
+    res = (float)(g - ldexp((double)q, -kFracBits));  // |res| <= 2^-25, exact difference
     tile = (int)(c >> logT);
     cell = (int)(c & (T - 1));
     const double b = (double)((q >> kFracBits) + k * (long long)n);  // floor, unwrapped frame
@@ -60,7 +62,8 @@ __device__ __forceinline__ void canon_axis(double g, int n, int H, int logT, int
 __global__ void canon_kernel(const double *__restrict__ uvw, const double *__restrict__ chans,
                              CanonParams p, unsigned *__restrict__ keys, int *__restrict__ idx,
                              uint2 *__restrict__ coords, float2 *__restrict__ phase,
-                             int *__restrict__ tile_counts, int *__restrict__ flags)
+                             int *__restrict__ tile_counts, int *__restrict__ flags,
+                             float2 *__restrict__ res)
 {
     const long long total = (long long)p.nrows * p.nch;
     for (long long n = blockIdx.x * (long long)blockDim.x + threadIdx.x; n < total;
@@ -77,6 +80,7 @@ __global__ void canon_kernel(const double *__restrict__ uvw, const double *__res
             idx[n] = (int)n;
             coords[n] = make_uint2(0, 0);
             phase[n] = make_float2(0.f, 0.f);
+            if (res) res[n] = make_float2(0.f, 0.f);
             continue;
         }
         if (p.guard && (fabs(ug) + p.w + 1 > 0.5 * p.nu || fabs(vg) + p.w + 1 > 0.5 * p.nv))
@@ -84,8 +88,10 @@ __global__ void canon_kernel(const double *__restrict__ uvw, const double *__res
         long long ku, kv;
         int tu, tv, lu, lv;
         uint32_t wu, wv;
-        canon_axis(ug, p.nu, p.Hu, p.logT, p.T, p.w, ku, tu, lu, wu);
-        canon_axis(vg, p.nv, p.Hv, p.logT, p.T, p.w, kv, tv, lv, wv);
+        float ru, rv;
+        canon_axis(ug, p.nu, p.Hu, p.logT, p.T, p.w, ku, tu, lu, wu, ru);
+        canon_axis(vg, p.nv, p.Hv, p.logT, p.T, p.w, kv, tv, lv, wv, rv);
+        if (res) res[n] = make_float2(ru, rv);
         const int tile = tu * p.ntv + tv;
         keys[n] = ((unsigned)tile << (2 * p.logT)) | ((unsigned)lu << p.logT) | (unsigned)lv;
         idx[n] = (int)n;
@@ -101,13 +107,15 @@ __global__ void canon_kernel(const double *__restrict__ uvw, const double *__res
 
 __global__ void gather_plan_kernel(const int *__restrict__ perm, const uint2 *__restrict__ cin,
                                    const float2 *__restrict__ pin, uint2 *__restrict__ cout,
-                                   float2 *__restrict__ pout, long long n)
+                                   float2 *__restrict__ pout, long long n,
+                                   const float2 *__restrict__ rin, float2 *__restrict__ rout)
 {
     for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < n;
          k += (long long)gridDim.x * blockDim.x) {
         const int s = perm[k];
         cout[k] = cin[s];
         pout[k] = pin[s];
+        if (rin) rout[k] = rin[s];
     }
 }
 
@@ -146,6 +154,47 @@ __global__ void from_plan_kernel(const int *__restrict__ perm, const float2 *__r
             dst.y = im;
         }
     }
+}
+
+// plan order <- user order in FP64 (c128 both sides)
+__global__ void to_plan64_kernel(const int *__restrict__ perm, const float2 *__restrict__ phase,
+                                 const double2 *__restrict__ vu, double2 *__restrict__ vp,
+                                 long long n)
+{
+    for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < n;
+         k += (long long)gridDim.x * blockDim.x) {
+        const double2 v = vu[perm[k]];
+        const double px = phase[k].x, py = phase[k].y;
+        vp[k] = make_double2(px * v.x + py * v.y, px * v.y - py * v.x);
+    }
+}
+
+// user order <- plan order in FP64: V[perm[k]] (+)= phase[k] * y[k]
+__global__ void from_plan64_kernel(const int *__restrict__ perm, const float2 *__restrict__ phase,
+                                   const double2 *__restrict__ vp, double2 *__restrict__ vu,
+                                   long long n, int accumulate)
+{
+    for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < n;
+         k += (long long)gridDim.x * blockDim.x) {
+        const double2 y = vp[k];
+        const double px = phase[k].x, py = phase[k].y;
+        const double re = px * y.x - py * y.y, im = px * y.y + py * y.x;
+        double2 &d = vu[perm[k]];
+        if (accumulate) {
+            d.x += re;
+            d.y += im;
+        } else {
+            d = make_double2(re, im);
+        }
+    }
+}
+
+__global__ void gather_real_kernel(const int *__restrict__ perm, const double *__restrict__ u,
+                                   double *__restrict__ out, long long n)
+{
+    for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < n;
+         k += (long long)gridDim.x * blockDim.x)
+        out[k] = u[perm[k]];
 }
 
 __global__ void c128_to_c64_kernel(const double2 *__restrict__ in, float2 *__restrict__ out,
@@ -207,7 +256,7 @@ int launch_canon(const double *uvw, const double *chans, const CanonParams &p, u
 {
     if (nvis <= 0) return LENTILS_OK;
     canon_kernel<<<grid_blocks(nvis), 256, 0, s>>>(uvw, chans, p, keys, idx, coords, phase,
-                                                   tile_counts, flags);
+                                                   tile_counts, flags, nullptr);
     LENTILS_CHECK_LAUNCH("canon_kernel");
     return LENTILS_OK;
 }
@@ -216,7 +265,8 @@ int launch_gather_plan(const int *perm, const uint2 *cin, const float2 *pin, uin
                        float2 *pout, long long n, cudaStream_t s)
 {
     if (n <= 0) return LENTILS_OK;
-    gather_plan_kernel<<<grid_blocks(n), 256, 0, s>>>(perm, cin, pin, cout, pout, n);
+    gather_plan_kernel<<<grid_blocks(n), 256, 0, s>>>(perm, cin, pin, cout, pout, n, nullptr,
+                                                      nullptr);
     LENTILS_CHECK_LAUNCH("gather_plan_kernel");
     return LENTILS_OK;
 }
@@ -260,6 +310,7 @@ static void free_plan_arrays(lentils_plan *p)
     cudaFree(p->coords);
     cudaFree(p->perm);
     cudaFree(p->phase);
+    cudaFree(p->coords_res);
     cudaFree(p->items);
     cudaFree(p->stage_vis64);
     cudaFree(p->stage_grid64);
@@ -307,17 +358,19 @@ static int plan_build(lentils_plan *p, const double *uvw, const double *chans, i
     unsigned *keys, *keys_sorted;
     int *idx, *tile_counts, *d_flags;
     uint2 *coords_user;
-    float2 *phase_user;
+    float2 *phase_user, *res_user;
     if ((st = tmp.alloc(&keys, nvis))) return st;
     if ((st = tmp.alloc(&keys_sorted, nvis))) return st;
     if ((st = tmp.alloc(&idx, nvis))) return st;
     if ((st = tmp.alloc(&coords_user, nvis))) return st;
     if ((st = tmp.alloc(&phase_user, nvis))) return st;
+    if ((st = tmp.alloc(&res_user, nvis))) return st;
     if ((st = tmp.alloc(&tile_counts, ntiles))) return st;
     if ((st = tmp.alloc(&d_flags, 1))) return st;
     if ((st = dev_alloc(&p->coords, nvis, &p->device_bytes))) return st;
     if ((st = dev_alloc(&p->perm, nvis, &p->device_bytes))) return st;
     if ((st = dev_alloc(&p->phase, nvis, &p->device_bytes))) return st;
+    if ((st = dev_alloc(&p->coords_res, nvis, &p->device_bytes))) return st;
     LENTILS_CUDA_TRY(cudaMemsetAsync(tile_counts, 0, sizeof(int) * ntiles, s));
     LENTILS_CUDA_TRY(cudaMemsetAsync(d_flags, 0, sizeof(int), s));
 
@@ -327,7 +380,7 @@ static int plan_build(lentils_plan *p, const double *uvw, const double *chans, i
     cp.guard = (flags & LENTILS_PLAN_NYQUIST_GUARD) ? 1 : 0;
     cp.du = p->desc.du; cp.dv = p->desc.dv; cp.gcx = p->desc.gcx; cp.gcy = p->desc.gcy;
     canon_kernel<<<grid_blocks(nvis), 256, 0, s>>>(d_uvw, d_ch, cp, keys, idx, coords_user,
-                                                   phase_user, tile_counts, d_flags);
+                                                   phase_user, tile_counts, d_flags, res_user);
     LENTILS_CHECK_LAUNCH("canon_kernel");
 
     // stable radix sort of (key, user index) pairs
@@ -344,7 +397,8 @@ static int plan_build(lentils_plan *p, const double *uvw, const double *chans, i
                                                      p->perm, (int64_t)nvis, 0,
                                                      std::min(32, key_bits), s));
     gather_plan_kernel<<<grid_blocks(nvis), 256, 0, s>>>(p->perm, coords_user, phase_user,
-                                                         p->coords, p->phase, nvis);
+                                                         p->coords, p->phase, nvis, res_user,
+                                                         p->coords_res);
     LENTILS_CHECK_LAUNCH("gather_plan_kernel");
 
     std::vector<int> counts(ntiles);
@@ -470,7 +524,7 @@ int lentils_plan_create(lentils_plan **out, const lentils_grid_desc *gd, const d
     p->nrows = nrows;
     p->nchannels = nchannels;
     p->has_phase = (gd->gcx != 0.0 || gd->gcy != 0.0) ? 1 : 0;
-    kb_poly_build(g.w, gd->kb_beta, &p->kb, nullptr);
+    kb_poly_build(g.w, gd->kb_beta, &p->kb, nullptr, &p->kb64);
 
     int st = LENTILS_OK;
     if (nvis > 0) st = plan_build(p, uvw, channels, flags, (cudaStream_t)stream);
@@ -561,6 +615,43 @@ int lentils_vis_from_plan(const lentils_plan *p, const float *vp, void *vu, int 
         from_plan_kernel<float2><<<grid_blocks(p->nvis), 256, 0, s>>>(
             p->perm, p->phase, (const float2 *)vp, (float2 *)vu, p->nvis, accumulate);
     LENTILS_CHECK_LAUNCH("from_plan_kernel");
+    return LENTILS_OK;
+}
+
+int lentils_vis_to_plan64(const lentils_plan *p, const double *vu, double *vp, void *stream)
+{
+    clear_error();
+    if (!p || (p->nvis > 0 && (!vu || !vp)))
+        return set_error(LENTILS_ERR_INVALID, "vis_to_plan64: null argument");
+    if (p->nvis == 0) return LENTILS_OK;
+    to_plan64_kernel<<<grid_blocks(p->nvis), 256, 0, (cudaStream_t)stream>>>(
+        p->perm, p->phase, (const double2 *)vu, (double2 *)vp, p->nvis);
+    LENTILS_CHECK_LAUNCH("to_plan64_kernel");
+    return LENTILS_OK;
+}
+
+int lentils_vis_from_plan64(const lentils_plan *p, const double *vp, double *vu, int accumulate,
+                            void *stream)
+{
+    clear_error();
+    if (!p || (p->nvis > 0 && (!vu || !vp)))
+        return set_error(LENTILS_ERR_INVALID, "vis_from_plan64: null argument");
+    if (p->nvis == 0) return LENTILS_OK;
+    from_plan64_kernel<<<grid_blocks(p->nvis), 256, 0, (cudaStream_t)stream>>>(
+        p->perm, p->phase, (const double2 *)vp, (double2 *)vu, p->nvis, accumulate);
+    LENTILS_CHECK_LAUNCH("from_plan64_kernel");
+    return LENTILS_OK;
+}
+
+int lentils_plan_gather_real(const lentils_plan *p, const double *u, double *out, void *stream)
+{
+    clear_error();
+    if (!p || (p->nvis > 0 && (!u || !out)))
+        return set_error(LENTILS_ERR_INVALID, "plan_gather_real: null argument");
+    if (p->nvis == 0) return LENTILS_OK;
+    gather_real_kernel<<<grid_blocks(p->nvis), 256, 0, (cudaStream_t)stream>>>(p->perm, u, out,
+                                                                               p->nvis);
+    LENTILS_CHECK_LAUNCH("gather_real_kernel");
     return LENTILS_OK;
 }
 

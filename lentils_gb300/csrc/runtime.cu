@@ -65,9 +65,10 @@ static double kb_profile(double a, double w, double beta)
 
 // Chebyshev interpolation (at the n Chebyshev points of the first kind) of each tap's weight
 // as a function of t = 2f - 1, converted to monomial coefficients in t.
-void kb_poly_build(int w, double beta, KBPoly *out, double *fit_err)
+void kb_poly_build(int w, double beta, KBPoly *out, double *fit_err, KBPoly64 *out64)
 {
     memset(out, 0, sizeof(*out));
+    if (out64) memset(out64, 0, sizeof(*out64));
     const int n = kPolyCoef;
     const double norm = 1.0 / (2.0 * w);
     double worst = 0.0;
@@ -109,6 +110,7 @@ void kb_poly_build(int w, double beta, KBPoly *out, double *fit_err)
             const float c = (float)mono[n - 1 - k];
             if (i & 1) out->cp[k][i >> 1].y = c;
             else out->cp[k][i >> 1].x = c;
+            if (out64) out64->cd[k][i] = mono[n - 1 - k];
         }
         if (fit_err) {
             for (int s = 0; s <= 400; ++s) {
@@ -123,6 +125,7 @@ void kb_poly_build(int w, double beta, KBPoly *out, double *fit_err)
     }
     // extra tap at argument exactly +w (frac == 0): profile I0(0) = 1, tap index -1 -> sign -1
     out->edge = (float)(-norm * kb_profile((double)w, w, beta));
+    if (out64) out64->edge = -norm * kb_profile((double)w, w, beta);
     if (fit_err) *fit_err = worst;
 }
 
