@@ -331,12 +331,91 @@ def run_ours(args):
                      "heaviest_tile_vis": st["heaviest_tile_vis"]},
             "clocks": clk,
         }
+        if not args.no_cg:
+            line["cg"] = run_cg_bench()
         if not args.no_cpu_baseline:
             line["cpu_baseline"] = cpu_baseline(four, uvw)
         print(json.dumps(line))
     if world > 1:
         dist.destroy_process_group()
     return 0
+
+
+# CG source inversion (512^2 image plane, 128^2 source grid, 2e6 visibilities, PEMD b=1.2",
+# q=0.7, gamma=2.0 + external shear (0.05, 20 deg), lambda=1e-2 gradient prior, sigma=1).
+CG_IMG, CG_PIX, CG_SRC, CG_SRC_HALF, CG_NVIS, CG_LAMBDA = 512, 0.01, 128, 0.64, 2_000_000, 1e-2
+
+
+def cg_problem(seed=SEED + 7):
+    import numpy as np
+    sys.path.insert(0, os.path.join(REPO, "oracle"))
+    import oracle as O  # synthetic-input generator only
+    from lentils_gb300.lens_models import ExternalPotential, GlobalLensModel, PowerLawEllipsoid
+    from lentils_gb300.operators import BilinearLensOperator, NUFFTOperator
+    from lentils_gb300.spaces import ImageSpace, VisibilitySpace
+    rng = np.random.default_rng(seed)
+    half = 0.5 * CG_IMG * CG_PIX
+    ims = ImageSpace((CG_IMG, CG_IMG), [(-half, half), (-half, half)])
+    srcs = ImageSpace((CG_SRC, CG_SRC), [(-CG_SRC_HALF, CG_SRC_HALF), (-CG_SRC_HALF, CG_SRC_HALF)])
+    img = O.ImageGeom((CG_IMG, CG_IMG), [(-half, half), (-half, half)])
+    four = O.FourierGeom(O.padded_geom(img, 2)[0])
+    uvw = O.synth_uv(rng, CG_NVIS, four, 0.45, 4)
+    c = 0.25 * CG_PIX  # lens centre off the pixel corners (the PEMD is singular at its centre)
+    glm = GlobalLensModel([PowerLawEllipsoid(z=0.5, b=1.2, th=0.0, f=0.7, x=c, y=c, rc=0.0,
+                                             qh=0.5),
+                           ExternalPotential(z=0.5, x=c, y=c, ss=0.05, sa=20.0)])
+    vs = VisibilitySpace(channels=[1.0], uvcoords=uvw)
+    xs = (srcs.xmin + srcs.dx * np.arange(CG_SRC))[:, None]
+    ys = (srcs.ymin + srcs.dy * np.arange(CG_SRC))[None, :]
+    s_true = (np.exp(-((xs - 0.05) ** 2 + (ys - 0.02) ** 2) / (2 * 0.06 ** 2))
+              + 0.5 * np.exp(-((xs + 0.1) ** 2 + (ys + 0.08) ** 2) / (2 * 0.04 ** 2)))
+    F = NUFFTOperator(vs, ims)
+    L = BilinearLensOperator(ims, srcs, glm, z_src=2.0)
+    d = (F * (L * s_true)).reshape(-1) + O.complex_normal(rng, CG_NVIS)
+    del F, L
+    return vs, d, ims, srcs, glm
+
+
+def run_cg_bench():
+    """Plain Jacobi-CG (FP32 operator, FP64 refinement, CUDA-graph inner iterations) to a true
+    FP64 relative residual of 1e-6 on the full-size inversion."""
+    import torch
+    from lentils_gb300.inversion import SourceInversion
+    vs, d, ims, srcs, glm = cg_problem()
+    t0 = time.perf_counter()
+    inv = SourceInversion(vs, d, 1.0, ims, srcs, glm, 2.0, CG_LAMBDA)
+    setup_s = time.perf_counter() - t0
+    inv.solve(tol=1e-2, use_graph=True)  # warm-up (graph capture, cuFFT plans, caches)
+    x, info = inv.solve(tol=1e-6, use_graph=True)
+    # one FP32 and one FP64 matvec, timed with events on the solver's stream
+    s32 = torch.randn(inv.nsrc, device="cuda", dtype=torch.float32)
+    s64 = s32.double()
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
+    import ctypes
+    from lentils_gb300 import _native as N
+    from lentils_gb300.gridding import _ptr
+    o32 = torch.empty_like(s32)
+    o64 = torch.empty_like(s64)
+    sp = ctypes.c_void_p(inv.stream.cuda_stream)
+    L = N.lib()
+    for _ in range(3):
+        N.check(L.lentils_normal_op_apply(inv.handle, _ptr(s32), _ptr(o32), sp))
+    ev[0].record(inv.stream)
+    for _ in range(10):
+        N.check(L.lentils_normal_op_apply(inv.handle, _ptr(s32), _ptr(o32), sp))
+    ev[1].record(inv.stream)
+    N.check(L.lentils_normal_op_apply64(inv.handle, _ptr(s64), _ptr(o64), sp))
+    ev[2].record(inv.stream)
+    N.check(L.lentils_normal_op_apply64(inv.handle, _ptr(s64), _ptr(o64), sp))
+    ev[3].record(inv.stream)
+    torch.cuda.synchronize()
+    return {"workload": "CG source inversion: 512^2 image (0.01\"), 128^2 source, 2e6 vis, "
+                        "PEMD b=1.2 q=0.7 gamma=2 + shear (0.05, 20 deg), lambda=1e-2",
+            "preconditioner": "jacobi", "tol": 1e-6, "converged": info["converged"],
+            "rel_residual_fp64": info["rel_residual"], "outer": info["outer"],
+            "inner_iterations": info["inner_total"], "solve_s": info["seconds"],
+            "setup_s": setup_s, "matvec32_ms": ev[0].elapsed_time(ev[1]) / 10,
+            "matvec64_ms": ev[2].elapsed_time(ev[3])}
 
 
 def cpu_baseline(four, uvw):
@@ -359,6 +438,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-cg", action="store_true")
     args = ap.parse_args()
     os.environ.setdefault("OMP_NUM_THREADS", str(os.cpu_count() or 1))
     if args.impl == "reference":

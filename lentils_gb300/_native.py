@@ -89,6 +89,7 @@ _SIGNATURES = [
                                     c_void_p, c_int, c_int, c_void_p]),
     ("lentils_plan_destroy", c_int, [c_void_p]),
     ("lentils_plan_get_stats", c_int, [c_void_p, POINTER(PlanStatsC)]),
+    ("lentils_plan_set_grid_variant", c_int, [c_void_p, c_int]),
     ("lentils_degrid", c_int, [c_void_p, c_void_p, c_void_p, c_void_p]),
     ("lentils_grid", c_int, [c_void_p, c_void_p, c_void_p, c_void_p]),
     ("lentils_vis_to_plan", c_int, [c_void_p, c_void_p, c_int, c_void_p, c_void_p]),

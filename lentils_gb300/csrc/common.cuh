@@ -58,8 +58,15 @@ int cuda_status(cudaError_t e, const char *what);
 // folded in. Tap i (0 <= i < 2w) of a visibility with fractional offset f in [0,1) sits at
 // kernel argument f + w - 1 - i.
 // ---------------------------------------------------------------------------------------
+//
+// Symmetry: the profile is even, so tap 2w-1-i is the reflection of tap i,
+// P_{2w-1-i}(t) = -P_i(-t). The FP32 table keeps only taps i < w, split into even and odd
+// parts in t^2 (P_i(t) = E_i(t^2) + t O_i(t^2)), so one evaluation of E_i and O_i gives both
+// taps i and 2w-1-i. ce/co[k][p] pair taps (2p, 2p+1), highest power of t^2 first.
+constexpr int kHalfCoef = kPolyCoef / 2;  // 5 even + 5 odd coefficients (degree 9)
 struct KBPoly {
-    float2 cp[kPolyCoef][kMaxW];
+    float2 ce[kHalfCoef][kMaxW / 2];
+    float2 co[kHalfCoef][kMaxW / 2];
     float edge;  // weight of the extra tap at argument +w (only when f == 0): -1/(2w)
 };
 
@@ -120,6 +127,7 @@ struct lentils_plan {
     int max_item;
     int heaviest_tile;
     int has_phase;
+    int grid_variant;     // visibilities per warp iteration in the gridding kernel (1 or 2)
     // plan-order arrays
     uint2 *coords;        // fixed-point tile-relative (u, v)
     float2 *coords_res;   // g - q*2^-24 per axis (exact in FP64, stored FP32): FP64 kernels only

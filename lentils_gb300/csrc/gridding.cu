@@ -40,16 +40,27 @@ template <int W2>
 __device__ __forceinline__ void kb_weights(const KBPoly &kb, uint32_t word, float (&wt)[W2],
                                            float /*res: FP64 kernels only*/ = 0.f)
 {
+    constexpr int w = W2 / 2;
     const float f = (float)(word & kFracMask) * (1.0f / (float)(1u << kFracBits));
     const float t = fmaf(2.0f, f, -1.0f);
     const float2 tt = make_float2(t, t);
+    const float2 uu = make_float2(t * t, t * t);
 #pragma unroll
-    for (int p = 0; p < W2 / 2; ++p) {
-        float2 acc = kb.cp[0][p];
+    for (int p = 0; p < (w + 1) / 2; ++p) {
+        float2 e = kb.ce[0][p], o = kb.co[0][p];
 #pragma unroll
-        for (int k = 1; k < kPolyCoef; ++k) acc = __ffma2_rn(acc, tt, kb.cp[k][p]);
-        wt[2 * p] = acc.x;
-        wt[2 * p + 1] = acc.y;
+        for (int k = 1; k < kHalfCoef; ++k) {
+            e = __ffma2_rn(e, uu, kb.ce[k][p]);
+            o = __ffma2_rn(o, uu, kb.co[k][p]);
+        }
+        const float2 lo = __ffma2_rn(tt, o, e);                               // P_i(t)
+        const float2 hi = __ffma2_rn(tt, o, make_float2(-e.x, -e.y));         // -P_i(-t)
+        wt[2 * p] = lo.x;
+        wt[W2 - 1 - 2 * p] = hi.x;
+        if (2 * p + 1 < w) {
+            wt[2 * p + 1] = lo.y;
+            wt[W2 - 2 - 2 * p] = hi.y;
+        }
     }
     if (word & kTopOffBit) wt[W2 - 1] = 0.f;
 }
@@ -236,29 +247,55 @@ __device__ __forceinline__ void grid_flush_extended(const typename Prec<R>::C *s
     }
 }
 
-// Taps per lane in the warp-cooperative gridder: the smallest divisor of 2w whose 32 lanes
-// cover all (2w)^2 taps, so each lane's taps lie in one row of the window.
-template <int W2>
-struct LaneTaps {
+constexpr int kGridBatch = 256;  // visibilities per weight batch (= threads per CTA)
+
+// Layout of one visibility's row in the gridding batch, in units of R:
+//   [0, W2)        v-axis weights wv
+//   [W2, 2W2)      u-axis weights wu
+//   2W2, 2W2+1     weighted value x (re, im)
+//   2W2+2          cell key (bit pattern of an int)
+// and the split of a warp into V sub-groups of 32/V lanes, each working on its own visibility;
+// every active lane owns PER adjacent taps of one row of the 2w x 2w window.
+template <int W2, int V, typename R>
+struct GridShape {
+    static constexpr int STR = 2 * W2 + 4;
+    static constexpr int LPV = 32 / V;  // lanes per visibility
     static constexpr int per()
     {
         for (int d = 1; d <= W2; ++d)
-            if (W2 % d == 0 && 32 * d >= W2 * W2) return d;
+            if (W2 % d == 0 && LPV * d >= W2 * W2) return d;
         return W2;
     }
     static constexpr int PER = per();
-    static constexpr int STR = 2 * W2 + 1;  // floats per visibility in the weight batch (odd)
 };
 
-constexpr int kGridBatch = 256;  // visibilities per weight batch (= threads per CTA)
+template <typename R>
+__device__ __forceinline__ R key_as(int k);
+template <>
+__device__ __forceinline__ float key_as<float>(int k) { return __int_as_float(k); }
+template <>
+__device__ __forceinline__ double key_as<double>(int k) { return __longlong_as_double((long long)k); }
+template <typename R>
+__device__ __forceinline__ int key_of(R v);
+template <>
+__device__ __forceinline__ int key_of<float>(float v) { return __float_as_int(v); }
+template <>
+__device__ __forceinline__ int key_of<double>(double v) { return (int)__double_as_longlong(v); }
 
-// Gridding: per batch of 256 sorted visibilities, each thread evaluates one visibility's 2w+2w
-// weights into shared memory; then each warp walks 32 consecutive visibilities, its lanes
-// owning PER taps of the 2w x 2w window (one row, PER adjacent columns) and accumulating them
-// in registers while the visibilities stay in one cell. A change of cell (or the end of the
-// warp's 32) flushes the lane's taps to the shared extended tile with PER*2 atomics on distinct
-// addresses; the whole warp flushes together.
-template <int W2, typename R>
+// Gridding. Per batch of 256 sorted visibilities, each thread evaluates one visibility's
+// weights into a shared row. Each warp then walks its 32 visibilities as V sub-groups of 32/V
+// lanes (sub-group h takes a contiguous 32/V of them); a lane owns PER adjacent taps of one
+// window row and accumulates them in registers while its sub-group's visibilities stay in one
+// cell (weights and value are broadcast reads of the shared row). A change of cell, or the
+// end of the sub-group's share, flushes the lane's taps into the extended tile.
+//
+// PRIV (V == 1 only): every warp has its own copy of the extended tile, flushed with plain
+// load-add-store -- with V == 1 the whole warp works on one visibility, so the flush branch is
+// warp-uniform, the lanes own distinct taps and no other warp writes the copy -- and the copies
+// are summed once per work item before the global flush. Otherwise (V == 2, whose half-warps
+// flush independently, or when the copies do not fit in shared memory) all warps share one
+// tile and flush with shared-memory atomics.
+template <int W2, int V, bool PRIV, typename R>
 __global__ void __launch_bounds__(kGridBatch)
     grid_kernel(const typename Prec<R>::C *__restrict__ vis, const uint2 *__restrict__ coords,
                 typename Prec<R>::C *__restrict__ grid, const WorkItem *__restrict__ items,
@@ -267,27 +304,30 @@ __global__ void __launch_bounds__(kGridBatch)
 {
     using P = Prec<R>;
     using C = typename P::C;
-    using LT = LaneTaps<W2>;
-    constexpr int PER = LT::PER, STR = LT::STR;
+    using GS = GridShape<W2, V, R>;
+    constexpr int STR = GS::STR, LPV = GS::LPV, PER = GS::PER;
+    constexpr int NW = kGridBatch / 32;
+    static_assert(!PRIV || V == 1, "private warp tiles need a warp-uniform flush (V == 1)");
     extern __shared__ __align__(16) unsigned char smraw[];
     const WorkItem it = items[blockIdx.x];
     const int E = g.E, S = g.stride;
-    C *sm = reinterpret_cast<C *>(smraw);                       // E x S extended tile
-    const size_t tile_bytes = ((sizeof(C) * (size_t)E * S) + 15) & ~size_t(15);
-    C *sx = reinterpret_cast<C *>(smraw + tile_bytes);           // per vis: weighted value
-    int *skey = reinterpret_cast<int *>(sx + kGridBatch);        // per vis: cell key
-    R *swt = reinterpret_cast<R *>(skey + kGridBatch);           // per vis: wu[W2] | wv[W2]
-    for (int e = threadIdx.x; e < E * S; e += blockDim.x) sm[e] = P::zero();
+    const int ntile = PRIV ? NW : 1;
+    C *tiles = reinterpret_cast<C *>(smraw);  // ntile x (E x S) extended tiles
+    const size_t tile_bytes = ((sizeof(C) * (size_t)ntile * E * S) + 15) & ~size_t(15);
+    R *rows = reinterpret_cast<R *>(smraw + tile_bytes);  // kGridBatch x STR
+    for (int e = threadIdx.x; e < ntile * E * S; e += blockDim.x) tiles[e] = P::zero();
 
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const int t0 = lane * PER;
+    C *mytile = tiles + (PRIV ? warp * E * S : 0);
+    const int sub = lane / LPV, sl = lane - sub * LPV;
+    const int t0 = sl * PER;
     const bool active = t0 < W2 * W2;
     const int ti = active ? t0 / W2 : 0;
-    const int tj = active ? t0 % W2 : 0;
+    const int tj = active ? t0 - ti * W2 : 0;
 
     for (int base = 0; base < it.count; base += kGridBatch) {
         const int n = min(kGridBatch, it.count - base);
-        __syncthreads();  // tile zeroed / previous batch consumed
+        __syncthreads();  // tiles zeroed / previous batch consumed
         if ((int)threadIdx.x < n) {
             const int k = threadIdx.x;
             const uint2 c = coords[it.begin + base + k];
@@ -299,52 +339,72 @@ __global__ void __launch_bounds__(kGridBatch)
             C x = vis[it.begin + base + k];
             const R h = tap_parity(it, g, lu, lv) ? (R)-0.5 : (R)0.5;
             x = P::scale(h, x);
-            R *wrow = swt + k * STR;
+            R *row = rows + k * STR;
 #pragma unroll
-            for (int i = 0; i < W2; ++i) wrow[i] = wu[i];
+            for (int j = 0; j < W2; ++j) row[j] = wv[j];
 #pragma unroll
-            for (int j = 0; j < W2; ++j) wrow[W2 + j] = wv[j];
-            sx[k] = x;
-            skey[k] = (lu << 6) | lv;
-            if ((c.x | c.y) & kExtraTapBit)
-                grid_extra_taps<W2, R>(sm, S, lu, lv, c, wu, wv, (R)kb.edge, x);
+            for (int i = 0; i < W2; ++i) row[W2 + i] = wu[i];
+            row[2 * W2] = x.x;
+            row[2 * W2 + 1] = x.y;
+            row[2 * W2 + 2] = key_as<R>((lu << 6) | lv);
+            if ((c.x | c.y) & kExtraTapBit)  // rare: straight into this warp's tile, atomically
+                grid_extra_taps<W2, R>(mytile, S, lu, lv, c, wu, wv, (R)kb.edge, x);
         }
         __syncthreads();
-        const int k0 = warp * 32, k1 = min(n, k0 + 32);
+        constexpr int share = 32 / V;
+        const int k0 = warp * 32 + sub * share;
+        const int k1 = min(n, k0 + share);
         C acc[PER];
 #pragma unroll
         for (int r = 0; r < PER; ++r) acc[r] = P::zero();
         int cur = -1;
-        for (int k = k0; k < k1; ++k) {
-            const int key = skey[k];
-            if (key != cur) {
-                if (cur >= 0 && active) {
-                    C *p = sm + ((cur >> 6) + 1 + ti) * S + (cur & 63) + 1 + tj;
-#pragma unroll
-                    for (int r = 0; r < PER; ++r) {
-                        atomicAdd(&p[r].x, acc[r].x);
-                        atomicAdd(&p[r].y, acc[r].y);
-                        acc[r] = P::zero();
-                    }
-                }
-                cur = key;
-            }
-            const R *wrow = swt + k * STR;
-            const C t = P::scale(wrow[ti], sx[k]);
-#pragma unroll
-            for (int r = 0; r < PER; ++r) acc[r] = P::fma(wrow[W2 + tj + r], t, acc[r]);
-        }
-        if (cur >= 0 && active) {
-            C *p = sm + ((cur >> 6) + 1 + ti) * S + (cur & 63) + 1 + tj;
+        auto flush = [&](int key) {
+            C *p = mytile + ((key >> 6) + 1 + ti) * S + (key & 63) + 1 + tj;
 #pragma unroll
             for (int r = 0; r < PER; ++r) {
-                atomicAdd(&p[r].x, acc[r].x);
-                atomicAdd(&p[r].y, acc[r].y);
+                if (PRIV) {
+                    C v = p[r];
+                    v.x += acc[r].x;
+                    v.y += acc[r].y;
+                    p[r] = v;
+                } else {
+                    atomicAdd(&p[r].x, acc[r].x);
+                    atomicAdd(&p[r].y, acc[r].y);
+                }
+                acc[r] = P::zero();
             }
+        };
+        for (int k = k0; k < k1; ++k) {
+            const R *row = rows + k * STR;
+            const int key = key_of<R>(row[2 * W2 + 2]);
+            if (key != cur) {
+                if (cur >= 0 && active) flush(cur);
+                cur = key;
+            }
+            C x;
+            x.x = row[2 * W2];
+            x.y = row[2 * W2 + 1];
+            const C t = P::scale(row[W2 + ti], x);
+#pragma unroll
+            for (int r = 0; r < PER; ++r) acc[r] = P::fma(row[tj + r], t, acc[r]);
         }
+        if (cur >= 0 && active) flush(cur);
     }
     __syncthreads();
-    grid_flush_extended<W2, R>(sm, grid, it, g);
+    if (PRIV) {  // sum the warps' copies into copy 0
+        for (int e = threadIdx.x; e < E * S; e += blockDim.x) {
+            C a = tiles[e];
+#pragma unroll
+            for (int q = 1; q < NW; ++q) {
+                const C b = tiles[q * E * S + e];
+                a.x += b.x;
+                a.y += b.y;
+            }
+            tiles[e] = a;
+        }
+        __syncthreads();
+    }
+    grid_flush_extended<W2, R>(tiles, grid, it, g);
 }
 
 template <typename K>
@@ -377,21 +437,200 @@ static int launch_degrid_t(const lentils_plan *p, const typename Prec<R>::C *gri
     return LENTILS_OK;
 }
 
+// Row-owner gridding (the default for float). The work item's sorted visibilities are split
+// into NG = 8 warps x G contiguous ranges, one per group of 2w lanes (G = 32/(2w) groups per
+// warp). Each batch gathers the next SHARE visibilities of every range (SHARE * NG <= 256, one
+// per thread), evaluates their weights into 80-byte shared rows [wv | wu | x, key], and the
+// groups consume them: lane i of a group owns row i of the 2w x 2w window and accumulates its
+// 2w taps in registers -- across batches -- while its range stays in one cell. So a dense
+// cell costs one flush per range, not one per batch. Every warp flushes into its own copy of
+// the extended tile with plain load-add-store, its groups taking turns (warp vote, then one
+// group at a time between __syncwarp), so no two lanes update a cell at once; the copies are
+// summed once per work item before the global flush.
+template <int W2>
+__global__ void __launch_bounds__(kGridBatch)
+    grid_rows_kernel(const float2 *__restrict__ vis, const uint2 *__restrict__ coords,
+                     float2 *__restrict__ grid, const WorkItem *__restrict__ items,
+                     const __grid_constant__ KBPoly kb, const GridGeom g)
+{
+    constexpr int STR = 2 * W2 + 4;                  // floats per row (16-byte multiple)
+    constexpr int G = 32 / W2;                        // visibility groups per warp
+    constexpr int NW = kGridBatch / 32;
+    constexpr int NG = NW * G;                        // groups per CTA
+    constexpr int SHARE = kGridBatch / NG;            // visibilities per group and batch
+    static_assert((STR % 4) == 0, "rows must stay 16-byte aligned");
+    extern __shared__ __align__(16) unsigned char smraw[];
+    const WorkItem it = items[blockIdx.x];
+    const int E = g.E, S = g.stride;
+    float2 *tiles = reinterpret_cast<float2 *>(smraw);  // NW x (E x S)
+    const size_t tile_bytes = ((sizeof(float2) * (size_t)NW * E * S) + 15) & ~size_t(15);
+    float *rows = reinterpret_cast<float *>(smraw + tile_bytes);  // NG*SHARE x STR
+    for (int e = threadIdx.x; e < NW * E * S; e += blockDim.x) tiles[e] = make_float2(0.f, 0.f);
+
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    float2 *mytile = tiles + warp * E * S;
+    const int grp = lane / W2, ri = lane - grp * W2;
+    const bool lane_on = grp < G;
+    const int gid = warp * G + (lane_on ? grp : 0);   // this lane's range
+    const int L = (it.count + NG - 1) / NG;           // range length
+    const int rbeg = min(it.count, gid * L), rend = min(it.count, rbeg + L);
+    // producer role: thread t fills row t for range t / SHARE
+    const int pg = threadIdx.x / SHARE, pj = threadIdx.x - pg * SHARE;
+    const int pbeg = min(it.count, pg * L), pend = min(it.count, pbeg + L);
+
+    float2 acc[W2];
+#pragma unroll
+    for (int j = 0; j < W2; ++j) acc[j] = make_float2(0.f, 0.f);
+    int cur = -1;
+    const int nbatch = (L + SHARE - 1) / SHARE;
+    for (int b = 0; b <= nbatch; ++b) {
+        __syncthreads();  // tiles zeroed / previous batch consumed
+        if (b < nbatch && pg < NG) {
+            const int kv = pbeg + b * SHARE + pj;
+            if (kv < pend) {
+                const uint2 c = coords[it.begin + kv];
+                const int lu = cell_of(c.x), lv = cell_of(c.y);
+                float wu[W2], wv[W2];
+                kb_weights<W2>(kb, c.x, wu);
+                kb_weights<W2>(kb, c.y, wv);
+                float2 x = vis[it.begin + kv];
+                const float h = tap_parity(it, g, lu, lv) ? -0.5f : 0.5f;
+                x = make_float2(h * x.x, h * x.y);
+                float *row = rows + threadIdx.x * STR;
+                float4 *row4 = reinterpret_cast<float4 *>(row);
+#pragma unroll
+                for (int q = 0; q < W2 / 4; ++q)
+                    row4[q] = make_float4(wv[4 * q], wv[4 * q + 1], wv[4 * q + 2], wv[4 * q + 3]);
+#pragma unroll
+                for (int j = (W2 / 4) * 4; j < W2; ++j) row[j] = wv[j];
+#pragma unroll
+                for (int i = 0; i < W2; ++i) row[W2 + i] = wu[i];
+                reinterpret_cast<float4 *>(row + 2 * W2)[0] =
+                    make_float4(x.x, x.y, __int_as_float((lu << 6) | lv), 0.f);
+                if ((c.x | c.y) & kExtraTapBit)  // rare: straight into a tile, atomically
+                    grid_extra_taps<W2, float>(tiles + warp * E * S, S, lu, lv, c, wu, wv,
+                                               kb.edge, x);
+            }
+        }
+        __syncthreads();
+        // consume this batch's rows of my range; after the last batch flush what is left
+        const int kfirst = rbeg + b * SHARE;
+        for (int step = 0; step < SHARE; ++step) {
+            const int k = kfirst + step;
+            const bool valid = lane_on && b < nbatch && k < rend;
+            float4 xk = make_float4(0.f, 0.f, 0.f, 0.f);
+            int key = cur;
+            const float *row = rows + (gid * SHARE + step) * STR;
+            if (valid) {
+                xk = reinterpret_cast<const float4 *>(row + 2 * W2)[0];
+                key = __float_as_int(xk.z);
+            }
+            const bool need = lane_on && cur >= 0 && (b == nbatch || key != cur);
+            if (__any_sync(0xffffffffu, need)) {
+                for (int hgrp = 0; hgrp < G; ++hgrp) {
+                    if (need && grp == hgrp) {
+                        float2 *p = mytile + ((cur >> 6) + 1 + ri) * S + (cur & 63) + 1;
+#pragma unroll
+                        for (int j = 0; j < W2; ++j) {
+                            float2 v = p[j];
+                            v.x += acc[j].x;
+                            v.y += acc[j].y;
+                            p[j] = v;
+                            acc[j] = make_float2(0.f, 0.f);
+                        }
+                    }
+                    __syncwarp();
+                }
+                if (need) cur = -1;
+            }
+            if (!valid) continue;
+            cur = key;
+            const float wui = row[W2 + ri];
+            const float2 t = make_float2(wui * xk.x, wui * xk.y);
+            float wv[W2];
+#pragma unroll
+            for (int q = 0; q < W2 / 4; ++q) {
+                const float4 v4 = reinterpret_cast<const float4 *>(row)[q];
+                wv[4 * q] = v4.x;
+                wv[4 * q + 1] = v4.y;
+                wv[4 * q + 2] = v4.z;
+                wv[4 * q + 3] = v4.w;
+            }
+#pragma unroll
+            for (int j = (W2 / 4) * 4; j < W2; ++j) wv[j] = row[j];
+#pragma unroll
+            for (int j = 0; j < W2; ++j) acc[j] = __ffma2_rn(f2(wv[j]), t, acc[j]);
+        }
+    }
+    __syncthreads();
+    for (int e = threadIdx.x; e < E * S; e += blockDim.x) {  // sum the warps' copies
+        float2 a = tiles[e];
+#pragma unroll
+        for (int q = 1; q < NW; ++q) {
+            const float2 bq = tiles[q * E * S + e];
+            a.x += bq.x;
+            a.y += bq.y;
+        }
+        tiles[e] = a;
+    }
+    __syncthreads();
+    grid_flush_extended<W2, float>(tiles, grid, it, g);
+}
+
+constexpr size_t kMaxGridSmem = 200 * 1024;
+
+template <int W2, int V, bool PRIV, typename R>
+static size_t grid_smem_bytes(const GridGeom &g)
+{
+    using C = typename Prec<R>::C;
+    const size_t ntile = PRIV ? kGridBatch / 32 : 1;
+    const size_t tile_bytes = ((sizeof(C) * ntile * g.E * g.stride) + 15) & ~size_t(15);
+    return tile_bytes + sizeof(R) * (size_t)kGridBatch * GridShape<W2, V, R>::STR;
+}
+
+template <int W2, int V, typename R>
+static int launch_grid_tv(const lentils_plan *p, const typename Prec<R>::C *vis,
+                          typename Prec<R>::C *grid, cudaStream_t s)
+{
+    const GridGeom &g = p->geom;
+    const float2 *cres = std::is_same<R, double>::value ? p->coords_res : nullptr;
+    constexpr bool kPriv = (V == 1);
+    const size_t smem_priv = grid_smem_bytes<W2, V, kPriv, R>(g);
+    if (kPriv && smem_priv <= kMaxGridSmem) {
+        if (int st = set_smem(grid_kernel<W2, V, kPriv, R>, smem_priv)) return st;
+        grid_kernel<W2, V, kPriv, R><<<p->nitems, kGridBatch, smem_priv, s>>>(
+            vis, p->coords, grid, p->items, table_of<R>(p), g, cres);
+    } else {
+        const size_t smem = grid_smem_bytes<W2, V, false, R>(g);
+        if (int st = set_smem(grid_kernel<W2, V, false, R>, smem)) return st;
+        grid_kernel<W2, V, false, R><<<p->nitems, kGridBatch, smem, s>>>(
+            vis, p->coords, grid, p->items, table_of<R>(p), g, cres);
+    }
+    LENTILS_CHECK_LAUNCH("grid_kernel");
+    return LENTILS_OK;
+}
+
 template <int W2, typename R>
 static int launch_grid_t(const lentils_plan *p, const typename Prec<R>::C *vis,
                          typename Prec<R>::C *grid, cudaStream_t s)
 {
-    using C = typename Prec<R>::C;
-    const GridGeom &g = p->geom;
-    const size_t tile_bytes = ((sizeof(C) * (size_t)g.E * g.stride) + 15) & ~size_t(15);
-    const size_t smem = tile_bytes + (sizeof(C) + sizeof(int)) * kGridBatch +
-                        sizeof(R) * (size_t)kGridBatch * LaneTaps<W2>::STR;
-    if (int st = set_smem(grid_kernel<W2, R>, smem)) return st;
-    const float2 *cres = std::is_same<R, double>::value ? p->coords_res : nullptr;
-    grid_kernel<W2, R><<<p->nitems, kGridBatch, smem, s>>>(vis, p->coords, grid, p->items,
-                                                          table_of<R>(p), g, cres);
-    LENTILS_CHECK_LAUNCH("grid_kernel");
-    return LENTILS_OK;
+    if constexpr (std::is_same<R, float>::value && (W2 % 2) == 0) {
+        if (p->grid_variant == 0) {
+            const GridGeom &g = p->geom;
+            const size_t tile_bytes =
+                ((sizeof(float2) * (size_t)(kGridBatch / 32) * g.E * g.stride) + 15) & ~size_t(15);
+            const size_t smem = tile_bytes + sizeof(float) * (size_t)kGridBatch * (2 * W2 + 4);
+            if (smem <= kMaxGridSmem) {
+                if (int st = set_smem(grid_rows_kernel<W2>, smem)) return st;
+                grid_rows_kernel<W2><<<p->nitems, kGridBatch, smem, s>>>(
+                    vis, p->coords, grid, p->items, p->kb, g);
+                LENTILS_CHECK_LAUNCH("grid_rows_kernel");
+                return LENTILS_OK;
+            }
+        }
+    }
+    if (p->grid_variant == 2) return launch_grid_tv<W2, 2, R>(p, vis, grid, s);
+    return launch_grid_tv<W2, 1, R>(p, vis, grid, s);
 }
 
 template <typename R>

@@ -186,7 +186,7 @@ int lentils_grid_noalloc(const lentils_grid_desc *gd, const double *uvw, int nro
     memset(&p, 0, sizeof(p));
     p.desc = *gd;
     int T = gd->tile;
-    if (T == 0) T = (std::max(gd->nu, gd->nv) >= 512) ? 32 : 16;
+    if (T == 0) T = 16;
     int logT = 0;
     while ((1 << logT) < T) ++logT;
     if ((1 << logT) != T || logT < 3 || logT > 6)
@@ -260,6 +260,7 @@ int lentils_grid_noalloc(const lentils_grid_desc *gd, const double *uvw, int nro
     noalloc_items_kernel<<<1, 1024, 0, s>>>(tile_counts, ntiles, g.ntv, kNoAllocChunk, items,
                                             max_items);
     LENTILS_CHECK_LAUNCH("noalloc_items_kernel");
+    p.grid_variant = 1;
     p.coords = coords_plan;
     p.items = items;
     p.nitems = max_items;

@@ -490,7 +490,7 @@ int lentils_plan_create(lentils_plan **out, const lentils_grid_desc *gd, const d
     p->desc = *gd;
     cudaGetDevice(&p->device);
     int T = gd->tile;
-    if (T == 0) T = (std::max(gd->nu, gd->nv) >= 512) ? 32 : 16;
+    if (T == 0) T = 16;  // measured best for both kernels (degrid and the row-owner gridder)
     const int logT = ilog2_exact(T);
     if (logT < 3 || logT > 6) {
         delete p;
@@ -524,6 +524,7 @@ int lentils_plan_create(lentils_plan **out, const lentils_grid_desc *gd, const d
     p->nrows = nrows;
     p->nchannels = nchannels;
     p->has_phase = (gd->gcx != 0.0 || gd->gcy != 0.0) ? 1 : 0;
+    p->grid_variant = 0;
     kb_poly_build(g.w, gd->kb_beta, &p->kb, nullptr, &p->kb64);
 
     int st = LENTILS_OK;
@@ -547,6 +548,15 @@ int lentils_plan_destroy(lentils_plan *p)
     if (!p) return LENTILS_OK;
     free_plan_arrays(p);
     delete p;
+    return LENTILS_OK;
+}
+
+int lentils_plan_set_grid_variant(lentils_plan *p, int variant)
+{
+    clear_error();
+    if (!p || variant < 0 || variant > 2)
+        return set_error(LENTILS_ERR_INVALID, "plan_set_grid_variant: variant 0, 1 or 2");
+    p->grid_variant = variant;
     return LENTILS_OK;
 }
 

@@ -73,7 +73,8 @@ void kb_poly_build(int w, double beta, KBPoly *out, double *fit_err, KBPoly64 *o
     const double norm = 1.0 / (2.0 * w);
     double worst = 0.0;
     const double peak = kb_profile(0.0, w, beta) * norm;
-    for (int i = 0; i < 2 * w; ++i) {
+    double mono_all[kMaxTaps][kPolyCoef];
+    for (int i = 0; i < w; ++i) {
         const double sgn = (i & 1) ? -1.0 : 1.0;
         double fval[kPolyCoef];
         for (int j = 0; j < n; ++j) {
@@ -105,18 +106,33 @@ void kb_poly_build(int w, double beta, KBPoly *out, double *fit_err, KBPoly64 *o
                 tk[d] = tkp1[d];
             }
         }
-        // store highest degree first, paired across taps
-        for (int k = 0; k < n; ++k) {
-            const float c = (float)mono[n - 1 - k];
-            if (i & 1) out->cp[k][i >> 1].y = c;
-            else out->cp[k][i >> 1].x = c;
-            if (out64) out64->cd[k][i] = mono[n - 1 - k];
+        for (int d = 0; d < n; ++d) {
+            mono_all[i][d] = mono[d];
+            // reflected tap 2w-1-i: P(t) = -P_i(-t)
+            mono_all[2 * w - 1 - i][d] = ((d & 1) ? 1.0 : -1.0) * mono[d];
         }
+        // FP32 even/odd table (highest power of t^2 first)
+        for (int k = 0; k < kHalfCoef; ++k) {
+            const float e = (float)mono[2 * (kHalfCoef - 1 - k)];
+            const float o = (float)mono[2 * (kHalfCoef - 1 - k) + 1];
+            if (i & 1) {
+                out->ce[k][i >> 1].y = e;
+                out->co[k][i >> 1].y = o;
+            } else {
+                out->ce[k][i >> 1].x = e;
+                out->co[k][i >> 1].x = o;
+            }
+        }
+    }
+    for (int i = 0; i < 2 * w; ++i) {
+        const double sgn = (i & 1) ? -1.0 : 1.0;
+        if (out64)
+            for (int k = 0; k < n; ++k) out64->cd[k][i] = mono_all[i][n - 1 - k];
         if (fit_err) {
             for (int s = 0; s <= 400; ++s) {
                 const double t = -1.0 + s / 200.0;
                 double acc = 0.0;
-                for (int d = n - 1; d >= 0; --d) acc = acc * t + mono[d];
+                for (int d = n - 1; d >= 0; --d) acc = acc * t + mono_all[i][d];
                 const double ref = sgn * norm * kb_profile(0.5 * (t + 1.0) + w - 1 - i, w, beta);
                 const double e = fabs(acc - ref) / peak;
                 if (e > worst) worst = e;
@@ -127,6 +143,25 @@ void kb_poly_build(int w, double beta, KBPoly *out, double *fit_err, KBPoly64 *o
     out->edge = (float)(-norm * kb_profile((double)w, w, beta));
     if (out64) out64->edge = -norm * kb_profile((double)w, w, beta);
     if (fit_err) *fit_err = worst;
+}
+
+// Full per-tap monomial table (highest degree first) reconstructed from the FP32 even/odd
+// table, as the kernels evaluate it.
+void kb_poly_taps(const KBPoly &p, int w, float *coef /* 2w x kPolyCoef */)
+{
+    for (int i = 0; i < w; ++i) {
+        float mono[kPolyCoef];
+        for (int k = 0; k < kHalfCoef; ++k) {
+            const float e = (i & 1) ? p.ce[k][i >> 1].y : p.ce[k][i >> 1].x;
+            const float o = (i & 1) ? p.co[k][i >> 1].y : p.co[k][i >> 1].x;
+            mono[2 * (kHalfCoef - 1 - k)] = e;
+            mono[2 * (kHalfCoef - 1 - k) + 1] = o;
+        }
+        for (int d = 0; d < kPolyCoef; ++d) {
+            coef[i * kPolyCoef + (kPolyCoef - 1 - d)] = mono[d];
+            coef[(2 * w - 1 - i) * kPolyCoef + (kPolyCoef - 1 - d)] = ((d & 1) ? 1.f : -1.f) * mono[d];
+        }
+    }
 }
 
 }  // namespace lentils
@@ -149,9 +184,7 @@ int lentils_kb_poly_table(int w, double beta, float *coef, int ncoef_capacity, d
         return lentils::set_error(LENTILS_ERR_INVALID, "kb_poly_table: capacity too small");
     lentils::KBPoly p;
     lentils::kb_poly_build(w, beta, &p, fit_err);
-    for (int i = 0; i < 2 * w; ++i)
-        for (int k = 0; k < lentils::kPolyCoef; ++k)
-            coef[i * lentils::kPolyCoef + k] = (i & 1) ? p.cp[k][i >> 1].y : p.cp[k][i >> 1].x;
+    lentils::kb_poly_taps(p, w, coef);
     return LENTILS_OK;
 }
 

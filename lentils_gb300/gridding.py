@@ -82,6 +82,10 @@ class GriddingPlan:
     def handle(self):
         return self._handle
 
+    def set_grid_variant(self, variant):
+        """Visibilities per warp iteration in the gridding kernel (1 or 2); tuning only."""
+        N.check(N.lib().lentils_plan_set_grid_variant(self._handle, int(variant)))
+
     @property
     def stats(self):
         s = N.PlanStatsC()
