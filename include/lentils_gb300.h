@@ -333,6 +333,16 @@ int lentils_prior_gradient_apply64(const double *s, double *out, int nx, int ny,
 int lentils_dot64(const double *a, const double *b, int n, double *out, void *stream);
 
 /* ------------------------------------------------------------------------------------------
+ * BF16 tensor-core GEMM (tcgen05, FP32 accumulation in tensor memory): C = A * B^T with A
+ * (M x K) and B (N x K) row-major BF16 and C (M x N) row-major FP32, all device pointers; N in
+ * {32, 64, 128, 256}, K a multiple of 8. The core of the learned preconditioner's kernels,
+ * exposed for testing. swap_lbo_sbo = 0. *err_dev (device int) is set to 1 if a bounded
+ * wait on the tensor core gave up (the result is then invalid).
+ * ---------------------------------------------------------------------------------------- */
+int lentils_tc_gemm_bf16(const void *A, const void *B, float *C, int M, int N, int K,
+                         int swap_lbo_sbo, int *err_dev, void *stream);
+
+/* ------------------------------------------------------------------------------------------
  * Gridding without device allocation. No counterpart in the reference: it exists for callers
  * that cannot call cudaMalloc -- code running where allocation is forbidden or impossible
  * (host callbacks and stream-ordered sections that must not synchronise, a memory budget that

@@ -133,6 +133,8 @@ _SIGNATURES = [
     ("lentils_prior_gradient_apply64", c_int, [c_void_p, c_void_p, c_int, c_int, c_double,
                                                c_double, c_double, c_void_p]),
     ("lentils_dot64", c_int, [c_void_p, c_void_p, c_int, POINTER(c_double), c_void_p]),
+    ("lentils_tc_gemm_bf16", c_int, [c_void_p, c_void_p, c_void_p, c_int, c_int, c_int, c_int,
+                                     c_void_p, c_void_p]),
     ("lentils_grid_noalloc", c_int, [POINTER(GridDescC), c_void_p, c_int, c_void_p, c_int,
                                      c_void_p, c_void_p, c_void_p]),
     ("lentils_noalloc_max_vis", c_int, []),
