@@ -343,6 +343,55 @@ int lentils_tc_gemm_bf16(const void *A, const void *B, float *C, int M, int N, i
                          int swap_lbo_sbo, int *err_dev, void *stream);
 
 /* ------------------------------------------------------------------------------------------
+ * Learned preconditioner (no counterpart in the reference): a 4-level convolutional U-Net on the
+ * source grid, BF16 activations and weights on the tensor cores (tcgen05) with FP32
+ * accumulation, trained on the GPU by its own forward and backward kernels.
+ *
+ * Parameters are one flat FP32 vector of lentils_unet_param_count() values: for each of the 8
+ * convolutions in order (3x3 2->32, 3x3 32->64, 3x3 64->128, 3x3 128->128, 1x1 128->64,
+ * 3x3 64->32, 3x3 32->32, 1x1 32->1) the weights [cout][kh*3+kw or 0][cin] then the biases
+ * [cout]. Input channels: (scaled residual, diagonal feature), each an (B, H, W) FP32 device
+ * array, H and W multiples of 8; output (B, H, W) FP32.
+ *
+ * Preconditioner form (lentils_unet_precondition, lentils_fcg_solve):
+ *   u = dinv * r,  s = rms(u),  f = log(dinv) - mean(log(dinv))
+ *   z = u + s * net(u / s, f)
+ * so the network learns the correction over Jacobi in units of the scaled residual.
+ * ---------------------------------------------------------------------------------------- */
+typedef struct lentils_unet lentils_unet;
+long long lentils_unet_param_count(void);
+int lentils_unet_create(lentils_unet **out, int H, int W, int max_batch, const float *init_params,
+                        void *stream);
+int lentils_unet_destroy(lentils_unet *net);
+int lentils_unet_get_params(lentils_unet *net, float *host_out);
+int lentils_unet_set_params(lentils_unet *net, const float *host_in, void *stream);
+int lentils_unet_forward(lentils_unet *net, const float *r, const float *d, float *out, int B,
+                         void *stream);
+/* forward + backward of the mean squared error against tgt; flat gradient and loss to HOST
+ * memory (either may be NULL); synchronises the stream */
+int lentils_unet_gradients(lentils_unet *net, const float *r, const float *d, const float *tgt,
+                           int B, float *grad_host, float *loss_host, void *stream);
+/* one Adam step (beta1 0.9, beta2 0.999, eps 1e-8) on the mean squared error; loss_dev
+ * (device float, may be NULL) receives the batch loss before the step; no synchronisation */
+int lentils_unet_train_step(lentils_unet *net, const float *r, const float *d, const float *tgt,
+                            int B, float lr, float *loss_dev, void *stream);
+/* 1 if a bounded tensor-core wait gave up since creation (results then invalid) */
+int lentils_unet_error_flag(lentils_unet *net, int *flag);
+/* f = log(dinv) - mean(log(dinv)) over n values (device) */
+int lentils_unet_features(const float *dinv, float *feat, int n, void *stream);
+/* z = M(r) for one H x W residual (device FP32), the preconditioner form above */
+int lentils_unet_precondition(lentils_unet *net, const float *r, const float *dinv,
+                              const float *feat, float *z, void *stream);
+/* Flexible CG (one-vector orthogonalisation, beta = -(z . A p) / (p . A p)) on the normal
+ * equations with the learned preconditioner inside the same FP64 iterative refinement as
+ * lentils_cg_solve. Where the network's direction is not a descent direction (z . r <= 0)
+ * that iteration uses the Jacobi direction instead; net = NULL runs the same iteration with
+ * Jacobi only. */
+int lentils_fcg_solve(lentils_normal_op *op, const double *b, double *x, const float *inv_diag32,
+                      lentils_unet *net, const lentils_cg_options *opt, lentils_cg_result *res,
+                      void *stream);
+
+/* ------------------------------------------------------------------------------------------
  * Gridding without device allocation. No counterpart in the reference: it exists for callers
  * that cannot call cudaMalloc -- code running where allocation is forbidden or impossible
  * (host callbacks and stream-ordered sections that must not synchronise, a memory budget that

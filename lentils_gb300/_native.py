@@ -135,6 +135,22 @@ _SIGNATURES = [
     ("lentils_dot64", c_int, [c_void_p, c_void_p, c_int, POINTER(c_double), c_void_p]),
     ("lentils_tc_gemm_bf16", c_int, [c_void_p, c_void_p, c_void_p, c_int, c_int, c_int, c_int,
                                      c_void_p, c_void_p]),
+    ("lentils_unet_param_count", c_longlong, []),
+    ("lentils_unet_create", c_int, [POINTER(c_void_p), c_int, c_int, c_int, c_void_p, c_void_p]),
+    ("lentils_unet_destroy", c_int, [c_void_p]),
+    ("lentils_unet_get_params", c_int, [c_void_p, c_void_p]),
+    ("lentils_unet_set_params", c_int, [c_void_p, c_void_p, c_void_p]),
+    ("lentils_unet_forward", c_int, [c_void_p, c_void_p, c_void_p, c_void_p, c_int, c_void_p]),
+    ("lentils_unet_gradients", c_int, [c_void_p, c_void_p, c_void_p, c_void_p, c_int, c_void_p,
+                                       c_void_p, c_void_p]),
+    ("lentils_unet_train_step", c_int, [c_void_p, c_void_p, c_void_p, c_void_p, c_int, c_float,
+                                        c_void_p, c_void_p]),
+    ("lentils_unet_error_flag", c_int, [c_void_p, POINTER(c_int)]),
+    ("lentils_unet_features", c_int, [c_void_p, c_void_p, c_int, c_void_p]),
+    ("lentils_unet_precondition", c_int, [c_void_p, c_void_p, c_void_p, c_void_p, c_void_p,
+                                          c_void_p]),
+    ("lentils_fcg_solve", c_int, [c_void_p, c_void_p, c_void_p, c_void_p, c_void_p,
+                                  POINTER(CGOptionsC), POINTER(CGResultC), c_void_p]),
     ("lentils_grid_noalloc", c_int, [POINTER(GridDescC), c_void_p, c_int, c_void_p, c_int,
                                      c_void_p, c_void_p, c_void_p]),
     ("lentils_noalloc_max_vis", c_int, []),

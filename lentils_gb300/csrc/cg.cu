@@ -25,6 +25,7 @@
 #include <vector>
 
 #include "common.cuh"
+#include "unet.cuh"
 
 struct lentils_normal_op {
     lentils_lensop *L;
@@ -264,6 +265,160 @@ __global__ void jacobi_kernel(const double *__restrict__ dltl, double wsum, doub
         if (inv) inv[e] = v;
         if (inv32) inv32[e] = (float)v;
     }
+}
+
+// -- flexible CG (learned preconditioner) --------------------------------------------------------
+struct FCGScalars {
+    double pap, pr, alpha, beta, rr, rr0, use_net, fallbacks;
+};
+
+// partials of p.ap and p.r
+__global__ void __launch_bounds__(256)
+    fcg_dot2_kernel(const float *__restrict__ p, const float *__restrict__ ap,
+                    const float *__restrict__ r, int n, double *__restrict__ partial)
+{
+    __shared__ double sh[8];
+    double a = 0.0, b = 0.0;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        a += (double)p[i] * (double)ap[i];
+        b += (double)p[i] * (double)r[i];
+    }
+    const double ta = block_sum(a, sh);
+    const double tb = block_sum(b, sh);
+    if (threadIdx.x == 0) {
+        partial[blockIdx.x] = ta;
+        partial[gridDim.x + blockIdx.x] = tb;
+    }
+}
+
+__global__ void fcg_alpha_kernel(const double *__restrict__ partial, int np, FCGScalars *sc)
+{
+    __shared__ double sh[8];
+    double a = 0.0, b = 0.0;
+    for (int i = threadIdx.x; i < np; i += blockDim.x) {
+        a += partial[i];
+        b += partial[np + i];
+    }
+    const double ta = block_sum(a, sh);
+    const double tb = block_sum(b, sh);
+    if (threadIdx.x == 0) {
+        sc->pap = ta;
+        sc->pr = tb;
+        sc->alpha = (ta != 0.0) ? tb / ta : 0.0;
+    }
+}
+
+// e += alpha p; r -= alpha ap; partials of r.r
+__global__ void __launch_bounds__(256)
+    fcg_update_kernel(float *__restrict__ e, float *__restrict__ r, const float *__restrict__ p,
+                      const float *__restrict__ ap, const FCGScalars *__restrict__ sc, int n,
+                      double *__restrict__ partial)
+{
+    __shared__ double sh[8];
+    const float alpha = (float)sc->alpha;
+    double rr = 0.0;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        e[i] = fmaf(alpha, p[i], e[i]);
+        const float ri = fmaf(-alpha, ap[i], r[i]);
+        r[i] = ri;
+        rr += (double)ri * (double)ri;
+    }
+    const double t = block_sum(rr, sh);
+    if (threadIdx.x == 0) partial[blockIdx.x] = t;
+}
+
+__global__ void fcg_rr_kernel(const double *__restrict__ partial, int np, FCGScalars *sc, int start)
+{
+    __shared__ double sh[8];
+    double a = 0.0;
+    for (int i = threadIdx.x; i < np; i += blockDim.x) a += partial[i];
+    const double t = block_sum(a, sh);
+    if (threadIdx.x == 0) {
+        sc->rr = t;
+        if (start) sc->rr0 = t;
+    }
+}
+
+// partials of z.ap, z.r and j.ap, with j = dinv r the Jacobi direction (z null: Jacobi only)
+__global__ void __launch_bounds__(256)
+    fcg_beta_dots_kernel(const float *__restrict__ z, const float *__restrict__ r,
+                         const float *__restrict__ ap, const float *__restrict__ dinv, int n,
+                         double *__restrict__ partial)
+{
+    __shared__ double sh[8];
+    double zap = 0.0, zr = 0.0, jap = 0.0;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const double j = (double)dinv[i] * (double)r[i];
+        const double zi = z ? (double)z[i] : j;
+        zap += zi * (double)ap[i];
+        zr += zi * (double)r[i];
+        jap += j * (double)ap[i];
+    }
+    const double a = block_sum(zap, sh);
+    const double b = block_sum(zr, sh);
+    const double c = block_sum(jap, sh);
+    if (threadIdx.x == 0) {
+        partial[blockIdx.x] = a;
+        partial[gridDim.x + blockIdx.x] = b;
+        partial[2 * gridDim.x + blockIdx.x] = c;
+    }
+}
+
+// beta = -(dir . ap) / (p . ap), dir = the network's z where it is a descent direction
+// (z . r > 0), else the Jacobi direction
+__global__ void fcg_beta_kernel(const double *__restrict__ partial, int np, FCGScalars *sc,
+                                int have_net)
+{
+    __shared__ double sh[8];
+    double a = 0.0, b = 0.0, c = 0.0;
+    for (int i = threadIdx.x; i < np; i += blockDim.x) {
+        a += partial[i];
+        b += partial[np + i];
+        c += partial[2 * np + i];
+    }
+    const double zap = block_sum(a, sh);
+    const double zr = block_sum(b, sh);
+    const double jap = block_sum(c, sh);
+    if (threadIdx.x == 0) {
+        const bool net_ok = have_net && zr > 0.0 && zap == zap;
+        sc->use_net = net_ok ? 1.0 : 0.0;
+        if (have_net && !net_ok) sc->fallbacks += 1.0;
+        const double num = net_ok ? zap : jap;
+        sc->beta = (sc->pap != 0.0) ? -num / sc->pap : 0.0;
+    }
+}
+
+// p = dir + beta p
+__global__ void fcg_p_kernel(float *__restrict__ p, const float *__restrict__ z,
+                             const float *__restrict__ r, const float *__restrict__ dinv,
+                             const FCGScalars *__restrict__ sc, int n)
+{
+    const float beta = (float)sc->beta;
+    const bool net = z && sc->use_net != 0.0;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const float d = net ? z[i] : dinv[i] * r[i];
+        p[i] = fmaf(beta, p[i], d);
+    }
+}
+
+// start of an inner solve: r32 = (float) r64, e = p = ap = 0; partials of r.r
+__global__ void __launch_bounds__(256)
+    fcg_start_kernel(const double *__restrict__ r64, float *__restrict__ r, float *__restrict__ e,
+                     float *__restrict__ p, float *__restrict__ ap, int n,
+                     double *__restrict__ partial)
+{
+    __shared__ double sh[8];
+    double rr = 0.0;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const float ri = (float)r64[i];
+        r[i] = ri;
+        e[i] = 0.f;
+        p[i] = 0.f;
+        ap[i] = 0.f;
+        rr += (double)ri * (double)ri;
+    }
+    const double t = block_sum(rr, sh);
+    if (threadIdx.x == 0) partial[blockIdx.x] = t;
 }
 
 static double host_dot64(const double *a, const double *b, int n, double *partial, double *out,
@@ -573,6 +728,163 @@ int lentils_cg_solve(lentils_normal_op *op, const double *b, double *x, const fl
     cudaFree(z32);
     cudaFree(p32);
     cudaFree(ap32);
+    cudaFree(r64);
+    cudaFree(ax64);
+    cudaFree(partial);
+    cudaFree(scal);
+    cudaFree(sc);
+    return st;
+}
+
+// Flexible CG inside the FP64 iterative refinement (see the header for the iteration). With
+// p = ap = 0 at the start of an inner solve, the direction step below yields p = dir.
+int lentils_fcg_solve(lentils_normal_op *op, const double *b, double *x, const float *inv_diag32,
+                      lentils_unet *net, const lentils_cg_options *opt, lentils_cg_result *res,
+                      void *stream)
+{
+    clear_error();
+    if (!op || !b || !x || !inv_diag32 || !opt || !res)
+        return set_error(LENTILS_ERR_INVALID, "fcg_solve: null");
+    if (net && unet_size(net) != op->nsrc)
+        return set_error(LENTILS_ERR_INVALID, "fcg_solve: network grid %d != source grid %d",
+                         unet_size(net), op->nsrc);
+    memset(res, 0, sizeof(*res));
+    cudaStream_t s = (cudaStream_t)stream;
+    const int n = op->nsrc;
+    float *e32 = nullptr, *r32 = nullptr, *z32 = nullptr, *p32 = nullptr, *ap32 = nullptr,
+          *feat = nullptr;
+    double *r64 = nullptr, *ax64 = nullptr, *partial = nullptr, *scal = nullptr;
+    FCGScalars *sc = nullptr;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t gexec = nullptr;
+    int st = LENTILS_OK;
+    cudaError_t e = cudaMalloc(&e32, sizeof(float) * n);
+    if (e == cudaSuccess) e = cudaMalloc(&r32, sizeof(float) * n);
+    if (e == cudaSuccess) e = cudaMalloc(&z32, sizeof(float) * n);
+    if (e == cudaSuccess) e = cudaMalloc(&p32, sizeof(float) * n);
+    if (e == cudaSuccess) e = cudaMalloc(&ap32, sizeof(float) * n);
+    if (e == cudaSuccess) e = cudaMalloc(&feat, sizeof(float) * n);
+    if (e == cudaSuccess) e = cudaMalloc(&r64, sizeof(double) * n);
+    if (e == cudaSuccess) e = cudaMalloc(&ax64, sizeof(double) * n);
+    if (e == cudaSuccess) e = cudaMalloc(&partial, sizeof(double) * 3 * kRedBlocks);
+    if (e == cudaSuccess) e = cudaMalloc(&scal, sizeof(double) * 2);
+    if (e == cudaSuccess) e = cudaMalloc(&sc, sizeof(FCGScalars));
+    if (e == cudaSuccess) e = cudaMemsetAsync(sc, 0, sizeof(FCGScalars), s);
+    if (e != cudaSuccess) st = cuda_status(e, "fcg_solve alloc");
+    if (!st && net) st = lentils_unet_features(inv_diag32, feat, n, stream);
+    if (!st && net) st = unet_prepare(net);
+    float *zdir = net ? z32 : nullptr;
+
+    // direction step: z = M(r); beta; p = dir + beta p
+    auto direction = [&]() -> int {
+        if (net) {
+            if (int q = unet_precondition(net, r32, inv_diag32, feat, z32, s)) return q;
+        }
+        fcg_beta_dots_kernel<<<kRedBlocks, 256, 0, s>>>(zdir, r32, ap32, inv_diag32, n, partial);
+        fcg_beta_kernel<<<1, 256, 0, s>>>(partial, kRedBlocks, sc, net ? 1 : 0);
+        fcg_p_kernel<<<nb(n), 256, 0, s>>>(p32, zdir, r32, inv_diag32, sc, n);
+        cudaError_t le = cudaGetLastError();
+        return le == cudaSuccess ? LENTILS_OK : cuda_status(le, "fcg direction");
+    };
+    auto inner_iteration = [&]() -> int {
+        int q = lentils_normal_op_apply(op, p32, ap32, s);
+        if (q) return q;
+        fcg_dot2_kernel<<<kRedBlocks, 256, 0, s>>>(p32, ap32, r32, n, partial);
+        fcg_alpha_kernel<<<1, 256, 0, s>>>(partial, kRedBlocks, sc);
+        fcg_update_kernel<<<kRedBlocks, 256, 0, s>>>(e32, r32, p32, ap32, sc, n, partial);
+        fcg_rr_kernel<<<1, 256, 0, s>>>(partial, kRedBlocks, sc, 0);
+        return direction();
+    };
+
+    const auto t0 = std::chrono::steady_clock::now();
+    double bnorm = 0.0, rel = 0.0;
+    if (!st) {
+        bnorm = sqrt(host_dot64(b, b, n, partial, scal, s));
+        st = lentils_normal_op_apply64(op, x, ax64, s);
+        if (!st) {
+            sub_kernel<<<nb(n), 256, 0, s>>>(b, ax64, r64, n);
+            rel = (bnorm > 0) ? sqrt(host_dot64(r64, r64, n, partial, scal, s)) / bnorm : 0.0;
+        }
+    }
+    if (!st && opt->use_graph) {
+        e = cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal);
+        if (e == cudaSuccess) {
+            const int q = inner_iteration();
+            cudaError_t ee = cudaStreamEndCapture(s, &graph);
+            if (q) st = q;
+            else if (ee != cudaSuccess) st = cuda_status(ee, "cudaStreamEndCapture");
+        } else {
+            st = cuda_status(e, "cudaStreamBeginCapture");
+        }
+        if (!st) {
+            e = cudaGraphInstantiate(&gexec, graph, 0);
+            if (e != cudaSuccess) st = cuda_status(e, "cudaGraphInstantiate");
+        }
+    }
+    int outer = 0, inner_total = 0;
+    const int check = std::max(1, opt->check_every);
+    while (!st && rel > opt->tol && outer < opt->max_outer) {
+        ++outer;
+        fcg_start_kernel<<<kRedBlocks, 256, 0, s>>>(r64, r32, e32, p32, ap32, n, partial);
+        fcg_rr_kernel<<<1, 256, 0, s>>>(partial, kRedBlocks, sc, 1);
+        if ((st = direction())) break;
+        FCGScalars hs;
+        int k = 0;
+        while (k < opt->max_inner) {
+            for (int c = 0; c < check && k < opt->max_inner; ++c, ++k) {
+                if (gexec) {
+                    e = cudaGraphLaunch(gexec, s);
+                    if (e != cudaSuccess) {
+                        st = cuda_status(e, "cudaGraphLaunch");
+                        break;
+                    }
+                } else if ((st = inner_iteration())) {
+                    break;
+                }
+            }
+            if (st) break;
+            e = cudaMemcpyAsync(&hs, sc, sizeof(FCGScalars), cudaMemcpyDeviceToHost, s);
+            if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+            if (e != cudaSuccess) {
+                st = cuda_status(e, "fcg residual read");
+                break;
+            }
+            if (!(hs.rr == hs.rr)) {
+                st = set_error(LENTILS_ERR_NONFINITE, "fcg_solve: NaN in the inner residual");
+                break;
+            }
+            if (hs.rr <= opt->inner_tol * opt->inner_tol * hs.rr0) break;
+        }
+        inner_total += k;
+        if (st) break;
+        add_f32_to_f64_kernel<<<nb(n), 256, 0, s>>>(x, e32, n);
+        if ((st = lentils_normal_op_apply64(op, x, ax64, s))) break;
+        sub_kernel<<<nb(n), 256, 0, s>>>(b, ax64, r64, n);
+        rel = (bnorm > 0) ? sqrt(host_dot64(r64, r64, n, partial, scal, s)) / bnorm : 0.0;
+    }
+    if (!st) {
+        e = cudaStreamSynchronize(s);
+        if (e != cudaSuccess) st = cuda_status(e, "fcg_solve sync");
+    }
+    if (!st && net) {
+        int flag = 0;
+        st = unet_error_flag_device(net, &flag);
+        if (!st && flag) st = set_error(LENTILS_ERR_TIMEOUT, "fcg_solve: a tensor-core wait gave up");
+    }
+    const auto t1 = std::chrono::steady_clock::now();
+    res->converged = (!st && rel <= opt->tol) ? 1 : 0;
+    res->outer = outer;
+    res->inner_total = inner_total;
+    res->rel_residual = rel;
+    res->seconds = std::chrono::duration<double>(t1 - t0).count();
+    if (gexec) cudaGraphExecDestroy(gexec);
+    if (graph) cudaGraphDestroy(graph);
+    cudaFree(e32);
+    cudaFree(r32);
+    cudaFree(z32);
+    cudaFree(p32);
+    cudaFree(ap32);
+    cudaFree(feat);
     cudaFree(r64);
     cudaFree(ax64);
     cudaFree(partial);

@@ -1,0 +1,958 @@
+// Learned preconditioner for the CG source inversion: a 4-level convolutional U-Net on the
+// source grid, trained and evaluated on the GPU with hand-written BF16 tensor-core kernels
+// (tcgen05, FP32 accumulation in tensor memory) -- no reference counterpart.
+//
+// Network (NHWC BF16 activations, channel counts padded to multiples of 8):
+//   x0  = [residual, diagonal, 0 x 6]                         H   x W   x 8
+//   e1  = relu(conv3x3(x0, 8->32))                            H   x W   x 32
+//   e2  = relu(conv3x3(pool2(e1), 32->64))                    H/2 x W/2 x 64
+//   e3  = relu(conv3x3(pool2(e2), 64->128))                   H/4 x W/4 x 128
+//   b   = relu(conv3x3(pool2(e3), 128->128))                  H/8 x W/8 x 128
+//   c3  = relu(conv1x1(up2(b) + e3, 128->64))                 H/4 x W/4 x 64
+//   c2  = relu(conv3x3(up2(c3) + e2, 64->32))                 H/2 x W/2 x 32
+//   c1  = relu(conv3x3(up2(c2) + e1, 32->32))                 H   x W   x 32
+//   out = conv1x1(c1, 32->1)                                  H   x W   (FP32)
+// (276k parameters; pool2 = 2x2 average, up2 = nearest-neighbour.)
+//
+// Every convolution is an implicit GEMM on the generic tcgen05 kernel (tc_gemm.cuh):
+//   forward        D[pixel][co] = sum_{tap,ci} X[pixel + off(tap)][ci] * W[co][tap][ci]
+//   data gradient  dX[pixel][ci] = sum_{tap,co} dY'[pixel - off(tap)][co] * W[co][tap][ci]
+//   weight grad.   dW[co][tap][ci] = sum_pixel dY'[pixel][co] * X[pixel + off(tap)][ci]
+// with dY' the output gradient masked by the ReLU (Y > 0); im2col is gathered by the operand
+// loaders while staging shared memory. Weight gradients split the pixel reduction over CTAs and
+// accumulate in FP32. Adam keeps FP32 master weights and refreshes the BF16 copies.
+#include <math.h>
+#include <string.h>
+
+#include <algorithm>
+#include <new>
+#include <vector>
+
+#include "common.cuh"
+#include "tc_gemm.cuh"
+#include "unet.cuh"
+
+namespace lentils {
+
+using bf16 = __nv_bfloat16;
+
+struct ConvSpec {
+    int cin, cout;        // real channels
+    int cin_p, cout_p;    // padded channels (multiples of 8; cout_p >= 32)
+    int ks;               // kernel size (3 or 1)
+    int relu;
+    int level;            // resolution level: 0 = H x W, 1 = H/2, ...
+};
+
+constexpr int kNumLayers = 8;
+static const ConvSpec kLayers[kNumLayers] = {
+    {2, 32, 8, 32, 3, 1, 0},       // e1
+    {32, 64, 32, 64, 3, 1, 1},     // e2
+    {64, 128, 64, 128, 3, 1, 2},   // e3
+    {128, 128, 128, 128, 3, 1, 3}, // b
+    {128, 64, 128, 64, 1, 1, 2},   // c3
+    {64, 32, 64, 32, 3, 1, 1},     // c2
+    {32, 32, 32, 32, 3, 1, 0},     // c1
+    {32, 1, 32, 32, 1, 0, 0},      // out
+};
+
+__device__ __forceinline__ float bf(bf16 v) { return __bfloat162float(v); }
+
+// -- operand loaders ---------------------------------------------------------------------------
+// im2col of an NHWC tensor: row = pixel (n, h, w), piece = 8 channels of one tap
+struct ConvFwdA {
+    const bf16 *x;
+    int npix, H, W, C, ks;
+    __device__ __forceinline__ uint4 operator()(int p, int kp) const
+    {
+        const int k = kp * 8;
+        const int t = k / C, c = k - t * C;
+        if (p >= npix || t >= ks * ks) return make_uint4(0, 0, 0, 0);
+        const int hw = H * W;
+        const int n = p / hw, r = p - n * hw, h = r / W, w = r - h * W;
+        const int hh = h + t / ks - ks / 2, ww = w + t % ks - ks / 2;
+        if (hh < 0 || hh >= H || ww < 0 || ww >= W) return make_uint4(0, 0, 0, 0);
+        return *reinterpret_cast<const uint4 *>(x + ((size_t)(n * H + hh) * W + ww) * C + c);
+    }
+};
+
+__device__ __forceinline__ uint4 relu_mask(uint4 g, uint4 y)
+{
+    const bf16 *gv = reinterpret_cast<const bf16 *>(&g);
+    const bf16 *yv = reinterpret_cast<const bf16 *>(&y);
+    uint4 out;
+    bf16 *ov = reinterpret_cast<bf16 *>(&out);
+#pragma unroll
+    for (int i = 0; i < 8; ++i) ov[i] = (bf(yv[i]) > 0.f) ? gv[i] : __float2bfloat16(0.f);
+    return out;
+}
+
+// data gradient: row = pixel, piece = 8 output channels of one tap, taken at pixel - off(tap)
+struct ConvBwdDataA {
+    const bf16 *dy, *y;  // y = layer output for the ReLU mask (null: no ReLU)
+    int npix, H, W, C, ks;
+    __device__ __forceinline__ uint4 operator()(int p, int kp) const
+    {
+        const int k = kp * 8;
+        const int t = k / C, c = k - t * C;
+        if (p >= npix || t >= ks * ks) return make_uint4(0, 0, 0, 0);
+        const int hw = H * W;
+        const int n = p / hw, r = p - n * hw, h = r / W, w = r - h * W;
+        const int hh = h - (t / ks - ks / 2), ww = w - (t % ks - ks / 2);
+        if (hh < 0 || hh >= H || ww < 0 || ww >= W) return make_uint4(0, 0, 0, 0);
+        const size_t off = ((size_t)(n * H + hh) * W + ww) * C + c;
+        const uint4 g = *reinterpret_cast<const uint4 *>(dy + off);
+        if (!y) return g;
+        return relu_mask(g, *reinterpret_cast<const uint4 *>(y + off));
+    }
+};
+
+// weight gradient, A side: row = output channel, piece = 8 pixels of the masked gradient
+struct ConvBwdWA {
+    const bf16 *dy, *y;
+    int npix, C;
+    __device__ __forceinline__ uint4 operator()(int co, int kp) const
+    {
+        uint4 out = make_uint4(0, 0, 0, 0);
+        if (co >= C) return out;
+        bf16 *ov = reinterpret_cast<bf16 *>(&out);
+        const int p0 = kp * 8;
+#pragma unroll
+        for (int j = 0; j < 8; ++j) {
+            const int p = p0 + j;
+            if (p < npix) {
+                const size_t o = (size_t)p * C + co;
+                const bf16 g = dy[o];
+                ov[j] = (!y || bf(y[o]) > 0.f) ? g : __float2bfloat16(0.f);
+            }
+        }
+        return out;
+    }
+};
+
+// weight gradient, B side: row = (tap, input channel), piece = 8 pixels of the shifted input
+struct ConvBwdWB {
+    const bf16 *x;
+    int npix, H, W, C, ks;
+    __device__ __forceinline__ uint4 operator()(int kk, int kp) const
+    {
+        uint4 out = make_uint4(0, 0, 0, 0);
+        const int t = kk / C, c = kk - t * C;
+        if (t >= ks * ks) return out;
+        bf16 *ov = reinterpret_cast<bf16 *>(&out);
+        const int dh = t / ks - ks / 2, dw = t % ks - ks / 2;
+        const int hw = H * W;
+        const int p0 = kp * 8;
+#pragma unroll
+        for (int j = 0; j < 8; ++j) {
+            const int p = p0 + j;
+            if (p < npix) {
+                const int n = p / hw, r = p - n * hw, h = r / W, w = r - h * W;
+                const int hh = h + dh, ww = w + dw;
+                if (hh >= 0 && hh < H && ww >= 0 && ww < W)
+                    ov[j] = x[((size_t)(n * H + hh) * W + ww) * C + c];
+            }
+        }
+        return out;
+    }
+};
+
+// -- epilogues -------------------------------------------------------------------------------------
+struct EpiAct {  // y[pixel][co] = bf16(relu?(v + bias))
+    bf16 *y;
+    const float *bias;
+    int npix, C, relu;
+    __device__ __forceinline__ void operator()(int p, int co, float v) const
+    {
+        if (p >= npix || co >= C) return;
+        v += bias[co];
+        if (relu) v = fmaxf(v, 0.f);
+        y[(size_t)p * C + co] = __float2bfloat16(v);
+    }
+};
+
+struct EpiOut {  // out[pixel] = v + bias (channel 0 only), FP32
+    float *out;
+    const float *bias;
+    int npix;
+    __device__ __forceinline__ void operator()(int p, int co, float v) const
+    {
+        if (co == 0 && p < npix) out[p] = v + bias[0];
+    }
+};
+
+struct EpiStoreBf16 {  // dx[pixel][ci] = bf16(v)
+    bf16 *dx;
+    int npix, C;
+    __device__ __forceinline__ void operator()(int p, int c, float v) const
+    {
+        if (p < npix && c < C) dx[(size_t)p * C + c] = __float2bfloat16(v);
+    }
+};
+
+struct EpiAtomicF32 {  // g[row][col] += v
+    float *g;
+    int rows, cols;
+    __device__ __forceinline__ void operator()(int r, int c, float v) const
+    {
+        if (r < rows && c < cols && v != 0.f) atomicAdd(&g[(size_t)r * cols + c], v);
+    }
+};
+
+// -- elementwise kernels ----------------------------------------------------------------------------
+static int blocks_n(long long n)
+{
+    long long b = (n + 255) / 256;
+    return (int)std::max(1LL, std::min(b, 152LL * 16));
+}
+
+#define LENTILS_GRID_STRIDE(i, n)                                                              \
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < (n);             \
+         i += (long long)gridDim.x * blockDim.x)
+
+__global__ void make_input_kernel(const float *__restrict__ r, const float *__restrict__ d,
+                                  bf16 *__restrict__ x0, long long npix)
+{
+    LENTILS_GRID_STRIDE(p, npix)
+    {
+        bf16 v[8];
+        v[0] = __float2bfloat16(r[p]);
+        v[1] = __float2bfloat16(d[p]);
+        for (int i = 2; i < 8; ++i) v[i] = __float2bfloat16(0.f);
+        *reinterpret_cast<uint4 *>(x0 + p * 8) = *reinterpret_cast<uint4 *>(v);
+    }
+}
+
+// out (n, H/2, W/2, C) = mean of the 2 x 2 block
+__global__ void pool2_kernel(const bf16 *__restrict__ x, bf16 *__restrict__ y, int Bn, int H,
+                             int W, int C)
+{
+    const int h2 = H / 2, w2 = W / 2;
+    const long long n = (long long)Bn * h2 * w2 * C;
+    LENTILS_GRID_STRIDE(e, n)
+    {
+        const int c = (int)(e % C);
+        long long r = e / C;
+        const int w = (int)(r % w2);
+        r /= w2;
+        const int h = (int)(r % h2);
+        const int b = (int)(r / h2);
+        const size_t base = ((size_t)(b * H + 2 * h) * W + 2 * w) * C + c;
+        const float s = bf(x[base]) + bf(x[base + C]) + bf(x[base + (size_t)W * C]) +
+                        bf(x[base + (size_t)W * C + C]);
+        y[e] = __float2bfloat16(0.25f * s);
+    }
+}
+
+// out (n, H, W, C) = up2(low) + skip
+__global__ void up2add_kernel(const bf16 *__restrict__ low, const bf16 *__restrict__ skip,
+                              bf16 *__restrict__ y, int Bn, int H, int W, int C)
+{
+    const long long n = (long long)Bn * H * W * C;
+    LENTILS_GRID_STRIDE(e, n)
+    {
+        const int c = (int)(e % C);
+        long long r = e / C;
+        const int w = (int)(r % W);
+        r /= W;
+        const int h = (int)(r % H);
+        const int b = (int)(r / H);
+        const float v = bf(low[((size_t)(b * (H / 2) + h / 2) * (W / 2) + w / 2) * C + c]) + bf(skip[e]);
+        y[e] = __float2bfloat16(v);
+    }
+}
+
+// dlow (n, H/2, W/2, C) = sum of the 2 x 2 children of dy (gradient of up2)
+__global__ void sum4_kernel(const bf16 *__restrict__ dy, bf16 *__restrict__ dlow, int Bn, int H,
+                            int W, int C)
+{
+    const int h2 = H / 2, w2 = W / 2;
+    const long long n = (long long)Bn * h2 * w2 * C;
+    LENTILS_GRID_STRIDE(e, n)
+    {
+        const int c = (int)(e % C);
+        long long r = e / C;
+        const int w = (int)(r % w2);
+        r /= w2;
+        const int h = (int)(r % h2);
+        const int b = (int)(r / h2);
+        const size_t base = ((size_t)(b * H + 2 * h) * W + 2 * w) * C + c;
+        const float s = bf(dy[base]) + bf(dy[base + C]) + bf(dy[base + (size_t)W * C]) +
+                        bf(dy[base + (size_t)W * C + C]);
+        dlow[e] = __float2bfloat16(s);
+    }
+}
+
+// d (n, H, W, C) = a + 0.25 * up2(dp) (gradient through pool2 added to another gradient)
+__global__ void add_pool_grad_kernel(const bf16 *__restrict__ a, const bf16 *__restrict__ dp,
+                                     bf16 *__restrict__ d, int Bn, int H, int W, int C)
+{
+    const long long n = (long long)Bn * H * W * C;
+    LENTILS_GRID_STRIDE(e, n)
+    {
+        const int c = (int)(e % C);
+        long long r = e / C;
+        const int w = (int)(r % W);
+        r /= W;
+        const int h = (int)(r % H);
+        const int b = (int)(r / H);
+        const float v = bf(a[e]) + 0.25f * bf(dp[((size_t)(b * (H / 2) + h / 2) * (W / 2) + w / 2) * C + c]);
+        d[e] = __float2bfloat16(v);
+    }
+}
+
+// loss = mean((out - tgt)^2); dy[pixel][0..31] = (2/npix (out - tgt), 0, ...)
+__global__ void mse_kernel(const float *__restrict__ out, const float *__restrict__ tgt,
+                           bf16 *__restrict__ dy, long long npix, float *__restrict__ loss)
+{
+    __shared__ float sh[256];
+    float acc = 0.f;
+    const float scale = 2.f / (float)npix;
+    LENTILS_GRID_STRIDE(p, npix)
+    {
+        const float e = out[p] - tgt[p];
+        acc += e * e;
+        bf16 v[8];
+        v[0] = __float2bfloat16(scale * e);
+        for (int i = 1; i < 8; ++i) v[i] = __float2bfloat16(0.f);
+        uint4 *dst = reinterpret_cast<uint4 *>(dy + p * 32);
+        dst[0] = *reinterpret_cast<uint4 *>(v);
+        dst[1] = dst[2] = dst[3] = make_uint4(0, 0, 0, 0);
+    }
+    sh[threadIdx.x] = acc;
+    __syncthreads();
+    for (int o = 128; o > 0; o >>= 1) {
+        if ((int)threadIdx.x < o) sh[threadIdx.x] += sh[threadIdx.x + o];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) atomicAdd(loss, sh[0] / (float)npix);
+}
+
+// db[co] += sum_pixel dy'[pixel][co]
+__global__ void bias_grad_kernel(const bf16 *__restrict__ dy, const bf16 *__restrict__ y,
+                                 float *__restrict__ db, long long npix, int C, int creal)
+{
+    // blockDim.x == C (padded channels, <= 128); each block sums a slice of pixels
+    const int c = threadIdx.x;
+    float acc = 0.f;
+    for (long long p = blockIdx.x; p < npix; p += gridDim.x) {
+        const size_t o = (size_t)p * C + c;
+        if (!y || bf(y[o]) > 0.f) acc += bf(dy[o]);
+    }
+    if (c < creal) atomicAdd(&db[c], acc);
+}
+
+// Adam step on a flat parameter vector; bias correction folded into the step size
+__global__ void adam_kernel(float *__restrict__ w, const float *__restrict__ g,
+                            float *__restrict__ m, float *__restrict__ v, long long n, float lr,
+                            float b1, float b2, float eps, float c1, float c2)
+{
+    LENTILS_GRID_STRIDE(i, n)
+    {
+        const float gi = g[i];
+        const float mi = b1 * m[i] + (1.f - b1) * gi;
+        const float vi = b2 * v[i] + (1.f - b2) * gi * gi;
+        m[i] = mi;
+        v[i] = vi;
+        w[i] -= lr * (mi / c1) / (sqrtf(vi / c2) + eps);
+    }
+}
+
+// BF16 copies of one layer's weights: fwd[co][tap*cin_p + ci], bwd[ci][tap*cout_p + co]
+__global__ void refresh_weights_kernel(const float *__restrict__ w, bf16 *__restrict__ fwd,
+                                       bf16 *__restrict__ bwd, int cin, int cout, int cin_p,
+                                       int cout_p, int taps)
+{
+    const long long n = (long long)cout_p * taps * cin_p;
+    LENTILS_GRID_STRIDE(e, n)
+    {
+        const int ci = (int)(e % cin_p);
+        long long r = e / cin_p;
+        const int t = (int)(r % taps);
+        const int co = (int)(r / taps);
+        float v = 0.f;
+        if (co < cout && ci < cin) v = w[((size_t)co * taps + t) * cin + ci];
+        const bf16 b = __float2bfloat16(v);
+        fwd[((size_t)co * taps + t) * cin_p + ci] = b;
+        bwd[((size_t)ci * taps + t) * cout_p + co] = b;
+    }
+}
+
+// gather padded FP32 weight gradients [cout_p][taps*cin_p] into the flat layout [cout][taps][cin]
+__global__ void gather_wgrad_kernel(const float *__restrict__ gp, float *__restrict__ g, int cin,
+                                    int cout, int cin_p, int taps)
+{
+    const long long n = (long long)cout * taps * cin;
+    LENTILS_GRID_STRIDE(e, n)
+    {
+        const int ci = (int)(e % cin);
+        long long r = e / cin;
+        const int t = (int)(r % taps);
+        const int co = (int)(r / taps);
+        g[e] = gp[(size_t)co * taps * cin_p + (size_t)t * cin_p + ci];
+    }
+}
+
+// Preconditioner pieces (one sample of n = H * W values):
+//   u = dinv * r, s = rms(u) (1 where u = 0), x0 = (u / s, feat, 0...), z = u + s * out
+__global__ void __launch_bounds__(1024)
+    precond_scale_kernel(const float *__restrict__ r, const float *__restrict__ dinv, int n,
+                         float *__restrict__ scale)
+{
+    __shared__ double sh[32];
+    double acc = 0.0;
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+        const double u = (double)dinv[i] * (double)r[i];
+        acc += u * u;
+    }
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+    if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = acc;
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        double t = (threadIdx.x < (blockDim.x >> 5)) ? sh[threadIdx.x] : 0.0;
+        for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+        if (threadIdx.x == 0) {
+            const double rms = sqrt(t / (double)n);
+            scale[0] = (rms > 0.0 && rms < 1e300) ? (float)rms : 1.f;
+        }
+    }
+}
+
+__global__ void precond_input_kernel(const float *__restrict__ r, const float *__restrict__ dinv,
+                                     const float *__restrict__ feat,
+                                     const float *__restrict__ scale, bf16 *__restrict__ x0, int n)
+{
+    const float inv = 1.f / scale[0];
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        bf16 v[8];
+        v[0] = __float2bfloat16(dinv[i] * r[i] * inv);
+        v[1] = __float2bfloat16(feat[i]);
+        for (int k = 2; k < 8; ++k) v[k] = __float2bfloat16(0.f);
+        *reinterpret_cast<uint4 *>(x0 + (size_t)i * 8) = *reinterpret_cast<uint4 *>(v);
+    }
+}
+
+__global__ void precond_combine_kernel(const float *__restrict__ r, const float *__restrict__ dinv,
+                                       const float *__restrict__ out,
+                                       const float *__restrict__ scale, float *__restrict__ z, int n)
+{
+    const float s = scale[0];
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+        z[i] = fmaf(s, out[i], dinv[i] * r[i]);
+}
+
+// feat = log(dinv) - mean(log(dinv)), one block
+__global__ void __launch_bounds__(1024)
+    features_kernel(const float *__restrict__ dinv, float *__restrict__ feat, int n)
+{
+    __shared__ double sh[32];
+    __shared__ double mean;
+    double acc = 0.0;
+    for (int i = threadIdx.x; i < n; i += blockDim.x) acc += log((double)dinv[i]);
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+    if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = acc;
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        double t = (threadIdx.x < (blockDim.x >> 5)) ? sh[threadIdx.x] : 0.0;
+        for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+        if (threadIdx.x == 0) mean = t / (double)n;
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < n; i += blockDim.x) feat[i] = (float)(log((double)dinv[i]) - mean);
+}
+
+}  // namespace lentils
+
+// ------------------------------------------------------------------------------------------------
+// Network object
+// ------------------------------------------------------------------------------------------------
+struct lentils_unet {
+    int H, W, maxB;
+    long long nparams;
+    // per layer
+    float *w32[lentils::kNumLayers], *b32[lentils::kNumLayers];  // views into params
+    lentils::bf16 *wf[lentils::kNumLayers], *wb[lentils::kNumLayers];
+    float *gw_pad[lentils::kNumLayers];  // FP32 weight gradients, padded layout
+    float *gw[lentils::kNumLayers], *gb[lentils::kNumLayers];  // views into grads
+    float *params, *grads, *adam_m, *adam_v;
+    long long step;
+    // activations (max batch)
+    lentils::bf16 *x0, *e1, *p1, *e2, *p2, *e3, *p3, *b, *u3, *c3, *u2, *c2, *u1, *c1;
+    float *out;
+    float *pscale;  // preconditioner scale (device)
+    // gradients
+    lentils::bf16 *dy_out, *d_c1, *d_u1, *d_c2, *d_u2, *d_c3, *d_u3, *d_b, *d_p3, *d_e3, *d_p2,
+        *d_e2, *d_p1, *d_e1;
+    float *loss;
+    int *err;
+    void *block;  // single allocation backing everything above
+};
+
+namespace lentils {
+
+static long long layer_wcount(int l)
+{
+    const ConvSpec &s = kLayers[l];
+    return (long long)s.cout * s.ks * s.ks * s.cin;
+}
+
+// raises the dynamic shared-memory limit of one kernel instantiation (once per process)
+template <int N, class LA, class LB, class EP>
+static cudaError_t gemm_smem_attr()
+{
+    static const cudaError_t e = cudaFuncSetAttribute(
+        tc::gemm_kernel<N, LA, LB, EP>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+        (int)tc::GemmSmem<N>::kBytes);
+    return e;
+}
+
+template <int N, class LA, class EP>
+static int conv_gemm(const LA &la, const tc::RowMajorLoader &lb, const EP &ep, int M, int K,
+                     int *err, cudaStream_t s)
+{
+    auto kern = tc::gemm_kernel<N, LA, tc::RowMajorLoader, EP>;
+    const size_t smem = tc::GemmSmem<N>::kBytes;
+    LENTILS_CUDA_TRY((gemm_smem_attr<N, LA, tc::RowMajorLoader, EP>()));
+    const int kp = (K + 7) / 8;
+    kern<<<dim3((M + 127) / 128, 1, 1), 128, smem, s>>>(la, lb, ep, kp, kp, err);
+    LENTILS_CHECK_LAUNCH("conv gemm");
+    return LENTILS_OK;
+}
+
+template <class LA, class EP>
+static int conv_gemm_n(int N, const LA &la, const tc::RowMajorLoader &lb, const EP &ep, int M,
+                       int K, int *err, cudaStream_t s)
+{
+    switch (N) {
+    case 32: return conv_gemm<32>(la, lb, ep, M, K, err, s);
+    case 64: return conv_gemm<64>(la, lb, ep, M, K, err, s);
+    case 128: return conv_gemm<128>(la, lb, ep, M, K, err, s);
+    }
+    return set_error(LENTILS_ERR_UNSUPPORTED, "conv gemm N=%d", N);
+}
+
+static int level_dims(const lentils_unet *net, int level, int &H, int &W)
+{
+    H = net->H >> level;
+    W = net->W >> level;
+    return LENTILS_OK;
+}
+
+// forward of layer l: y = act(conv(x))
+static int layer_forward(lentils_unet *net, int l, const bf16 *x, void *y, int Bn, cudaStream_t s)
+{
+    const ConvSpec &c = kLayers[l];
+    int H, W;
+    level_dims(net, c.level, H, W);
+    const int npix = Bn * H * W;
+    const int K = c.ks * c.ks * c.cin_p;
+    ConvFwdA la{x, npix, H, W, c.cin_p, c.ks};
+    tc::RowMajorLoader lb{net->wf[l], c.cout_p, K, K};
+    if (l == kNumLayers - 1) {
+        EpiOut ep{(float *)y, net->b32[l], npix};
+        return conv_gemm_n(c.cout_p, la, lb, ep, npix, K, net->err, s);
+    }
+    EpiAct ep{(bf16 *)y, net->b32[l], npix, c.cout_p, c.relu};
+    return conv_gemm_n(c.cout_p, la, lb, ep, npix, K, net->err, s);
+}
+
+// backward of layer l: dy (gradient of its output, before the ReLU mask), y (its output, for
+// the mask; null for the output layer), x (its input); accumulates gw/gb, writes dx (optional)
+static int layer_backward(lentils_unet *net, int l, const bf16 *dy, const bf16 *y, const bf16 *x,
+                          bf16 *dx, int Bn, cudaStream_t s)
+{
+    const ConvSpec &c = kLayers[l];
+    int H, W;
+    level_dims(net, c.level, H, W);
+    const int npix = Bn * H * W;
+    const int taps = c.ks * c.ks;
+    const bf16 *mask = c.relu ? y : nullptr;
+    // bias gradient
+    bias_grad_kernel<<<std::min(npix, 1024), c.cout_p, 0, s>>>(dy, mask, net->gb[l], npix, c.cout_p, c.cout);
+    LENTILS_CHECK_LAUNCH("bias_grad_kernel");
+    // weight gradient: M = cout_p (one tile), N = taps * cin_p in tiles of <= 256, K = pixels
+    {
+        const int Kw = taps * c.cin_p;
+        ConvBwdWA la{dy, mask, npix, c.cout_p};
+        ConvBwdWB lb{x, npix, H, W, c.cin_p, c.ks};
+        EpiAtomicF32 ep{net->gw_pad[l], c.cout_p, Kw};
+        const int kpieces = (npix + 7) / 8;
+        const int split = 128;  // pieces (1024 pixels) per CTA along K
+        const int nz = (kpieces + split - 1) / split;
+        if (Kw <= 32) {
+            auto kern = tc::gemm_kernel<32, ConvBwdWA, ConvBwdWB, EpiAtomicF32>;
+            const size_t smem = tc::GemmSmem<32>::kBytes;
+            LENTILS_CUDA_TRY((gemm_smem_attr<32, ConvBwdWA, ConvBwdWB, EpiAtomicF32>()));
+            kern<<<dim3(1, 1, nz), 128, smem, s>>>(la, lb, ep, kpieces, split, net->err);
+        } else if (Kw <= 128) {
+            auto kern = tc::gemm_kernel<128, ConvBwdWA, ConvBwdWB, EpiAtomicF32>;
+            const size_t smem = tc::GemmSmem<128>::kBytes;
+            LENTILS_CUDA_TRY((gemm_smem_attr<128, ConvBwdWA, ConvBwdWB, EpiAtomicF32>()));
+            kern<<<dim3(1, 1, nz), 128, smem, s>>>(la, lb, ep, kpieces, split, net->err);
+        } else {
+            auto kern = tc::gemm_kernel<256, ConvBwdWA, ConvBwdWB, EpiAtomicF32>;
+            const size_t smem = tc::GemmSmem<256>::kBytes;
+            LENTILS_CUDA_TRY((gemm_smem_attr<256, ConvBwdWA, ConvBwdWB, EpiAtomicF32>()));
+            kern<<<dim3(1, (Kw + 255) / 256, nz), 128, smem, s>>>(la, lb, ep, kpieces, split, net->err);
+        }
+        LENTILS_CHECK_LAUNCH("weight gradient gemm");
+    }
+    // data gradient
+    if (dx) {
+        const int K = taps * c.cout_p;
+        ConvBwdDataA la{dy, mask, npix, H, W, c.cout_p, c.ks};
+        tc::RowMajorLoader lb{net->wb[l], c.cin_p, K, K};
+        EpiStoreBf16 ep{dx, npix, c.cin_p};
+        if (int st = conv_gemm_n(std::max(32, c.cin_p), la, lb, ep, npix, K, net->err, s)) return st;
+    }
+    return LENTILS_OK;
+}
+
+// all layers, from the packed input x0 to out
+static int net_layers_forward(lentils_unet *net, int Bn, cudaStream_t s)
+{
+    const int H = net->H, W = net->W;
+    const long long np0 = (long long)Bn * H * W;
+    int st;
+    if ((st = layer_forward(net, 0, net->x0, net->e1, Bn, s))) return st;
+    pool2_kernel<<<blocks_n(np0 / 4 * 32), 256, 0, s>>>(net->e1, net->p1, Bn, H, W, 32);
+    if ((st = layer_forward(net, 1, net->p1, net->e2, Bn, s))) return st;
+    pool2_kernel<<<blocks_n(np0 / 16 * 64), 256, 0, s>>>(net->e2, net->p2, Bn, H / 2, W / 2, 64);
+    if ((st = layer_forward(net, 2, net->p2, net->e3, Bn, s))) return st;
+    pool2_kernel<<<blocks_n(np0 / 64 * 128), 256, 0, s>>>(net->e3, net->p3, Bn, H / 4, W / 4, 128);
+    if ((st = layer_forward(net, 3, net->p3, net->b, Bn, s))) return st;
+    up2add_kernel<<<blocks_n(np0 / 16 * 128), 256, 0, s>>>(net->b, net->e3, net->u3, Bn, H / 4, W / 4, 128);
+    if ((st = layer_forward(net, 4, net->u3, net->c3, Bn, s))) return st;
+    up2add_kernel<<<blocks_n(np0 / 4 * 64), 256, 0, s>>>(net->c3, net->e2, net->u2, Bn, H / 2, W / 2, 64);
+    if ((st = layer_forward(net, 5, net->u2, net->c2, Bn, s))) return st;
+    up2add_kernel<<<blocks_n(np0 * 32), 256, 0, s>>>(net->c2, net->e1, net->u1, Bn, H, W, 32);
+    if ((st = layer_forward(net, 6, net->u1, net->c1, Bn, s))) return st;
+    if ((st = layer_forward(net, 7, net->c1, net->out, Bn, s))) return st;
+    LENTILS_CHECK_LAUNCH("unet forward");
+    return LENTILS_OK;
+}
+
+static int net_forward(lentils_unet *net, const float *r, const float *d, int Bn, cudaStream_t s)
+{
+    const long long np0 = (long long)Bn * net->H * net->W;
+    make_input_kernel<<<blocks_n(np0), 256, 0, s>>>(r, d, net->x0, np0);
+    return net_layers_forward(net, Bn, s);
+}
+
+// gradients of the mean squared error against tgt (forward must have run for this batch)
+static int net_backward(lentils_unet *net, const float *tgt, int Bn, cudaStream_t s)
+{
+    const int H = net->H, W = net->W;
+    const long long np0 = (long long)Bn * H * W;
+    LENTILS_CUDA_TRY(cudaMemsetAsync(net->grads, 0, sizeof(float) * net->nparams, s));
+    for (int l = 0; l < kNumLayers; ++l) {
+        const ConvSpec &c = kLayers[l];
+        LENTILS_CUDA_TRY(cudaMemsetAsync(net->gw_pad[l], 0,
+                                         sizeof(float) * c.cout_p * c.ks * c.ks * c.cin_p, s));
+    }
+    LENTILS_CUDA_TRY(cudaMemsetAsync(net->loss, 0, sizeof(float), s));
+    mse_kernel<<<blocks_n(np0), 256, 0, s>>>(net->out, tgt, net->dy_out, np0, net->loss);
+    int st;
+    if ((st = layer_backward(net, 7, net->dy_out, nullptr, net->c1, net->d_c1, Bn, s))) return st;
+    if ((st = layer_backward(net, 6, net->d_c1, net->c1, net->u1, net->d_u1, Bn, s))) return st;
+    // u1 = up2(c2) + e1
+    sum4_kernel<<<blocks_n(np0 / 4 * 32), 256, 0, s>>>(net->d_u1, net->d_c2, Bn, H, W, 32);
+    if ((st = layer_backward(net, 5, net->d_c2, net->c2, net->u2, net->d_u2, Bn, s))) return st;
+    sum4_kernel<<<blocks_n(np0 / 16 * 64), 256, 0, s>>>(net->d_u2, net->d_c3, Bn, H / 2, W / 2, 64);
+    if ((st = layer_backward(net, 4, net->d_c3, net->c3, net->u3, net->d_u3, Bn, s))) return st;
+    sum4_kernel<<<blocks_n(np0 / 64 * 128), 256, 0, s>>>(net->d_u3, net->d_b, Bn, H / 4, W / 4, 128);
+    if ((st = layer_backward(net, 3, net->d_b, net->b, net->p3, net->d_p3, Bn, s))) return st;
+    // e3 feeds u3 (skip) and p3 (pool)
+    add_pool_grad_kernel<<<blocks_n(np0 / 16 * 128), 256, 0, s>>>(net->d_u3, net->d_p3, net->d_e3, Bn, H / 4, W / 4, 128);
+    if ((st = layer_backward(net, 2, net->d_e3, net->e3, net->p2, net->d_p2, Bn, s))) return st;
+    add_pool_grad_kernel<<<blocks_n(np0 / 4 * 64), 256, 0, s>>>(net->d_u2, net->d_p2, net->d_e2, Bn, H / 2, W / 2, 64);
+    if ((st = layer_backward(net, 1, net->d_e2, net->e2, net->p1, net->d_p1, Bn, s))) return st;
+    add_pool_grad_kernel<<<blocks_n(np0 * 32), 256, 0, s>>>(net->d_u1, net->d_p1, net->d_e1, Bn, H, W, 32);
+    if ((st = layer_backward(net, 0, net->d_e1, net->e1, net->x0, nullptr, Bn, s))) return st;
+    for (int l = 0; l < kNumLayers; ++l) {
+        const ConvSpec &c = kLayers[l];
+        gather_wgrad_kernel<<<blocks_n(layer_wcount(l)), 256, 0, s>>>(
+            net->gw_pad[l], net->gw[l], c.cin, c.cout, c.cin_p, c.ks * c.ks);
+    }
+    LENTILS_CHECK_LAUNCH("unet backward");
+    return LENTILS_OK;
+}
+
+static int refresh_all(lentils_unet *net, cudaStream_t s)
+{
+    for (int l = 0; l < kNumLayers; ++l) {
+        const ConvSpec &c = kLayers[l];
+        refresh_weights_kernel<<<blocks_n((long long)c.cout_p * c.ks * c.ks * c.cin_p), 256, 0, s>>>(
+            net->w32[l], net->wf[l], net->wb[l], c.cin, c.cout, c.cin_p, c.cout_p, c.ks * c.ks);
+    }
+    LENTILS_CHECK_LAUNCH("refresh_weights_kernel");
+    return LENTILS_OK;
+}
+
+// Sets the shared-memory limits of every GEMM instantiation the forward pass uses, so that a
+// forward pass can be captured into a CUDA graph without first-use set-up inside the capture.
+static int prepare_forward()
+{
+    LENTILS_CUDA_TRY((gemm_smem_attr<32, ConvFwdA, tc::RowMajorLoader, EpiAct>()));
+    LENTILS_CUDA_TRY((gemm_smem_attr<64, ConvFwdA, tc::RowMajorLoader, EpiAct>()));
+    LENTILS_CUDA_TRY((gemm_smem_attr<128, ConvFwdA, tc::RowMajorLoader, EpiAct>()));
+    LENTILS_CUDA_TRY((gemm_smem_attr<32, ConvFwdA, tc::RowMajorLoader, EpiOut>()));
+    return LENTILS_OK;
+}
+
+int unet_precondition(lentils_unet *net, const float *r, const float *dinv, const float *feat,
+                      float *z, cudaStream_t s)
+{
+    const int n = net->H * net->W;
+    precond_scale_kernel<<<1, 1024, 0, s>>>(r, dinv, n, net->pscale);
+    precond_input_kernel<<<blocks_n(n), 256, 0, s>>>(r, dinv, feat, net->pscale, net->x0, n);
+    LENTILS_CHECK_LAUNCH("precond input");
+    if (int st = net_layers_forward(net, 1, s)) return st;
+    precond_combine_kernel<<<blocks_n(n), 256, 0, s>>>(r, dinv, net->out, net->pscale, z, n);
+    LENTILS_CHECK_LAUNCH("precond_combine_kernel");
+    return LENTILS_OK;
+}
+
+int unet_prepare(lentils_unet *net) { return net ? prepare_forward() : LENTILS_OK; }
+
+int unet_size(const lentils_unet *net) { return net ? net->H * net->W : 0; }
+
+int unet_error_flag_device(lentils_unet *net, int *flag)
+{
+    LENTILS_CUDA_TRY(cudaMemcpy(flag, net->err, sizeof(int), cudaMemcpyDeviceToHost));
+    return LENTILS_OK;
+}
+
+}  // namespace lentils
+
+using namespace lentils;
+
+extern "C" {
+
+int lentils_unet_features(const float *dinv, float *feat, int n, void *stream)
+{
+    clear_error();
+    if (!dinv || !feat || n < 1) return set_error(LENTILS_ERR_INVALID, "unet_features: bad arguments");
+    features_kernel<<<1, 1024, 0, (cudaStream_t)stream>>>(dinv, feat, n);
+    LENTILS_CHECK_LAUNCH("features_kernel");
+    return LENTILS_OK;
+}
+
+int lentils_unet_precondition(lentils_unet *net, const float *r, const float *dinv,
+                              const float *feat, float *z, void *stream)
+{
+    clear_error();
+    if (!net || !r || !dinv || !feat || !z)
+        return set_error(LENTILS_ERR_INVALID, "unet_precondition: null");
+    return unet_precondition(net, r, dinv, feat, z, (cudaStream_t)stream);
+}
+
+
+long long lentils_unet_param_count(void)
+{
+    long long n = 0;
+    for (int l = 0; l < kNumLayers; ++l) n += layer_wcount(l) + kLayers[l].cout;
+    return n;
+}
+
+// Parameters are one flat FP32 vector: for each layer in order, the weights [cout][ks*ks][cin]
+// then the biases [cout].
+int lentils_unet_create(lentils_unet **out, int H, int W, int max_batch, const float *init_params,
+                        void *stream)
+{
+    clear_error();
+    if (!out || !init_params || H < 16 || W < 16 || (H % 8) || (W % 8) || max_batch < 1)
+        return set_error(LENTILS_ERR_INVALID, "unet_create: H, W multiples of 8 (>= 16)");
+    *out = nullptr;
+    lentils_unet *net = new (std::nothrow) lentils_unet();
+    if (!net) return set_error(LENTILS_ERR_ALLOC, "unet_create: host allocation");
+    memset(net, 0, sizeof(*net));
+    net->H = H;
+    net->W = W;
+    net->maxB = max_batch;
+    net->nparams = lentils_unet_param_count();
+    const long long np0 = (long long)max_batch * H * W;
+    // carve one allocation
+    std::vector<std::pair<void **, size_t>> parts;
+    auto add = [&](void **p, size_t bytes) { parts.push_back({p, (bytes + 255) & ~size_t(255)}); };
+    add((void **)&net->params, sizeof(float) * net->nparams);
+    add((void **)&net->grads, sizeof(float) * net->nparams);
+    add((void **)&net->adam_m, sizeof(float) * net->nparams);
+    add((void **)&net->adam_v, sizeof(float) * net->nparams);
+    for (int l = 0; l < kNumLayers; ++l) {
+        const ConvSpec &c = kLayers[l];
+        const size_t n = (size_t)c.cout_p * c.ks * c.ks * c.cin_p;
+        add((void **)&net->wf[l], sizeof(bf16) * n);
+        add((void **)&net->wb[l], sizeof(bf16) * n);
+        add((void **)&net->gw_pad[l], sizeof(float) * n);
+    }
+    const size_t b2 = sizeof(bf16);
+    add((void **)&net->x0, b2 * np0 * 8);
+    add((void **)&net->e1, b2 * np0 * 32);
+    add((void **)&net->p1, b2 * np0 / 4 * 32);
+    add((void **)&net->e2, b2 * np0 / 4 * 64);
+    add((void **)&net->p2, b2 * np0 / 16 * 64);
+    add((void **)&net->e3, b2 * np0 / 16 * 128);
+    add((void **)&net->p3, b2 * np0 / 64 * 128);
+    add((void **)&net->b, b2 * np0 / 64 * 128);
+    add((void **)&net->u3, b2 * np0 / 16 * 128);
+    add((void **)&net->c3, b2 * np0 / 16 * 64);
+    add((void **)&net->u2, b2 * np0 / 4 * 64);
+    add((void **)&net->c2, b2 * np0 / 4 * 32);
+    add((void **)&net->u1, b2 * np0 * 32);
+    add((void **)&net->c1, b2 * np0 * 32);
+    add((void **)&net->out, sizeof(float) * np0);
+    add((void **)&net->dy_out, b2 * np0 * 32);
+    add((void **)&net->d_c1, b2 * np0 * 32);
+    add((void **)&net->d_u1, b2 * np0 * 32);
+    add((void **)&net->d_c2, b2 * np0 / 4 * 32);
+    add((void **)&net->d_u2, b2 * np0 / 4 * 64);
+    add((void **)&net->d_c3, b2 * np0 / 16 * 64);
+    add((void **)&net->d_u3, b2 * np0 / 16 * 128);
+    add((void **)&net->d_b, b2 * np0 / 64 * 128);
+    add((void **)&net->d_p3, b2 * np0 / 64 * 128);
+    add((void **)&net->d_e3, b2 * np0 / 16 * 128);
+    add((void **)&net->d_p2, b2 * np0 / 16 * 64);
+    add((void **)&net->d_e2, b2 * np0 / 4 * 64);
+    add((void **)&net->d_p1, b2 * np0 / 4 * 32);
+    add((void **)&net->d_e1, b2 * np0 * 32);
+    add((void **)&net->loss, sizeof(float));
+    add((void **)&net->pscale, sizeof(float));
+    add((void **)&net->err, sizeof(int));
+    size_t total = 0;
+    for (auto &p : parts) total += p.second;
+    cudaError_t e = cudaMalloc(&net->block, total);
+    if (e != cudaSuccess) {
+        delete net;
+        return cuda_status(e, "unet_create alloc");
+    }
+    size_t off = 0;
+    for (auto &p : parts) {
+        *p.first = (unsigned char *)net->block + off;
+        off += p.second;
+    }
+    // parameter views
+    long long po = 0;
+    for (int l = 0; l < kNumLayers; ++l) {
+        net->w32[l] = net->params + po;
+        net->gw[l] = net->grads + po;
+        po += layer_wcount(l);
+        net->b32[l] = net->params + po;
+        net->gb[l] = net->grads + po;
+        po += kLayers[l].cout;
+    }
+    cudaStream_t s = (cudaStream_t)stream;
+    e = cudaMemcpyAsync(net->params, init_params, sizeof(float) * net->nparams, cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess) e = cudaMemsetAsync(net->adam_m, 0, sizeof(float) * net->nparams, s);
+    if (e == cudaSuccess) e = cudaMemsetAsync(net->adam_v, 0, sizeof(float) * net->nparams, s);
+    if (e == cudaSuccess) e = cudaMemsetAsync(net->err, 0, sizeof(int), s);
+    int st = (e == cudaSuccess) ? refresh_all(net, s) : cuda_status(e, "unet_create init");
+    if (!st) {
+        e = cudaStreamSynchronize(s);
+        if (e != cudaSuccess) st = cuda_status(e, "unet_create sync");
+    }
+    if (st) {
+        cudaFree(net->block);
+        delete net;
+        return st;
+    }
+    *out = net;
+    return LENTILS_OK;
+}
+
+int lentils_unet_destroy(lentils_unet *net)
+{
+    clear_error();
+    if (!net) return LENTILS_OK;
+    cudaFree(net->block);
+    delete net;
+    return LENTILS_OK;
+}
+
+int lentils_unet_get_params(lentils_unet *net, float *host_out)
+{
+    clear_error();
+    if (!net || !host_out) return set_error(LENTILS_ERR_INVALID, "unet_get_params: null");
+    LENTILS_CUDA_TRY(cudaMemcpy(host_out, net->params, sizeof(float) * net->nparams, cudaMemcpyDeviceToHost));
+    return LENTILS_OK;
+}
+
+int lentils_unet_set_params(lentils_unet *net, const float *host_in, void *stream)
+{
+    clear_error();
+    if (!net || !host_in) return set_error(LENTILS_ERR_INVALID, "unet_set_params: null");
+    cudaStream_t s = (cudaStream_t)stream;
+    LENTILS_CUDA_TRY(cudaMemcpyAsync(net->params, host_in, sizeof(float) * net->nparams, cudaMemcpyHostToDevice, s));
+    return refresh_all(net, s);
+}
+
+// out = net(r, d) for Bn samples of H x W (device FP32 arrays)
+int lentils_unet_forward(lentils_unet *net, const float *r, const float *d, float *out, int Bn,
+                         void *stream)
+{
+    clear_error();
+    if (!net || !r || !d || !out || Bn < 1 || Bn > net->maxB)
+        return set_error(LENTILS_ERR_INVALID, "unet_forward: bad arguments");
+    cudaStream_t s = (cudaStream_t)stream;
+    if (int st = net_forward(net, r, d, Bn, s)) return st;
+    LENTILS_CUDA_TRY(cudaMemcpyAsync(out, net->out, sizeof(float) * Bn * net->H * net->W,
+                                     cudaMemcpyDeviceToDevice, s));
+    return LENTILS_OK;
+}
+
+// forward + backward without updating: flat gradient (host) and loss (host)
+int lentils_unet_gradients(lentils_unet *net, const float *r, const float *d, const float *tgt,
+                           int Bn, float *grad_host, float *loss_host, void *stream)
+{
+    clear_error();
+    if (!net || !r || !d || !tgt || Bn < 1 || Bn > net->maxB)
+        return set_error(LENTILS_ERR_INVALID, "unet_gradients: bad arguments");
+    cudaStream_t s = (cudaStream_t)stream;
+    int st;
+    if ((st = net_forward(net, r, d, Bn, s))) return st;
+    if ((st = net_backward(net, tgt, Bn, s))) return st;
+    if (grad_host)
+        LENTILS_CUDA_TRY(cudaMemcpyAsync(grad_host, net->grads, sizeof(float) * net->nparams, cudaMemcpyDeviceToHost, s));
+    if (loss_host)
+        LENTILS_CUDA_TRY(cudaMemcpyAsync(loss_host, net->loss, sizeof(float), cudaMemcpyDeviceToHost, s));
+    int herr = 0;
+    LENTILS_CUDA_TRY(cudaMemcpyAsync(&herr, net->err, sizeof(int), cudaMemcpyDeviceToHost, s));
+    LENTILS_CUDA_TRY(cudaStreamSynchronize(s));
+    if (herr) return set_error(LENTILS_ERR_TIMEOUT, "unet: a tensor-core wait gave up");
+    return LENTILS_OK;
+}
+
+// one Adam step on the mean squared error; loss_dev (device float) receives the batch loss
+int lentils_unet_train_step(lentils_unet *net, const float *r, const float *d, const float *tgt,
+                            int Bn, float lr, float *loss_dev, void *stream)
+{
+    clear_error();
+    if (!net || !r || !d || !tgt || Bn < 1 || Bn > net->maxB)
+        return set_error(LENTILS_ERR_INVALID, "unet_train_step: bad arguments");
+    cudaStream_t s = (cudaStream_t)stream;
+    int st;
+    if ((st = net_forward(net, r, d, Bn, s))) return st;
+    if ((st = net_backward(net, tgt, Bn, s))) return st;
+    net->step += 1;
+    const float b1 = 0.9f, b2 = 0.999f;
+    const float c1 = 1.f - powf(b1, (float)net->step), c2 = 1.f - powf(b2, (float)net->step);
+    adam_kernel<<<blocks_n(net->nparams), 256, 0, s>>>(net->params, net->grads, net->adam_m,
+                                                       net->adam_v, net->nparams, lr, b1, b2,
+                                                       1e-8f, c1, c2);
+    LENTILS_CHECK_LAUNCH("adam_kernel");
+    if ((st = refresh_all(net, s))) return st;
+    if (loss_dev)
+        LENTILS_CUDA_TRY(cudaMemcpyAsync(loss_dev, net->loss, sizeof(float), cudaMemcpyDeviceToDevice, s));
+    return LENTILS_OK;
+}
+
+// status of the bounded tensor-core waits since creation (1 = a wait gave up)
+int lentils_unet_error_flag(lentils_unet *net, int *flag)
+{
+    clear_error();
+    if (!net || !flag) return set_error(LENTILS_ERR_INVALID, "unet_error_flag: null");
+    LENTILS_CUDA_TRY(cudaMemcpy(flag, net->err, sizeof(int), cudaMemcpyDeviceToHost));
+    return LENTILS_OK;
+}
+
+}  // extern "C"

@@ -21,11 +21,14 @@ from .operators import BilinearLensOperator, NUFFTOperator
 
 class SourceInversion:
     def __init__(self, vis_space, data, sigma, image_space, source_space, lensmodel, z_src,
-                 strength, kernel_support=4, pad_factor=2, kb_beta=None, data_mask=None):
+                 strength, kernel_support=4, pad_factor=2, kb_beta=None, data_mask=None,
+                 nufft=None):
+        """nufft: an existing NUFFTOperator for vis_space and image_space to share (lens-model
+        sweeps over one visibility set); built here when None."""
         self.stream = torch.cuda.Stream()
         with torch.cuda.stream(self.stream):
-            self.nufft = NUFFTOperator(vis_space, image_space, pad_factor, kernel_support,
-                                       kb_beta)
+            self.nufft = nufft if nufft is not None else NUFFTOperator(
+                vis_space, image_space, pad_factor, kernel_support, kb_beta)
             self.lens = BilinearLensOperator(image_space, source_space, lensmodel, z_src)
             self.source_space = source_space
             self.image_space = image_space
@@ -97,6 +100,25 @@ class SourceInversion:
             self._normal, _ptr(self.b), _ptr(x),
             _ptr(self.inv_diag32) if precondition else None, ctypes.byref(opt),
             ctypes.byref(res), ctypes.c_void_p(self.stream.cuda_stream)))
+        self.stream.synchronize()
+        info = {f: getattr(res, f) for f, _ in res._fields_}
+        return x, info
+
+    def solve_flexible(self, net=None, tol=1e-6, inner_tol=1e-2, max_outer=30, max_inner=5000,
+                       check_every=10, use_graph=True, x0=None):
+        """Flexible CG with the learned preconditioner `net` (learned.UNet on the source grid;
+        None: the same iteration with Jacobi directions only), inside the same FP64 iterative
+        refinement as solve(). Returns (x float64 CUDA tensor, info)."""
+        x = torch.zeros(self.nsrc, dtype=torch.float64, device="cuda") if x0 is None else \
+            torch.as_tensor(x0, dtype=torch.float64).reshape(-1).cuda().clone()
+        opt = N.CGOptionsC(float(tol), float(inner_tol), int(max_outer), int(max_inner),
+                           int(check_every), 1 if use_graph else 0)
+        res = N.CGResultC()
+        torch.cuda.synchronize()
+        N.check(N.lib().lentils_fcg_solve(
+            self._normal, _ptr(self.b), _ptr(x), _ptr(self.inv_diag32),
+            net.handle if net is not None else None, ctypes.byref(opt), ctypes.byref(res),
+            ctypes.c_void_p(self.stream.cuda_stream)))
         self.stream.synchronize()
         info = {f: getattr(res, f) for f, _ in res._fields_}
         return x, info

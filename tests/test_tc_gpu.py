@@ -9,7 +9,8 @@ pytestmark = pytest.mark.gpu
 
 
 @pytest.mark.parametrize("M,N,K", [(128, 64, 64), (256, 64, 192), (384, 128, 576),
-                                   (128, 32, 64), (200, 256, 128), (1000, 128, 1152)])
+                                   (128, 32, 64), (200, 256, 128), (1000, 128, 1152),
+                                   (128, 32, 72), (256, 64, 200)])
 def test_tc_gemm_bf16(native, M, N, K):
     L = native.lib()
     g = torch.Generator(device="cuda").manual_seed(M * 7 + N + K)

@@ -1,0 +1,137 @@
+"""The learned preconditioner's network on the tensor cores against the CPU oracle (PyTorch
+FP64 autograd): forward outputs and parameter gradients, with and without BF16 emulation in
+the oracle; Adam training on the GPU; the preconditioner form; flexible CG."""
+import numpy as np
+import pytest
+import torch
+
+import unet_oracle as U
+
+pytestmark = pytest.mark.gpu
+
+# BF16-emulating oracle: differences come from FP32 accumulation order only, amplified where a
+# value lands on the other side of a BF16 rounding boundary (the oracle itself moves by up to
+# 2e-3 relative L2 under a 1e-7 relative perturbation of its parameters)
+REL_EMULATED = 6e-3
+# exact FP64 network: the BF16 storage of weights and activations
+REL_EXACT = 3e-2
+
+
+def _rel(a, b):
+    return float(np.linalg.norm(np.asarray(a) - np.asarray(b)) / np.linalg.norm(np.asarray(b)))
+
+
+def _problem(seed, B, H, W):
+    from lentils_gb300 import learned
+    rng = np.random.default_rng(seed)
+    p = learned.init_params(seed, out_scale=1.0)
+    # non-zero biases exercise the bias paths
+    o = 0
+    for ci, co, k, _, _ in learned.LAYERS:
+        o += co * k * k * ci
+        p[o:o + co] = rng.normal(0, 0.05, co)
+        o += co
+    x = rng.normal(size=(B, H, W)).astype(np.float32)
+    f = rng.normal(size=(B, H, W)).astype(np.float32)
+    t = rng.normal(size=(B, H, W)).astype(np.float32)
+    return p, x, f, t
+
+
+def _cuda(*a):
+    return [torch.as_tensor(v).cuda() for v in a]
+
+
+@pytest.mark.parametrize("B,H,W", [(1, 16, 16), (2, 32, 48), (3, 64, 64)])
+def test_unet_forward_matches_oracle(native, B, H, W):
+    from lentils_gb300 import learned
+    p, x, f, _ = _problem(10 + H, B, H, W)
+    net = learned.UNet(H, W, max_batch=B, params=p)
+    xc, fc = _cuda(x, f)
+    out = net.forward(xc, fc).cpu().numpy()
+    assert net.error_flag() == 0
+    ref_e = U.forward(p, x, f, emulate_bf16=True)
+    ref_x = U.forward(p, x, f, emulate_bf16=False)
+    assert _rel(out, ref_e) < REL_EMULATED
+    assert _rel(out, ref_x) < REL_EXACT
+
+
+@pytest.mark.parametrize("B,H,W", [(1, 16, 16), (2, 32, 32)])
+def test_unet_gradients_match_oracle(native, B, H, W):
+    from lentils_gb300 import learned
+    p, x, f, t = _problem(20 + H, B, H, W)
+    net = learned.UNet(H, W, max_batch=B, params=p)
+    xc, fc, tc = _cuda(x, f, t)
+    g, loss = net.gradients(xc, fc, tc)
+    assert net.error_flag() == 0
+    le, ge = U.loss_and_grads(p, x, f, t, emulate_bf16=True)
+    lx, gx = U.loss_and_grads(p, x, f, t, emulate_bf16=False)
+    assert abs(loss - le) <= 1e-3 * le
+    o = 0
+    for li, (ci, co, k, _, _) in enumerate(learned.LAYERS):
+        n = co * k * k * ci
+        for name, sl in (("w", slice(o, o + n)), ("b", slice(o + n, o + n + co))):
+            assert _rel(g[sl], ge[sl]) < 1e-2, (li, name, _rel(g[sl], ge[sl]))
+            # against the exact network only the weights: a bias gradient is a sum over pixels
+            # of residuals that largely cancel, so BF16 storage moves it by its own size
+            if name == "w":
+                assert _rel(g[sl], gx[sl]) < 1e-1, (li, name, _rel(g[sl], gx[sl]))
+        o += n + co
+    assert _rel(g, ge) < 5e-3
+    assert _rel(g, gx) < 1e-1
+
+
+def test_unet_adam_overfits_one_batch(native):
+    from lentils_gb300 import learned
+    p, x, f, _ = _problem(31, 4, 32, 32)
+    # a smooth target the network can represent
+    yy, xx = np.meshgrid(np.linspace(-1, 1, 32), np.linspace(-1, 1, 32), indexing="ij")
+    t = np.broadcast_to(np.sin(2 * xx) * np.cos(3 * yy), (4, 32, 32)).astype(np.float32).copy()
+    net = learned.UNet(32, 32, max_batch=4, params=learned.init_params(5))
+    xc, fc, tc = _cuda(x, f, t)
+    _, l0 = net.gradients(xc, fc, tc)
+    lbuf = torch.zeros(1, device="cuda")
+    for _ in range(150):
+        net.train_step(xc, fc, tc, 2e-3, lbuf)
+    _, l1 = net.gradients(xc, fc, tc)
+    assert net.error_flag() == 0
+    assert l1 < 0.1 * l0, (l0, l1)
+
+
+def test_unet_precondition_form(native):
+    from lentils_gb300 import learned
+    H = W = 32
+    rng = np.random.default_rng(7)
+    net = learned.UNet(H, W, max_batch=1, params=learned.init_params(2, out_scale=1.0))
+    r = torch.as_tensor(rng.normal(size=(H, W)).astype(np.float32)).cuda()
+    dinv = torch.as_tensor(np.exp(rng.normal(size=(H, W))).astype(np.float32)).cuda()
+    feat = learned.features(dinv.reshape(-1)).reshape(H, W)
+    ref_feat = torch.log(dinv.double()) - torch.log(dinv.double()).mean()
+    assert torch.allclose(feat.double(), ref_feat, atol=1e-5)
+    z = net.precondition(r, dinv, feat)
+    xs, fs = learned.scaled_inputs(r[None], dinv[None], feat[None])
+    out = net.forward(xs, fs)[0]
+    u = dinv * r
+    s = torch.sqrt(torch.mean(u.double() ** 2)).float()
+    assert _rel(z.cpu().numpy(), (u + s * out).cpu().numpy()) < 1e-5
+
+
+@pytest.mark.parametrize("with_net", [False, True])
+@pytest.mark.parametrize("use_graph", [True, False])
+def test_flexible_cg_reaches_true_residual(native, with_net, use_graph):
+    """Flexible CG (Jacobi directions only, or an untrained network with the Jacobi fallback)
+    reaches a true FP64 relative residual of 1e-6, checked again with the oracle operator."""
+    import oracle as O
+    from lentils_gb300 import learned
+    from test_operators_gpu import _inversion, _oracle_normal
+    rng = np.random.default_rng(29)
+    inv, img, src, four, uvw, d = _inversion(rng, n_img=96, n_src=48, nvis=8000)
+    net = learned.UNet(48, 48, max_batch=1, params=learned.init_params(3)) if with_net else None
+    x, info = inv.solve_flexible(net, tol=1e-6, use_graph=use_graph)
+    assert info["converged"] == 1, info
+    pts = inv.lens.source_points.cpu().numpy()
+    A, rhs = _oracle_normal(img, src, four, uvw, pts, np.ones(uvw.shape[0]), 1e-2)
+    b = rhs(d)
+    assert np.linalg.norm(b - A(x.cpu().numpy())) / np.linalg.norm(b) < 1.5e-6
+    if not with_net:
+        _, ref = inv.solve(tol=1e-6, use_graph=use_graph)
+        assert info["inner_total"] <= 1.2 * ref["inner_total"] + 10, (info, ref)
