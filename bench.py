@@ -53,14 +53,12 @@ def workload_config():
 
 def make_uv():
     import numpy as np
-    sys.path.insert(0, os.path.join(REPO, "oracle"))
-    import oracle as O  # synthetic-input generator only (not the measured path)
+    from lentils_gb300.spaces import ImageSpace
+    from lentils_gb300.synthetic import padded_fourier_space, synth_uv_blobs
     rng = np.random.default_rng(SEED)
     half = 0.5 * IMG * PIX
-    img = O.ImageGeom((IMG, IMG), [(-half, half), (-half, half)])
-    padded, _, _ = O.padded_geom(img, 2)
-    four = O.FourierGeom(padded)
-    uvw = O.synth_uv_blobs(rng, NVIS, four, 0.48, WSUP)
+    four = padded_fourier_space(ImageSpace((IMG, IMG), [(-half, half), (-half, half)]), 2)
+    uvw = synth_uv_blobs(rng, NVIS, four, 0.48, WSUP)
     return four, uvw
 
 
@@ -148,8 +146,19 @@ def cpu_reference_lib():
     return O, False
 
 
+def _oracle_fourier(O, four):
+    """The oracle's geometry record for a package FourierSpace."""
+    import numpy as np
+    f = O.FourierGeom.__new__(O.FourierGeom)
+    f.nu, f.nv, f.half_nv = int(four.nu), int(four.nv), int(four.half_nv)
+    f.du, f.dv, f.gcx, f.gcy = float(four.du), float(four.dv), float(four.gcx), float(four.gcy)
+    f._chan = np.zeros(1)
+    return f
+
+
 def time_cpu_gridder(O, use_ref, four, uvw, nsample, reps=1):
     import numpy as np
+    four = _oracle_fourier(O, four)
     rng = np.random.default_rng(SEED + 1)
     idx = rng.choice(uvw.shape[0], nsample, replace=False)
     vis = O.VisGeom(uvw[idx], [1.0])
@@ -343,63 +352,66 @@ def run_ours(args):
 
 # CG source inversion (512^2 image plane, 128^2 source grid, 2e6 visibilities, PEMD b=1.2",
 # q=0.7, gamma=2.0 + external shear (0.05, 20 deg), lambda=1e-2 gradient prior, sigma=1).
-CG_IMG, CG_PIX, CG_SRC, CG_SRC_HALF, CG_NVIS, CG_LAMBDA = 512, 0.01, 128, 0.64, 2_000_000, 1e-2
-
-
-def cg_problem(seed=SEED + 7):
-    import numpy as np
-    sys.path.insert(0, os.path.join(REPO, "oracle"))
-    import oracle as O  # synthetic-input generator only
-    from lentils_gb300.lens_models import ExternalPotential, GlobalLensModel, PowerLawEllipsoid
-    from lentils_gb300.operators import BilinearLensOperator, NUFFTOperator
-    from lentils_gb300.spaces import ImageSpace, VisibilitySpace
-    rng = np.random.default_rng(seed)
-    half = 0.5 * CG_IMG * CG_PIX
-    ims = ImageSpace((CG_IMG, CG_IMG), [(-half, half), (-half, half)])
-    srcs = ImageSpace((CG_SRC, CG_SRC), [(-CG_SRC_HALF, CG_SRC_HALF), (-CG_SRC_HALF, CG_SRC_HALF)])
-    img = O.ImageGeom((CG_IMG, CG_IMG), [(-half, half), (-half, half)])
-    four = O.FourierGeom(O.padded_geom(img, 2)[0])
-    uvw = O.synth_uv(rng, CG_NVIS, four, 0.45, 4)
-    c = 0.25 * CG_PIX  # lens centre off the pixel corners (the PEMD is singular at its centre)
-    glm = GlobalLensModel([PowerLawEllipsoid(z=0.5, b=1.2, th=0.0, f=0.7, x=c, y=c, rc=0.0,
-                                             qh=0.5),
-                           ExternalPotential(z=0.5, x=c, y=c, ss=0.05, sa=20.0)])
-    vs = VisibilitySpace(channels=[1.0], uvcoords=uvw)
-    xs = (srcs.xmin + srcs.dx * np.arange(CG_SRC))[:, None]
-    ys = (srcs.ymin + srcs.dy * np.arange(CG_SRC))[None, :]
-    s_true = (np.exp(-((xs - 0.05) ** 2 + (ys - 0.02) ** 2) / (2 * 0.06 ** 2))
-              + 0.5 * np.exp(-((xs + 0.1) ** 2 + (ys + 0.08) ** 2) / (2 * 0.04 ** 2)))
-    F = NUFFTOperator(vs, ims)
-    L = BilinearLensOperator(ims, srcs, glm, z_src=2.0)
-    d = (F * (L * s_true)).reshape(-1) + O.complex_normal(rng, CG_NVIS)
-    del F, L
-    return vs, d, ims, srcs, glm
-
-
-def run_cg_bench():
-    """Plain Jacobi-CG (FP32 operator, FP64 refinement, CUDA-graph inner iterations) to a true
-    FP64 relative residual of 1e-6 on the full-size inversion."""
+def run_cg_bench(repeats=3):
+    """CG source inversion to a true FP64 relative residual of 1e-6 (FP32 operator inside FP64
+    iterative refinement, CUDA-graph inner iterations), three ways, each the best of `repeats`
+    solves after a warm-up solve: plain Jacobi-PCG; flexible CG with Jacobi directions and an
+    8-direction A-orthogonalisation window; the same with the learned preconditioner
+    (committed weights, trained on the GPU by lentils_gb300.train_preconditioner)."""
+    import ctypes
     import torch
-    from lentils_gb300.inversion import SourceInversion
-    vs, d, ims, srcs, glm = cg_problem()
+    from lentils_gb300 import _native as N
+    from lentils_gb300 import learned, workloads
+    from lentils_gb300 import train_preconditioner as T
+    from lentils_gb300.gridding import _ptr
     t0 = time.perf_counter()
-    inv = SourceInversion(vs, d, 1.0, ims, srcs, glm, 2.0, CG_LAMBDA)
+    inv, _, _ = workloads.inversion()
     setup_s = time.perf_counter() - t0
-    inv.solve(tol=1e-2, use_graph=True)  # warm-up (graph capture, cuFFT plans, caches)
-    x, info = inv.solve(tol=1e-6, use_graph=True)
-    # one FP32 and one FP64 matvec, timed with events on the solver's stream
+    params, meta = T.load(T.DEFAULT_WEIGHTS)
+    net = learned.UNet(workloads.SRC, workloads.SRC, max_batch=1, params=params)
+    net.set_jacobi_weight(0.3)
+    inner_tol = 1e-3
+    runs = {
+        "plain_jacobi_pcg": lambda tol: inv.solve(tol=tol, inner_tol=inner_tol),
+        "jacobi_fcg8": lambda tol: inv.solve_flexible(None, tol=tol, inner_tol=inner_tol,
+                                                      window=8),
+        "learned_fcg8": lambda tol: inv.solve_flexible(net, tol=tol, inner_tol=inner_tol,
+                                                       window=8),
+    }
+    out = {"workload": workloads.DESCRIPTION, "tol": 1e-6, "inner_tol": inner_tol,
+           "setup_s": setup_s}
+    for name, fn in runs.items():
+        fn(1e-2)  # warm-up: graph capture, cuFFT plans, caches
+        best = None
+        for _ in range(repeats):
+            _, info = fn(1e-6)
+            if best is None or info["seconds"] < best["seconds"]:
+                best = info
+        out[name] = {"converged": best["converged"], "rel_residual_fp64": best["rel_residual"],
+                     "outer": best["outer"], "inner_iterations": best["inner_total"],
+                     "solve_s": best["seconds"]}
+        if name == "learned_fcg8":
+            out[name].update({"net_iterations": best["net_iterations"],
+                              "fallback": best["fallback"], "jacobi_weight": 0.3,
+                              "training": {k: meta[k] for k in ("draws", "pairs", "steps",
+                                                                "loss")}})
+    p, lr = out["plain_jacobi_pcg"], out["learned_fcg8"]
+    out["learned_vs_plain_time"] = p["solve_s"] / lr["solve_s"]
+    out["learned_vs_plain_iterations"] = p["inner_iterations"] / max(1, lr["inner_iterations"])
+    out["learned_vs_jacobi_fcg8_time"] = out["jacobi_fcg8"]["solve_s"] / lr["solve_s"]
+    # per-iteration pieces, timed with events on the solver's stream
     s32 = torch.randn(inv.nsrc, device="cuda", dtype=torch.float32)
     s64 = s32.double()
-    ev = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
-    import ctypes
-    from lentils_gb300 import _native as N
-    from lentils_gb300.gridding import _ptr
-    o32 = torch.empty_like(s32)
-    o64 = torch.empty_like(s64)
+    o32, o64 = torch.empty_like(s32), torch.empty_like(s64)
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(6)]
     sp = ctypes.c_void_p(inv.stream.cuda_stream)
     L = N.lib()
+    dinv, feat = inv.inv_diag32, learned.features(inv.inv_diag32)
+    torch.cuda.synchronize()
     for _ in range(3):
         N.check(L.lentils_normal_op_apply(inv.handle, _ptr(s32), _ptr(o32), sp))
+        N.check(L.lentils_unet_precondition(net.handle, _ptr(s32), _ptr(dinv), _ptr(feat),
+                                            _ptr(o32), sp))
     ev[0].record(inv.stream)
     for _ in range(10):
         N.check(L.lentils_normal_op_apply(inv.handle, _ptr(s32), _ptr(o32), sp))
@@ -408,14 +420,15 @@ def run_cg_bench():
     ev[2].record(inv.stream)
     N.check(L.lentils_normal_op_apply64(inv.handle, _ptr(s64), _ptr(o64), sp))
     ev[3].record(inv.stream)
+    for _ in range(10):
+        N.check(L.lentils_unet_precondition(net.handle, _ptr(s32), _ptr(dinv), _ptr(feat),
+                                            _ptr(o32), sp))
+    ev[4].record(inv.stream)
     torch.cuda.synchronize()
-    return {"workload": "CG source inversion: 512^2 image (0.01\"), 128^2 source, 2e6 vis, "
-                        "PEMD b=1.2 q=0.7 gamma=2 + shear (0.05, 20 deg), lambda=1e-2",
-            "preconditioner": "jacobi", "tol": 1e-6, "converged": info["converged"],
-            "rel_residual_fp64": info["rel_residual"], "outer": info["outer"],
-            "inner_iterations": info["inner_total"], "solve_s": info["seconds"],
-            "setup_s": setup_s, "matvec32_ms": ev[0].elapsed_time(ev[1]) / 10,
-            "matvec64_ms": ev[2].elapsed_time(ev[3])}
+    out.update({"matvec32_ms": ev[0].elapsed_time(ev[1]) / 10,
+                "matvec64_ms": ev[2].elapsed_time(ev[3]),
+                "precondition_ms": ev[3].elapsed_time(ev[4]) / 10})
+    return out
 
 
 def cpu_baseline(four, uvw):

@@ -307,6 +307,8 @@ typedef struct {
     int max_inner;
     int check_every;   /* inner iterations between host reads of the residual norm         */
     int use_graph;     /* capture one inner iteration in a CUDA graph and replay it        */
+    int window;        /* lentils_fcg_solve: directions kept for A-orthogonalisation (1-8;
+                          0 means 1); ignored by lentils_cg_solve                          */
 } lentils_cg_options;
 
 typedef struct {
@@ -315,6 +317,8 @@ typedef struct {
     int inner_total;
     double rel_residual; /* final true FP64 relative residual */
     double seconds;      /* wall time of the solve            */
+    int net_iterations;  /* flexible CG: iterations that took the network's direction */
+    int fallback;        /* flexible CG: 1 if it switched to plain Jacobi-CG on stagnation */
 } lentils_cg_result;
 
 /* Iterative refinement: outer FP64 residuals r = b - A x, inner Jacobi-preconditioned CG with
@@ -355,8 +359,10 @@ int lentils_tc_gemm_bf16(const void *A, const void *B, float *C, int M, int N, i
  *
  * Preconditioner form (lentils_unet_precondition, lentils_fcg_solve):
  *   u = dinv * r,  s = rms(u),  f = log(dinv) - mean(log(dinv))
- *   z = u + s * net(u / s, f)
- * so the network learns the correction over Jacobi in units of the scaled residual.
+ *   z = gamma * u + s * net(u / s, f)
+ * The network is trained to give the direction of the error e = A^-1 r (target e / rms(e));
+ * flexible CG is invariant to the scale of z. gamma (lentils_unet_set_jacobi_weight, default
+ * 0) adds a share of the Jacobi direction.
  * ---------------------------------------------------------------------------------------- */
 typedef struct lentils_unet lentils_unet;
 long long lentils_unet_param_count(void);
@@ -375,6 +381,13 @@ int lentils_unet_gradients(lentils_unet *net, const float *r, const float *d, co
  * (device float, may be NULL) receives the batch loss before the step; no synchronisation */
 int lentils_unet_train_step(lentils_unet *net, const float *r, const float *d, const float *tgt,
                             int B, float lr, float *loss_dev, void *stream);
+/* backward pass from the activations of the most recent lentils_unet_forward (same B) for an
+ * external gradient dout (B, H, W) FP32 (device) of the output; then an Adam step if lr > 0,
+ * and a copy of the flat parameter gradient to HOST grad_host if non-NULL (synchronising) */
+int lentils_unet_backward(lentils_unet *net, const float *dout, int B, float lr,
+                          float *grad_host, void *stream);
+/* gamma of the preconditioner form (default 0) */
+int lentils_unet_set_jacobi_weight(lentils_unet *net, float gamma);
 /* 1 if a bounded tensor-core wait gave up since creation (results then invalid) */
 int lentils_unet_error_flag(lentils_unet *net, int *flag);
 /* f = log(dinv) - mean(log(dinv)) over n values (device) */
@@ -382,11 +395,12 @@ int lentils_unet_features(const float *dinv, float *feat, int n, void *stream);
 /* z = M(r) for one H x W residual (device FP32), the preconditioner form above */
 int lentils_unet_precondition(lentils_unet *net, const float *r, const float *dinv,
                               const float *feat, float *z, void *stream);
-/* Flexible CG (one-vector orthogonalisation, beta = -(z . A p) / (p . A p)) on the normal
- * equations with the learned preconditioner inside the same FP64 iterative refinement as
+/* Truncated flexible CG (each new direction A-orthogonalised against the last opt->window
+ * directions: p = d - sum_j (d . A p_j) / (p_j . A p_j) p_j) on the normal equations with the learned preconditioner inside the same FP64 iterative refinement as
  * lentils_cg_solve. Where the network's direction is not a descent direction (z . r <= 0)
- * that iteration uses the Jacobi direction instead; net = NULL runs the same iteration with
- * Jacobi only. */
+ * that iteration uses the Jacobi direction instead; if the inner residual has not halved over
+ * the last 20 checks (20 * check_every iterations), the solve continues as plain Jacobi-CG
+ * (res->fallback = 1). net = NULL runs the same iteration with Jacobi only. */
 int lentils_fcg_solve(lentils_normal_op *op, const double *b, double *x, const float *inv_diag32,
                       lentils_unet *net, const lentils_cg_options *opt, lentils_cg_result *res,
                       void *stream);

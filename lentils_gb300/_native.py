@@ -60,12 +60,14 @@ class GridDescC(Structure):
 
 class CGOptionsC(Structure):
     _fields_ = [("tol", c_double), ("inner_tol", c_double), ("max_outer", c_int),
-                ("max_inner", c_int), ("check_every", c_int), ("use_graph", c_int)]
+                ("max_inner", c_int), ("check_every", c_int), ("use_graph", c_int),
+                ("window", c_int)]
 
 
 class CGResultC(Structure):
     _fields_ = [("converged", c_int), ("outer", c_int), ("inner_total", c_int),
-                ("rel_residual", c_double), ("seconds", c_double)]
+                ("rel_residual", c_double), ("seconds", c_double), ("net_iterations", c_int),
+                ("fallback", c_int)]
 
 
 class PlanStatsC(Structure):
@@ -146,6 +148,8 @@ _SIGNATURES = [
     ("lentils_unet_train_step", c_int, [c_void_p, c_void_p, c_void_p, c_void_p, c_int, c_float,
                                         c_void_p, c_void_p]),
     ("lentils_unet_error_flag", c_int, [c_void_p, POINTER(c_int)]),
+    ("lentils_unet_set_jacobi_weight", c_int, [c_void_p, c_float]),
+    ("lentils_unet_backward", c_int, [c_void_p, c_void_p, c_int, c_float, c_void_p, c_void_p]),
     ("lentils_unet_features", c_int, [c_void_p, c_void_p, c_int, c_void_p]),
     ("lentils_unet_precondition", c_int, [c_void_p, c_void_p, c_void_p, c_void_p, c_void_p,
                                           c_void_p]),

@@ -269,7 +269,7 @@ __global__ void jacobi_kernel(const double *__restrict__ dltl, double wsum, doub
 
 // -- flexible CG (learned preconditioner) --------------------------------------------------------
 struct FCGScalars {
-    double pap, pr, alpha, beta, rr, rr0, use_net, fallbacks;
+    double pap, pr, alpha, beta, rr, rr0, use_net, fallbacks, net_iters, pad;
 };
 
 // partials of p.ap and p.r
@@ -339,65 +339,135 @@ __global__ void fcg_rr_kernel(const double *__restrict__ partial, int np, FCGSca
     }
 }
 
-// partials of z.ap, z.r and j.ap, with j = dinv r the Jacobi direction (z null: Jacobi only)
-__global__ void __launch_bounds__(256)
-    fcg_beta_dots_kernel(const float *__restrict__ z, const float *__restrict__ r,
-                         const float *__restrict__ ap, const float *__restrict__ dinv, int n,
-                         double *__restrict__ partial)
+// Truncated flexible CG keeps the last `m` directions P[j] and their images Q[j] = A P[j]
+// (ring buffers, fixed device addresses so that one iteration replays as a CUDA graph; the
+// ring position lives in device memory).
+constexpr int kMaxWindow = 8;
+struct FCGWindow {
+    double pq[kMaxWindow];    // P[j] . Q[j]
+    double beta[kMaxWindow];  // coefficients of the current orthogonalisation
+    int slot, count, m, pad;
+};
+
+// P[slot] = p, Q[slot] = ap, pq[slot] = p . ap (from the alpha step)
+__global__ void fcg_store_kernel(const float *__restrict__ p, const float *__restrict__ ap,
+                                 float *__restrict__ P, float *__restrict__ Q,
+                                 const FCGScalars *__restrict__ sc, FCGWindow *__restrict__ win,
+                                 int n)
 {
-    __shared__ double sh[8];
-    double zap = 0.0, zr = 0.0, jap = 0.0;
+    const int slot = win->slot;
+    float *ps = P + (size_t)slot * n;
+    float *qs = Q + (size_t)slot * n;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        const double j = (double)dinv[i] * (double)r[i];
-        const double zi = z ? (double)z[i] : j;
-        zap += zi * (double)ap[i];
-        zr += zi * (double)r[i];
-        jap += j * (double)ap[i];
+        ps[i] = p[i];
+        qs[i] = ap[i];
     }
-    const double a = block_sum(zap, sh);
-    const double b = block_sum(zr, sh);
-    const double c = block_sum(jap, sh);
-    if (threadIdx.x == 0) {
-        partial[blockIdx.x] = a;
-        partial[gridDim.x + blockIdx.x] = b;
-        partial[2 * gridDim.x + blockIdx.x] = c;
-    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) win->pq[slot] = sc->pap;
 }
 
-// beta = -(dir . ap) / (p . ap), dir = the network's z where it is a descent direction
-// (z . r > 0), else the Jacobi direction
-__global__ void fcg_beta_kernel(const double *__restrict__ partial, int np, FCGScalars *sc,
-                                int have_net)
+// partials of z.r and j.r, j = dinv r the Jacobi direction (z null: Jacobi only)
+__global__ void __launch_bounds__(256)
+    fcg_descent_dots_kernel(const float *__restrict__ z, const float *__restrict__ r,
+                            const float *__restrict__ dinv, int n, double *__restrict__ partial)
 {
     __shared__ double sh[8];
-    double a = 0.0, b = 0.0, c = 0.0;
-    for (int i = threadIdx.x; i < np; i += blockDim.x) {
-        a += partial[i];
-        b += partial[np + i];
-        c += partial[2 * np + i];
+    double zr = 0.0;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const double ri = (double)r[i];
+        const double zi = z ? (double)z[i] : (double)dinv[i] * ri;
+        zr += zi * ri;
     }
-    const double zap = block_sum(a, sh);
-    const double zr = block_sum(b, sh);
-    const double jap = block_sum(c, sh);
+    const double t = block_sum(zr, sh);
+    if (threadIdx.x == 0) partial[blockIdx.x] = t;
+}
+
+// the network's z is used where it is a descent direction (z . r > 0), else dinv r
+__global__ void fcg_select_kernel(const double *__restrict__ partial, int np, FCGScalars *sc,
+                                  int have_net)
+{
+    __shared__ double sh[8];
+    double a = 0.0;
+    for (int i = threadIdx.x; i < np; i += blockDim.x) a += partial[i];
+    const double zr = block_sum(a, sh);
     if (threadIdx.x == 0) {
-        const bool net_ok = have_net && zr > 0.0 && zap == zap;
+        const bool net_ok = have_net && zr > 0.0 && zr < 1e300;
         sc->use_net = net_ok ? 1.0 : 0.0;
         if (have_net && !net_ok) sc->fallbacks += 1.0;
-        const double num = net_ok ? zap : jap;
-        sc->beta = (sc->pap != 0.0) ? -num / sc->pap : 0.0;
+        if (net_ok) sc->net_iters += 1.0;
     }
 }
 
-// p = dir + beta p
-__global__ void fcg_p_kernel(float *__restrict__ p, const float *__restrict__ z,
-                             const float *__restrict__ r, const float *__restrict__ dinv,
-                             const FCGScalars *__restrict__ sc, int n)
+// dir = z (network) or dinv r (Jacobi), written to d
+__global__ void fcg_dir_kernel(const float *__restrict__ z, const float *__restrict__ r,
+                               const float *__restrict__ dinv, const FCGScalars *__restrict__ sc,
+                               float *__restrict__ d, int n)
 {
-    const float beta = (float)sc->beta;
     const bool net = z && sc->use_net != 0.0;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+        d[i] = net ? z[i] : dinv[i] * r[i];
+}
+
+// partials of d . Q[j] for j < m (blocks x m)
+__global__ void __launch_bounds__(256)
+    fcg_window_dots_kernel(const float *__restrict__ d, const float *__restrict__ Q, int m, int n,
+                           double *__restrict__ partial)
+{
+    __shared__ double sh[8];
+    double acc[kMaxWindow];
+#pragma unroll
+    for (int j = 0; j < kMaxWindow; ++j) acc[j] = 0.0;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        const float d = net ? z[i] : dinv[i] * r[i];
-        p[i] = fmaf(beta, p[i], d);
+        const double di = (double)d[i];
+#pragma unroll
+        for (int j = 0; j < kMaxWindow; ++j)
+            if (j < m) acc[j] += di * (double)Q[(size_t)j * n + i];
+    }
+    for (int j = 0; j < m; ++j) {
+        const double t = block_sum(acc[j], sh);
+        if (threadIdx.x == 0) partial[j * gridDim.x + blockIdx.x] = t;
+    }
+}
+
+// beta_j = -(d . Q[j]) / pq[j] over the stored directions (the one just stored included);
+// then the ring advances. first != 0 (start of an inner solve): no stored directions.
+__global__ void fcg_window_beta_kernel(const double *__restrict__ partial, int np,
+                                       FCGWindow *__restrict__ win, int first)
+{
+    __shared__ double sh[8];
+    const int m = win->m;
+    const int valid = first ? 0 : min(win->count + 1, m);
+    for (int j = 0; j < m; ++j) {
+        double a = 0.0;
+        if (j < valid)
+            for (int i = threadIdx.x; i < np; i += blockDim.x) a += partial[j * np + i];
+        const double t = block_sum(a, sh);
+        if (threadIdx.x == 0)
+            win->beta[j] = (j < valid && win->pq[j] != 0.0) ? -t / win->pq[j] : 0.0;
+    }
+    if (threadIdx.x == 0) {
+        if (first) {
+            win->count = 0;
+            win->slot = 0;
+        } else {
+            win->count = valid;
+            win->slot = (win->slot + 1) % m;
+        }
+    }
+}
+
+// p = d + sum_j beta_j P[j]
+__global__ void fcg_window_p_kernel(float *__restrict__ p, const float *__restrict__ d,
+                                    const float *__restrict__ P,
+                                    const FCGWindow *__restrict__ win, int n)
+{
+    __shared__ float beta[kMaxWindow];
+    const int m = win->m;
+    if (threadIdx.x < kMaxWindow) beta[threadIdx.x] = (threadIdx.x < m) ? (float)win->beta[threadIdx.x] : 0.f;
+    __syncthreads();
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        float v = d[i];
+        for (int j = 0; j < m; ++j) v = fmaf(beta[j], P[(size_t)j * n + i], v);
+        p[i] = v;
     }
 }
 
@@ -751,10 +821,12 @@ int lentils_fcg_solve(lentils_normal_op *op, const double *b, double *x, const f
     memset(res, 0, sizeof(*res));
     cudaStream_t s = (cudaStream_t)stream;
     const int n = op->nsrc;
+    const int m = std::min(kMaxWindow, std::max(1, opt->window));
     float *e32 = nullptr, *r32 = nullptr, *z32 = nullptr, *p32 = nullptr, *ap32 = nullptr,
-          *feat = nullptr;
+          *feat = nullptr, *d32 = nullptr, *Pw = nullptr, *Qw = nullptr;
     double *r64 = nullptr, *ax64 = nullptr, *partial = nullptr, *scal = nullptr;
     FCGScalars *sc = nullptr;
+    FCGWindow *win = nullptr;
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t gexec = nullptr;
     int st = LENTILS_OK;
@@ -764,25 +836,43 @@ int lentils_fcg_solve(lentils_normal_op *op, const double *b, double *x, const f
     if (e == cudaSuccess) e = cudaMalloc(&p32, sizeof(float) * n);
     if (e == cudaSuccess) e = cudaMalloc(&ap32, sizeof(float) * n);
     if (e == cudaSuccess) e = cudaMalloc(&feat, sizeof(float) * n);
+    if (e == cudaSuccess) e = cudaMalloc(&d32, sizeof(float) * n);
+    if (e == cudaSuccess) e = cudaMalloc(&Pw, sizeof(float) * n * m);
+    if (e == cudaSuccess) e = cudaMalloc(&Qw, sizeof(float) * n * m);
     if (e == cudaSuccess) e = cudaMalloc(&r64, sizeof(double) * n);
     if (e == cudaSuccess) e = cudaMalloc(&ax64, sizeof(double) * n);
-    if (e == cudaSuccess) e = cudaMalloc(&partial, sizeof(double) * 3 * kRedBlocks);
+    if (e == cudaSuccess) e = cudaMalloc(&partial, sizeof(double) * kMaxWindow * kRedBlocks);
     if (e == cudaSuccess) e = cudaMalloc(&scal, sizeof(double) * 2);
     if (e == cudaSuccess) e = cudaMalloc(&sc, sizeof(FCGScalars));
+    if (e == cudaSuccess) e = cudaMalloc(&win, sizeof(FCGWindow));
     if (e == cudaSuccess) e = cudaMemsetAsync(sc, 0, sizeof(FCGScalars), s);
+    // unused ring slots enter the direction update with a zero coefficient: keep them finite
+    if (e == cudaSuccess) e = cudaMemsetAsync(Pw, 0, sizeof(float) * n * m, s);
+    if (e == cudaSuccess) e = cudaMemsetAsync(Qw, 0, sizeof(float) * n * m, s);
+    if (e == cudaSuccess) {
+        FCGWindow hw;
+        memset(&hw, 0, sizeof(hw));
+        hw.m = m;
+        e = cudaMemcpy(win, &hw, sizeof(hw), cudaMemcpyHostToDevice);
+    }
     if (e != cudaSuccess) st = cuda_status(e, "fcg_solve alloc");
     if (!st && net) st = lentils_unet_features(inv_diag32, feat, n, stream);
     if (!st && net) st = unet_prepare(net);
-    float *zdir = net ? z32 : nullptr;
+    bool use_net = net != nullptr;  // false after a stagnation fallback
 
-    // direction step: z = M(r); beta; p = dir + beta p
-    auto direction = [&]() -> int {
-        if (net) {
+    // direction step: z = M(r); d = z or the Jacobi direction; p = d - sum_j (d.Q[j] / pq[j]) P[j]
+    auto direction = [&](bool first) -> int {
+        float *zdir = use_net ? z32 : nullptr;
+        if (use_net) {
             if (int q = unet_precondition(net, r32, inv_diag32, feat, z32, s)) return q;
+            fcg_descent_dots_kernel<<<kRedBlocks, 256, 0, s>>>(z32, r32, inv_diag32, n, partial);
+            fcg_select_kernel<<<1, 256, 0, s>>>(partial, kRedBlocks, sc, 1);
         }
-        fcg_beta_dots_kernel<<<kRedBlocks, 256, 0, s>>>(zdir, r32, ap32, inv_diag32, n, partial);
-        fcg_beta_kernel<<<1, 256, 0, s>>>(partial, kRedBlocks, sc, net ? 1 : 0);
-        fcg_p_kernel<<<nb(n), 256, 0, s>>>(p32, zdir, r32, inv_diag32, sc, n);
+        fcg_dir_kernel<<<nb(n), 256, 0, s>>>(zdir, r32, inv_diag32, sc, d32, n);
+        if (!first)
+            fcg_window_dots_kernel<<<kRedBlocks, 256, 0, s>>>(d32, Qw, m, n, partial);
+        fcg_window_beta_kernel<<<1, 256, 0, s>>>(partial, kRedBlocks, win, first ? 1 : 0);
+        fcg_window_p_kernel<<<nb(n), 256, 0, s>>>(p32, d32, Pw, win, n);
         cudaError_t le = cudaGetLastError();
         return le == cudaSuccess ? LENTILS_OK : cuda_status(le, "fcg direction");
     };
@@ -793,7 +883,8 @@ int lentils_fcg_solve(lentils_normal_op *op, const double *b, double *x, const f
         fcg_alpha_kernel<<<1, 256, 0, s>>>(partial, kRedBlocks, sc);
         fcg_update_kernel<<<kRedBlocks, 256, 0, s>>>(e32, r32, p32, ap32, sc, n, partial);
         fcg_rr_kernel<<<1, 256, 0, s>>>(partial, kRedBlocks, sc, 0);
-        return direction();
+        fcg_store_kernel<<<nb(n), 256, 0, s>>>(p32, ap32, Pw, Qw, sc, win, n);
+        return direction(false);
     };
 
     const auto t0 = std::chrono::steady_clock::now();
@@ -806,30 +897,34 @@ int lentils_fcg_solve(lentils_normal_op *op, const double *b, double *x, const f
             rel = (bnorm > 0) ? sqrt(host_dot64(r64, r64, n, partial, scal, s)) / bnorm : 0.0;
         }
     }
-    if (!st && opt->use_graph) {
-        e = cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal);
-        if (e == cudaSuccess) {
-            const int q = inner_iteration();
-            cudaError_t ee = cudaStreamEndCapture(s, &graph);
-            if (q) st = q;
-            else if (ee != cudaSuccess) st = cuda_status(ee, "cudaStreamEndCapture");
-        } else {
-            st = cuda_status(e, "cudaStreamBeginCapture");
-        }
-        if (!st) {
-            e = cudaGraphInstantiate(&gexec, graph, 0);
-            if (e != cudaSuccess) st = cuda_status(e, "cudaGraphInstantiate");
-        }
-    }
-    int outer = 0, inner_total = 0;
+    // one inner iteration captured as a graph (again after a fallback changes the iteration)
+    auto capture = [&]() -> int {
+        if (gexec) cudaGraphExecDestroy(gexec);
+        if (graph) cudaGraphDestroy(graph);
+        gexec = nullptr;
+        graph = nullptr;
+        cudaError_t ce = cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal);
+        if (ce != cudaSuccess) return cuda_status(ce, "cudaStreamBeginCapture");
+        const int q = inner_iteration();
+        ce = cudaStreamEndCapture(s, &graph);
+        if (q) return q;
+        if (ce != cudaSuccess) return cuda_status(ce, "cudaStreamEndCapture");
+        ce = cudaGraphInstantiate(&gexec, graph, 0);
+        return ce == cudaSuccess ? LENTILS_OK : cuda_status(ce, "cudaGraphInstantiate");
+    };
+    if (!st && opt->use_graph) st = capture();
+    int outer = 0, inner_total = 0, fallback = 0;
     const int check = std::max(1, opt->check_every);
+    const int stall_checks = 20;
     while (!st && rel > opt->tol && outer < opt->max_outer) {
         ++outer;
         fcg_start_kernel<<<kRedBlocks, 256, 0, s>>>(r64, r32, e32, p32, ap32, n, partial);
         fcg_rr_kernel<<<1, 256, 0, s>>>(partial, kRedBlocks, sc, 1);
-        if ((st = direction())) break;
+        if ((st = direction(true))) break;
         FCGScalars hs;
         int k = 0;
+        double mark_rr = -1.0;
+        int mark_k = 0;
         while (k < opt->max_inner) {
             for (int c = 0; c < check && k < opt->max_inner; ++c, ++k) {
                 if (gexec) {
@@ -854,6 +949,16 @@ int lentils_fcg_solve(lentils_normal_op *op, const double *b, double *x, const f
                 break;
             }
             if (hs.rr <= opt->inner_tol * opt->inner_tol * hs.rr0) break;
+            // stagnation: the residual norm has not halved over the last stall_checks checks
+            if (mark_rr < 0.0 || hs.rr <= 0.25 * mark_rr) {
+                mark_rr = hs.rr;
+                mark_k = k;
+            } else if (use_net && k - mark_k >= stall_checks * check) {
+                use_net = false;
+                fallback = 1;
+                mark_k = k;
+                if (gexec && (st = capture())) break;
+            }
         }
         inner_total += k;
         if (st) break;
@@ -866,12 +971,20 @@ int lentils_fcg_solve(lentils_normal_op *op, const double *b, double *x, const f
         e = cudaStreamSynchronize(s);
         if (e != cudaSuccess) st = cuda_status(e, "fcg_solve sync");
     }
+    const auto t1 = std::chrono::steady_clock::now();
+    FCGScalars hs_end;
+    memset(&hs_end, 0, sizeof(hs_end));
+    if (!st) {
+        e = cudaMemcpy(&hs_end, sc, sizeof(FCGScalars), cudaMemcpyDeviceToHost);
+        if (e != cudaSuccess) st = cuda_status(e, "fcg_solve scalars");
+    }
     if (!st && net) {
         int flag = 0;
         st = unet_error_flag_device(net, &flag);
         if (!st && flag) st = set_error(LENTILS_ERR_TIMEOUT, "fcg_solve: a tensor-core wait gave up");
     }
-    const auto t1 = std::chrono::steady_clock::now();
+    res->net_iterations = (int)hs_end.net_iters;
+    res->fallback = fallback;
     res->converged = (!st && rel <= opt->tol) ? 1 : 0;
     res->outer = outer;
     res->inner_total = inner_total;
@@ -885,6 +998,10 @@ int lentils_fcg_solve(lentils_normal_op *op, const double *b, double *x, const f
     cudaFree(p32);
     cudaFree(ap32);
     cudaFree(feat);
+    cudaFree(d32);
+    cudaFree(Pw);
+    cudaFree(Qw);
+    cudaFree(win);
     cudaFree(r64);
     cudaFree(ax64);
     cudaFree(partial);

@@ -328,6 +328,21 @@ __global__ void mse_kernel(const float *__restrict__ out, const float *__restric
     if (threadIdx.x == 0) atomicAdd(loss, sh[0] / (float)npix);
 }
 
+// dy[pixel][0..31] = (dout[pixel], 0, ...): an external gradient of the output
+__global__ void pack_dout_kernel(const float *__restrict__ dout, bf16 *__restrict__ dy,
+                                 long long npix)
+{
+    LENTILS_GRID_STRIDE(p, npix)
+    {
+        bf16 v[8];
+        v[0] = __float2bfloat16(dout[p]);
+        for (int i = 1; i < 8; ++i) v[i] = __float2bfloat16(0.f);
+        uint4 *dst = reinterpret_cast<uint4 *>(dy + p * 32);
+        dst[0] = *reinterpret_cast<uint4 *>(v);
+        dst[1] = dst[2] = dst[3] = make_uint4(0, 0, 0, 0);
+    }
+}
+
 // db[co] += sum_pixel dy'[pixel][co]
 __global__ void bias_grad_kernel(const bf16 *__restrict__ dy, const bf16 *__restrict__ y,
                                  float *__restrict__ db, long long npix, int C, int creal)
@@ -394,7 +409,8 @@ __global__ void gather_wgrad_kernel(const float *__restrict__ gp, float *__restr
 }
 
 // Preconditioner pieces (one sample of n = H * W values):
-//   u = dinv * r, s = rms(u) (1 where u = 0), x0 = (u / s, feat, 0...), z = u + s * out
+//   u = dinv * r, s = rms(u) (1 where u = 0), x0 = (u / s, feat, 0...),
+//   z = gamma * u + s * out
 __global__ void __launch_bounds__(1024)
     precond_scale_kernel(const float *__restrict__ r, const float *__restrict__ dinv, int n,
                          float *__restrict__ scale)
@@ -434,11 +450,12 @@ __global__ void precond_input_kernel(const float *__restrict__ r, const float *_
 
 __global__ void precond_combine_kernel(const float *__restrict__ r, const float *__restrict__ dinv,
                                        const float *__restrict__ out,
-                                       const float *__restrict__ scale, float *__restrict__ z, int n)
+                                       const float *__restrict__ scale, float gamma,
+                                       float *__restrict__ z, int n)
 {
     const float s = scale[0];
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
-        z[i] = fmaf(s, out[i], dinv[i] * r[i]);
+        z[i] = fmaf(s, out[i], gamma * dinv[i] * r[i]);
 }
 
 // feat = log(dinv) - mean(log(dinv)), one block
@@ -468,6 +485,7 @@ __global__ void __launch_bounds__(1024)
 // ------------------------------------------------------------------------------------------------
 struct lentils_unet {
     int H, W, maxB;
+    float jacobi_weight;  // gamma of the preconditioner form
     long long nparams;
     // per layer
     float *w32[lentils::kNumLayers], *b32[lentils::kNumLayers];  // views into params
@@ -639,8 +657,10 @@ static int net_forward(lentils_unet *net, const float *r, const float *d, int Bn
     return net_layers_forward(net, Bn, s);
 }
 
-// gradients of the mean squared error against tgt (forward must have run for this batch)
-static int net_backward(lentils_unet *net, const float *tgt, int Bn, cudaStream_t s)
+// parameter gradients (forward must have run for this batch): of the mean squared error
+// against tgt, or, with dout, for the given gradient of the output
+static int net_backward(lentils_unet *net, const float *tgt, const float *dout, int Bn,
+                        cudaStream_t s)
 {
     const int H = net->H, W = net->W;
     const long long np0 = (long long)Bn * H * W;
@@ -651,7 +671,10 @@ static int net_backward(lentils_unet *net, const float *tgt, int Bn, cudaStream_
                                          sizeof(float) * c.cout_p * c.ks * c.ks * c.cin_p, s));
     }
     LENTILS_CUDA_TRY(cudaMemsetAsync(net->loss, 0, sizeof(float), s));
-    mse_kernel<<<blocks_n(np0), 256, 0, s>>>(net->out, tgt, net->dy_out, np0, net->loss);
+    if (dout)
+        pack_dout_kernel<<<blocks_n(np0), 256, 0, s>>>(dout, net->dy_out, np0);
+    else
+        mse_kernel<<<blocks_n(np0), 256, 0, s>>>(net->out, tgt, net->dy_out, np0, net->loss);
     int st;
     if ((st = layer_backward(net, 7, net->dy_out, nullptr, net->c1, net->d_c1, Bn, s))) return st;
     if ((st = layer_backward(net, 6, net->d_c1, net->c1, net->u1, net->d_u1, Bn, s))) return st;
@@ -708,7 +731,8 @@ int unet_precondition(lentils_unet *net, const float *r, const float *dinv, cons
     precond_input_kernel<<<blocks_n(n), 256, 0, s>>>(r, dinv, feat, net->pscale, net->x0, n);
     LENTILS_CHECK_LAUNCH("precond input");
     if (int st = net_layers_forward(net, 1, s)) return st;
-    precond_combine_kernel<<<blocks_n(n), 256, 0, s>>>(r, dinv, net->out, net->pscale, z, n);
+    precond_combine_kernel<<<blocks_n(n), 256, 0, s>>>(r, dinv, net->out, net->pscale,
+                                                       net->jacobi_weight, z, n);
     LENTILS_CHECK_LAUNCH("precond_combine_kernel");
     return LENTILS_OK;
 }
@@ -721,6 +745,18 @@ int unet_error_flag_device(lentils_unet *net, int *flag)
 {
     LENTILS_CUDA_TRY(cudaMemcpy(flag, net->err, sizeof(int), cudaMemcpyDeviceToHost));
     return LENTILS_OK;
+}
+
+static int adam_update(lentils_unet *net, float lr, cudaStream_t s)
+{
+    net->step += 1;
+    const float b1 = 0.9f, b2 = 0.999f;
+    const float c1 = 1.f - powf(b1, (float)net->step), c2 = 1.f - powf(b2, (float)net->step);
+    adam_kernel<<<blocks_n(net->nparams), 256, 0, s>>>(net->params, net->grads, net->adam_m,
+                                                       net->adam_v, net->nparams, lr, b1, b2,
+                                                       1e-8f, c1, c2);
+    LENTILS_CHECK_LAUNCH("adam_kernel");
+    return refresh_all(net, s);
 }
 
 }  // namespace lentils
@@ -910,7 +946,7 @@ int lentils_unet_gradients(lentils_unet *net, const float *r, const float *d, co
     cudaStream_t s = (cudaStream_t)stream;
     int st;
     if ((st = net_forward(net, r, d, Bn, s))) return st;
-    if ((st = net_backward(net, tgt, Bn, s))) return st;
+    if ((st = net_backward(net, tgt, nullptr, Bn, s))) return st;
     if (grad_host)
         LENTILS_CUDA_TRY(cudaMemcpyAsync(grad_host, net->grads, sizeof(float) * net->nparams, cudaMemcpyDeviceToHost, s));
     if (loss_host)
@@ -932,17 +968,38 @@ int lentils_unet_train_step(lentils_unet *net, const float *r, const float *d, c
     cudaStream_t s = (cudaStream_t)stream;
     int st;
     if ((st = net_forward(net, r, d, Bn, s))) return st;
-    if ((st = net_backward(net, tgt, Bn, s))) return st;
-    net->step += 1;
-    const float b1 = 0.9f, b2 = 0.999f;
-    const float c1 = 1.f - powf(b1, (float)net->step), c2 = 1.f - powf(b2, (float)net->step);
-    adam_kernel<<<blocks_n(net->nparams), 256, 0, s>>>(net->params, net->grads, net->adam_m,
-                                                       net->adam_v, net->nparams, lr, b1, b2,
-                                                       1e-8f, c1, c2);
-    LENTILS_CHECK_LAUNCH("adam_kernel");
-    if ((st = refresh_all(net, s))) return st;
+    if ((st = net_backward(net, tgt, nullptr, Bn, s))) return st;
+    if ((st = adam_update(net, lr, s))) return st;
     if (loss_dev)
         LENTILS_CUDA_TRY(cudaMemcpyAsync(loss_dev, net->loss, sizeof(float), cudaMemcpyDeviceToDevice, s));
+    return LENTILS_OK;
+}
+
+// backward from the most recent forward pass (same batch size) for an external gradient of
+// the output; optional Adam step (lr > 0) and copy of the flat gradient to host memory
+int lentils_unet_backward(lentils_unet *net, const float *dout, int Bn, float lr,
+                          float *grad_host, void *stream)
+{
+    clear_error();
+    if (!net || !dout || Bn < 1 || Bn > net->maxB)
+        return set_error(LENTILS_ERR_INVALID, "unet_backward: bad arguments");
+    cudaStream_t s = (cudaStream_t)stream;
+    int st;
+    if ((st = net_backward(net, nullptr, dout, Bn, s))) return st;
+    if (grad_host) {
+        LENTILS_CUDA_TRY(cudaMemcpyAsync(grad_host, net->grads, sizeof(float) * net->nparams,
+                                         cudaMemcpyDeviceToHost, s));
+        LENTILS_CUDA_TRY(cudaStreamSynchronize(s));
+    }
+    if (lr > 0.f && (st = adam_update(net, lr, s))) return st;
+    return LENTILS_OK;
+}
+
+int lentils_unet_set_jacobi_weight(lentils_unet *net, float gamma)
+{
+    clear_error();
+    if (!net || !(gamma >= 0.f)) return set_error(LENTILS_ERR_INVALID, "unet_set_jacobi_weight");
+    net->jacobi_weight = gamma;
     return LENTILS_OK;
 }
 

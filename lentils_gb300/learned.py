@@ -2,10 +2,13 @@
 
 A 4-level convolutional U-Net on the source grid (276k parameters, BF16 on the tcgen05 tensor
 cores with FP32 accumulation, kernels in csrc/unet.cu) maps a scaled Jacobi-preconditioned
-residual to a correction over Jacobi:
+residual to the direction of the error it stands for:
 
     u = dinv * r,  s = rms(u),  f = log(dinv) - mean(log(dinv))
-    M(r) = u + s * net(u / s, f)
+    M(r) = gamma * u + s * net(u / s, f),     net trained on e / rms(e), e = A^-1 r
+
+Flexible CG takes the step length from a line search, so only the direction of M(r) matters;
+gamma (default 0) mixes in the Jacobi direction.
 
 It is trained on the GPU, by its own forward and backward kernels and Adam, on (residual,
 correction) pairs taken from plain Jacobi-CG trajectories of the inversion over random lens
@@ -76,17 +79,20 @@ def features(dinv):
     return f
 
 
+def _rms(t):
+    s = torch.sqrt(torch.mean(t.double() ** 2, dim=(-2, -1), keepdim=True)).float()
+    return torch.where(s > 0, s, torch.ones_like(s))
+
+
 def scaled_inputs(r, dinv, feat, e=None):
     """Network inputs (and the training target for a correction e) of the preconditioner form,
-    batched over the leading dimension: (u / s, f, (e - u) / s)."""
+    batched over the leading dimension: (u / rms(u), f, e / rms(e))."""
     u = dinv * r
-    s = torch.sqrt(torch.mean(u.double() ** 2, dim=(-2, -1), keepdim=True)).float()
-    s = torch.where(s > 0, s, torch.ones_like(s))
-    x = u / s
+    x = u / _rms(u)
     f = feat.expand_as(x)
     if e is None:
         return x.contiguous(), f.contiguous()
-    return x.contiguous(), f.contiguous(), ((e - u) / s).contiguous()
+    return x.contiguous(), f.contiguous(), (e / _rms(e)).contiguous()
 
 
 class UNet:
@@ -155,6 +161,16 @@ class UNet:
                                                 _ptr(loss_out) if loss_out is not None else None,
                                                 self._sp()))
 
+    def backward(self, dout, lr=0.0, want_grad=False):
+        """Backward pass from the most recent forward() for the output gradient dout (same
+        shape); Adam step if lr > 0; returns the flat gradient if want_grad."""
+        dout = dout.contiguous()
+        B = self._check(dout)
+        g = np.empty(param_count(), np.float32) if want_grad else None
+        N.check(N.lib().lentils_unet_backward(self._h, _ptr(dout), B, float(lr),
+                                              g.ctypes.data if want_grad else None, self._sp()))
+        return g
+
     @property
     def params(self):
         p = np.empty(param_count(), np.float32)
@@ -175,7 +191,103 @@ class UNet:
                                                   _ptr(z), self._sp()))
         return z
 
+    def set_jacobi_weight(self, gamma):
+        N.check(N.lib().lentils_unet_set_jacobi_weight(self._h, float(gamma)))
+
     def error_flag(self):
         f = ctypes.c_int()
         N.check(N.lib().lentils_unet_error_flag(self._h, ctypes.byref(f)))
         return f.value
+
+
+# ------------------------------------------------------------------------------------------------
+# Training data: (residual, correction) pairs from plain Jacobi-CG trajectories
+# ------------------------------------------------------------------------------------------------
+def lens_draw(rng, centre=(0.0, 0.0), jitter=0.05):
+    """A PEMD + external shear drawn from the sweep priors: b in [0.8, 1.6], axis ratio q in
+    [0.5, 0.95], slope gamma in [1.8, 2.3] (qh = (gamma - 1) / 2), shear strength in [0, 0.1];
+    position angles uniform; centre jittered by +-jitter arcsec."""
+    from .lens_models import ExternalPotential, GlobalLensModel, PowerLawEllipsoid
+    b = rng.uniform(0.8, 1.6)
+    q = rng.uniform(0.5, 0.95)
+    gamma = rng.uniform(1.8, 2.3)
+    th = rng.uniform(0.0, 180.0)
+    ss = rng.uniform(0.0, 0.1)
+    sa = rng.uniform(0.0, 180.0)
+    x0, y0 = np.asarray(centre, float) + rng.uniform(-jitter, jitter, 2)
+    return GlobalLensModel([
+        PowerLawEllipsoid(z=0.5, b=b, th=th, f=q, x=x0, y=y0, rc=0.0, qh=0.5 * (gamma - 1.0)),
+        ExternalPotential(z=0.5, x=x0, y=y0, ss=ss, sa=sa)])
+
+
+def random_source(rng, source_space, nblobs=(1, 5)):
+    """Sum of a few Gaussian blobs (widths 0.02-0.08 arcsec) inside the inner 60% of the
+    source grid, x-major (nx, ny) float64."""
+    sp = source_space
+    xs = (sp.xmin + sp.dx * np.arange(sp.nx))[:, None]
+    ys = (sp.ymin + sp.dy * np.arange(sp.ny))[None, :]
+    hx, hy = 0.3 * (sp.xmax - sp.xmin), 0.3 * (sp.ymax - sp.ymin)
+    cx, cy = 0.5 * (sp.xmin + sp.xmax), 0.5 * (sp.ymin + sp.ymax)
+    s = np.zeros((sp.nx, sp.ny))
+    for _ in range(rng.integers(nblobs[0], nblobs[1] + 1)):
+        x0, y0 = cx + rng.uniform(-hx, hx), cy + rng.uniform(-hy, hy)
+        w = rng.uniform(0.02, 0.08)
+        s += rng.uniform(0.3, 1.0) * np.exp(-((xs - x0) ** 2 + (ys - y0) ** 2) / (2 * w * w))
+    return s
+
+
+def jacobi_cg_trajectory(inv, max_iter=8000, rtol=1e-6, check_every=50):
+    """Plain Jacobi-preconditioned CG on inv's normal equations from x = 0 with the FP32
+    operator (FP64-accumulated dot products), recording every iterate. Returns the iterates
+    (K, n) float32 CUDA tensor, including x_0 = 0."""
+    import ctypes as _ct
+    n = inv.nsrc
+    L = N.lib()
+    xs = torch.zeros((max_iter + 1, n), dtype=torch.float32, device="cuda")
+    b = inv.b.float()
+    dinv = inv.inv_diag32
+    bn = float(torch.linalg.vector_norm(inv.b))
+    sp = _ct.c_void_p(torch.cuda.current_stream().cuda_stream)
+    x = torch.zeros(n, dtype=torch.float32, device="cuda")
+    r = b.clone()
+    z = dinv * r
+    p = z.clone()
+    ap = torch.empty_like(p)
+    rz = torch.dot(r.double(), z.double())
+    k = 0
+    while k < max_iter:
+        N.check(L.lentils_normal_op_apply(inv.handle, _ptr(p), _ptr(ap), sp))
+        alpha = (rz / torch.dot(p.double(), ap.double())).float()
+        x.add_(alpha * p)
+        r.sub_(alpha * ap)
+        k += 1
+        xs[k] = x
+        z = dinv * r
+        rz_new = torch.dot(r.double(), z.double())
+        p = z + (rz_new / rz).float() * p
+        rz = rz_new
+        if k % check_every == 0 and float(torch.linalg.vector_norm(r.double())) <= rtol * bn:
+            break
+    return xs[:k + 1]
+
+
+def trajectory_pairs(inv, npairs, rng, max_iter=8000, tol_star=1e-9):
+    """(residual, correction) pairs of one inversion: iterates x_k of plain Jacobi-CG at
+    geometrically spaced iterations, the true FP64 residual r_k = b - A x_k and the correction
+    e_k = x* - x_k to the FP64-refined solution x*. Returns float32 CUDA tensors (npairs, n)."""
+    import ctypes as _ct
+    x_star, info = inv.solve(tol=tol_star, max_outer=60)
+    xs = jacobi_cg_trajectory(inv, max_iter=max_iter)
+    K = xs.shape[0]
+    idx = np.unique(np.clip(np.round(np.geomspace(1, K, npairs * 2)).astype(int) - 1, 0, K - 1))
+    idx = np.sort(rng.choice(idx, size=min(npairs, idx.size), replace=False))
+    L = N.lib()
+    sp = _ct.c_void_p(torch.cuda.current_stream().cuda_stream)
+    rs, es = [], []
+    ax = torch.empty(inv.nsrc, dtype=torch.float64, device="cuda")
+    for k in idx:
+        xk = xs[int(k)].double()
+        N.check(L.lentils_normal_op_apply64(inv.handle, _ptr(xk), _ptr(ax), sp))
+        rs.append((inv.b - ax).float())
+        es.append((x_star - xk).float())
+    return torch.stack(rs), torch.stack(es), K - 1, info

@@ -1,0 +1,303 @@
+"""Train the learned CG preconditioner on the GPU and compare it with plain Jacobi-CG.
+
+    python -m lentils_gb300.train_preconditioner --draws 100 --pairs 100 --steps 4000 \
+        --out lentils_gb300/weights/unet_source128.npz
+
+1. Training set: for each of `draws` random lens models (PEMD + shear from the sweep priors,
+   learned.lens_draw) and random sources, the inversion workload's normal equations are solved
+   by plain Jacobi-CG from zero; `pairs` iterates x_k along the trajectory give pairs
+   (r_k = b - A x_k, e_k = x* - x_k) with x* the FP64-refined solution (learned.trajectory_pairs).
+   All draws share the workload's visibility set and NUFFT operator.
+2. Training: Adam on the energy-norm loss -- the fraction of the A-norm error left after a
+   line search along the network's direction, 1 - (z.r)^2 / ((z.Az)(e.r)), each sample with
+   its own normal operator -- or (--loss mse) on the mean squared error against the
+   correction's direction e / rms(e) with minibatches of random pairs under random flips and transposes of the grid
+   (applied to residual, correction and diagonal together), cosine learning-rate decay; every
+   step is the network's own forward and backward kernels.
+3. Evaluation: the workload inversion solved to a true FP64 relative residual of 1e-6 by plain
+   Jacobi-CG (lentils_cg_solve) and by flexible CG with the network (lentils_fcg_solve).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import time
+
+import numpy as np
+import torch
+
+from . import learned, workloads
+
+DEFAULT_WEIGHTS = os.path.join(os.path.dirname(os.path.abspath(__file__)), "weights",
+                               "unet_source128.npz")
+
+
+def build_training_set(nufft, geom, draws, pairs, seed, log=print, keep_operators=True,
+                       lam=workloads.LAMBDA, z_src=workloads.Z_SRC, max_iter=8000):
+    """Pairs from `draws` random lens models and sources on geom = (visibility space, image
+    space, source space, uvw), all sharing `nufft`."""
+    from .inversion import SourceInversion
+    vs, ims, srcs, _ = geom
+    rng = np.random.default_rng(seed)
+    R, E, D, Fe, idx, iters, invs = [], [], [], [], [], [], []
+    t0 = time.perf_counter()
+    for k in range(draws):
+        glm = learned.lens_draw(rng, centre=(0.25 * ims.dx, 0.25 * ims.dy))
+        s = learned.random_source(rng, srcs)
+        d = workloads.simulate(nufft, ims, srcs, glm, s, rng, z_src=z_src)
+        inv = SourceInversion(vs, d, 1.0, ims, srcs, glm, z_src, lam, nufft=nufft)
+        r, e, K, _ = learned.trajectory_pairs(inv, pairs, rng, max_iter=max_iter)
+        R.append(r)
+        E.append(e)
+        D.append(inv.inv_diag32.clone())
+        Fe.append(learned.features(inv.inv_diag32))
+        idx.append(torch.full((r.shape[0],), k, dtype=torch.long, device="cuda"))
+        iters.append(K)
+        if keep_operators:
+            invs.append(inv)
+        del inv
+        if (k + 1) % 10 == 0 or k + 1 == draws:
+            log(f"draw {k + 1}/{draws}: {sum(x.shape[0] for x in R)} pairs, "
+                f"plain CG iterations {K}, {time.perf_counter() - t0:.1f} s")
+    r, e = torch.cat(R), torch.cat(E)
+    return {"r": r, "e": e, "er": (e.double() * r.double()).sum(dim=1),
+            "dinv": torch.stack(D), "feat": torch.stack(Fe), "draw": torch.cat(idx),
+            "inversions": invs, "cg_iterations": iters, "seconds": time.perf_counter() - t0}
+
+
+def _dihedral(t, k):
+    """One of the 8 flips/transposes of the last two axes."""
+    if k & 4:
+        t = t.transpose(-2, -1)
+    if k & 1:
+        t = t.flip(-2)
+    if k & 2:
+        t = t.flip(-1)
+    return t
+
+
+def batch(data, ids, H, W, aug):
+    r = data["r"][ids].view(-1, H, W)
+    e = data["e"][ids].view(-1, H, W)
+    di = data["draw"][ids]
+    dinv = data["dinv"][di].view(-1, H, W)
+    feat = data["feat"][di].view(-1, H, W)
+    if aug is not None:  # square grids: the 8 symmetries keep the shape
+        aug = torch.as_tensor(aug, device=r.device)
+        ts = [r.clone(), e.clone(), dinv.clone(), feat.clone()]
+        for k in range(1, 8):
+            m = aug == k
+            if bool(m.any()):
+                for dst, src in zip(ts, (r, e, dinv, feat)):
+                    dst[m] = _dihedral(src[m], k)
+        r, e, dinv, feat = ts
+    return learned.scaled_inputs(r, dinv, feat, e)
+
+
+def train(net, data, steps, batch_size, lr, seed, val_frac=0.05, log=print, log_every=250):
+    H, W = net.H, net.W
+    n = data["r"].shape[0]
+    g = torch.Generator(device="cpu").manual_seed(seed)
+    perm = torch.randperm(n, generator=g)
+    nval = max(batch_size, int(val_frac * n))
+    val, tr = perm[:nval].cuda(), perm[nval:].cuda()
+    losses = torch.zeros(steps, device="cuda")
+    t0 = time.perf_counter()
+
+    def val_loss():
+        tot = 0.0
+        for i in range(0, nval - batch_size + 1, batch_size):
+            x, f, t = batch(data, val[i:i + batch_size], H, W, None)
+            tot += net.gradients(x, f, t)[1]
+        return tot / max(1, nval // batch_size)
+
+    history = [{"step": 0, "val": val_loss()}]
+    for it in range(steps):
+        ids = tr[torch.randint(0, tr.numel(), (batch_size,), generator=g).cuda()]
+        aug = torch.randint(0, 8, (batch_size,), generator=g).tolist()
+        x, f, t = batch(data, ids, H, W, aug)
+        lr_t = lr * 0.5 * (1.0 + math.cos(math.pi * it / steps))
+        net.train_step(x, f, t, lr_t, losses[it:it + 1])
+        if (it + 1) % log_every == 0 or it + 1 == steps:
+            tl = float(losses[max(0, it + 1 - log_every):it + 1].mean())
+            vl = val_loss()
+            history.append({"step": it + 1, "train": tl, "val": vl})
+            log(f"step {it + 1}/{steps}: train {tl:.4g} val {vl:.4g} "
+                f"({time.perf_counter() - t0:.1f} s)")
+    torch.cuda.synchronize()
+    if net.error_flag():
+        raise RuntimeError("a tensor-core wait gave up during training")
+    return history, time.perf_counter() - t0
+
+
+def _apply_batch(data, ids, z):
+    """A_j z_j with each sample's own normal operator (FP32)."""
+    import ctypes
+    from . import _native as N
+    from .gridding import _ptr
+    L = N.lib()
+    sp = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+    az = torch.empty_like(z)
+    zf = z.reshape(z.shape[0], -1)
+    af = az.reshape(z.shape[0], -1)
+    for j, d in enumerate(data["draw"][ids].tolist()):
+        N.check(L.lentils_normal_op_apply(data["inversions"][d].handle, _ptr(zf[j]),
+                                          _ptr(af[j]), sp))
+    return az
+
+
+def energy_loss(data, ids, z):
+    """Per-sample fraction of the A-norm error left after a line search along z:
+    1 - (z.r)^2 / ((z.A z)(e.r)), and its gradient with respect to z."""
+    B = z.shape[0]
+    r = data["r"][ids].view_as(z)
+    az = _apply_batch(data, ids, z)
+    zr = (z.double() * r.double()).sum(dim=(1, 2))
+    zaz = (z.double() * az.double()).sum(dim=(1, 2))
+    er = data["er"][ids]
+    zaz = torch.where(zaz > 0, zaz, torch.ones_like(zaz))
+    frac = 1.0 - zr * zr / (zaz * er)
+    coef = (-2.0 * zr / (zaz * er) / B).float()[:, None, None]
+    step = (zr / zaz).float()[:, None, None]
+    grad = coef * (r - step * az)
+    return frac, grad
+
+
+def train_energy(net, data, steps, batch_size, lr, seed, val_frac=0.05, log=print,
+                 log_every=250):
+    """Adam on the mean energy-norm loss (energy_loss) of the network direction."""
+    H, W = net.H, net.W
+    n = data["r"].shape[0]
+    g = torch.Generator(device="cpu").manual_seed(seed)
+    perm = torch.randperm(n, generator=g)
+    nval = max(batch_size, int(val_frac * n))
+    val, tr = perm[:nval].cuda(), perm[nval:].cuda()
+    t0 = time.perf_counter()
+
+    def inputs(ids):
+        r = data["r"][ids].view(-1, H, W)
+        di = data["draw"][ids]
+        return learned.scaled_inputs(r, data["dinv"][di].view(-1, H, W),
+                                     data["feat"][di].view(-1, H, W))
+
+    def val_loss():
+        tot, totj, cnt = 0.0, 0.0, 0
+        for i in range(0, nval - batch_size + 1, batch_size):
+            ids = val[i:i + batch_size]
+            x, f = inputs(ids)
+            tot += float(energy_loss(data, ids, net.forward(x, f))[0].sum())
+            totj += float(energy_loss(data, ids, x)[0].sum())  # Jacobi direction
+            cnt += ids.numel()
+        return tot / cnt, totj / cnt
+
+    v, vj = val_loss()
+    history = [{"step": 0, "val": v, "val_jacobi": vj}]
+    log(f"energy loss at start: val {v:.4f} (Jacobi direction {vj:.4f})")
+    run = []
+    for it in range(steps):
+        ids = tr[torch.randint(0, tr.numel(), (batch_size,), generator=g).cuda()]
+        x, f = inputs(ids)
+        out = net.forward(x, f)
+        frac, grad = energy_loss(data, ids, out)
+        run.append(frac.mean())
+        lr_t = lr * 0.5 * (1.0 + math.cos(math.pi * it / steps))
+        net.backward(grad, lr=lr_t)
+        if (it + 1) % log_every == 0 or it + 1 == steps:
+            tl = float(torch.stack(run).mean())
+            run = []
+            v, vj = val_loss()
+            history.append({"step": it + 1, "train": tl, "val": v, "val_jacobi": vj})
+            log(f"step {it + 1}/{steps}: train {tl:.4f} val {v:.4f} (Jacobi {vj:.4f}) "
+                f"({time.perf_counter() - t0:.1f} s)")
+    torch.cuda.synchronize()
+    if net.error_flag():
+        raise RuntimeError("a tensor-core wait gave up during training")
+    return history, time.perf_counter() - t0
+
+
+def evaluate(net, inv, tol=1e-6, inner_tol=1e-3, repeats=2, gammas=(0.0,), windows=(1,)):
+    """Plain Jacobi-CG against flexible CG with the network on one inversion (best of
+    `repeats` after a warm-up solve of each), for each Jacobi share gamma and direction
+    window."""
+    def best_of(fn):
+        best = None
+        for _ in range(repeats):
+            _, info = fn()
+            if best is None or info["seconds"] < best["seconds"]:
+                best = info
+        return best
+
+    inv.solve(tol=1e-2)
+    inv.solve_flexible(net, tol=1e-2)
+    out = {"plain": best_of(lambda: inv.solve(tol=tol, inner_tol=inner_tol)), "learned": {}}
+    out["jacobi_fcg"] = {}
+    for w in windows:
+        out["jacobi_fcg"][str(w)] = best_of(lambda: inv.solve_flexible(
+            None, tol=tol, inner_tol=inner_tol, window=w))
+        for g in gammas:
+            net.set_jacobi_weight(g)
+            out["learned"][f"{g}/{w}"] = best_of(lambda: inv.solve_flexible(
+                net, tol=tol, inner_tol=inner_tol, window=w))
+    key = min(out["learned"], key=lambda k: out["learned"][k]["seconds"])
+    lb = out["learned"][key]
+    g, w = key.split("/")
+    out["best"] = {"gamma": float(g), "window": int(w)}
+    out["iteration_ratio"] = out["plain"]["inner_total"] / max(1, lb["inner_total"])
+    out["time_ratio"] = out["plain"]["seconds"] / max(1e-12, lb["seconds"])
+    net.set_jacobi_weight(float(g))
+    return out
+
+
+def save(path, params, meta):
+    os.makedirs(os.path.dirname(os.path.abspath(path)), exist_ok=True)
+    np.savez_compressed(path, params=params, meta=json.dumps(meta))
+
+
+def load(path):
+    z = np.load(path)
+    return z["params"], json.loads(str(z["meta"]))
+
+
+def main(argv=None):
+    ap = argparse.ArgumentParser(description=__doc__.split("\n")[0])
+    ap.add_argument("--draws", type=int, default=100)
+    ap.add_argument("--pairs", type=int, default=100)
+    ap.add_argument("--steps", type=int, default=4000)
+    ap.add_argument("--batch", type=int, default=32)
+    ap.add_argument("--lr", type=float, default=1e-3)
+    ap.add_argument("--seed", type=int, default=7)
+    ap.add_argument("--out", default=DEFAULT_WEIGHTS)
+    ap.add_argument("--no-eval", action="store_true")
+    ap.add_argument("--loss", choices=["energy", "mse"], default="energy")
+    a = ap.parse_args(argv)
+
+    def log(msg):
+        print(msg, flush=True)
+
+    from .operators import NUFFTOperator
+    vs, ims, srcs, uvw, _ = workloads.geometry()
+    F = NUFFTOperator(vs, ims)
+    data = build_training_set(F, (vs, ims, srcs, uvw), a.draws, a.pairs, a.seed, log,
+                              keep_operators=a.loss == "energy")
+    net = learned.UNet(workloads.SRC, workloads.SRC, max_batch=a.batch, seed=a.seed)
+    fit = train_energy if a.loss == "energy" else train
+    history, train_s = fit(net, data, a.steps, a.batch, a.lr, a.seed, log=log)
+    meta = {"loss": a.loss, "draws": a.draws, "pairs": int(data["r"].shape[0]), "steps": a.steps,
+            "batch": a.batch, "lr": a.lr, "seed": a.seed, "data_seconds": data["seconds"],
+            "train_seconds": train_s, "history": history,
+            "plain_cg_iterations_mean": float(np.mean(data["cg_iterations"]))}
+    del data
+    if not a.no_eval:
+        inv, _, _ = workloads.inversion(nufft=F)
+        pnet = learned.UNet(workloads.SRC, workloads.SRC, max_batch=1, params=net.params)
+        meta["evaluation"] = evaluate(pnet, inv, gammas=(0.0, 0.3), windows=(1, 8))
+        log(json.dumps(meta["evaluation"]))
+    save(a.out, net.params, meta)
+    log(f"saved {a.out}")
+    return 0
+
+
+if __name__ == "__main__":
+    raise SystemExit(main())
