@@ -347,6 +347,48 @@ int lentils_tc_gemm_bf16(const void *A, const void *B, float *C, int M, int N, i
                          int swap_lbo_sbo, int *err_dev, void *stream);
 
 /* ------------------------------------------------------------------------------------------
+ * Batched lens-parameter sweep (no counterpart in the reference, whose operators run one lens
+ * model at a time): per sample, deflection of its pixel grid, degridding of its grid and
+ * gridding of its visibilities, for all samples in ONE persistent kernel launch (captured in a
+ * CUDA graph by lentils_sweep_run with use_graph = 1).
+ *
+ * Each sample names its plan (KB width 6 or 8; tile and chunk are the plan's), DEVICE buffers
+ * in the plan's order and frame as for lentils_degrid / lentils_grid -- grid_in (half plane
+ * c64) -> vis_out (c64), vis_in (c64) -> grid_out (half plane c64, OVERWRITTEN) -- its lens
+ * models (HOST array, at most 8, packed as for deflect_points) and its pixel grid: points
+ * (x0 + i dx, y0 + j dy), i < nx, j < ny, x-major, deflected to beta = theta - sum alpha into
+ * beta_out (device, nx * ny interleaved float (x, y)). plan = NULL or nx * ny = 0 skips that
+ * part. Plans and buffers must outlive the sweep.
+ * ---------------------------------------------------------------------------------------- */
+typedef struct lentils_sweep lentils_sweep;
+typedef struct {
+    lentils_plan *plan;
+    const float *grid_in;
+    float *vis_out;
+    const float *vis_in;
+    float *grid_out;
+    const lentils_mass_model *lenses;
+    int nlenses;
+    int nx, ny;
+    double x0, y0, dx, dy;
+    float *beta_out;
+} lentils_sweep_sample;
+typedef struct {
+    int nsamples;
+    int nwork;        /* work items in the queue                       */
+    int blocks;       /* persistent CTAs (resident slots on all SMs)    */
+    long long smem_bytes;
+    long long total_vis;
+    long long total_pixels;
+    double algorithmic_bytes; /* per run: 2 x (16 B per visibility + grid) + 8 B per pixel */
+} lentils_sweep_stats;
+int lentils_sweep_create(lentils_sweep **sweep, const lentils_sweep_sample *samples, int n,
+                         int flags, void *stream);
+int lentils_sweep_destroy(lentils_sweep *sweep);
+int lentils_sweep_run(lentils_sweep *sweep, int use_graph, void *stream);
+int lentils_sweep_get_stats(const lentils_sweep *sweep, lentils_sweep_stats *stats);
+
+/* ------------------------------------------------------------------------------------------
  * Learned preconditioner (no counterpart in the reference): a 4-level convolutional U-Net on the
  * source grid, BF16 activations and weights on the tensor cores (tcgen05) with FP32
  * accumulation, trained on the GPU by its own forward and backward kernels.

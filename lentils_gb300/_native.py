@@ -70,6 +70,19 @@ class CGResultC(Structure):
                 ("fallback", c_int)]
 
 
+class SweepSampleC(Structure):
+    _fields_ = [("plan", c_void_p), ("grid_in", c_void_p), ("vis_out", c_void_p),
+                ("vis_in", c_void_p), ("grid_out", c_void_p), ("lenses", c_void_p),
+                ("nlenses", c_int), ("nx", c_int), ("ny", c_int), ("x0", c_double),
+                ("y0", c_double), ("dx", c_double), ("dy", c_double), ("beta_out", c_void_p)]
+
+
+class SweepStatsC(Structure):
+    _fields_ = [("nsamples", c_int), ("nwork", c_int), ("blocks", c_int),
+                ("smem_bytes", c_longlong), ("total_vis", c_longlong),
+                ("total_pixels", c_longlong), ("algorithmic_bytes", c_double)]
+
+
 class PlanStatsC(Structure):
     _fields_ = [("nvis", c_longlong), ("ntiles_u", c_int), ("ntiles_v", c_int), ("tile", c_int),
                 ("nitems", c_int), ("max_item_vis", c_int), ("heaviest_tile_vis", c_int),
@@ -155,6 +168,11 @@ _SIGNATURES = [
                                           c_void_p]),
     ("lentils_fcg_solve", c_int, [c_void_p, c_void_p, c_void_p, c_void_p, c_void_p,
                                   POINTER(CGOptionsC), POINTER(CGResultC), c_void_p]),
+    ("lentils_sweep_create", c_int, [POINTER(c_void_p), POINTER(SweepSampleC), c_int, c_int,
+                                     c_void_p]),
+    ("lentils_sweep_destroy", c_int, [c_void_p]),
+    ("lentils_sweep_run", c_int, [c_void_p, c_int, c_void_p]),
+    ("lentils_sweep_get_stats", c_int, [c_void_p, POINTER(SweepStatsC)]),
     ("lentils_grid_noalloc", c_int, [POINTER(GridDescC), c_void_p, c_int, c_void_p, c_int,
                                      c_void_p, c_void_p, c_void_p]),
     ("lentils_noalloc_max_vis", c_int, []),

@@ -1,0 +1,384 @@
+// Per-work-item Kaiser-Bessel degridding and gridding device functions, shared by the
+// one-item-per-CTA kernels (gridding.cu) and the persistent batched sweep (sweep.cu).
+// Conventions (tap set, fixed-point cells, fold, factors) are documented in gridding.cu.
+#pragma once
+
+#include "common.cuh"
+
+namespace lentils {
+
+__device__ __forceinline__ int wrap_index(int a, int n)
+{
+    int r = a % n;
+    return r < 0 ? r + n : r;
+}
+
+template <int W2>
+__device__ __forceinline__ void kb_weights(const KBPoly &kb, uint32_t word, float (&wt)[W2],
+                                           float /*res: FP64 kernels only*/ = 0.f)
+{
+    constexpr int w = W2 / 2;
+    const float f = (float)(word & kFracMask) * (1.0f / (float)(1u << kFracBits));
+    const float t = fmaf(2.0f, f, -1.0f);
+    const float2 tt = make_float2(t, t);
+    const float2 uu = make_float2(t * t, t * t);
+#pragma unroll
+    for (int p = 0; p < (w + 1) / 2; ++p) {
+        float2 e = kb.ce[0][p], o = kb.co[0][p];
+#pragma unroll
+        for (int k = 1; k < kHalfCoef; ++k) {
+            e = __ffma2_rn(e, uu, kb.ce[k][p]);
+            o = __ffma2_rn(o, uu, kb.co[k][p]);
+        }
+        const float2 lo = __ffma2_rn(tt, o, e);                               // P_i(t)
+        const float2 hi = __ffma2_rn(tt, o, make_float2(-e.x, -e.y));         // -P_i(-t)
+        wt[2 * p] = lo.x;
+        wt[W2 - 1 - 2 * p] = hi.x;
+        if (2 * p + 1 < w) {
+            wt[2 * p + 1] = lo.y;
+            wt[W2 - 2 - 2 * p] = hi.y;
+        }
+    }
+    if (word & kTopOffBit) wt[W2 - 1] = 0.f;
+}
+
+__device__ __forceinline__ float2 f2(float a) { return make_float2(a, a); }
+
+__device__ __forceinline__ int cell_of(uint32_t word) { return (int)((word >> kFracBits) & kCellMask); }
+
+// Precision traits: the float kernels are the hot path (packed FP32x2 FMAs, float2 global
+// atomics); the double kernels apply the FP64 operator used for refinement residuals.
+template <typename R>
+struct Prec;
+template <>
+struct Prec<float> {
+    using C = float2;
+    using Table = KBPoly;
+    __device__ static C zero() { return make_float2(0.f, 0.f); }
+    __device__ static C fma(float w, C a, C acc) { return __ffma2_rn(f2(w), a, acc); }
+    __device__ static C scale(float w, C a) { return make_float2(w * a.x, w * a.y); }
+    __device__ static void gadd(C *dst, C v) { atomicAdd(dst, v); }
+};
+template <>
+struct Prec<double> {
+    using C = double2;
+    using Table = KBPoly64;
+    __device__ static C zero() { return make_double2(0.0, 0.0); }
+    __device__ static C fma(double w, C a, C acc)
+    {
+        return make_double2(fma_(w, a.x, acc.x), fma_(w, a.y, acc.y));
+    }
+    __device__ static double fma_(double a, double b, double c) { return ::fma(a, b, c); }
+    __device__ static C scale(double w, C a) { return make_double2(w * a.x, w * a.y); }
+    __device__ static void gadd(C *dst, C v)
+    {
+        atomicAdd(&dst->x, v.x);
+        atomicAdd(&dst->y, v.y);
+    }
+};
+
+template <int W2>
+__device__ __forceinline__ void kb_weights(const KBPoly64 &kb, uint32_t word, double (&wt)[W2],
+                                           float res)
+{
+    const double f = (double)(word & kFracMask) * (1.0 / (double)(1u << kFracBits)) + (double)res;
+    const double t = 2.0 * f - 1.0;
+#pragma unroll
+    for (int i = 0; i < W2; ++i) {
+        double acc = kb.cd[0][i];
+#pragma unroll
+        for (int k = 1; k < kPolyCoef; ++k) acc = ::fma(acc, t, kb.cd[k][i]);
+        wt[i] = acc;
+    }
+    if (word & kTopOffBit) wt[W2 - 1] = 0.0;
+}
+
+// Parity of the first regular tap (canonical cell index) of a visibility in the item's tile.
+__device__ __forceinline__ int tap_parity(const WorkItem &it, const GridGeom &g, int lu, int lv)
+{
+    return (it.tu * g.T - g.Hu + lu - g.w + 1 + it.tv * g.T - g.Hv + lv - g.w + 1) & 1;
+}
+
+// Degridding of one work item by the whole CTA (any block size); smraw: E x stride cells.
+template <int W2, typename R>
+__device__ __forceinline__ void degrid_item(const typename Prec<R>::C *__restrict__ grid,
+                                            const uint2 *__restrict__ coords,
+                                            typename Prec<R>::C *__restrict__ out,
+                                            const WorkItem &it,
+                                            const typename Prec<R>::Table &kb, const GridGeom &g,
+                                            const float2 *__restrict__ cres,
+                                            unsigned char *smraw)
+{
+    using P = Prec<R>;
+    using C = typename P::C;
+    C *sm = reinterpret_cast<C *>(smraw);
+    constexpr int w = W2 / 2;
+    const int a0 = it.tu * g.T - g.Hu - w;  // canonical index of extended row 0
+    const int b0 = it.tv * g.T - g.Hv - w;
+    const int E = g.E, S = g.stride;
+    for (int e = threadIdx.x; e < E * E; e += blockDim.x) {
+        const int ea = e / E, eb = e - ea * E;
+        int au = wrap_index(a0 + ea, g.nu);
+        int bv = wrap_index(b0 + eb, g.nv);
+        C val;
+        if (bv >= g.half_nv) {
+            au = (g.nu - au) % g.nu;
+            bv = g.nv - bv;
+            val = grid[(long long)au * g.half_nv + bv];
+            val.y = -val.y;
+        } else {
+            val = grid[(long long)au * g.half_nv + bv];
+        }
+        sm[ea * S + eb] = val;
+    }
+    __syncthreads();
+
+    for (int k = threadIdx.x; k < it.count; k += blockDim.x) {
+        const uint2 c = coords[it.begin + k];
+        const int lu = cell_of(c.x), lv = cell_of(c.y);
+        const float2 rr = cres ? cres[it.begin + k] : make_float2(0.f, 0.f);
+        R wu[W2], wv[W2];
+        kb_weights<W2>(kb, c.x, wu, rr.x);
+        kb_weights<W2>(kb, c.y, wv, rr.y);
+        const C *p = sm + (lu + 1) * S + (lv + 1);
+        C acc = P::zero();
+#pragma unroll
+        for (int i = 0; i < W2; ++i) {
+            C r = P::zero();
+#pragma unroll
+            for (int j = 0; j < W2; ++j) r = P::fma(wv[j], p[i * S + j], r);
+            acc = P::fma(wu[i], r, acc);
+        }
+        if ((c.x | c.y) & kExtraTapBit) {
+            // extra taps at argument +w: extended row lu (u) / column lv (v)
+            const R eu = (c.x & kExtraTapBit) ? (R)kb.edge : (R)0;
+            const R ev = (c.y & kExtraTapBit) ? (R)kb.edge : (R)0;
+            const C *q = sm + lu * S + lv;
+            C r = P::zero();
+            for (int j = 0; j < W2; ++j) r = P::fma(wv[j], q[j + 1], r);
+            r = P::fma(ev, q[0], r);
+            acc = P::fma(eu, r, acc);
+            C cs = P::zero();
+            for (int i = 0; i < W2; ++i) cs = P::fma(wu[i], q[(i + 1) * S], cs);
+            acc = P::fma(ev, cs, acc);
+        }
+        if (tap_parity(it, g, lu, lv)) {
+            acc.x = -acc.x;
+            acc.y = -acc.y;
+        }
+        out[it.begin + k] = acc;
+    }
+}
+
+// Extra taps of one visibility (rare): added to shared memory directly.
+template <int W2, typename R>
+__device__ __forceinline__ void grid_extra_taps(typename Prec<R>::C *sm, int S, int lu, int lv,
+                                                uint2 c, const R (&wu)[W2], const R (&wv)[W2],
+                                                R edge, typename Prec<R>::C x)
+{
+    using C = typename Prec<R>::C;
+    const R eu = (c.x & kExtraTapBit) ? edge : (R)0;
+    const R ev = (c.y & kExtraTapBit) ? edge : (R)0;
+    C *q = sm + lu * S + lv;
+    if (eu != (R)0) {
+        const C t = Prec<R>::scale(eu, x);
+        for (int j = 0; j < W2; ++j) {
+            atomicAdd(&q[j + 1].x, wv[j] * t.x);
+            atomicAdd(&q[j + 1].y, wv[j] * t.y);
+        }
+        atomicAdd(&q[0].x, ev * t.x);
+        atomicAdd(&q[0].y, ev * t.y);
+    }
+    if (ev != (R)0) {
+        for (int i = 0; i < W2; ++i) {
+            atomicAdd(&q[(i + 1) * S].x, wu[i] * ev * x.x);
+            atomicAdd(&q[(i + 1) * S].y, wu[i] * ev * x.y);
+        }
+    }
+}
+
+template <int W2, typename R>
+__device__ __forceinline__ void grid_flush_extended(const typename Prec<R>::C *sm,
+                                                    typename Prec<R>::C *__restrict__ grid,
+                                                    const WorkItem &it, const GridGeom &g)
+{
+    using C = typename Prec<R>::C;
+    constexpr int w = W2 / 2;
+    const int a0 = it.tu * g.T - g.Hu - w;
+    const int b0 = it.tv * g.T - g.Hv - w;
+    const int E = g.E, S = g.stride;
+    for (int e = threadIdx.x; e < E * E; e += blockDim.x) {
+        const int ea = e / E, eb = e - ea * E;
+        C val = sm[ea * S + eb];
+        if (val.x == (R)0 && val.y == (R)0) continue;
+        int au = wrap_index(a0 + ea, g.nu);
+        int bv = wrap_index(b0 + eb, g.nv);
+        if (bv >= g.half_nv) {
+            au = (g.nu - au) % g.nu;
+            bv = g.nv - bv;
+            val.y = -val.y;
+        } else if (bv == 0) {
+            val.x *= (R)2;
+            val.y *= (R)2;
+        }
+        Prec<R>::gadd(&grid[(long long)au * g.half_nv + bv], val);
+    }
+}
+
+constexpr int kGridBatch = 256;  // visibilities per weight batch (= threads per CTA)
+
+// Row-owner gridding (the default for float). The work item's sorted visibilities are split
+// into NG = 8 warps x G contiguous ranges, one per group of 2w lanes (G = 32/(2w) groups per
+// warp). Each batch gathers the next SHARE visibilities of every range (SHARE * NG <= 256, one
+// per thread), evaluates their weights into 80-byte shared rows [wv | wu | x, key], and the
+// groups consume them: lane i of a group owns row i of the 2w x 2w window and accumulates its
+// 2w taps in registers -- across batches -- while its range stays in one cell. So a dense
+// cell costs one flush per range, not one per batch. Every warp flushes into its own copy of
+// the extended tile with plain load-add-store, its groups taking turns (warp vote, then one
+// group at a time between __syncwarp), so no two lanes update a cell at once; the copies are
+// summed once per work item before the global flush.
+// One work item by a CTA of kGridBatch threads; smraw: grid_rows_smem_bytes<W2>(g).
+template <int W2>
+__device__ __forceinline__ void grid_rows_item(const float2 *__restrict__ vis,
+                                               const uint2 *__restrict__ coords,
+                                               float2 *__restrict__ grid, const WorkItem &it,
+                                               const KBPoly &kb, const GridGeom &g,
+                                               unsigned char *smraw)
+{
+    constexpr int STR = 2 * W2 + 4;                  // floats per row (16-byte multiple)
+    constexpr int G = 32 / W2;                        // visibility groups per warp
+    constexpr int NW = kGridBatch / 32;
+    constexpr int NG = NW * G;                        // groups per CTA
+    constexpr int SHARE = kGridBatch / NG;            // visibilities per group and batch
+    static_assert((STR % 4) == 0, "rows must stay 16-byte aligned");
+    const int E = g.E, S = g.stride;
+    float2 *tiles = reinterpret_cast<float2 *>(smraw);  // NW x (E x S)
+    const size_t tile_bytes = ((sizeof(float2) * (size_t)NW * E * S) + 15) & ~size_t(15);
+    float *rows = reinterpret_cast<float *>(smraw + tile_bytes);  // NG*SHARE x STR
+    for (int e = threadIdx.x; e < NW * E * S; e += blockDim.x) tiles[e] = make_float2(0.f, 0.f);
+
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    float2 *mytile = tiles + warp * E * S;
+    const int grp = lane / W2, ri = lane - grp * W2;
+    const bool lane_on = grp < G;
+    const int gid = warp * G + (lane_on ? grp : 0);   // this lane's range
+    const int L = (it.count + NG - 1) / NG;           // range length
+    const int rbeg = min(it.count, gid * L), rend = min(it.count, rbeg + L);
+    // producer role: thread t fills row t for range t / SHARE
+    const int pg = threadIdx.x / SHARE, pj = threadIdx.x - pg * SHARE;
+    const int pbeg = min(it.count, pg * L), pend = min(it.count, pbeg + L);
+
+    float2 acc[W2];
+#pragma unroll
+    for (int j = 0; j < W2; ++j) acc[j] = make_float2(0.f, 0.f);
+    int cur = -1;
+    const int nbatch = (L + SHARE - 1) / SHARE;
+    for (int b = 0; b <= nbatch; ++b) {
+        __syncthreads();  // tiles zeroed / previous batch consumed
+        if (b < nbatch && pg < NG) {
+            const int kv = pbeg + b * SHARE + pj;
+            if (kv < pend) {
+                const uint2 c = coords[it.begin + kv];
+                const int lu = cell_of(c.x), lv = cell_of(c.y);
+                float wu[W2], wv[W2];
+                kb_weights<W2>(kb, c.x, wu);
+                kb_weights<W2>(kb, c.y, wv);
+                float2 x = vis[it.begin + kv];
+                const float h = tap_parity(it, g, lu, lv) ? -0.5f : 0.5f;
+                x = make_float2(h * x.x, h * x.y);
+                float *row = rows + threadIdx.x * STR;
+                float4 *row4 = reinterpret_cast<float4 *>(row);
+#pragma unroll
+                for (int q = 0; q < W2 / 4; ++q)
+                    row4[q] = make_float4(wv[4 * q], wv[4 * q + 1], wv[4 * q + 2], wv[4 * q + 3]);
+#pragma unroll
+                for (int j = (W2 / 4) * 4; j < W2; ++j) row[j] = wv[j];
+#pragma unroll
+                for (int i = 0; i < W2; ++i) row[W2 + i] = wu[i];
+                reinterpret_cast<float4 *>(row + 2 * W2)[0] =
+                    make_float4(x.x, x.y, __int_as_float((lu << 6) | lv), 0.f);
+                if ((c.x | c.y) & kExtraTapBit)  // rare: straight into a tile, atomically
+                    grid_extra_taps<W2, float>(tiles + warp * E * S, S, lu, lv, c, wu, wv,
+                                               kb.edge, x);
+            }
+        }
+        __syncthreads();
+        // consume this batch's rows of my range; after the last batch flush what is left
+        const int kfirst = rbeg + b * SHARE;
+        for (int step = 0; step < SHARE; ++step) {
+            const int k = kfirst + step;
+            const bool valid = lane_on && b < nbatch && k < rend;
+            float4 xk = make_float4(0.f, 0.f, 0.f, 0.f);
+            int key = cur;
+            const float *row = rows + (gid * SHARE + step) * STR;
+            if (valid) {
+                xk = reinterpret_cast<const float4 *>(row + 2 * W2)[0];
+                key = __float_as_int(xk.z);
+            }
+            const bool need = lane_on && cur >= 0 && (b == nbatch || key != cur);
+            if (__any_sync(0xffffffffu, need)) {
+                for (int hgrp = 0; hgrp < G; ++hgrp) {
+                    if (need && grp == hgrp) {
+                        float2 *p = mytile + ((cur >> 6) + 1 + ri) * S + (cur & 63) + 1;
+#pragma unroll
+                        for (int j = 0; j < W2; ++j) {
+                            float2 v = p[j];
+                            v.x += acc[j].x;
+                            v.y += acc[j].y;
+                            p[j] = v;
+                            acc[j] = make_float2(0.f, 0.f);
+                        }
+                    }
+                    __syncwarp();
+                }
+                if (need) cur = -1;
+            }
+            if (!valid) continue;
+            cur = key;
+            const float wui = row[W2 + ri];
+            const float2 t = make_float2(wui * xk.x, wui * xk.y);
+            float wv[W2];
+#pragma unroll
+            for (int q = 0; q < W2 / 4; ++q) {
+                const float4 v4 = reinterpret_cast<const float4 *>(row)[q];
+                wv[4 * q] = v4.x;
+                wv[4 * q + 1] = v4.y;
+                wv[4 * q + 2] = v4.z;
+                wv[4 * q + 3] = v4.w;
+            }
+#pragma unroll
+            for (int j = (W2 / 4) * 4; j < W2; ++j) wv[j] = row[j];
+#pragma unroll
+            for (int j = 0; j < W2; ++j) acc[j] = __ffma2_rn(f2(wv[j]), t, acc[j]);
+        }
+    }
+    __syncthreads();
+    for (int e = threadIdx.x; e < E * S; e += blockDim.x) {  // sum the warps' copies
+        float2 a = tiles[e];
+#pragma unroll
+        for (int q = 1; q < NW; ++q) {
+            const float2 bq = tiles[q * E * S + e];
+            a.x += bq.x;
+            a.y += bq.y;
+        }
+        tiles[e] = a;
+    }
+    __syncthreads();
+    grid_flush_extended<W2, float>(tiles, grid, it, g);
+}
+
+template <int W2>
+__host__ __device__ inline size_t grid_rows_smem_bytes(const GridGeom &g)
+{
+    const size_t tile_bytes =
+        ((sizeof(float2) * (size_t)(kGridBatch / 32) * g.E * g.stride) + 15) & ~size_t(15);
+    return tile_bytes + sizeof(float) * (size_t)kGridBatch * (2 * W2 + 4);
+}
+
+template <typename R>
+__host__ __device__ inline size_t degrid_smem_bytes(const GridGeom &g)
+{
+    return sizeof(typename Prec<R>::C) * (size_t)g.E * g.stride;
+}
+
+}  // namespace lentils

@@ -42,6 +42,7 @@ class GriddingPlan:
         self.nu, self.nv = int(nu), int(nv)
         self.half_nv = self.nv // 2 + 1
         self.wsup, self.kb_beta = int(wsup), float(kb_beta)
+        self.du, self.dv, self.gcx, self.gcy = float(du), float(dv), float(gcx), float(gcy)
         desc = N.GridDescC(self.nu, self.nv, float(du), float(dv), float(gcx), float(gcy),
                            self.wsup, self.kb_beta, int(tile), int(chunk))
         flags = N.PLAN_NYQUIST_GUARD if nyquist_guard else 0
