@@ -1,4 +1,4 @@
-// Lens-equation kernel ("K4"): beta = theta - sum_l alpha_l(theta) for a batch of points,
+// Lens-equation kernel: beta = theta - sum_l alpha_l(theta) for a batch of points,
 // one thread per point, FP32 arithmetic with FP64 kept for the input offsets, the output sum
 // and the tail of the 2F1 series when |u| nears 1.
 //

@@ -1,4 +1,4 @@
-// Kaiser-Bessel degridding ("K1") and gridding ("K2") on plan-ordered visibilities.
+// Kaiser-Bessel degridding and gridding on plan-ordered visibilities.
 //
 // One CTA per work item (a tile of T x T uv cells and up to `chunk` of its visibilities,
 // sorted by cell). The CTA stages the tile plus a w-cell halo ("extended tile", E x E cells,

@@ -1,4 +1,4 @@
-// Gridding plan: one-time binning of visibilities by uv tile (the "K3" step), the frame
+// Gridding plan: one-time binning of visibilities by uv tile, the frame
 // transforms between the reference's row order and plan order, and the host-buffer forms of
 // degrid/grid.
 //

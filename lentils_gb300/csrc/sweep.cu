@@ -70,7 +70,9 @@ __device__ __forceinline__ void deflect_chunk(const SweepSampleDev &s,
     }
 }
 
-__global__ void __launch_bounds__(kGridBatch)
+// Three CTAs per SM (80 registers, a few bytes of spill) beat two at 128 registers: the items
+// are latency-bound and the third CTA hides the staging loads.
+__global__ void __launch_bounds__(kGridBatch, 3)
     sweep_kernel(const SweepSampleDev *__restrict__ samples, const SweepWork *__restrict__ work,
                  int nwork, const DevLens *__restrict__ lenses, int *__restrict__ counter)
 {

@@ -55,7 +55,7 @@ def test_golden(native, golden_dir, case):
 
 
 def test_config0_pemd(native):
-    """Config 0: 128^2 pixel grid, b = 1.0, q = 0.8, PA 30, gamma = 2.1, centre (0.05, -0.03)."""
+    """128^2 pixel grid, b = 1.0, q = 0.8, PA 30, gamma = 2.1, centre (0.05, -0.03)."""
     img = O.ImageGeom((128, 128), [(-1.28, 1.28), (-1.28, 1.28)])
     lenses = O.lens_array([O.pemd_cpars(1.0, 30.0, 0.8, 0.05, -0.03, 0.55)])
     check(lenses, img.points())

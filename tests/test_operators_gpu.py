@@ -143,7 +143,7 @@ def test_normal_operator_vs_oracle(native):
 def test_cg_reaches_true_residual(native, use_graph):
     """Jacobi-PCG with FP32 operator and FP64 refinement reaches a true relative residual of
     1e-6, measured again with the oracle's FP64 operator (exact Kaiser-Bessel weights and
-    scipy FFTs), the judge of convergence."""
+    scipy FFTs), which decides convergence."""
     rng = np.random.default_rng(23)
     inv, img, src, four, uvw, d = _inversion(rng, n_img=96, n_src=40, nvis=8000)
     x, info = inv.solve(tol=1e-6, use_graph=use_graph)
