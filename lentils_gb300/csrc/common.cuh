@@ -132,6 +132,7 @@ struct lentils_plan {
     uint2 *coords;        // fixed-point tile-relative (u, v)
     float2 *coords_res;   // g - q*2^-24 per axis (exact in FP64, stored FP32): FP64 kernels only
     int *perm;            // plan index -> user index (channel*nrows + row)
+    int *iperm;           // user index -> plan index (host-buffer forms)
     float2 *phase;        // s * e^{-i phi} per visibility (plan order)
     lentils::WorkItem *items;
     long long device_bytes;

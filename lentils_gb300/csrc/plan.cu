@@ -156,6 +156,57 @@ __global__ void from_plan_kernel(const int *__restrict__ perm, const float2 *__r
     }
 }
 
+// Host-buffer forms on page-locked host memory read and write the user-order (host) side
+// directly from the kernels, so the host side must be the coalesced one:
+// plan order <- user order, by user index:  x[iperm[u]] = conj(phase) * V[u]
+template <typename TU>
+__global__ void to_plan_scatter_kernel(const int *__restrict__ iperm,
+                                       const float2 *__restrict__ phase,
+                                       const TU *__restrict__ vu, float2 *__restrict__ vp,
+                                       long long n)
+{
+    for (long long u = blockIdx.x * (long long)blockDim.x + threadIdx.x; u < n;
+         u += (long long)gridDim.x * blockDim.x) {
+        const int k = iperm[u];
+        const TU v = vu[u];
+        const float2 ph = phase[k];
+        const float re = (float)v.x, im = (float)v.y;
+        vp[k] = make_float2(ph.x * re + ph.y * im, ph.x * im - ph.y * re);
+    }
+}
+
+// user order <- plan order, by user index:  V[u] (+)= phase * y[iperm[u]]
+template <typename TU>
+__global__ void from_plan_gather_kernel(const int *__restrict__ iperm,
+                                        const float2 *__restrict__ phase,
+                                        const float2 *__restrict__ vp, TU *__restrict__ vu,
+                                        long long n, int accumulate)
+{
+    for (long long u = blockIdx.x * (long long)blockDim.x + threadIdx.x; u < n;
+         u += (long long)gridDim.x * blockDim.x) {
+        const int k = iperm[u];
+        const float2 y = vp[k];
+        const float2 ph = phase[k];
+        TU out;
+        out.x = ph.x * y.x - ph.y * y.y;
+        out.y = ph.x * y.y + ph.y * y.x;
+        if (accumulate) {
+            const TU old = vu[u];
+            out.x += old.x;
+            out.y += old.y;
+        }
+        vu[u] = out;
+    }
+}
+
+__global__ void invert_perm_kernel(const int *__restrict__ perm, int *__restrict__ iperm,
+                                   long long n)
+{
+    for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < n;
+         k += (long long)gridDim.x * blockDim.x)
+        iperm[perm[k]] = (int)k;
+}
+
 // plan order <- user order in FP64 (c128 both sides)
 __global__ void to_plan64_kernel(const int *__restrict__ perm, const float2 *__restrict__ phase,
                                  const double2 *__restrict__ vu, double2 *__restrict__ vp,
@@ -309,6 +360,7 @@ static void free_plan_arrays(lentils_plan *p)
 {
     cudaFree(p->coords);
     cudaFree(p->perm);
+    cudaFree(p->iperm);
     cudaFree(p->phase);
     cudaFree(p->coords_res);
     cudaFree(p->items);
@@ -369,6 +421,7 @@ static int plan_build(lentils_plan *p, const double *uvw, const double *chans, i
     if ((st = tmp.alloc(&d_flags, 1))) return st;
     if ((st = dev_alloc(&p->coords, nvis, &p->device_bytes))) return st;
     if ((st = dev_alloc(&p->perm, nvis, &p->device_bytes))) return st;
+    if ((st = dev_alloc(&p->iperm, nvis, &p->device_bytes))) return st;
     if ((st = dev_alloc(&p->phase, nvis, &p->device_bytes))) return st;
     if ((st = dev_alloc(&p->coords_res, nvis, &p->device_bytes))) return st;
     LENTILS_CUDA_TRY(cudaMemsetAsync(tile_counts, 0, sizeof(int) * ntiles, s));
@@ -400,6 +453,8 @@ static int plan_build(lentils_plan *p, const double *uvw, const double *chans, i
                                                          p->coords, p->phase, nvis, res_user,
                                                          p->coords_res);
     LENTILS_CHECK_LAUNCH("gather_plan_kernel");
+    invert_perm_kernel<<<grid_blocks(nvis), 256, 0, s>>>(p->perm, p->iperm, nvis);
+    LENTILS_CHECK_LAUNCH("invert_perm_kernel");
 
     std::vector<int> counts(ntiles);
     int hflags = 0;
@@ -442,6 +497,30 @@ static int plan_build(lentils_plan *p, const double *uvw, const double *chans, i
         LENTILS_CUDA_TRY(cudaMemcpyAsync(p->items, items.data(), sizeof(WorkItem) * items.size(),
                                          cudaMemcpyHostToDevice, s));
     LENTILS_CUDA_TRY(cudaStreamSynchronize(s));
+    return LENTILS_OK;
+}
+
+// Page-locked (or device) memory that kernels can address directly: its device address, else
+// null (pageable memory goes through the staging copies).
+static void *kernel_address(const void *ptr)
+{
+    cudaPointerAttributes a;
+    if (cudaPointerGetAttributes(&a, ptr) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    if (a.type == cudaMemoryTypeHost || a.type == cudaMemoryTypeDevice ||
+        a.type == cudaMemoryTypeManaged)
+        return a.devicePointer;
+    return nullptr;
+}
+
+static int ensure_device_staging(lentils_plan *p)
+{
+    const long long ng = (long long)p->geom.nu * p->geom.half_nv;
+    int st;
+    if (!p->stage_vis32 && (st = dev_alloc(&p->stage_vis32, p->nvis))) return st;
+    if (!p->stage_grid32 && (st = dev_alloc(&p->stage_grid32, ng))) return st;
     return LENTILS_OK;
 }
 
@@ -673,9 +752,21 @@ int lentils_degrid_host(lentils_plan *p, const double *grid_host, double *vis_ho
         return set_error(LENTILS_ERR_INVALID, "degrid_host: null argument");
     if (p->nvis == 0) return LENTILS_OK;
     int st;
-    if ((st = ensure_staging(p))) return st;
     cudaStream_t s = (cudaStream_t)stream;
     const long long ng = (long long)p->geom.nu * p->geom.half_nv;
+    const double2 *grid_k = (const double2 *)kernel_address(grid_host);
+    double2 *vis_k = (double2 *)kernel_address(vis_host);
+    if (grid_k && vis_k) {  // page-locked: the kernels read and write host memory directly
+        if ((st = ensure_device_staging(p))) return st;
+        if ((st = launch_c128_to_c64(grid_k, p->stage_grid32, ng, s))) return st;
+        if ((st = launch_degrid(p, p->stage_grid32, p->stage_vis32, s))) return st;
+        from_plan_gather_kernel<double2><<<grid_blocks(p->nvis), 256, 0, s>>>(
+            p->iperm, p->phase, p->stage_vis32, vis_k, p->nvis, accumulate);
+        LENTILS_CHECK_LAUNCH("from_plan_gather_kernel");
+        LENTILS_CUDA_TRY(cudaStreamSynchronize(s));
+        return LENTILS_OK;
+    }
+    if ((st = ensure_staging(p))) return st;
     LENTILS_CUDA_TRY(cudaMemcpyAsync(p->stage_grid64, grid_host, sizeof(double2) * ng,
                                      cudaMemcpyHostToDevice, s));
     if ((st = launch_c128_to_c64(p->stage_grid64, p->stage_grid32, ng, s))) return st;
@@ -700,9 +791,22 @@ int lentils_grid_host(lentils_plan *p, const double *vis_host, double *grid_host
         return set_error(LENTILS_ERR_INVALID, "grid_host: null argument");
     if (p->nvis == 0) return LENTILS_OK;
     int st;
-    if ((st = ensure_staging(p))) return st;
     cudaStream_t s = (cudaStream_t)stream;
     const long long ng = (long long)p->geom.nu * p->geom.half_nv;
+    const double2 *vis_k = (const double2 *)kernel_address(vis_host);
+    double2 *grid_k = (double2 *)kernel_address(grid_host);
+    if (grid_k && vis_k) {  // page-locked: the kernels read and write host memory directly
+        if ((st = ensure_device_staging(p))) return st;
+        to_plan_scatter_kernel<double2><<<grid_blocks(p->nvis), 256, 0, s>>>(
+            p->iperm, p->phase, vis_k, p->stage_vis32, p->nvis);
+        LENTILS_CHECK_LAUNCH("to_plan_scatter_kernel");
+        LENTILS_CUDA_TRY(cudaMemsetAsync(p->stage_grid32, 0, sizeof(float2) * ng, s));
+        if ((st = launch_grid(p, p->stage_vis32, p->stage_grid32, s))) return st;
+        if ((st = launch_c64_to_c128(p->stage_grid32, grid_k, ng, accumulate, s))) return st;
+        LENTILS_CUDA_TRY(cudaStreamSynchronize(s));
+        return LENTILS_OK;
+    }
+    if ((st = ensure_staging(p))) return st;
     LENTILS_CUDA_TRY(cudaMemcpyAsync(p->stage_vis64, vis_host, sizeof(double2) * p->nvis,
                                      cudaMemcpyHostToDevice, s));
     if ((st = lentils_vis_to_plan(p, p->stage_vis64, 1, (float *)p->stage_vis32, stream)))

@@ -145,26 +145,42 @@ class GriddingPlan:
         return out
 
     # --- host-buffer forms (numpy complex128, reference row order) ------------------------
+    @staticmethod
+    def _host(a, n, name):
+        """Pointer of a contiguous complex128 host buffer: a numpy array or a CPU tensor
+        (page-locked tensors take the direct path, pageable memory the staging copies)."""
+        if isinstance(a, torch.Tensor):
+            assert not a.is_cuda and a.dtype == torch.complex128 and a.is_contiguous(), name
+            assert a.numel() == n, name
+            return a, ctypes.c_void_p(a.data_ptr())
+        a = np.ascontiguousarray(a, dtype=np.complex128)
+        assert a.size == n, name
+        return a, ctypes.c_void_p(a.ctypes.data)
+
     def degrid_host(self, grid, vis_out=None, accumulate=False, stream=None):
-        g = np.ascontiguousarray(grid, dtype=np.complex128)
-        assert g.size == self.nu * self.half_nv
+        """Reference-layout host buffers (numpy or CPU tensors, complex128): half-plane grid ->
+        row-order visibilities, accumulated into vis_out when accumulate=True."""
+        g, gp = self._host(grid, self.nu * self.half_nv, "grid")
         if vis_out is None:
             vis_out = np.zeros(self.nvis, dtype=np.complex128)
-        assert vis_out.dtype == np.complex128 and vis_out.flags.c_contiguous
-        N.check(N.lib().lentils_degrid_host(self._handle, ctypes.c_void_p(g.ctypes.data),
-                                            ctypes.c_void_p(vis_out.ctypes.data),
-                                            1 if accumulate else 0, _stream_ptr(stream)))
+        if isinstance(vis_out, np.ndarray):
+            assert vis_out.dtype == np.complex128 and vis_out.flags.c_contiguous
+        vis_out, vp = self._host(vis_out, self.nvis, "vis_out")
+        N.check(N.lib().lentils_degrid_host(self._handle, gp, vp, 1 if accumulate else 0,
+                                            _stream_ptr(stream)))
         return vis_out
 
     def grid_host(self, vis, grid_out=None, accumulate=False, stream=None):
-        v = np.ascontiguousarray(vis, dtype=np.complex128).reshape(-1)
-        assert v.size == self.nvis
+        """Row-order host visibilities -> half-plane host grid (accumulated when
+        accumulate=True); buffers as for degrid_host."""
+        v, vp = self._host(vis, self.nvis, "vis")
         if grid_out is None:
             grid_out = np.zeros((self.nu, self.half_nv), dtype=np.complex128)
-        assert grid_out.dtype == np.complex128 and grid_out.flags.c_contiguous
-        N.check(N.lib().lentils_grid_host(self._handle, ctypes.c_void_p(v.ctypes.data),
-                                          ctypes.c_void_p(grid_out.ctypes.data),
-                                          1 if accumulate else 0, _stream_ptr(stream)))
+        if isinstance(grid_out, np.ndarray):
+            assert grid_out.dtype == np.complex128 and grid_out.flags.c_contiguous
+        grid_out, gp = self._host(grid_out, self.nu * self.half_nv, "grid_out")
+        N.check(N.lib().lentils_grid_host(self._handle, vp, gp, 1 if accumulate else 0,
+                                          _stream_ptr(stream)))
         return grid_out
 
 
