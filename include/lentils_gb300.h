@@ -321,6 +321,30 @@ typedef struct {
     int fallback;        /* flexible CG: 1 if it switched to plain Jacobi-CG on stagnation */
 } lentils_cg_result;
 
+/* ------------------------------------------------------------------------------------------
+ * Dirty-beam (blurred covariance) form of F^T C^-1 F, the reference's production CG data term
+ * (RadioDataset.blurred_covariance_operator, lentils/common/data_base.py:115-129):
+ *   B x = crop(pad(x) (*) roll(beam))   (circular convolution on the 2nx x 2ny padded grid)
+ * beam: the dirty beam NUFFT_beam^T C^-1 1 on the beam space (2nx x 2ny pixels, bounds
+ * +-(nx dx, ny dy), data_base.py:147-172), device FP64, x-major; nx, ny even. Applied with
+ * cuFFT in FP32 (lentils_bcb_apply) or FP64 (lentils_bcb_apply64) on (nx, ny) images.
+ * ---------------------------------------------------------------------------------------- */
+typedef struct lentils_bcb lentils_bcb;
+int lentils_bcb_create(lentils_bcb **op, const double *beam, int nx, int ny, void *stream);
+int lentils_bcb_destroy(lentils_bcb *op);
+int lentils_bcb_apply(lentils_bcb *op, const float *x, float *out, void *stream);
+int lentils_bcb_apply64(lentils_bcb *op, const double *x, double *out, void *stream);
+double lentils_bcb_centre(const lentils_bcb *op);
+/* The normal operator with the dirty-beam data term: A = L^T B L + lambda R^T R (nimg = nx*ny
+ * of B); its right-hand side from the dirty image F^T C^-1 d by lentils_normal_op_rhs_image64.
+ * Works with lentils_cg_solve / lentils_fcg_solve as the visibility form does. */
+int lentils_normal_op_create_bcb(lentils_normal_op **out, lentils_lensop *L, lentils_bcb *B,
+                                 int nimg, int nsx, int nsy, double src_dx, double src_dy,
+                                 double lambda, void *stream);
+/* b = L^T d_img (FP64, device) */
+int lentils_normal_op_rhs_image64(lentils_normal_op *op, const double *d_img, double *b,
+                                  void *stream);
+
 /* Iterative refinement: outer FP64 residuals r = b - A x, inner Jacobi-preconditioned CG with
  * the FP32 operator (inv_diag32 may be NULL for no preconditioner). x (f64, device) holds the
  * initial guess and receives the solution. */

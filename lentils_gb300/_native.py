@@ -141,6 +141,14 @@ _SIGNATURES = [
     ("lentils_normal_op_rhs64", c_int, [c_void_p, c_void_p, c_void_p, c_void_p]),
     ("lentils_normal_op_jacobi", c_int, [c_void_p, c_void_p, c_void_p, c_void_p]),
     ("lentils_normal_op_weight_sum", c_double, [c_void_p]),
+    ("lentils_bcb_create", c_int, [POINTER(c_void_p), c_void_p, c_int, c_int, c_void_p]),
+    ("lentils_bcb_destroy", c_int, [c_void_p]),
+    ("lentils_bcb_apply", c_int, [c_void_p, c_void_p, c_void_p, c_void_p]),
+    ("lentils_bcb_apply64", c_int, [c_void_p, c_void_p, c_void_p, c_void_p]),
+    ("lentils_bcb_centre", c_double, [c_void_p]),
+    ("lentils_normal_op_create_bcb", c_int, [POINTER(c_void_p), c_void_p, c_void_p, c_int, c_int,
+                                             c_int, c_double, c_double, c_double, c_void_p]),
+    ("lentils_normal_op_rhs_image64", c_int, [c_void_p, c_void_p, c_void_p, c_void_p]),
     ("lentils_cg_solve", c_int, [c_void_p, c_void_p, c_void_p, c_void_p, POINTER(CGOptionsC),
                                  POINTER(CGResultC), c_void_p]),
     ("lentils_prior_gradient_apply", c_int, [c_void_p, c_void_p, c_int, c_int, c_double,

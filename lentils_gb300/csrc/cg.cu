@@ -27,9 +27,17 @@
 #include "common.cuh"
 #include "unet.cuh"
 
+namespace lentils {
+int bcb_apply32(lentils_bcb *op, const float *x, float *out, cudaStream_t s);
+int bcb_apply64(lentils_bcb *op, const double *x, double *out, cudaStream_t s);
+double bcb_centre(const lentils_bcb *op);
+int bcb_image_size(const lentils_bcb *op);
+}  // namespace lentils
+
 struct lentils_normal_op {
     lentils_lensop *L;
     lentils_nufft *F;
+    lentils_bcb *bcb;  // dirty-beam form of F^T C^-1 F (then F is unused)
     int nsx, nsy, nsrc, nimg;
     long long nvis;
     double lambda, idx2, idy2;
@@ -586,6 +594,56 @@ int lentils_normal_op_create(lentils_normal_op **out, lentils_lensop *L, lentils
     return LENTILS_OK;
 }
 
+// The same operator with the dirty-beam form of the data term: A = L^T B L + lambda R^T R with
+// B the blurred covariance (lentils_bcb); no visibilities in the matvec.
+int lentils_normal_op_create_bcb(lentils_normal_op **out, lentils_lensop *L, lentils_bcb *B,
+                                 int nimg, int nsx, int nsy, double src_dx, double src_dy,
+                                 double lambda, void *stream)
+{
+    clear_error();
+    if (!out || !L || !B || nimg < 1 || nsx < 1 || nsy < 1 || !(src_dx > 0) || !(src_dy > 0))
+        return set_error(LENTILS_ERR_INVALID, "normal_op_create_bcb: bad arguments");
+    if (bcb_image_size(B) != nimg)
+        return set_error(LENTILS_ERR_INVALID, "normal_op_create_bcb: beam image %d != %d pixels",
+                         bcb_image_size(B), nimg);
+    (void)stream;
+    *out = nullptr;
+    lentils_normal_op *op = new (std::nothrow) lentils_normal_op();
+    if (!op) return set_error(LENTILS_ERR_ALLOC, "normal_op_create_bcb: host allocation");
+    memset(op, 0, sizeof(*op));
+    op->L = L;
+    op->bcb = B;
+    op->nsx = nsx;
+    op->nsy = nsy;
+    op->nsrc = nsx * nsy;
+    op->nimg = nimg;
+    op->lambda = lambda;
+    op->idx2 = 1.0 / (src_dx * src_dx);
+    op->idy2 = 1.0 / (src_dy * src_dy);
+    op->wsum = bcb_centre(B);  // diagonal of B: the beam at zero offset
+    cudaError_t e = cudaMalloc(&op->img32a, sizeof(float) * nimg);
+    if (e == cudaSuccess) e = cudaMalloc(&op->img32b, sizeof(float) * nimg);
+    if (e == cudaSuccess) e = cudaMalloc(&op->img64a, sizeof(double) * nimg);
+    if (e == cudaSuccess) e = cudaMalloc(&op->img64b, sizeof(double) * nimg);
+    if (e != cudaSuccess) {
+        const int st = cuda_status(e, "normal_op_create_bcb");
+        normal_op_free(op);
+        delete op;
+        return st;
+    }
+    *out = op;
+    return LENTILS_OK;
+}
+
+// b = L^T d_img in FP64 for an image-plane data vector (the dirty image F^T C^-1 d)
+int lentils_normal_op_rhs_image64(lentils_normal_op *op, const double *d_img, double *b,
+                                  void *stream)
+{
+    clear_error();
+    if (!op || !d_img || !b) return set_error(LENTILS_ERR_INVALID, "normal_op_rhs_image64: null");
+    return lentils_lensop_apply_t64(op->L, d_img, b, stream);
+}
+
 int lentils_normal_op_destroy(lentils_normal_op *op)
 {
     clear_error();
@@ -602,10 +660,15 @@ int lentils_normal_op_apply(lentils_normal_op *op, const float *s_in, float *out
     cudaStream_t s = (cudaStream_t)stream;
     int st;
     if ((st = lentils_lensop_apply(op->L, s_in, op->img32a, stream))) return st;
-    if ((st = lentils_nufft_forward(op->F, op->img32a, (float *)op->vis32, stream))) return st;
-    scale_vis_kernel<float2, float><<<nb(op->nvis), 256, 0, s>>>(op->vis32, op->w32, op->nvis);
-    LENTILS_CHECK_LAUNCH("scale_vis_kernel");
-    if ((st = lentils_nufft_adjoint(op->F, (const float *)op->vis32, op->img32b, stream))) return st;
+    if (op->bcb) {
+        if ((st = bcb_apply32(op->bcb, op->img32a, op->img32b, s))) return st;
+    } else {
+        if ((st = lentils_nufft_forward(op->F, op->img32a, (float *)op->vis32, stream))) return st;
+        scale_vis_kernel<float2, float><<<nb(op->nvis), 256, 0, s>>>(op->vis32, op->w32, op->nvis);
+        LENTILS_CHECK_LAUNCH("scale_vis_kernel");
+        if ((st = lentils_nufft_adjoint(op->F, (const float *)op->vis32, op->img32b, stream)))
+            return st;
+    }
     if ((st = lentils_lensop_apply_t(op->L, op->img32b, out, stream))) return st;
     rtr_kernel<float><<<nb(op->nsrc), 256, 0, s>>>(s_in, out, op->nsx, op->nsy, (float)op->idx2,
                                                    (float)op->idy2, (float)op->lambda, 1);
@@ -621,11 +684,17 @@ int lentils_normal_op_apply64(lentils_normal_op *op, const double *s_in, double 
     cudaStream_t s = (cudaStream_t)stream;
     int st;
     if ((st = lentils_lensop_apply64(op->L, s_in, op->img64a, stream))) return st;
-    if ((st = lentils_nufft_forward64(op->F, op->img64a, (double *)op->vis64, stream))) return st;
-    scale_vis_kernel<double2, double><<<nb(op->nvis), 256, 0, s>>>(op->vis64, op->w64, op->nvis);
-    LENTILS_CHECK_LAUNCH("scale_vis_kernel");
-    if ((st = lentils_nufft_adjoint64(op->F, (const double *)op->vis64, op->img64b, stream)))
-        return st;
+    if (op->bcb) {
+        if ((st = bcb_apply64(op->bcb, op->img64a, op->img64b, s))) return st;
+    } else {
+        if ((st = lentils_nufft_forward64(op->F, op->img64a, (double *)op->vis64, stream)))
+            return st;
+        scale_vis_kernel<double2, double><<<nb(op->nvis), 256, 0, s>>>(op->vis64, op->w64,
+                                                                        op->nvis);
+        LENTILS_CHECK_LAUNCH("scale_vis_kernel");
+        if ((st = lentils_nufft_adjoint64(op->F, (const double *)op->vis64, op->img64b, stream)))
+            return st;
+    }
     if ((st = lentils_lensop_apply_t64(op->L, op->img64b, out, stream))) return st;
     rtr_kernel<double><<<nb(op->nsrc), 256, 0, s>>>(s_in, out, op->nsx, op->nsy, op->idx2,
                                                     op->idy2, op->lambda, 1);
@@ -638,6 +707,9 @@ int lentils_normal_op_rhs64(lentils_normal_op *op, const double *d_plan, double 
 {
     clear_error();
     if (!op || !d_plan || !b) return set_error(LENTILS_ERR_INVALID, "normal_op_rhs64: null");
+    if (op->bcb)
+        return set_error(LENTILS_ERR_INVALID,
+                         "normal_op_rhs64: dirty-beam operator; use normal_op_rhs_image64");
     cudaStream_t s = (cudaStream_t)stream;
     LENTILS_CUDA_TRY(cudaMemcpyAsync(op->vis64, d_plan, sizeof(double2) * op->nvis,
                                      cudaMemcpyDeviceToDevice, s));

@@ -16,15 +16,21 @@ import torch
 
 from . import _native as N
 from .gridding import _ptr
-from .operators import BilinearLensOperator, NUFFTOperator
+from .operators import BilinearLensOperator, BlurredCovarianceOperator, NUFFTOperator
 
 
 class SourceInversion:
     def __init__(self, vis_space, data, sigma, image_space, source_space, lensmodel, z_src,
                  strength, kernel_support=4, pad_factor=2, kb_beta=None, data_mask=None,
-                 nufft=None):
+                 nufft=None, data_term="visibilities"):
         """nufft: an existing NUFFTOperator for vis_space and image_space to share (lens-model
-        sweeps over one visibility set); built here when None."""
+        sweeps over one visibility set); built here when None. data_term: "visibilities"
+        (F^T C^-1 F through the gridder every matvec) or "bcb" (the dirty-beam convolution,
+        RadioDataset.blurred_covariance_operator, data_base.py:115-129, with the right-hand
+        side L^T times the dirty image F^T C^-1 d)."""
+        if data_term not in ("visibilities", "bcb"):
+            raise ValueError("data_term: 'visibilities' or 'bcb'")
+        self.data_term = data_term
         self.stream = torch.cuda.Stream()
         with torch.cuda.stream(self.stream):
             self.nufft = nufft if nufft is not None else NUFFTOperator(
@@ -45,16 +51,32 @@ class SourceInversion:
             L = N.lib()
             N.check(L.lentils_plan_gather_real(plan.handle, _ptr(wu), _ptr(self.weights), sp))
             self._normal = ctypes.c_void_p()
-            N.check(L.lentils_normal_op_create(
-                ctypes.byref(self._normal), self.lens.handle, self.nufft.handle,
-                _ptr(self.weights), nvis, image_space.nx * image_space.ny, source_space.nx,
-                source_space.ny, source_space.dx, source_space.dy, float(strength), sp))
-            d = torch.as_tensor(np.ascontiguousarray(data, dtype=np.complex128).reshape(-1)).cuda()
-            dp = torch.empty(nvis, dtype=torch.complex128, device="cuda")
-            N.check(L.lentils_vis_to_plan64(plan.handle, _ptr(d), _ptr(dp), sp))
             self.nsrc = source_space.nx * source_space.ny
             self.b = torch.empty(self.nsrc, dtype=torch.float64, device="cuda")
-            N.check(L.lentils_normal_op_rhs64(self._normal, _ptr(dp), _ptr(self.b), sp))
+            nimg = image_space.nx * image_space.ny
+            if data_term == "bcb":
+                self.bcb = BlurredCovarianceOperator(vis_space, image_space, w_user,
+                                                     kernel_support, pad_factor, kb_beta)
+                N.check(L.lentils_normal_op_create_bcb(
+                    ctypes.byref(self._normal), self.lens.handle, self.bcb.handle, nimg,
+                    source_space.nx, source_space.ny, source_space.dx, source_space.dy,
+                    float(strength), sp))
+                dv = np.ascontiguousarray(data, dtype=np.complex128).reshape(-1)
+                dirty = self.nufft.T * (w_user * dv)   # dirty image, FP64 on the GPU
+                self.dirty_image = np.asarray(dirty, dtype=np.float64).reshape(-1)
+                di = torch.as_tensor(self.dirty_image).cuda()
+                N.check(L.lentils_normal_op_rhs_image64(self._normal, _ptr(di), _ptr(self.b),
+                                                        sp))
+            else:
+                N.check(L.lentils_normal_op_create(
+                    ctypes.byref(self._normal), self.lens.handle, self.nufft.handle,
+                    _ptr(self.weights), nvis, nimg, source_space.nx, source_space.ny,
+                    source_space.dx, source_space.dy, float(strength), sp))
+                d = torch.as_tensor(np.ascontiguousarray(data, dtype=np.complex128)
+                                    .reshape(-1)).cuda()
+                dp = torch.empty(nvis, dtype=torch.complex128, device="cuda")
+                N.check(L.lentils_vis_to_plan64(plan.handle, _ptr(d), _ptr(dp), sp))
+                N.check(L.lentils_normal_op_rhs64(self._normal, _ptr(dp), _ptr(self.b), sp))
             self.inv_diag = torch.empty(self.nsrc, dtype=torch.float64, device="cuda")
             self.inv_diag32 = torch.empty(self.nsrc, dtype=torch.float32, device="cuda")
             N.check(L.lentils_normal_op_jacobi(self._normal, _ptr(self.inv_diag),

@@ -357,3 +357,60 @@ class PriorCovarianceOperator(Operator):
         return out.cpu().numpy().reshape(sp.shape) if host else out.reshape(sp.nx, sp.ny)
 
     _transpose = _forward
+
+
+class BlurredCovarianceOperator(Operator):
+    """F^T C^-1 F as a convolution with the dirty beam (RadioDataset.blurred_covariance_operator,
+    lentils/common/data_base.py:115-129): the beam NUFFT_beam^T C^-1 1 is computed once on the
+    beam space (2nx x 2ny pixels, bounds +-(nx dx, ny dy), data_base.py:147-172) by the FP64
+    NUFFT adjoint on the GPU; each application is pad, rFFT, multiply, inverse rFFT, crop
+    (lentils_bcb). `weights` are C^-1 per visibility in the reference's row order. Symmetric.
+    numpy in -> FP64 on the GPU -> numpy out; a float32 CUDA tensor -> FP32."""
+
+    def __init__(self, vis_space, image_space, weights, kernel_support=4, pad_factor=2,
+                 kb_beta=None):
+        nx, ny = image_space.nx, image_space.ny
+        if nx % 2 or ny % 2:
+            raise ValueError("the dirty-beam form needs even image sizes")
+        rx, ry = image_space.dx * nx, image_space.dy * ny
+        self.beam_space = ImageSpace(shape=(2 * nx, 2 * ny), bounds=[(-rx, rx), (-ry, ry)])
+        nufft_beam = NUFFTOperator(vis_space, self.beam_space, pad_factor, kernel_support,
+                                   kb_beta)
+        w = np.asarray(weights, dtype=np.float64).reshape(-1)
+        self.dirty_beam = np.ascontiguousarray(
+            (nufft_beam.T * (w + 0.0j)).reshape(2 * nx, 2 * ny), dtype=np.float64)
+        nufft_beam.close()
+        beam_d = torch.as_tensor(self.dirty_beam).cuda()
+        self._h = ctypes.c_void_p()
+        N.check(N.lib().lentils_bcb_create(ctypes.byref(self._h), _ptr(beam_d), nx, ny,
+                                           _stream_ptr()))
+        torch.cuda.current_stream().synchronize()
+        super().__init__(image_space, image_space)
+        self._T = self
+
+    @property
+    def handle(self):
+        return self._h
+
+    @property
+    def centre(self):
+        return N.lib().lentils_bcb_centre(self._h)
+
+    def __del__(self):
+        try:
+            if self._h.value:
+                N.lib().lentils_bcb_destroy(self._h)
+        except Exception:
+            pass
+
+    def _forward(self, x):
+        host = not _is_tensor(x)
+        sp = self.space_left
+        v = torch.as_tensor(np.ascontiguousarray(x, dtype=np.float64).reshape(-1)).cuda() if host \
+            else x.contiguous().reshape(-1)
+        out = torch.empty_like(v)
+        fn = N.lib().lentils_bcb_apply if v.dtype == torch.float32 else N.lib().lentils_bcb_apply64
+        N.check(fn(self._h, _ptr(v), _ptr(out), _stream_ptr()))
+        return out.cpu().numpy().reshape(sp.nx, sp.ny) if host else out.reshape(sp.nx, sp.ny)
+
+    _transpose = _forward

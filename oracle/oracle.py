@@ -346,6 +346,38 @@ class NufftOracle:
                                            self.use_ref))
 
 
+def beam_geom(img: ImageGeom):
+    """Beam space of an image: 2nx x 2ny pixels, bounds +-(nx dx, ny dy); restates
+    RadioDataset._make_beam_space, data_base.py:147-158."""
+    rx, ry = img.dx * img.nx, img.dy * img.ny
+    return ImageGeom((2 * img.nx, 2 * img.ny), [(-rx, rx), (-ry, ry)])
+
+
+def dirty_beam(vis: VisGeom, img: ImageGeom, weights, wsup=4, beta=None):
+    """NUFFT_beam^T C^-1 1 on the beam space; restates RadioDataset.dirty_beam,
+    data_base.py:160-172."""
+    nb = NufftOracle(vis, beam_geom(img), 2, wsup, beta)
+    return nb.adjoint(np.asarray(weights, dtype=np.float64) + 0.0j)
+
+
+def bcb_apply(beam, img: ImageGeom, x):
+    """Blurred covariance F^T C^-1 F x as the dirty-beam convolution; restates
+    RadioDataset.blurred_covariance_operator, data_base.py:115-129: zero padding by
+    ((p-1)n+1)//2 per side (fourier_operators.py:33-47), rfft2 (norm 'backward'), the spectrum
+    of the beam rolled by half the padded size over the padded pixel count, irfft2 (norm
+    'forward'), crop."""
+    nx, ny = img.nx, img.ny
+    padx, pady = (nx + 1) // 2, (ny + 1) // 2
+    shape = (nx + 2 * padx, ny + 2 * pady)
+    z = np.zeros(shape)
+    z[padx:padx + nx, pady:pady + ny] = np.asarray(x, dtype=np.float64).reshape(nx, ny)
+    db = np.roll(np.asarray(beam, dtype=np.float64).reshape(shape),
+                 [shape[0] // 2, shape[1] // 2], axis=[-2, -1])
+    dbfft = sfft.rfft2(db, norm="backward") / np.prod(db.shape)
+    y = sfft.irfft2(dbfft * sfft.rfft2(z, norm="backward"), s=shape, norm="forward")
+    return y[padx:padx + nx, pady:pady + ny].copy()
+
+
 def dft_matrix(vis: VisGeom, img: ImageGeom):
     """Dense DFT matrix (2*nrows x npix, rows cos/sin interleaved); restates dft_matrix_csr,
     nufft.c:128-161, densely (masked columns zero)."""

@@ -111,3 +111,19 @@ def test_adjoint_relations(oracle_mod):
     a = np.vdot(y, nufft.forward(x)).real
     b = np.sum(x * nufft.adjoint(y))
     assert abs(a - b) <= 1e-12 * abs(a)
+
+
+def test_oracle_dirty_beam_form_matches_explicit_normal_operator():
+    """The dirty-beam convolution (data_base.py:115-129) equals F^T C^-1 F through the
+    visibilities up to the NUFFT's own accuracy (small image, W = 8)."""
+    rng = np.random.default_rng(12)
+    img = O.ImageGeom((24, 20), [(-0.24, 0.24), (-0.2, 0.2)])
+    four = O.FourierGeom(O.padded_geom(img, 2)[0])
+    vis = O.VisGeom(O.synth_uv(rng, 3000, four, 0.45, 4), [1.0])
+    w = rng.uniform(0.5, 2.0, vis.nvis)
+    ora = O.NufftOracle(vis, img, 2, 4)
+    beam = O.dirty_beam(vis, img, w, 4)
+    assert beam.shape == (48, 40)
+    x = rng.normal(size=img.shape)
+    explicit = ora.adjoint(w * ora.forward(x))
+    assert O.rel_l2(O.bcb_apply(beam, img, x), explicit) < 1e-6
