@@ -394,6 +394,27 @@ def run_cg_bench(repeats=3):
                               "fallback": best["fallback"], "jacobi_weight": 0.3,
                               "training": {k: meta[k] for k in ("draws", "pairs", "steps",
                                                                 "loss")}})
+    # the same inversion with the dirty-beam data term (the reference's production form)
+    t1 = time.perf_counter()
+    inv_b = workloads.inversion(nufft=inv.nufft, data_term="bcb")[0]
+    out["bcb_setup_s"] = time.perf_counter() - t1
+    runs_b = {
+        "bcb_plain_jacobi_pcg": lambda tol: inv_b.solve(tol=tol, inner_tol=inner_tol),
+        "bcb_jacobi_fcg8": lambda tol: inv_b.solve_flexible(None, tol=tol, inner_tol=inner_tol,
+                                                            window=8),
+        "bcb_learned_fcg8": lambda tol: inv_b.solve_flexible(net, tol=tol, inner_tol=inner_tol,
+                                                             window=8),
+    }
+    for name, fn in runs_b.items():
+        fn(1e-2)
+        best = None
+        for _ in range(repeats):
+            _, info = fn(1e-6)
+            if best is None or info["seconds"] < best["seconds"]:
+                best = info
+        out[name] = {"converged": best["converged"], "rel_residual_fp64": best["rel_residual"],
+                     "outer": best["outer"], "inner_iterations": best["inner_total"],
+                     "solve_s": best["seconds"]}
     p, lr = out["plain_jacobi_pcg"], out["learned_fcg8"]
     out["learned_vs_plain_time"] = p["solve_s"] / lr["solve_s"]
     out["learned_vs_plain_iterations"] = p["inner_iterations"] / max(1, lr["inner_iterations"])
@@ -402,7 +423,7 @@ def run_cg_bench(repeats=3):
     s32 = torch.randn(inv.nsrc, device="cuda", dtype=torch.float32)
     s64 = s32.double()
     o32, o64 = torch.empty_like(s32), torch.empty_like(s64)
-    ev = [torch.cuda.Event(enable_timing=True) for _ in range(6)]
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(8)]
     sp = ctypes.c_void_p(inv.stream.cuda_stream)
     L = N.lib()
     dinv, feat = inv.inv_diag32, learned.features(inv.inv_diag32)
@@ -423,10 +444,18 @@ def run_cg_bench(repeats=3):
         N.check(L.lentils_unet_precondition(net.handle, _ptr(s32), _ptr(dinv), _ptr(feat),
                                             _ptr(o32), sp))
     ev[4].record(inv.stream)
+    spb = ctypes.c_void_p(inv_b.stream.cuda_stream)
+    for _ in range(3):
+        N.check(L.lentils_normal_op_apply(inv_b.handle, _ptr(s32), _ptr(o32), spb))
+    ev[5].record(inv_b.stream)
+    for _ in range(10):
+        N.check(L.lentils_normal_op_apply(inv_b.handle, _ptr(s32), _ptr(o32), spb))
+    ev[6].record(inv_b.stream)
     torch.cuda.synchronize()
     out.update({"matvec32_ms": ev[0].elapsed_time(ev[1]) / 10,
                 "matvec64_ms": ev[2].elapsed_time(ev[3]),
-                "precondition_ms": ev[3].elapsed_time(ev[4]) / 10})
+                "precondition_ms": ev[3].elapsed_time(ev[4]) / 10,
+                "bcb_matvec32_ms": ev[5].elapsed_time(ev[6]) / 10})
     return out
 
 

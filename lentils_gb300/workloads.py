@@ -57,13 +57,15 @@ def simulate(nufft, ims, srcs, glm, s_true, rng, sigma=1.0, z_src=Z_SRC):
     return model.reshape(-1) + complex_normal(rng, model.size, sigma)
 
 
-def inversion(seed=SEED, nufft=None):
-    """(SourceInversion of the workload, shared NUFFT operator, geometry tuple)."""
+def inversion(seed=SEED, nufft=None, data_term="visibilities"):
+    """(SourceInversion of the workload, shared NUFFT operator, geometry tuple); data_term
+    "bcb" uses the dirty-beam form of F^T C^-1 F."""
     from .inversion import SourceInversion
     from .operators import NUFFTOperator
     vs, ims, srcs, uvw, rng = geometry(seed)
     F = nufft if nufft is not None else NUFFTOperator(vs, ims)
     glm = lens_model()
     d = simulate(F, ims, srcs, glm, two_blob_source(srcs), rng)
-    inv = SourceInversion(vs, d, 1.0, ims, srcs, glm, Z_SRC, LAMBDA, nufft=F)
+    inv = SourceInversion(vs, d, 1.0, ims, srcs, glm, Z_SRC, LAMBDA, nufft=F,
+                          data_term=data_term)
     return inv, F, (vs, ims, srcs, uvw)
