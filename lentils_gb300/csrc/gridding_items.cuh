@@ -237,8 +237,12 @@ constexpr int kGridBatch = 256;  // visibilities per weight batch (= threads per
 // the extended tile with plain load-add-store, its groups taking turns (warp vote, then one
 // group at a time between __syncwarp), so no two lanes update a cell at once; the copies are
 // summed once per work item before the global flush.
-// One work item by a CTA of kGridBatch threads; smraw: grid_rows_smem_bytes<W2>(g).
-template <int W2>
+// SHARED = true: one extended tile for the whole CTA, flushed by every group at once with
+// shared-memory float atomics (collisions only where two groups' windows overlap), which
+// removes the turn-taking and the final summation of copies and needs an eighth of the tile
+// memory.
+// One work item by a CTA of kGridBatch threads; smraw: grid_rows_smem_bytes<W2, SHARED>(g).
+template <int W2, bool SHARED = false>
 __device__ __forceinline__ void grid_rows_item(const float2 *__restrict__ vis,
                                                const uint2 *__restrict__ coords,
                                                float2 *__restrict__ grid, const WorkItem &it,
@@ -251,14 +255,15 @@ __device__ __forceinline__ void grid_rows_item(const float2 *__restrict__ vis,
     constexpr int NG = NW * G;                        // groups per CTA
     constexpr int SHARE = kGridBatch / NG;            // visibilities per group and batch
     static_assert((STR % 4) == 0, "rows must stay 16-byte aligned");
+    constexpr int NT = SHARED ? 1 : NW;               // tile copies
     const int E = g.E, S = g.stride;
-    float2 *tiles = reinterpret_cast<float2 *>(smraw);  // NW x (E x S)
-    const size_t tile_bytes = ((sizeof(float2) * (size_t)NW * E * S) + 15) & ~size_t(15);
+    float2 *tiles = reinterpret_cast<float2 *>(smraw);  // NT x (E x S)
+    const size_t tile_bytes = ((sizeof(float2) * (size_t)NT * E * S) + 15) & ~size_t(15);
     float *rows = reinterpret_cast<float *>(smraw + tile_bytes);  // NG*SHARE x STR
-    for (int e = threadIdx.x; e < NW * E * S; e += blockDim.x) tiles[e] = make_float2(0.f, 0.f);
+    for (int e = threadIdx.x; e < NT * E * S; e += blockDim.x) tiles[e] = make_float2(0.f, 0.f);
 
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    float2 *mytile = tiles + warp * E * S;
+    float2 *mytile = tiles + (SHARED ? 0 : warp) * E * S;
     const int grp = lane / W2, ri = lane - grp * W2;
     const bool lane_on = grp < G;
     const int gid = warp * G + (lane_on ? grp : 0);   // this lane's range
@@ -298,8 +303,8 @@ __device__ __forceinline__ void grid_rows_item(const float2 *__restrict__ vis,
                 reinterpret_cast<float4 *>(row + 2 * W2)[0] =
                     make_float4(x.x, x.y, __int_as_float((lu << 6) | lv), 0.f);
                 if ((c.x | c.y) & kExtraTapBit)  // rare: straight into a tile, atomically
-                    grid_extra_taps<W2, float>(tiles + warp * E * S, S, lu, lv, c, wu, wv,
-                                               kb.edge, x);
+                    grid_extra_taps<W2, float>(tiles + (SHARED ? 0 : warp) * E * S, S, lu, lv,
+                                               c, wu, wv, kb.edge, x);
             }
         }
         __syncthreads();
@@ -316,7 +321,18 @@ __device__ __forceinline__ void grid_rows_item(const float2 *__restrict__ vis,
                 key = __float_as_int(xk.z);
             }
             const bool need = lane_on && cur >= 0 && (b == nbatch || key != cur);
-            if (__any_sync(0xffffffffu, need)) {
+            if constexpr (SHARED) {
+                if (need) {
+                    float2 *p = mytile + ((cur >> 6) + 1 + ri) * S + (cur & 63) + 1;
+#pragma unroll
+                    for (int j = 0; j < W2; ++j) {
+                        atomicAdd(&p[j].x, acc[j].x);
+                        atomicAdd(&p[j].y, acc[j].y);
+                        acc[j] = make_float2(0.f, 0.f);
+                    }
+                    cur = -1;
+                }
+            } else if (__any_sync(0xffffffffu, need)) {
                 for (int hgrp = 0; hgrp < G; ++hgrp) {
                     if (need && grp == hgrp) {
                         float2 *p = mytile + ((cur >> 6) + 1 + ri) * S + (cur & 63) + 1;
@@ -353,25 +369,27 @@ __device__ __forceinline__ void grid_rows_item(const float2 *__restrict__ vis,
         }
     }
     __syncthreads();
-    for (int e = threadIdx.x; e < E * S; e += blockDim.x) {  // sum the warps' copies
-        float2 a = tiles[e];
+    if constexpr (!SHARED) {
+        for (int e = threadIdx.x; e < E * S; e += blockDim.x) {  // sum the warps' copies
+            float2 a = tiles[e];
 #pragma unroll
-        for (int q = 1; q < NW; ++q) {
-            const float2 bq = tiles[q * E * S + e];
-            a.x += bq.x;
-            a.y += bq.y;
+            for (int q = 1; q < NW; ++q) {
+                const float2 bq = tiles[q * E * S + e];
+                a.x += bq.x;
+                a.y += bq.y;
+            }
+            tiles[e] = a;
         }
-        tiles[e] = a;
+        __syncthreads();
     }
-    __syncthreads();
     grid_flush_extended<W2, float>(tiles, grid, it, g);
 }
 
-template <int W2>
+template <int W2, bool SHARED = false>
 __host__ __device__ inline size_t grid_rows_smem_bytes(const GridGeom &g)
 {
-    const size_t tile_bytes =
-        ((sizeof(float2) * (size_t)(kGridBatch / 32) * g.E * g.stride) + 15) & ~size_t(15);
+    const size_t ntile = SHARED ? 1 : kGridBatch / 32;
+    const size_t tile_bytes = ((sizeof(float2) * ntile * g.E * g.stride) + 15) & ~size_t(15);
     return tile_bytes + sizeof(float) * (size_t)kGridBatch * (2 * W2 + 4);
 }
 

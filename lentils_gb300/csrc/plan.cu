@@ -633,8 +633,8 @@ int lentils_plan_destroy(lentils_plan *p)
 int lentils_plan_set_grid_variant(lentils_plan *p, int variant)
 {
     clear_error();
-    if (!p || variant < 0 || variant > 2)
-        return set_error(LENTILS_ERR_INVALID, "plan_set_grid_variant: variant 0, 1 or 2");
+    if (!p || variant < 0 || variant > 3)
+        return set_error(LENTILS_ERR_INVALID, "plan_set_grid_variant: variant 0, 1, 2 or 3");
     p->grid_variant = variant;
     return LENTILS_OK;
 }
