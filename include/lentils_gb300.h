@@ -129,9 +129,10 @@ void grid_cpu(lentils_visibility_space visspace, double *vis, lentils_fourier_sp
               double *grid, int wsup, double kb_beta, int direction);
 
 /* Lens equation beta = theta - sum_l alpha_l(theta) for npoints interleaved (x, y) points.
- * Replaces deflect_points, lentils/backend/deflect.c:60-66. want_deriv must be 0 in this
- * build (the reference's Python never requests derivatives; lentils_last_error() reports
- * LENTILS_ERR_UNSUPPORTED otherwise and p_out is left untouched). */
+ * Replaces deflect_points, lentils/backend/deflect.c:60-66. With want_deriv != 0 it also does
+ * what the reference does with its single deriv pointer: deriv[0..11] += the PEMD parameter
+ * derivatives d alpha / d (b, qh, q, x, y, th), (x, y) components, summed over all points and
+ * PEMD lenses (deflect.c:330-338; the per-point layout is lentils_deflect_grad). */
 void deflect_points(lentils_global_lens_model glm, double *p_in, int npoints, double *p_out,
                     int want_deriv, double *deriv);
 
@@ -510,6 +511,17 @@ int lentils_deflect_f32(const lentils_mass_model *lenses, int nlenses, const flo
                         float *out, long long npoints, void *stream);
 int lentils_deflect_f64io(const lentils_mass_model *lenses, int nlenses, const double *points,
                           double *out, long long npoints, void *stream);
+/* Parameter derivatives of the deflection at each point, FP64: grads (device, float64) is
+ * (8, npoints, 2), OVERWRITTEN, for the parameters (b, qh, q, x, y, th, ss, sa) summed over
+ * the lenses -- the per-point layout the reference's GlobalLensModel.deflect(deriv=True)
+ * allocates (lens_models.py:71-73). PEMD terms as deflect_PEMD_series computes them
+ * (deflect.c:304-338, hyp2f1_series :186-236); external shear (x, y, ss, sa) as the
+ * derivative block of deflect_external_potential states it (deflect.c:110-119, compiled out
+ * in the reference); multipoles contribute none. At most 8 lenses. The drop-in
+ * deflect_points(want_deriv = 1) keeps the reference's own accumulation instead: deriv[0..11]
+ * += the PEMD terms summed over all points. */
+int lentils_deflect_grad(const lentils_mass_model *lenses, int nlenses, const double *points,
+                         double *grads, long long npoints, void *stream);
 
 #ifdef __cplusplus
 }

@@ -188,6 +188,8 @@ _SIGNATURES = [
     ("lentils_deflect_f32", c_int, [c_void_p, c_int, c_void_p, c_void_p, c_longlong, c_void_p]),
     ("lentils_deflect_f64io", c_int, [c_void_p, c_int, c_void_p, c_void_p, c_longlong,
                                       c_void_p]),
+    ("lentils_deflect_grad", c_int, [c_void_p, c_int, c_void_p, c_void_p, c_longlong,
+                                     c_void_p]),
 ]
 
 _LIB = None

@@ -6,6 +6,11 @@
 
 #include "common.cuh"
 
+namespace lentils {
+int deflect_derivatives(const lentils_mass_model *lenses, int nlenses, const double *points,
+                        double *grads, double *sum12, long long n, cudaStream_t s);
+}  // namespace lentils
+
 using namespace lentils;
 
 namespace {
@@ -90,14 +95,14 @@ int grid_cpu_impl(lentils_visibility_space vs, double *vis, lentils_fourier_spac
     return LENTILS_OK;
 }
 
+// want_deriv != 0: deriv[0..11] += the PEMD derivatives d alpha / d (b, qh, q, x, y, th)
+// (x, y components) summed over all points and PEMD lenses, which is what the reference's
+// deflect_points does with its single deriv pointer (deflect.c:26-66, 330-338).
 int deflect_points_impl(lentils_global_lens_model glm, double *pin, int n, double *pout,
-                        int want_deriv)
+                        int want_deriv, double *deriv)
 {
-    if (want_deriv)
-        return set_error(LENTILS_ERR_UNSUPPORTED,
-                         "deflect_points: parameter derivatives (want_deriv) are not built");
     if (n < 0 || (n > 0 && (!pin || !pout)) || glm.num_lenses < 0 ||
-        (glm.num_lenses > 0 && !glm.lenses))
+        (glm.num_lenses > 0 && !glm.lenses) || (want_deriv && !deriv))
         return set_error(LENTILS_ERR_INVALID, "deflect_points: bad arguments");
     if (n == 0) return LENTILS_OK;
     double *din = nullptr, *dout = nullptr;
@@ -111,6 +116,21 @@ int deflect_points_impl(lentils_global_lens_model glm, double *pin, int n, doubl
     if (!st) {
         e = cudaMemcpy(pout, dout, bytes, cudaMemcpyDeviceToHost);
         if (e != cudaSuccess) st = cuda_status(e, "deflect_points copy back");
+    }
+    if (!st && want_deriv) {
+        double *dsum = nullptr;
+        double hsum[12];
+        e = cudaMalloc(&dsum, sizeof(hsum));
+        if (e == cudaSuccess) e = cudaMemset(dsum, 0, sizeof(hsum));
+        if (e != cudaSuccess) st = cuda_status(e, "deflect_points derivatives");
+        if (!st) st = deflect_derivatives(glm.lenses, glm.num_lenses, din, nullptr, dsum, n, nullptr);
+        if (!st) {
+            e = cudaMemcpy(hsum, dsum, sizeof(hsum), cudaMemcpyDeviceToHost);
+            if (e != cudaSuccess) st = cuda_status(e, "deflect_points derivatives copy back");
+        }
+        if (!st)
+            for (int k = 0; k < 12; ++k) deriv[k] += hsum[k];
+        cudaFree(dsum);
     }
     cudaFree(din);
     cudaFree(dout);
@@ -160,9 +180,9 @@ void grid_cpu(lentils_visibility_space vs, double *vis, lentils_fourier_space gs
 void deflect_points(lentils_global_lens_model glm, double *p_in, int npoints, double *p_out,
                     int want_deriv, double *deriv)
 {
-    (void)deriv;
     clear_error();
-    if (deflect_points_impl(glm, p_in, npoints, p_out, want_deriv)) report("deflect_points");
+    if (deflect_points_impl(glm, p_in, npoints, p_out, want_deriv, deriv))
+        report("deflect_points");
 }
 
 void grad_matrix_findiff_csr(lentils_image_space imspace, int *row_inds, int *cols, double *vals)

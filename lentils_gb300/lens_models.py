@@ -121,11 +121,24 @@ class GlobalLensModel:
 
     def deflect(self, points, z_s, deriv=False):
         """Source-plane positions of `points` (..., 2): numpy float64 in -> numpy out, or a CUDA
-        tensor (float64 or float32) in -> CUDA tensor out."""
-        if deriv:
-            raise N.LentilsError(5, "parameter derivatives are not built")
+        tensor (float64 or float32) in -> CUDA tensor out. deriv=True also returns the
+        per-point parameter derivatives d alpha / d (b, qh, q, x, y, th, ss, sa) summed over
+        the lenses, shaped (8,) + points.shape like the reference allocates them
+        (lens_models.py:71-73), in FP64 (lentils_deflect_grad)."""
         lenses = self.setup_raytracing(z_s)
-        return deflect_points(lenses, points)
+        out = deflect_points(lenses, points)
+        if not deriv:
+            return out
+        host = not isinstance(points, torch.Tensor)
+        p = torch.as_tensor(np.ascontiguousarray(points, dtype=np.float64)).cuda() if host \
+            else points.to(torch.float64).contiguous()
+        g = torch.empty((8,) + tuple(p.shape), dtype=torch.float64, device=p.device)
+        s = torch.cuda.current_stream()
+        N.check(N.lib().lentils_deflect_grad(ctypes.c_void_p(lenses.ctypes.data), len(lenses),
+                                             ctypes.c_void_p(p.data_ptr()),
+                                             ctypes.c_void_p(g.data_ptr()), p.numel() // 2,
+                                             ctypes.c_void_p(s.cuda_stream)))
+        return out, (g.cpu().numpy() if host else g)
 
 
 def deflect_points(lenses, points, stream=None):

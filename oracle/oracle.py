@@ -502,6 +502,32 @@ def deflect(lenses, points, use_ref=False):
     return out
 
 
+def deflect_derivatives_ref(lenses, points):
+    """The compiled reference's want_deriv output (deflect_points, deflect.c:26-66,243-339):
+    (the 12 numbers it accumulates over all points in one call, and the same 12 numbers per
+    point from one-point calls). Needs oracle/_ref."""
+    lenses = np.ascontiguousarray(lenses, dtype=MASS_MODEL_DTYPE)
+    pts = np.ascontiguousarray(points, dtype=np.float64).reshape(-1, 2)
+    lib = ref_lib("deflect")
+    if lib is None:
+        raise RuntimeError("compiled reference not available (oracle/_ref)")
+    glm = CGlobalLensModel()
+    glm.num_lenses = lenses.shape[0]
+    glm.num_zplanes = 1
+    glm.lenses = lenses.ctypes.data
+    out = np.zeros_like(pts)
+    total = np.zeros(16)
+    lib.deflect_points(glm, pts.ctypes.data, pts.shape[0], out.ctypes.data, 1, total.ctypes.data)
+    per = np.zeros((pts.shape[0], 12))
+    one = np.zeros(2)
+    for p in range(pts.shape[0]):
+        d = np.zeros(16)
+        lib.deflect_points(glm, pts[p].ctypes.data, 1, one.ctypes.data, 1, d.ctypes.data)
+        per[p] = d[:12]
+    assert not np.any(total[12:])
+    return total[:12], per
+
+
 # ---------------------------------------------------------------------------------------------
 # Bilinear lens operator and the CG normal equations (no reference counterpart for the
 # bilinear interpolation; the CG pattern follows lentils/tests/solver_tests.py:77-114)

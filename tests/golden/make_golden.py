@@ -80,6 +80,42 @@ def deflect_case():
     print("deflect", pts.shape)
 
 
+def deflect_deriv_case():
+    """Parameter derivatives (want_deriv) from the compiled reference, summed and per point;
+    central finite differences of the reference's FP64 deflection for the external shear's
+    parameters (whose derivative block the reference compiles out)."""
+    rng = np.random.default_rng(13)
+    img = O.ImageGeom((24, 20), [(-1.3, 1.1), (-1.0, 1.2)])
+    pts = np.concatenate([img.points().reshape(-1, 2) + 0.013, rng.uniform(-2, 2, (100, 2))])
+    cases = {
+        "pemd_shear": O.lens_array([O.pemd_cpars(1.0, 30.0, 0.8, 0.05, -0.03, 0.55),
+                                    O.shear_cpars(0.05, -0.03, 0.05, 20.0)]),
+        "two_pemd": O.lens_array([O.pemd_cpars(1.2, -40.0, 0.55, 0.1, 0.2, 0.45),
+                                  O.pemd_cpars(0.3, 75.0, 0.9, -0.4, 0.3, 0.6)]),
+    }
+    out = {"points": pts}
+    for k, lenses in cases.items():
+        total, per = O.deflect_derivatives_ref(lenses, pts)
+        out[f"{k}_lenses"] = lenses.view(np.uint8).reshape(len(lenses), -1)
+        out[f"{k}_sum12"] = total
+        out[f"{k}_per_point"] = per
+    # shear only: d beta / d (x, y, ss, sa) by central differences (beta = theta - alpha)
+    par = dict(x=0.05, y=-0.03, ss=0.07, sa=20.0)
+    steps = dict(x=1e-6, y=1e-6, ss=1e-6, sa=1e-4)
+    fd = np.zeros((4, pts.shape[0], 2))
+    for i, name in enumerate(("x", "y", "ss", "sa")):
+        hi, lo = dict(par), dict(par)
+        hi[name] += steps[name]
+        lo[name] -= steps[name]
+        bh = O.deflect(O.lens_array([O.shear_cpars(**hi)]), pts, use_ref=True)
+        bl = O.deflect(O.lens_array([O.shear_cpars(**lo)]), pts, use_ref=True)
+        fd[i] = -(bh - bl) / (2 * steps[name])  # d alpha = -d beta
+    out["shear_lenses"] = O.lens_array([O.shear_cpars(**par)]).view(np.uint8).reshape(1, -1)
+    out["shear_fd"] = fd
+    np.savez_compressed(os.path.join(HERE, "deflect_deriv.npz"), **out)
+    print("deflect_deriv", pts.shape)
+
+
 def grad_case():
     img = O.ImageGeom((13, 17), [(-0.4, 0.9), (-0.2, 0.6)])
     rows, cols, vals = O.grad_csr(img, use_ref=True)
@@ -102,4 +138,5 @@ if __name__ == "__main__":
     nufft_case("nufft_tiny_w1", (12, 9), [(-0.2, 0.3), (-0.1, 0.2)], [1.0], 1, 60, 0.5, 3,
                extra_uv=integer_points)
     deflect_case()
+    deflect_deriv_case()
     grad_case()

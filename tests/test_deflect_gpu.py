@@ -111,9 +111,60 @@ def test_dropin_deflect_points(native, golden_dir):
     ref = d["pemd_shear_out"]
     fin = np.isfinite(ref).all(axis=-1)
     assert O.rel_l2((pts - out)[fin].reshape(-1), (pts - ref)[fin].reshape(-1)) < REL_ALPHA
-    # derivatives are not built: the call reports UNSUPPORTED and leaves p_out untouched
-    out2 = np.full_like(pts, 7.0)
-    N.lib().deflect_points(glm, pts.ctypes.data, pts.shape[0], out2.ctypes.data, 1,
-                           dummy.ctypes.data)
-    assert N.lib().lentils_last_error() == 5
-    assert np.all(out2 == 7.0)
+
+
+
+def _deriv_case(golden_dir, name):
+    d = np.load(f"{golden_dir}/deflect_deriv.npz")
+    lenses = np.ascontiguousarray(d[f"{name}_lenses"]).view(O.MASS_MODEL_DTYPE).reshape(-1)
+    return d, lenses, np.ascontiguousarray(d["points"])
+
+
+@pytest.mark.parametrize("name", ["pemd_shear", "two_pemd"])
+def test_dropin_deflect_points_want_deriv(native, golden_dir, name):
+    """want_deriv = 1: deriv[0..11] += the PEMD derivatives summed over the points, exactly
+    what the compiled reference accumulates (deflect.c:330-338); the rest of the caller's
+    gradient array (allocated (8, npoints, 2) by lens_models.py:71-73) is left alone."""
+    from lentils_gb300 import _native as N
+    d, lenses, pts = _deriv_case(golden_dir, name)
+    glm = N.GlobalLensModelC(len(lenses), 1, lenses.ctypes.data)
+    out = np.zeros_like(pts)
+    rng = np.random.default_rng(1)
+    deriv0 = rng.normal(size=(8,) + pts.shape)
+    deriv = deriv0.copy()
+    N.lib().deflect_points(glm, pts.ctypes.data, pts.shape[0], out.ctypes.data, 1,
+                           deriv.ctypes.data)
+    N.check_last()
+    flat, flat0 = deriv.reshape(-1), deriv0.reshape(-1)
+    scale = np.abs(d[f"{name}_per_point"]).sum(axis=0) + 1e-300
+    err = np.abs((flat[:12] - flat0[:12]) - d[f"{name}_sum12"]) / scale
+    assert err.max() < 1e-12, err
+    assert np.array_equal(flat[12:], flat0[12:])
+
+
+def test_deflect_gradients_per_point(native, golden_dir):
+    """lentils_deflect_grad against the compiled reference's per-point PEMD derivatives, and
+    the external shear's (x, y, ss, sa) derivatives against central differences of the
+    reference's deflection."""
+    from lentils_gb300 import _native as N
+    from lentils_gb300.gridding import _ptr
+    L = N.lib()
+    for name, params in (("two_pemd", range(6)), ("pemd_shear", (0, 1, 2, 5))):
+        d, lenses, pts = _deriv_case(golden_dir, name)
+        p = torch.as_tensor(pts).cuda()
+        g = torch.empty((8,) + pts.shape, dtype=torch.float64, device="cuda")
+        N.check(L.lentils_deflect_grad(lenses.ctypes.data, len(lenses), _ptr(p), _ptr(g),
+                                       pts.shape[0], None))
+        got = g.cpu().numpy()
+        ref = d[f"{name}_per_point"].reshape(-1, 6, 2).transpose(1, 0, 2)
+        for k in params:
+            assert O.rel_l2(got[k], ref[k]) < 1e-11, (name, k, O.rel_l2(got[k], ref[k]))
+    d = np.load(f"{golden_dir}/deflect_deriv.npz")
+    lenses = np.ascontiguousarray(d["shear_lenses"]).view(O.MASS_MODEL_DTYPE).reshape(-1)
+    p = torch.as_tensor(np.ascontiguousarray(d["points"])).cuda()
+    g = torch.empty((8,) + tuple(p.shape), dtype=torch.float64, device="cuda")
+    N.check(L.lentils_deflect_grad(lenses.ctypes.data, 1, _ptr(p), _ptr(g), p.shape[0], None))
+    got = g.cpu().numpy()
+    for k, i in ((3, 0), (4, 1), (6, 2), (7, 3)):
+        assert O.rel_l2(got[k], d["shear_fd"][i]) < 1e-6, (k, O.rel_l2(got[k], d["shear_fd"][i]))
+    assert np.abs(got[[0, 1, 2, 5]]).max() == 0.0

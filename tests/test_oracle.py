@@ -3,6 +3,8 @@
 restated NUFFT composition against the direct Fourier transform (the reference's
 test_gridder_and_apodization, lentils/tests/nufft_tests.py:43-66, seeded); the adjoint
 relations of the r2c gridder."""
+import os
+
 import numpy as np
 import pytest
 import scipy.special as sp
@@ -127,3 +129,18 @@ def test_oracle_dirty_beam_form_matches_explicit_normal_operator():
     x = rng.normal(size=img.shape)
     explicit = ora.adjoint(w * ora.forward(x))
     assert O.rel_l2(O.bcb_apply(beam, img, x), explicit) < 1e-6
+
+
+def test_derivative_fixture_matches_reference():
+    """The committed derivative fixture is what the compiled reference computes (regenerated
+    here when oracle/_ref is available)."""
+    import pytest
+    if not O.ref_available():
+        pytest.skip("compiled reference not available")
+    from helpers import GOLDEN
+    d = np.load(os.path.join(GOLDEN, "deflect_deriv.npz"))
+    for name in ("pemd_shear", "two_pemd"):
+        lenses = np.ascontiguousarray(d[f"{name}_lenses"]).view(O.MASS_MODEL_DTYPE).reshape(-1)
+        total, per = O.deflect_derivatives_ref(lenses, d["points"])
+        assert np.array_equal(total, d[f"{name}_sum12"])
+        assert np.array_equal(per, d[f"{name}_per_point"])
