@@ -106,6 +106,10 @@ int lentils_last_error(void);
 const char *lentils_last_error_message(void);
 /* Library version as major*10000 + minor*100 + patch. */
 int lentils_version(void);
+/* Copy bytes from a device array to host memory (synchronous). */
+int lentils_copy_to_host(void *dst, const void *src, long long bytes);
+/* Release a device array that an entry point allocated for the caller (cudaFree). */
+int lentils_device_free(void *ptr);
 
 /* Host-only (no GPU needed): the per-tap Kaiser-Bessel polynomial table the gridding kernels
  * evaluate, 2w taps x lentils_kb_poly_ncoef() coefficients in t = 2*frac - 1 (highest degree
@@ -267,6 +271,24 @@ int lentils_nufft_adjoint64(lentils_nufft *op, const double *vis_plan, double *i
  * src = L^T img (both overwrite).
  * ---------------------------------------------------------------------------------------- */
 typedef struct lentils_lensop lentils_lensop;
+/* A general lens matrix in CSR form (device arrays, copied): nimg rows (image pixels), nsrc
+ * columns, int32 row pointers and columns, FP64 values; L^T by a stable sort on the column. */
+int lentils_lensop_create_csr(lentils_lensop **op, const int *row_ptr, const int *cols,
+                              const double *vals, int nimg, int nsrc, int nnz, void *stream);
+/* The reference's ManifoldLensOperator matrix (manifold_lens_matrix_csr,
+ * lentils/backend/raster.c:272-395) built on the GPU in FP64, one image pixel per thread: 9
+ * deflected points per unmasked pixel, 8 triangles fanned around the centre, recursively split
+ * along source-pixel lines, areas from the barycentric corners, and the reference's per-pixel
+ * reduction of the sorted fragments (including its two quirks: the first fragment of every
+ * column after the first is not added, and a pixel without fragments gets one zero entry in
+ * the previous such column). im, src: image and source spaces (host structs; src.mask unused);
+ * lenses: HOST array; mask_dev: nx*ny bytes on the device. Outputs are device arrays allocated
+ * here (free with cudaFree): *row_inds (nx*ny + 1), *cols, *vals (*nnz). A stack or fragment
+ * overflow (which the reference only prints) returns LENTILS_ERR_UNSUPPORTED. */
+int lentils_manifold_lens_matrix(const lentils_image_space *im, const lentils_image_space *src,
+                                 const lentils_mass_model *lenses, int nlenses,
+                                 const unsigned char *mask_dev, int **row_inds, int **cols,
+                                 double **vals, long long *nnz, void *stream);
 int lentils_lensop_create(lentils_lensop **op, const double *src_points,
                           const unsigned char *mask, int nimg, int nsx, int nsy, double sxmin,
                           double symin, double sdx, double sdy, void *stream);

@@ -141,6 +141,13 @@ _SIGNATURES = [
     ("lentils_normal_op_rhs64", c_int, [c_void_p, c_void_p, c_void_p, c_void_p]),
     ("lentils_normal_op_jacobi", c_int, [c_void_p, c_void_p, c_void_p, c_void_p]),
     ("lentils_normal_op_weight_sum", c_double, [c_void_p]),
+    ("lentils_device_free", c_int, [c_void_p]),
+    ("lentils_copy_to_host", c_int, [c_void_p, c_void_p, c_longlong]),
+    ("lentils_lensop_create_csr", c_int, [POINTER(c_void_p), c_void_p, c_void_p, c_void_p, c_int,
+                                          c_int, c_int, c_void_p]),
+    ("lentils_manifold_lens_matrix", c_int, [c_void_p, c_void_p, c_void_p, c_int, c_void_p,
+                                             POINTER(c_void_p), POINTER(c_void_p),
+                                             POINTER(c_void_p), POINTER(c_longlong), c_void_p]),
     ("lentils_bcb_create", c_int, [POINTER(c_void_p), c_void_p, c_int, c_int, c_void_p]),
     ("lentils_bcb_destroy", c_int, [c_void_p]),
     ("lentils_bcb_apply", c_int, [c_void_p, c_void_p, c_void_p, c_void_p]),

@@ -25,6 +25,11 @@ NVFLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-I",
                   "-I", CSRC, "--expt-relaxed-constexpr", "-Xptxas", "-warn-spills"]
 
 
+# Per-unit flags: the manifold rasteriser reproduces the reference's plain-C FP64 arithmetic,
+# so multiply-adds are not fused there.
+UNIT_FLAGS = {"manifold.cu": ["-fmad=false"]}
+
+
 def nvcc_path():
     for cand in (os.environ.get("NVCC"), shutil.which("nvcc"), "/usr/local/cuda/bin/nvcc"):
         if cand and os.path.exists(cand):
@@ -42,7 +47,8 @@ def _compile(src, extra):
     if (os.path.exists(obj) and os.path.getmtime(obj) >= os.path.getmtime(src)
             and os.path.getmtime(obj) >= _newest_header() and not extra):
         return obj, ""
-    cmd = [nvcc_path(), *NVFLAGS, *extra, "-c", src, "-o", obj]
+    cmd = [nvcc_path(), *NVFLAGS, *UNIT_FLAGS.get(os.path.basename(src), []), *extra, "-c", src,
+           "-o", obj]
     out = subprocess.run(cmd, capture_output=True, text=True)
     if out.returncode != 0:
         raise RuntimeError(f"nvcc failed for {src}:\n{' '.join(cmd)}\n{out.stdout}{out.stderr}")

@@ -27,6 +27,10 @@ struct lentils_lensop {
     int *ell_col;     // 4 * nimg
     double *ell_val64;
     float *ell_val32;
+    int *f_ptr;       // general CSR form (nimg + 1; null for the 4-wide bilinear form)
+    int *f_col;
+    double *f_val64;
+    float *f_val32;
     int *t_ptr;       // nsrc + 1
     int *t_row;       // nnz (image pixel of each entry)
     double *t_val64;
@@ -117,6 +121,51 @@ __global__ void lens_apply_kernel(const int *__restrict__ col, const R *__restri
 }
 
 template <typename R>
+__global__ void lens_apply_csr_kernel(const int *__restrict__ ptr, const int *__restrict__ col,
+                                      const R *__restrict__ val, const R *__restrict__ src,
+                                      R *__restrict__ img, int nimg)
+{
+    for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < nimg;
+         p += (long long)gridDim.x * blockDim.x) {
+        R acc = (R)0;
+        for (int e = ptr[p]; e < ptr[p + 1]; ++e) acc += val[e] * src[col[e]];
+        img[p] = acc;
+    }
+}
+
+// CSR entry -> row; per-column counts; FP32 copy of the values
+__global__ void csr_rows_kernel(const int *__restrict__ ptr, const int *__restrict__ col,
+                                const double *__restrict__ v64, int *__restrict__ rowof,
+                                unsigned *__restrict__ keys, int *__restrict__ ids,
+                                int *__restrict__ counts, float *__restrict__ v32, int nimg)
+{
+    for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < nimg;
+         p += (long long)gridDim.x * blockDim.x) {
+        for (int e = ptr[p]; e < ptr[p + 1]; ++e) {
+            rowof[e] = (int)p;
+            keys[e] = (unsigned)col[e];
+            ids[e] = e;
+            v32[e] = (float)v64[e];
+            atomicAdd(&counts[col[e]], 1);
+        }
+    }
+}
+
+__global__ void csr_transpose_fill_kernel(const int *__restrict__ ids, const int *__restrict__ rowof,
+                                          const double *__restrict__ v64, int *__restrict__ trow,
+                                          double *__restrict__ tv64, float *__restrict__ tv32,
+                                          int nnz)
+{
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < nnz;
+         i += (long long)gridDim.x * blockDim.x) {
+        const int e = ids[i];
+        trow[i] = rowof[e];
+        tv64[i] = v64[e];
+        tv32[i] = (float)v64[e];
+    }
+}
+
+template <typename R>
 __global__ void lens_apply_t_kernel(const int *__restrict__ ptr, const int *__restrict__ row,
                                     const R *__restrict__ val, const R *__restrict__ img,
                                     R *__restrict__ src, int nsrc)
@@ -146,6 +195,10 @@ using namespace lentils;
 
 static void lensop_free(lentils_lensop *op)
 {
+    cudaFree(op->f_ptr);
+    cudaFree(op->f_col);
+    cudaFree(op->f_val64);
+    cudaFree(op->f_val32);
     cudaFree(op->ell_col);
     cudaFree(op->ell_val64);
     cudaFree(op->ell_val32);
@@ -245,6 +298,90 @@ int lentils_lensop_create(lentils_lensop **out, const double *src_points, const 
     return LENTILS_OK;
 }
 
+// A general lens matrix in CSR form (device arrays, copied): nimg rows, nsrc columns, FP64
+// values; the transpose is built by a stable sort on the column.
+int lentils_lensop_create_csr(lentils_lensop **out, const int *row_ptr, const int *cols,
+                              const double *vals, int nimg, int nsrc, int nnz, void *stream)
+{
+    clear_error();
+    if (!out || !row_ptr || (nnz > 0 && (!cols || !vals)) || nimg < 1 || nsrc < 1 || nnz < 0)
+        return set_error(LENTILS_ERR_INVALID, "lensop_create_csr: bad arguments");
+    *out = nullptr;
+    cudaStream_t s = (cudaStream_t)stream;
+    lentils_lensop *op = new (std::nothrow) lentils_lensop();
+    if (!op) return set_error(LENTILS_ERR_ALLOC, "lensop_create_csr: host allocation");
+    memset(op, 0, sizeof(*op));
+    op->nimg = nimg;
+    op->nsrc = nsrc;
+    op->nnz = nnz;
+    const size_t nz = (size_t)std::max(1, nnz);
+    unsigned *keys = nullptr, *keys_sorted = nullptr;
+    int *ids = nullptr, *ids_sorted = nullptr, *counts = nullptr, *rowof = nullptr;
+    void *tmp = nullptr;
+    int st = LENTILS_OK;
+    cudaError_t e = cudaMalloc(&op->f_ptr, sizeof(int) * (nimg + 1));
+    if (e == cudaSuccess) e = cudaMalloc(&op->f_col, sizeof(int) * nz);
+    if (e == cudaSuccess) e = cudaMalloc(&op->f_val64, sizeof(double) * nz);
+    if (e == cudaSuccess) e = cudaMalloc(&op->f_val32, sizeof(float) * nz);
+    if (e == cudaSuccess) e = cudaMalloc(&op->t_ptr, sizeof(int) * (nsrc + 1));
+    if (e == cudaSuccess) e = cudaMalloc(&op->t_row, sizeof(int) * nz);
+    if (e == cudaSuccess) e = cudaMalloc(&op->t_val64, sizeof(double) * nz);
+    if (e == cudaSuccess) e = cudaMalloc(&op->t_val32, sizeof(float) * nz);
+    if (e == cudaSuccess) e = cudaMalloc(&keys, sizeof(unsigned) * nz);
+    if (e == cudaSuccess) e = cudaMalloc(&keys_sorted, sizeof(unsigned) * nz);
+    if (e == cudaSuccess) e = cudaMalloc(&ids, sizeof(int) * nz);
+    if (e == cudaSuccess) e = cudaMalloc(&ids_sorted, sizeof(int) * nz);
+    if (e == cudaSuccess) e = cudaMalloc(&rowof, sizeof(int) * nz);
+    if (e == cudaSuccess) e = cudaMalloc(&counts, sizeof(int) * (nsrc + 1));
+    if (e == cudaSuccess) e = cudaMemcpyAsync(op->f_ptr, row_ptr, sizeof(int) * (nimg + 1), cudaMemcpyDeviceToDevice, s);
+    if (e == cudaSuccess && nnz > 0)
+        e = cudaMemcpyAsync(op->f_col, cols, sizeof(int) * nnz, cudaMemcpyDeviceToDevice, s);
+    if (e == cudaSuccess && nnz > 0)
+        e = cudaMemcpyAsync(op->f_val64, vals, sizeof(double) * nnz, cudaMemcpyDeviceToDevice, s);
+    if (e == cudaSuccess) e = cudaMemsetAsync(counts, 0, sizeof(int) * (nsrc + 1), s);
+    if (e == cudaSuccess) {
+        csr_rows_kernel<<<blocks_for(nimg), 256, 0, s>>>(op->f_ptr, op->f_col, op->f_val64, rowof,
+                                                         keys, ids, counts, op->f_val32, nimg);
+        e = cudaGetLastError();
+    }
+    int bits = 1;
+    while ((1LL << bits) <= nsrc) ++bits;
+    size_t tmp_bytes = 0, scan_bytes = 0;
+    if (e == cudaSuccess)
+        e = cub::DeviceRadixSort::SortPairs(nullptr, tmp_bytes, keys, keys_sorted, ids, ids_sorted,
+                                            (int64_t)nnz, 0, bits, s);
+    if (e == cudaSuccess)
+        e = cub::DeviceScan::ExclusiveSum(nullptr, scan_bytes, counts, op->t_ptr, nsrc + 1, s);
+    if (e == cudaSuccess) e = cudaMalloc(&tmp, std::max<size_t>(1, std::max(tmp_bytes, scan_bytes)));
+    if (e == cudaSuccess && nnz > 0)
+        e = cub::DeviceRadixSort::SortPairs(tmp, tmp_bytes, keys, keys_sorted, ids, ids_sorted,
+                                            (int64_t)nnz, 0, bits, s);
+    if (e == cudaSuccess)
+        e = cub::DeviceScan::ExclusiveSum(tmp, scan_bytes, counts, op->t_ptr, nsrc + 1, s);
+    if (e == cudaSuccess && nnz > 0) {
+        csr_transpose_fill_kernel<<<blocks_for(nnz), 256, 0, s>>>(ids_sorted, rowof, op->f_val64,
+                                                                 op->t_row, op->t_val64,
+                                                                 op->t_val32, nnz);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) st = cuda_status(e, "lensop_create_csr");
+    cudaFree(keys);
+    cudaFree(keys_sorted);
+    cudaFree(ids);
+    cudaFree(ids_sorted);
+    cudaFree(rowof);
+    cudaFree(counts);
+    cudaFree(tmp);
+    if (st) {
+        lensop_free(op);
+        delete op;
+        return st;
+    }
+    *out = op;
+    return LENTILS_OK;
+}
+
 int lentils_lensop_destroy(lentils_lensop *op)
 {
     clear_error();
@@ -260,8 +397,12 @@ int lentils_lensop_apply(const lentils_lensop *op, const float *src, float *img,
 {
     clear_error();
     if (!op || !src || !img) return set_error(LENTILS_ERR_INVALID, "lensop_apply: null argument");
-    lens_apply_kernel<float><<<blocks_for(op->nimg), 256, 0, (cudaStream_t)stream>>>(
-        op->ell_col, op->ell_val32, src, img, op->nimg);
+    if (op->f_ptr)
+        lens_apply_csr_kernel<float><<<blocks_for(op->nimg), 256, 0, (cudaStream_t)stream>>>(
+            op->f_ptr, op->f_col, op->f_val32, src, img, op->nimg);
+    else
+        lens_apply_kernel<float><<<blocks_for(op->nimg), 256, 0, (cudaStream_t)stream>>>(
+            op->ell_col, op->ell_val32, src, img, op->nimg);
     LENTILS_CHECK_LAUNCH("lens_apply_kernel");
     return LENTILS_OK;
 }
@@ -280,8 +421,12 @@ int lentils_lensop_apply64(const lentils_lensop *op, const double *src, double *
 {
     clear_error();
     if (!op || !src || !img) return set_error(LENTILS_ERR_INVALID, "lensop_apply64: null argument");
-    lens_apply_kernel<double><<<blocks_for(op->nimg), 256, 0, (cudaStream_t)stream>>>(
-        op->ell_col, op->ell_val64, src, img, op->nimg);
+    if (op->f_ptr)
+        lens_apply_csr_kernel<double><<<blocks_for(op->nimg), 256, 0, (cudaStream_t)stream>>>(
+            op->f_ptr, op->f_col, op->f_val64, src, img, op->nimg);
+    else
+        lens_apply_kernel<double><<<blocks_for(op->nimg), 256, 0, (cudaStream_t)stream>>>(
+            op->ell_col, op->ell_val64, src, img, op->nimg);
     LENTILS_CHECK_LAUNCH("lens_apply_kernel");
     return LENTILS_OK;
 }

@@ -172,6 +172,24 @@ int lentils_last_error(void) { return lentils::t_err; }
 const char *lentils_last_error_message(void) { return lentils::t_msg; }
 int lentils_version(void) { return 10000; }
 
+// copy `bytes` from a device array to host memory (synchronous)
+int lentils_copy_to_host(void *dst, const void *src, long long bytes)
+{
+    lentils::clear_error();
+    if (bytes < 0 || (bytes > 0 && (!dst || !src)))
+        return lentils::set_error(LENTILS_ERR_INVALID, "copy_to_host: bad arguments");
+    if (bytes) LENTILS_CUDA_TRY(cudaMemcpy(dst, src, (size_t)bytes, cudaMemcpyDeviceToHost));
+    return LENTILS_OK;
+}
+
+// release a device array that an entry point allocated for the caller
+int lentils_device_free(void *ptr)
+{
+    lentils::clear_error();
+    LENTILS_CUDA_TRY(cudaFree(ptr));
+    return LENTILS_OK;
+}
+
 // Host-only helper (no GPU needed): the per-tap polynomial table for (w, beta), as
 // kPolyCoef x 2w floats, tap-major (coef[i*kPolyCoef + k], highest degree first), and the
 // FP64 fit error relative to the kernel peak. Exposed for tests and diagnostics.

@@ -16,13 +16,14 @@ import torch
 
 from . import _native as N
 from .gridding import _ptr
-from .operators import BilinearLensOperator, BlurredCovarianceOperator, NUFFTOperator
+from .operators import (BilinearLensOperator, BlurredCovarianceOperator, ManifoldLensOperator,
+                        NUFFTOperator)
 
 
 class SourceInversion:
     def __init__(self, vis_space, data, sigma, image_space, source_space, lensmodel, z_src,
                  strength, kernel_support=4, pad_factor=2, kb_beta=None, data_mask=None,
-                 nufft=None, data_term="visibilities"):
+                 nufft=None, data_term="visibilities", lens_operator="bilinear"):
         """nufft: an existing NUFFTOperator for vis_space and image_space to share (lens-model
         sweeps over one visibility set); built here when None. data_term: "visibilities"
         (F^T C^-1 F through the gridder every matvec) or "bcb" (the dirty-beam convolution,
@@ -30,12 +31,16 @@ class SourceInversion:
         side L^T times the dirty image F^T C^-1 d)."""
         if data_term not in ("visibilities", "bcb"):
             raise ValueError("data_term: 'visibilities' or 'bcb'")
+        if lens_operator not in ("bilinear", "manifold"):
+            raise ValueError("lens_operator: 'bilinear' or 'manifold'")
         self.data_term = data_term
         self.stream = torch.cuda.Stream()
         with torch.cuda.stream(self.stream):
             self.nufft = nufft if nufft is not None else NUFFTOperator(
                 vis_space, image_space, pad_factor, kernel_support, kb_beta)
-            self.lens = BilinearLensOperator(image_space, source_space, lensmodel, z_src)
+            lens_cls = ManifoldLensOperator if lens_operator == "manifold" else \
+                BilinearLensOperator
+            self.lens = lens_cls(image_space, source_space, lensmodel, z_src)
             self.source_space = source_space
             self.image_space = image_space
             plan = self.nufft.plan

@@ -333,6 +333,46 @@ class BilinearLensOperator(Operator):
         return self._run(img, False)
 
 
+class ManifoldLensOperator(BilinearLensOperator):
+    """The reference's ManifoldLensOperator (lentils/operators/lens_operators.py:21-38,
+    manifold_lens_matrix_csr of lentils/backend/raster.c:272-395): image pixels <- source
+    pixels weighted by the rasterised overlap of each pixel's 8 deflected triangles, built on
+    the GPU in FP64 (lentils_manifold_lens_matrix) and applied as CSR / transposed CSR.
+    `matrix` holds a scipy copy of the CSR."""
+
+    def __init__(self, image_space, source_space, lensmodel, z_src):
+        import scipy.sparse as sps
+        lenses = lensmodel.setup_raytracing(z_src)
+        mask = torch.as_tensor(np.ascontiguousarray(image_space.mask.reshape(-1))
+                               .astype(np.uint8)).cuda()
+        L = N.lib()
+        rows, cols, vals = ctypes.c_void_p(), ctypes.c_void_p(), ctypes.c_void_p()
+        nnz = ctypes.c_longlong()
+        torch.cuda.current_stream().synchronize()
+        N.check(L.lentils_manifold_lens_matrix(
+            ctypes.byref(image_space), ctypes.byref(source_space),
+            ctypes.c_void_p(lenses.ctypes.data), len(lenses), _ptr(mask), ctypes.byref(rows),
+            ctypes.byref(cols), ctypes.byref(vals), ctypes.byref(nnz), _stream_ptr()))
+        nimg, nsrc, n = image_space.nx * image_space.ny, source_space.nx * source_space.ny, nnz.value
+        try:
+            self._handle = ctypes.c_void_p()
+            N.check(L.lentils_lensop_create_csr(ctypes.byref(self._handle), rows, cols, vals, nimg,
+                                                nsrc, int(n), _stream_ptr()))
+            h_rows = np.empty(nimg + 1, np.int32)
+            h_cols = np.empty(max(1, n), np.int32)
+            h_vals = np.empty(max(1, n), np.float64)
+            for dst, src, nb in ((h_rows, rows, 4 * (nimg + 1)), (h_cols, cols, 4 * n),
+                                 (h_vals, vals, 8 * n)):
+                N.check(L.lentils_copy_to_host(ctypes.c_void_p(dst.ctypes.data), src, nb))
+        finally:
+            for ptr in (rows, cols, vals):
+                if ptr.value:
+                    L.lentils_device_free(ptr)
+        self.matrix = sps.csr_matrix((h_vals[:n], h_cols[:n], h_rows), shape=(nimg, nsrc))
+        self._mask = mask
+        Operator.__init__(self, image_space, source_space)
+
+
 class PriorCovarianceOperator(Operator):
     """lambda * R^T R with R the forward-difference gradient of grad_matrix_findiff_csr
     ('gradient' prior of operator_base.py:200-251), matrix-free; symmetric."""

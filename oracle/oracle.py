@@ -142,6 +142,10 @@ def ref_lib(name):
         lib.deflect_points.restype = None
         lib.deflect_points.argtypes = [CGlobalLensModel, c_void_p, c_int, c_void_p, c_int,
                                        c_void_p]
+    if name == "raster":
+        lib.manifold_lens_matrix_csr.restype = None
+        lib.manifold_lens_matrix_csr.argtypes = [CImageSpace, CImageSpace, CGlobalLensModel,
+                                                 c_void_p, c_void_p, c_void_p]
     _REF[name] = lib
     return lib
 
@@ -500,6 +504,29 @@ def deflect(lenses, points, use_ref=False):
     else:
         port_lib().oracle_deflect_points(glm, pts.ctypes.data, n, out.ctypes.data)
     return out
+
+
+def manifold_lens_matrix_ref(img: ImageGeom, src: ImageGeom, lenses):
+    """The compiled reference's ManifoldLensOperator matrix (manifold_lens_matrix_csr,
+    raster.c:272-395, called as lens_operators.py:21-38 does): (row_inds, cols, vals) with
+    nnz = row_inds[-1]. Needs oracle/_ref."""
+    lib = ref_lib("raster")
+    if lib is None:
+        raise RuntimeError("compiled reference not available (oracle/_ref)")
+    lenses = np.ascontiguousarray(lenses, dtype=MASS_MODEL_DTYPE)
+    glm = CGlobalLensModel()
+    glm.num_lenses = lenses.shape[0]
+    glm.num_zplanes = 1
+    glm.lenses = lenses.ctypes.data
+    nrows = img.nx * img.ny
+    rows = np.zeros(nrows + 1, dtype=np.int32)
+    cols = np.zeros(50 * nrows, dtype=np.int32)
+    vals = np.zeros(50 * nrows, dtype=np.float64)
+    ic, sc = img.cstruct(), src.cstruct()
+    lib.manifold_lens_matrix_csr(ic, sc, glm, rows.ctypes.data, cols.ctypes.data,
+                                 vals.ctypes.data)
+    nnz = int(rows[-1])
+    return rows, cols[:nnz].copy(), vals[:nnz].copy()
 
 
 def deflect_derivatives_ref(lenses, points):

@@ -116,6 +116,33 @@ def deflect_deriv_case():
     print("deflect_deriv", pts.shape)
 
 
+def manifold_case():
+    """The reference's ManifoldLensOperator matrix (raster.c:272-395) on two small cases: a
+    PEMD + shear with a masked region, and a source grid smaller than the lensed image (pixels
+    whose triangles miss it, which the reference gives a zero entry)."""
+    out = {}
+    cases = {
+        "wide": (O.ImageGeom((24, 20), [(-0.6, 0.6), (-0.5, 0.5)]),
+                 O.ImageGeom((16, 16), [(-0.4, 0.4), (-0.4, 0.4)]),
+                 O.lens_array([O.pemd_cpars(0.45, 30.0, 0.75, 0.013, -0.011, 0.5),
+                               O.shear_cpars(0.013, -0.011, 0.05, 20.0)])),
+        "small_src": (O.ImageGeom((30, 26), [(-0.75, 0.75), (-0.65, 0.65)]),
+                      O.ImageGeom((8, 10), [(-0.12, 0.12), (-0.15, 0.15)]),
+                      O.lens_array([O.pemd_cpars(0.5, -20.0, 0.6, -0.02, 0.017, 0.6)])),
+    }
+    for k, (img, src, lenses) in cases.items():
+        if k == "wide":
+            img.mask[3:6, 4:9] = False
+        r, c, v = O.manifold_lens_matrix_ref(img, src, lenses)
+        out[f"{k}_img"] = np.concatenate([[img.nx, img.ny], img.bounds])
+        out[f"{k}_src"] = np.concatenate([[src.nx, src.ny], src.bounds])
+        out[f"{k}_mask"] = img.mask.astype(np.uint8)
+        out[f"{k}_lenses"] = lenses.view(np.uint8).reshape(len(lenses), -1)
+        out[f"{k}_rows"], out[f"{k}_cols"], out[f"{k}_vals"] = r, c, v
+    np.savez_compressed(os.path.join(HERE, "manifold.npz"), **out)
+    print("manifold", {k: int(out[f"{k}_rows"][-1]) for k in cases})
+
+
 def grad_case():
     img = O.ImageGeom((13, 17), [(-0.4, 0.9), (-0.2, 0.6)])
     rows, cols, vals = O.grad_csr(img, use_ref=True)
@@ -139,4 +166,5 @@ if __name__ == "__main__":
                extra_uv=integer_points)
     deflect_case()
     deflect_deriv_case()
+    manifold_case()
     grad_case()

@@ -144,3 +144,21 @@ def test_derivative_fixture_matches_reference():
         total, per = O.deflect_derivatives_ref(lenses, d["points"])
         assert np.array_equal(total, d[f"{name}_sum12"])
         assert np.array_equal(per, d[f"{name}_per_point"])
+
+
+def test_manifold_fixture_matches_reference():
+    """The committed manifold-matrix fixture is what the compiled reference computes."""
+    import pytest
+    if O.ref_lib("raster") is None:
+        pytest.skip("compiled reference not available")
+    from helpers import GOLDEN
+    d = np.load(os.path.join(GOLDEN, "manifold.npz"))
+    for name in ("wide", "small_src"):
+        gi, gs = d[f"{name}_img"], d[f"{name}_src"]
+        img = O.ImageGeom((int(gi[0]), int(gi[1])), gi[2:6])
+        img.mask[...] = d[f"{name}_mask"].astype(bool)
+        src = O.ImageGeom((int(gs[0]), int(gs[1])), gs[2:6])
+        lenses = np.ascontiguousarray(d[f"{name}_lenses"]).view(O.MASS_MODEL_DTYPE).reshape(-1)
+        r, c, v = O.manifold_lens_matrix_ref(img, src, lenses)
+        assert np.array_equal(r, d[f"{name}_rows"]) and np.array_equal(c, d[f"{name}_cols"])
+        assert np.array_equal(v, d[f"{name}_vals"])
