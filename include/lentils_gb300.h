@@ -289,6 +289,23 @@ int lentils_manifold_lens_matrix(const lentils_image_space *im, const lentils_im
                                  const lentils_mass_model *lenses, int nlenses,
                                  const unsigned char *mask_dev, int **row_inds, int **cols,
                                  double **vals, long long *nnz, void *stream);
+/* FP64 deflection with the reference's formulas (deflect.c; PEMD, shear, multipoles), device
+ * points and output (interleaved x, y); synchronises the stream. */
+int lentils_deflect64(const lentils_mass_model *lenses, int nlenses, const double *points,
+                      double *out, long long npoints, void *stream);
+/* The reference's DelaunayLensOperator matrix (delaunay_lens_matrix_csr,
+ * lentils/backend/triangles.c:105-140): unmasked image pixels on the ncast lattice are casted
+ * points (one entry 1.0 in their own column, numbered in row-major order); every other
+ * unmasked pixel takes the barycentric weights (triangle_geometry, triangles.c:7-30) of its
+ * deflected position in its triangle tri_inds[u] (no entries when < 0), u numbering the
+ * uncasted pixels in row-major order. The triangulation (triangles, 3 ints each, over
+ * tri_points) and the point location come from the caller, as the reference takes them from
+ * scipy's Delaunay (lens_operators.py:67-70). Device inputs; outputs as for
+ * lentils_manifold_lens_matrix. */
+int lentils_delaunay_lens_matrix(const unsigned char *mask_dev, int nx, int ny, int ncast,
+                                 const double *uncasted_points, const int *uncasted_tri_inds,
+                                 const int *triangles, const double *tri_points, int **row_inds,
+                                 int **cols, double **vals, long long *nnz, void *stream);
 int lentils_lensop_create(lentils_lensop **op, const double *src_points,
                           const unsigned char *mask, int nimg, int nsx, int nsy, double sxmin,
                           double symin, double sdx, double sdy, void *stream);

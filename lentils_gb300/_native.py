@@ -148,6 +148,11 @@ _SIGNATURES = [
     ("lentils_manifold_lens_matrix", c_int, [c_void_p, c_void_p, c_void_p, c_int, c_void_p,
                                              POINTER(c_void_p), POINTER(c_void_p),
                                              POINTER(c_void_p), POINTER(c_longlong), c_void_p]),
+    ("lentils_deflect64", c_int, [c_void_p, c_int, c_void_p, c_void_p, c_longlong, c_void_p]),
+    ("lentils_delaunay_lens_matrix", c_int, [c_void_p, c_int, c_int, c_int, c_void_p, c_void_p,
+                                             c_void_p, c_void_p, POINTER(c_void_p),
+                                             POINTER(c_void_p), POINTER(c_void_p),
+                                             POINTER(c_longlong), c_void_p]),
     ("lentils_bcb_create", c_int, [POINTER(c_void_p), c_void_p, c_int, c_int, c_void_p]),
     ("lentils_bcb_destroy", c_int, [c_void_p]),
     ("lentils_bcb_apply", c_int, [c_void_p, c_void_p, c_void_p, c_void_p]),

@@ -592,3 +592,194 @@ int lentils_manifold_lens_matrix(const lentils_image_space *im, const lentils_im
 }
 
 }  // extern "C"
+
+// ------------------------------------------------------------------------------------------------
+// FP64 deflection with the reference's formulas, and the Delaunay lens matrix
+// (delaunay_lens_matrix_csr, lentils/backend/triangles.c:105-140, with the barycentric weights
+// of triangle_geometry :7-30).
+// ------------------------------------------------------------------------------------------------
+namespace lentils {
+
+__global__ void deflect64_kernel(const lentils_mass_model *__restrict__ lenses, int nl,
+                                 const double2 *__restrict__ pin, double2 *__restrict__ pout,
+                                 long long n)
+{
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+         i += (long long)gridDim.x * blockDim.x) {
+        const double2 p = pin[i];
+        double bx, by;
+        deflect64(lenses, nl, p.x, p.y, bx, by);
+        pout[i] = make_double2(bx, by);
+    }
+}
+
+// per pixel: 1 if unmasked and casted / uncasted (for the running indices of the reference)
+__global__ void delaunay_flags_kernel(const unsigned char *__restrict__ mask, int nx, int ny,
+                                      int ncast, int *__restrict__ cflag, int *__restrict__ uflag)
+{
+    const long long n = (long long)nx * ny;
+    for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < n;
+         p += (long long)gridDim.x * blockDim.x) {
+        const int i = (int)(p / ny), j = (int)(p - (long long)i * ny);
+        const bool on = mask[p] != 0;
+        const bool cast = (i % ncast == 0) && (j % ncast == 0);
+        cflag[p] = (on && cast) ? 1 : 0;
+        uflag[p] = (on && !cast) ? 1 : 0;
+    }
+}
+
+// entries per pixel (counts) or the entries themselves (rows != null)
+__global__ void delaunay_entries_kernel(const unsigned char *__restrict__ mask, int nx, int ny,
+                                        int ncast, const int *__restrict__ cidx,
+                                        const int *__restrict__ uidx,
+                                        const double2 *__restrict__ upts,
+                                        const int *__restrict__ tind, const int *__restrict__ tris,
+                                        const double2 *__restrict__ tpts, int *__restrict__ counts,
+                                        const int *__restrict__ rows, int *__restrict__ cols,
+                                        double *__restrict__ vals)
+{
+    const long long n = (long long)nx * ny;
+    for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < n;
+         p += (long long)gridDim.x * blockDim.x) {
+        int k = 0;
+        if (mask[p]) {
+            const int i = (int)(p / ny), j = (int)(p - (long long)i * ny);
+            if ((i % ncast) || (j % ncast)) {
+                const int u = uidx[p];
+                const int t = tind[u];
+                if (t >= 0) {
+                    k = 3;
+                    if (rows) {
+                        const double2 s = upts[u];
+                        int pv[3];
+                        double a[3][2];
+                        for (int v = 0; v < 3; ++v) {
+                            pv[v] = tris[3 * t + v];
+                            a[v][0] = tpts[pv[v]].x - s.x;
+                            a[v][1] = tpts[pv[v]].y - s.y;
+                        }
+                        double w0 = a[1][0] * a[2][1] - a[2][0] * a[1][1];
+                        double w1 = a[2][0] * a[0][1] - a[0][0] * a[2][1];
+                        double w2 = a[0][0] * a[1][1] - a[1][0] * a[0][1];
+                        const double area = w0 + w1 + w2;
+                        const double inv = 1.0 / area;
+                        w0 *= inv;
+                        w1 *= inv;
+                        w2 *= inv;
+                        const int b = rows[p];
+                        vals[b] = w0;
+                        cols[b] = pv[0];
+                        vals[b + 1] = w1;
+                        cols[b + 1] = pv[1];
+                        vals[b + 2] = w2;
+                        cols[b + 2] = pv[2];
+                    }
+                }
+            } else {
+                k = 1;
+                if (rows) {
+                    vals[rows[p]] = 1.0;
+                    cols[rows[p]] = cidx[p];
+                }
+            }
+        }
+        if (counts) counts[p] = k;
+    }
+}
+
+}  // namespace lentils
+
+extern "C" {
+
+int lentils_deflect64(const lentils_mass_model *lenses, int nlenses, const double *points,
+                      double *out, long long npoints, void *stream)
+{
+    clear_error();
+    if ((nlenses > 0 && !lenses) || nlenses < 0 || npoints < 0 ||
+        (npoints > 0 && (!points || !out)))
+        return set_error(LENTILS_ERR_INVALID, "deflect64: bad arguments");
+    if (npoints == 0) return LENTILS_OK;
+    cudaStream_t s = (cudaStream_t)stream;
+    DevScratch tmp;
+    lentils_mass_model *dl;
+    if (int st = tmp.alloc(&dl, nlenses)) return st;
+    if (nlenses > 0)
+        LENTILS_CUDA_TRY(cudaMemcpyAsync(dl, lenses, sizeof(lentils_mass_model) * nlenses,
+                                         cudaMemcpyHostToDevice, s));
+    deflect64_kernel<<<nblocks(npoints, 256), 256, 0, s>>>(dl, nlenses, (const double2 *)points,
+                                                           (double2 *)out, npoints);
+    LENTILS_CHECK_LAUNCH("deflect64_kernel");
+    LENTILS_CUDA_TRY(cudaStreamSynchronize(s));
+    return LENTILS_OK;
+}
+
+int lentils_delaunay_lens_matrix(const unsigned char *mask_dev, int nx, int ny, int ncast,
+                                 const double *uncasted_points, const int *uncasted_tri_inds,
+                                 const int *triangles, const double *tri_points, int **row_inds,
+                                 int **cols, double **vals, long long *nnz_out, void *stream)
+{
+    clear_error();
+    if (!mask_dev || nx < 1 || ny < 1 || ncast < 1 || !row_inds || !cols || !vals || !nnz_out)
+        return set_error(LENTILS_ERR_INVALID, "delaunay_lens_matrix: bad arguments");
+    *row_inds = nullptr;
+    *cols = nullptr;
+    *vals = nullptr;
+    *nnz_out = 0;
+    cudaStream_t s = (cudaStream_t)stream;
+    const long long npix = (long long)nx * ny;
+    DevScratch tmp;
+    int *cflag, *uflag, *cidx, *uidx, *counts;
+    int st;
+    if ((st = tmp.alloc(&cflag, npix))) return st;
+    if ((st = tmp.alloc(&uflag, npix))) return st;
+    if ((st = tmp.alloc(&cidx, npix))) return st;
+    if ((st = tmp.alloc(&uidx, npix))) return st;
+    if ((st = tmp.alloc(&counts, npix + 1))) return st;
+    delaunay_flags_kernel<<<nblocks(npix, 256), 256, 0, s>>>(mask_dev, nx, ny, ncast, cflag, uflag);
+    LENTILS_CHECK_LAUNCH("delaunay_flags_kernel");
+    size_t tb = 0;
+    LENTILS_CUDA_TRY(cub::DeviceScan::ExclusiveSum(nullptr, tb, cflag, cidx, npix, s));
+    unsigned char *t1;
+    if ((st = tmp.alloc(&t1, tb))) return st;
+    LENTILS_CUDA_TRY(cub::DeviceScan::ExclusiveSum(t1, tb, cflag, cidx, npix, s));
+    LENTILS_CUDA_TRY(cub::DeviceScan::ExclusiveSum(t1, tb, uflag, uidx, npix, s));
+    delaunay_entries_kernel<<<nblocks(npix, 256), 256, 0, s>>>(
+        mask_dev, nx, ny, ncast, cidx, uidx, (const double2 *)uncasted_points, uncasted_tri_inds,
+        triangles, (const double2 *)tri_points, counts, nullptr, nullptr, nullptr);
+    LENTILS_CHECK_LAUNCH("delaunay_entries_kernel (count)");
+    LENTILS_CUDA_TRY(cudaMemsetAsync(counts + npix, 0, sizeof(int), s));
+    int *rows_out = nullptr, *cols_out = nullptr;
+    double *vals_out = nullptr;
+    tb = 0;
+    LENTILS_CUDA_TRY(cub::DeviceScan::ExclusiveSum(nullptr, tb, counts, counts, npix + 1, s));
+    unsigned char *t2;
+    if ((st = tmp.alloc(&t2, tb))) return st;
+    LENTILS_CUDA_TRY(cudaMalloc(&rows_out, sizeof(int) * (npix + 1)));
+    cudaError_t e = cub::DeviceScan::ExclusiveSum(t2, tb, counts, rows_out, npix + 1, s);
+    int nnz = 0;
+    if (e == cudaSuccess) e = cudaMemcpyAsync(&nnz, rows_out + npix, sizeof(int), cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e == cudaSuccess) e = cudaMalloc(&cols_out, sizeof(int) * std::max(1, nnz));
+    if (e == cudaSuccess) e = cudaMalloc(&vals_out, sizeof(double) * std::max(1, nnz));
+    if (e == cudaSuccess) {
+        delaunay_entries_kernel<<<nblocks(npix, 256), 256, 0, s>>>(
+            mask_dev, nx, ny, ncast, cidx, uidx, (const double2 *)uncasted_points,
+            uncasted_tri_inds, triangles, (const double2 *)tri_points, nullptr, rows_out,
+            cols_out, vals_out);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) {
+        cudaFree(rows_out);
+        cudaFree(cols_out);
+        cudaFree(vals_out);
+        return cuda_status(e, "delaunay_lens_matrix");
+    }
+    *row_inds = rows_out;
+    *cols = cols_out;
+    *vals = vals_out;
+    *nnz_out = nnz;
+    return LENTILS_OK;
+}
+
+}  // extern "C"

@@ -18,7 +18,7 @@ import torch
 
 from . import _native as N
 from .gridding import GriddingPlan, _ptr, _stream_ptr
-from .spaces import FourierSpace, ImageSpace
+from .spaces import DelaunaySpace, FourierSpace, ImageSpace
 
 
 def _is_tensor(x):
@@ -341,7 +341,6 @@ class ManifoldLensOperator(BilinearLensOperator):
     `matrix` holds a scipy copy of the CSR."""
 
     def __init__(self, image_space, source_space, lensmodel, z_src):
-        import scipy.sparse as sps
         lenses = lensmodel.setup_raytracing(z_src)
         mask = torch.as_tensor(np.ascontiguousarray(image_space.mask.reshape(-1))
                                .astype(np.uint8)).cuda()
@@ -353,24 +352,99 @@ class ManifoldLensOperator(BilinearLensOperator):
             ctypes.byref(image_space), ctypes.byref(source_space),
             ctypes.c_void_p(lenses.ctypes.data), len(lenses), _ptr(mask), ctypes.byref(rows),
             ctypes.byref(cols), ctypes.byref(vals), ctypes.byref(nnz), _stream_ptr()))
-        nimg, nsrc, n = image_space.nx * image_space.ny, source_space.nx * source_space.ny, nnz.value
-        try:
-            self._handle = ctypes.c_void_p()
-            N.check(L.lentils_lensop_create_csr(ctypes.byref(self._handle), rows, cols, vals, nimg,
-                                                nsrc, int(n), _stream_ptr()))
-            h_rows = np.empty(nimg + 1, np.int32)
-            h_cols = np.empty(max(1, n), np.int32)
-            h_vals = np.empty(max(1, n), np.float64)
-            for dst, src, nb in ((h_rows, rows, 4 * (nimg + 1)), (h_cols, cols, 4 * n),
-                                 (h_vals, vals, 8 * n)):
-                N.check(L.lentils_copy_to_host(ctypes.c_void_p(dst.ctypes.data), src, nb))
-        finally:
-            for ptr in (rows, cols, vals):
-                if ptr.value:
-                    L.lentils_device_free(ptr)
-        self.matrix = sps.csr_matrix((h_vals[:n], h_cols[:n], h_rows), shape=(nimg, nsrc))
+        nimg, nsrc = image_space.nx * image_space.ny, source_space.nx * source_space.ny
+        self._handle, self.matrix = _csr_lensop(rows, cols, vals, nnz.value, nimg, nsrc)
         self._mask = mask
         Operator.__init__(self, image_space, source_space)
+
+
+def _csr_lensop(rows, cols, vals, nnz, nimg, nsrc):
+    """lensop handle and scipy copy of a device CSR an entry point returned (freed here)."""
+    import scipy.sparse as sps
+    L = N.lib()
+    n = int(nnz)
+    try:
+        h = ctypes.c_void_p()
+        N.check(L.lentils_lensop_create_csr(ctypes.byref(h), rows, cols, vals, nimg, nsrc, n,
+                                            _stream_ptr()))
+        h_rows = np.empty(nimg + 1, np.int32)
+        h_cols = np.empty(max(1, n), np.int32)
+        h_vals = np.empty(max(1, n), np.float64)
+        for dst, src, nb in ((h_rows, rows, 4 * (nimg + 1)), (h_cols, cols, 4 * n),
+                             (h_vals, vals, 8 * n)):
+            N.check(L.lentils_copy_to_host(ctypes.c_void_p(dst.ctypes.data), src, nb))
+    finally:
+        for ptr in (rows, cols, vals):
+            if ptr.value:
+                L.lentils_device_free(ptr)
+    return h, sps.csr_matrix((h_vals[:n], h_cols[:n], h_rows), shape=(nimg, nsrc))
+
+
+def deflect64(lenses, points):
+    """FP64 deflection with the reference's formulas (lentils_deflect64): numpy (..., 2) in and
+    out."""
+    p = torch.as_tensor(np.ascontiguousarray(points, dtype=np.float64)).cuda()
+    out = torch.empty_like(p)
+    lenses = np.ascontiguousarray(lenses)
+    N.check(N.lib().lentils_deflect64(ctypes.c_void_p(lenses.ctypes.data), len(lenses),
+                                      _ptr(p), _ptr(out), p.numel() // 2, _stream_ptr()))
+    return out.cpu().numpy()
+
+
+class DelaunayLensOperator(BilinearLensOperator):
+    """The reference's DelaunayLensOperator (lentils/operators/lens_operators.py:43-80): image
+    pixels on the `ncasted` lattice are the source vertices, deflected in FP64 on the GPU;
+    scipy triangulates them and locates the other deflected pixels, as the reference does; the
+    barycentric CSR (delaunay_lens_matrix_csr, triangles.c:105-140) is assembled on the GPU.
+    `source_space` is the DelaunaySpace of the casted points; `matrix` a scipy copy."""
+
+    def __init__(self, image_space, lensmodel, z_src, ncasted=1):
+        lenses = lensmodel.setup_raytracing(z_src)
+        mask = image_space.mask
+        pts = image_space.points
+        cmask = np.zeros_like(mask)
+        cmask[::ncasted, ::ncasted] = True
+        umask = ~cmask
+        cmask = cmask & mask
+        umask = umask & mask
+        self.casted_points = deflect64(lenses, pts[cmask])
+        self.uncasted_points = deflect64(lenses, pts[umask])
+        self.source_space = DelaunaySpace(self.casted_points)
+        tind = self.source_space.delaunay.find_simplex(self.uncasted_points)
+        nimg = image_space.nx * image_space.ny
+        dev = lambda a, dt: torch.as_tensor(np.ascontiguousarray(a, dtype=dt)).cuda()
+        mask_d = dev(mask.reshape(-1).astype(np.uint8), np.uint8)
+        up = dev(self.uncasted_points.reshape(-1, 2), np.float64)
+        ti = dev(tind, np.int32)
+        tr = dev(self.source_space.triangles, np.int32)
+        tp = dev(self.casted_points.reshape(-1, 2), np.float64)
+        rows, cols, vals = ctypes.c_void_p(), ctypes.c_void_p(), ctypes.c_void_p()
+        nnz = ctypes.c_longlong()
+        N.check(N.lib().lentils_delaunay_lens_matrix(
+            _ptr(mask_d), image_space.nx, image_space.ny, int(ncasted), _ptr(up), _ptr(ti),
+            _ptr(tr), _ptr(tp), ctypes.byref(rows), ctypes.byref(cols), ctypes.byref(vals),
+            ctypes.byref(nnz), _stream_ptr()))
+        self._nsrc = self.source_space.num_points
+        self._handle, self.matrix = _csr_lensop(rows, cols, vals, nnz.value, nimg, self._nsrc)
+        self._mask = mask_d
+        Operator.__init__(self, image_space, self.source_space)
+
+    def _run(self, x, fwd):
+        L = N.lib()
+        nout = self.space_left.nx * self.space_left.ny if fwd else self._nsrc
+        host = not _is_tensor(x)
+        t = torch.as_tensor(np.ascontiguousarray(x, dtype=np.float64).reshape(-1)).cuda() if host \
+            else x.contiguous().reshape(-1)
+        out = torch.empty(nout, dtype=t.dtype, device=t.device)
+        if t.dtype == torch.float32:
+            fn = L.lentils_lensop_apply if fwd else L.lentils_lensop_apply_t
+        else:
+            fn = L.lentils_lensop_apply64 if fwd else L.lentils_lensop_apply_t64
+        N.check(fn(self._handle, _ptr(t), _ptr(out), _stream_ptr()))
+        if fwd:
+            sp = self.space_left
+            return out.cpu().numpy().reshape(sp.shape) if host else out.reshape(sp.nx, sp.ny)
+        return out.cpu().numpy() if host else out
 
 
 class PriorCovarianceOperator(Operator):

@@ -124,3 +124,24 @@ class ImageSpace(Space, ImageSpaceC):
         centers[:, :, 0] = (self.xmin + self.dx * np.arange(self.nx))[:, None]
         centers[:, :, 1] = (self.ymin + self.dy * np.arange(self.ny))[None, :]
         return centers
+
+
+class DelaunaySpace(Space):
+    """Source space of Delaunay-triangulated points (lentils/common/space_base.py:139-158):
+    `points` (N, 2), `triangles` (M, 3) and the scipy triangulation `delaunay`."""
+
+    def __init__(self, points, channels=(0.0,), stokes=("I",)):
+        from scipy.spatial import Delaunay
+        self.num_channels, self.num_stokes = 1, 1
+        self.delaunay = Delaunay(np.asarray(points, dtype=np.float64))
+        self.edge = np.unique(self.delaunay.convex_hull.flatten())
+        self.vertices = self.delaunay.points
+        self.num_points = self.vertices.shape[0]
+        self.triangles = self.delaunay.simplices
+        self.num_triangles = self.triangles.shape[0]
+        super().__init__(shape=(self.num_channels, self.num_stokes, self.num_points))
+
+    @property
+    def points(self):
+        return self.vertices
+

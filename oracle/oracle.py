@@ -56,6 +56,13 @@ class CVisibilitySpace(Structure):
                 ("uv", POINTER(c_double)), ("channels", POINTER(c_double))]
 
 
+class CDelaunaySpace(Structure):
+    """delaunay_space, lentils/backend/common.h:24-35."""
+    _fields_ = [("num_points", c_int), ("num_tris", c_int), ("nchannels", c_int),
+                ("nstokes", c_int), ("channels", POINTER(c_double)), ("points", c_void_p),
+                ("triangles", c_void_p)]
+
+
 class CGlobalLensModel(Structure):
     _fields_ = [("num_lenses", c_int), ("num_zplanes", c_int), ("lenses", c_void_p)]
 
@@ -132,7 +139,9 @@ def ref_lib(name):
     if not os.path.exists(path):
         return None
     lib = ctypes.CDLL(path)
-    if name == "nufft":
+    if name == "triangles":
+        pass
+    elif name == "nufft":
         lib.grid_cpu.restype = None
         lib.grid_cpu.argtypes = [CVisibilitySpace, c_void_p, CFourierSpace, c_void_p, c_int,
                                  c_double, c_int]
@@ -142,6 +151,10 @@ def ref_lib(name):
         lib.deflect_points.restype = None
         lib.deflect_points.argtypes = [CGlobalLensModel, c_void_p, c_int, c_void_p, c_int,
                                        c_void_p]
+    if name == "triangles":
+        lib.delaunay_lens_matrix_csr.restype = None
+        lib.delaunay_lens_matrix_csr.argtypes = [CImageSpace, CDelaunaySpace, c_int, c_void_p,
+                                                 c_void_p, c_void_p, c_void_p, c_void_p]
     if name == "raster":
         lib.manifold_lens_matrix_csr.restype = None
         lib.manifold_lens_matrix_csr.argtypes = [CImageSpace, CImageSpace, CGlobalLensModel,
@@ -525,6 +538,31 @@ def manifold_lens_matrix_ref(img: ImageGeom, src: ImageGeom, lenses):
     ic, sc = img.cstruct(), src.cstruct()
     lib.manifold_lens_matrix_csr(ic, sc, glm, rows.ctypes.data, cols.ctypes.data,
                                  vals.ctypes.data)
+    nnz = int(rows[-1])
+    return rows, cols[:nnz].copy(), vals[:nnz].copy()
+
+
+def delaunay_lens_matrix_ref(img: ImageGeom, ncast, casted_points, uncasted_points,
+                             triangles, tri_inds):
+    """The compiled reference's delaunay_lens_matrix_csr (triangles.c:105-140) for a given
+    triangulation of the casted points and point location of the uncasted ones (the reference
+    takes both from scipy's Delaunay, lens_operators.py:67-70): (row_inds, cols, vals)."""
+    lib = ref_lib("triangles")
+    if lib is None:
+        raise RuntimeError("compiled reference not available (oracle/_ref)")
+    cp = np.ascontiguousarray(casted_points, dtype=np.float64).reshape(-1, 2)
+    up = np.ascontiguousarray(uncasted_points, dtype=np.float64).reshape(-1, 2)
+    tr = np.ascontiguousarray(triangles, dtype=np.int32).reshape(-1, 3)
+    ti = np.ascontiguousarray(tri_inds, dtype=np.int32).reshape(-1)
+    ds = CDelaunaySpace()
+    ds.num_points, ds.num_tris, ds.nchannels, ds.nstokes = cp.shape[0], tr.shape[0], 1, 1
+    ds.points, ds.triangles = cp.ctypes.data, tr.ctypes.data
+    n = img.nx * img.ny
+    rows = np.zeros(n + 1, np.int32)
+    cols = np.zeros(cp.shape[0] + 3 * up.shape[0] + 1, np.int32)
+    vals = np.zeros(cols.size)
+    lib.delaunay_lens_matrix_csr(img.cstruct(), ds, int(ncast), up.ctypes.data, ti.ctypes.data,
+                                 rows.ctypes.data, cols.ctypes.data, vals.ctypes.data)
     nnz = int(rows[-1])
     return rows, cols[:nnz].copy(), vals[:nnz].copy()
 

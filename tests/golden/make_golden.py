@@ -143,6 +143,36 @@ def manifold_case():
     print("manifold", {k: int(out[f"{k}_rows"][-1]) for k in cases})
 
 
+def delaunay_case():
+    """The reference's DelaunayLensOperator pieces (lens_operators.py:43-80): rays deflected by
+    the reference's deflect_points, scipy's triangulation and point location, and
+    delaunay_lens_matrix_csr (triangles.c:105-140), for ncasted = 2 with a masked region."""
+    from scipy.spatial import Delaunay
+    img = O.ImageGeom((22, 18), [(-0.55, 0.55), (-0.45, 0.45)])
+    img.mask[2:5, 3:7] = False
+    lenses = O.lens_array([O.pemd_cpars(0.35, 25.0, 0.8, 0.011, -0.013, 0.5),
+                           O.shear_cpars(0.011, -0.013, 0.04, 60.0)])
+    ncast = 2
+    pts = img.points()
+    cmask = np.zeros(img.shape, bool)
+    cmask[::ncast, ::ncast] = True
+    umask = ~cmask
+    cmask &= img.mask
+    umask &= img.mask
+    casted = O.deflect(lenses, pts[cmask], use_ref=True)
+    uncasted = O.deflect(lenses, pts[umask], use_ref=True)
+    tri = Delaunay(casted)
+    tind = tri.find_simplex(uncasted)
+    r, c, v = O.delaunay_lens_matrix_ref(img, ncast, casted, uncasted, tri.simplices, tind)
+    np.savez_compressed(os.path.join(HERE, "delaunay.npz"), img=np.concatenate([[img.nx, img.ny], img.bounds]),
+                        mask=img.mask.astype(np.uint8), ncast=ncast,
+                        lenses=lenses.view(np.uint8).reshape(len(lenses), -1),
+                        image_casted=pts[cmask], image_uncasted=pts[umask], casted=casted,
+                        uncasted=uncasted, triangles=tri.simplices.astype(np.int32),
+                        tri_inds=tind.astype(np.int32), rows=r, cols=c, vals=v)
+    print("delaunay", int(r[-1]))
+
+
 def grad_case():
     img = O.ImageGeom((13, 17), [(-0.4, 0.9), (-0.2, 0.6)])
     rows, cols, vals = O.grad_csr(img, use_ref=True)
@@ -167,4 +197,5 @@ if __name__ == "__main__":
     deflect_case()
     deflect_deriv_case()
     manifold_case()
+    delaunay_case()
     grad_case()

@@ -99,3 +99,54 @@ def test_cg_with_manifold_lens_operator(native):
     b = M.T @ ora.adjoint(d).reshape(-1)
     Ax = M.T @ ora.adjoint(ora.forward((M @ xs).reshape(img.shape))).reshape(-1) + R @ xs
     assert np.linalg.norm(b - Ax) / np.linalg.norm(b) < 1.5e-6
+
+
+def _delaunay_fixture(golden_dir):
+    from lentils_gb300.spaces import ImageSpace
+    d = np.load(f"{golden_dir}/delaunay.npz")
+    gi = d["img"]
+    img = ImageSpace((int(gi[0]), int(gi[1])), [(gi[2], gi[3]), (gi[4], gi[5])])
+    img.mask[...] = d["mask"].astype(bool)
+    lenses = np.ascontiguousarray(d["lenses"]).view(O.MASS_MODEL_DTYPE).reshape(-1)
+    return d, img, lenses
+
+
+def test_delaunay_matrix_assembly_matches_reference(native, golden_dir):
+    """Same rays, triangulation and point location as the reference: the GPU assembly gives
+    the reference's CSR (triangles.c:105-140)."""
+    from lentils_gb300 import _native as N
+    from lentils_gb300.gridding import _ptr
+    from lentils_gb300.operators import _csr_lensop
+    d, img, _ = _delaunay_fixture(golden_dir)
+    dev = lambda a, dt: torch.as_tensor(np.ascontiguousarray(a, dtype=dt)).cuda()
+    import ctypes
+    rows, cols, vals = ctypes.c_void_p(), ctypes.c_void_p(), ctypes.c_void_p()
+    nnz = ctypes.c_longlong()
+    args = [dev(d["mask"].reshape(-1), np.uint8), img.nx, img.ny, int(d["ncast"]),
+            dev(d["uncasted"], np.float64), dev(d["tri_inds"], np.int32),
+            dev(d["triangles"], np.int32), dev(d["casted"], np.float64)]
+    N.check(N.lib().lentils_delaunay_lens_matrix(
+        *[_ptr(a) if isinstance(a, torch.Tensor) else a for a in args], ctypes.byref(rows),
+        ctypes.byref(cols), ctypes.byref(vals), ctypes.byref(nnz), None))
+    _, M = _csr_lensop(rows, cols, vals, nnz.value, img.nx * img.ny, d["casted"].shape[0])
+    assert np.array_equal(M.indptr, d["rows"]) and np.array_equal(M.indices, d["cols"])
+    assert np.max(np.abs(M.data - d["vals"])) <= 1e-12
+
+
+def test_delaunay_lens_operator(native, golden_dir):
+    """End to end: FP64 GPU rays equal the reference's deflect_points to rounding, and the
+    operator's matrix equals the reference's for the same lens."""
+    from lentils_gb300.operators import DelaunayLensOperator, deflect64
+    d, img, lenses = _delaunay_fixture(golden_dir)
+    assert np.max(np.abs(deflect64(lenses, d["image_casted"]) - d["casted"])) < 1e-13
+    assert np.max(np.abs(deflect64(lenses, d["image_uncasted"]) - d["uncasted"])) < 1e-13
+    op = DelaunayLensOperator(img, _Model(lenses), 2.0, ncasted=int(d["ncast"]))
+    assert np.array_equal(op.source_space.triangles, d["triangles"])
+    M = op.matrix
+    assert np.array_equal(M.indptr, d["rows"]) and np.array_equal(M.indices, d["cols"])
+    assert np.max(np.abs(M.data - d["vals"])) <= 1e-10
+    rng = np.random.default_rng(5)
+    x = rng.normal(size=op.source_space.num_points)
+    assert O.rel_l2((op * x).reshape(-1), M @ x) < 1e-12
+    y = rng.normal(size=img.shape)
+    assert O.rel_l2(op.T * y, M.T @ y.reshape(-1)) < 1e-12

@@ -162,3 +162,22 @@ def test_manifold_fixture_matches_reference():
         r, c, v = O.manifold_lens_matrix_ref(img, src, lenses)
         assert np.array_equal(r, d[f"{name}_rows"]) and np.array_equal(c, d[f"{name}_cols"])
         assert np.array_equal(v, d[f"{name}_vals"])
+
+
+def test_delaunay_fixture_matches_reference():
+    """The committed Delaunay fixture is what the compiled reference (deflect_points and
+    delaunay_lens_matrix_csr) computes with scipy's triangulation."""
+    import pytest
+    if O.ref_lib("triangles") is None or not O.ref_available():
+        pytest.skip("compiled reference not available")
+    from helpers import GOLDEN
+    d = np.load(os.path.join(GOLDEN, "delaunay.npz"))
+    lenses = np.ascontiguousarray(d["lenses"]).view(O.MASS_MODEL_DTYPE).reshape(-1)
+    assert np.array_equal(O.deflect(lenses, d["image_casted"], use_ref=True), d["casted"])
+    gi = d["img"]
+    img = O.ImageGeom((int(gi[0]), int(gi[1])), gi[2:6])
+    img.mask[...] = d["mask"].astype(bool)
+    r, c, v = O.delaunay_lens_matrix_ref(img, int(d["ncast"]), d["casted"], d["uncasted"],
+                                         d["triangles"], d["tri_inds"])
+    assert np.array_equal(r, d["rows"]) and np.array_equal(c, d["cols"])
+    assert np.array_equal(v, d["vals"])
