@@ -362,6 +362,21 @@ typedef struct {
 } lentils_cg_result;
 
 /* ------------------------------------------------------------------------------------------
+ * Direct Fourier sum (DFTOperator, lentils/operators/fourier_operators.py:130-145, matrix of
+ * dft_matrix_csr, lentils/backend/nufft.c:128-161), FP64 on the GPU, as a validator of the
+ * NUFFT: V_k = sum_p x_p e^{i a_kp} over unmasked pixels, a_kp = -2 pi ARCSEC_TO_RADIANS
+ * (u x + v y) with u = uv[0] ch[0], v = -uv[1] ch[0] and x = xmin + i dx, y = ymin + j dy;
+ * the adjoint is its real transpose. Device arrays: uvw (nrows x 3), channels (first used),
+ * mask (nx*ny bytes), image (nx*ny f64), vis (nrows c128); im is a host struct.
+ * ---------------------------------------------------------------------------------------- */
+int lentils_dft_forward(const double *uvw, int nrows, const double *channels,
+                        const lentils_image_space *im, const unsigned char *mask,
+                        const double *image, double *vis, void *stream);
+int lentils_dft_adjoint(const double *uvw, int nrows, const double *channels,
+                        const lentils_image_space *im, const unsigned char *mask,
+                        const double *vis, double *image, void *stream);
+
+/* ------------------------------------------------------------------------------------------
  * Dirty-beam (blurred covariance) form of F^T C^-1 F, the reference's production CG data term
  * (RadioDataset.blurred_covariance_operator, lentils/common/data_base.py:115-129):
  *   B x = crop(pad(x) (*) roll(beam))   (circular convolution on the 2nx x 2ny padded grid)

@@ -153,6 +153,10 @@ _SIGNATURES = [
                                              c_void_p, c_void_p, POINTER(c_void_p),
                                              POINTER(c_void_p), POINTER(c_void_p),
                                              POINTER(c_longlong), c_void_p]),
+    ("lentils_dft_forward", c_int, [c_void_p, c_int, c_void_p, c_void_p, c_void_p, c_void_p,
+                                    c_void_p, c_void_p]),
+    ("lentils_dft_adjoint", c_int, [c_void_p, c_int, c_void_p, c_void_p, c_void_p, c_void_p,
+                                    c_void_p, c_void_p]),
     ("lentils_bcb_create", c_int, [POINTER(c_void_p), c_void_p, c_int, c_int, c_void_p]),
     ("lentils_bcb_destroy", c_int, [c_void_p]),
     ("lentils_bcb_apply", c_int, [c_void_p, c_void_p, c_void_p, c_void_p]),

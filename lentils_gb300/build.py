@@ -25,9 +25,9 @@ NVFLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-I",
                   "-I", CSRC, "--expt-relaxed-constexpr", "-Xptxas", "-warn-spills"]
 
 
-# Per-unit flags: the manifold rasteriser reproduces the reference's plain-C FP64 arithmetic,
-# so multiply-adds are not fused there.
-UNIT_FLAGS = {"manifold.cu": ["-fmad=false"]}
+# Per-unit flags: the manifold rasteriser and the direct Fourier sum reproduce the reference's
+# plain-C FP64 arithmetic, so multiply-adds are not fused there.
+UNIT_FLAGS = {"manifold.cu": ["-fmad=false"], "dft.cu": ["-fmad=false"]}
 
 
 def nvcc_path():

@@ -447,6 +447,41 @@ class DelaunayLensOperator(BilinearLensOperator):
         return out.cpu().numpy() if host else out
 
 
+class DFTOperator(Operator):
+    """The direct Fourier sum (DFTOperator, lentils/operators/fourier_operators.py:130-145)
+    in FP64 on the GPU (lentils_dft_forward / lentils_dft_adjoint): image (nx, ny) ->
+    visibilities (nrows,) complex128 and the real transpose back. A validator of the NUFFT;
+    numpy in, numpy out."""
+
+    def __init__(self, vis_space, image_space):
+        self._uvw = torch.as_tensor(np.ascontiguousarray(vis_space.uvw, dtype=np.float64)
+                                    .reshape(-1, 3)).cuda()
+        self._ch = torch.as_tensor(np.ascontiguousarray(vis_space.channels, dtype=np.float64)
+                                   .reshape(-1)).cuda()
+        self._mask = torch.as_tensor(np.ascontiguousarray(image_space.mask.reshape(-1))
+                                     .astype(np.uint8)).cuda()
+        self._nrows = self._uvw.shape[0]
+        super().__init__(vis_space, image_space)
+
+    def _forward(self, image):
+        sp = self.space_right
+        x = torch.as_tensor(np.ascontiguousarray(image, dtype=np.float64).reshape(-1)).cuda()
+        out = torch.empty(self._nrows, dtype=torch.complex128, device="cuda")
+        N.check(N.lib().lentils_dft_forward(_ptr(self._uvw), self._nrows, _ptr(self._ch),
+                                            ctypes.byref(sp), _ptr(self._mask), _ptr(x),
+                                            _ptr(out), _stream_ptr()))
+        return out.cpu().numpy()
+
+    def _transpose(self, vis):
+        sp = self.space_right
+        v = torch.as_tensor(np.ascontiguousarray(vis, dtype=np.complex128).reshape(-1)).cuda()
+        out = torch.empty(sp.nx * sp.ny, dtype=torch.float64, device="cuda")
+        N.check(N.lib().lentils_dft_adjoint(_ptr(self._uvw), self._nrows, _ptr(self._ch),
+                                            ctypes.byref(sp), _ptr(self._mask), _ptr(v),
+                                            _ptr(out), _stream_ptr()))
+        return out.cpu().numpy().reshape(sp.nx, sp.ny)
+
+
 class PriorCovarianceOperator(Operator):
     """lambda * R^T R with R the forward-difference gradient of grad_matrix_findiff_csr
     ('gradient' prior of operator_base.py:200-251), matrix-free; symmetric."""
