@@ -12,6 +12,11 @@ synthetic visibility set of the class (density ~ 1/|uv| out to 0.45 of Nyquist) 
 degrid + grid pass with CUDA events (best of a few runs after a warm-up); the fastest wins.
 Results are stored per class in a JSON file (default lentils_gb300/tuning/<arch>.json, or the
 LENTILS_TUNING_CACHE path) and reused.
+
+Batched mode (mode="batched", for the persistent lens sweep) times every candidate inside the
+sweep kernel itself, on a small batch of synthetic samples of the class, because there the
+parallelism comes from the many samples: fewer, larger work items win where a single plan
+needs many small ones to fill the GPU. Its cache is <arch>_batched.json.
 """
 from __future__ import annotations
 
@@ -51,10 +56,22 @@ def nvis_bucket(nvis):
     return int(round(math.log2(max(1, nvis))))
 
 
+BATCH_TILES = (8, 16)
+BATCH_CHUNKS = (1024, 2048, 4096)
+
+
 class Autotuner:
-    def __init__(self, path=None, tiles=TILES, chunks=CHUNKS, reps=3):
+    def __init__(self, path=None, tiles=None, chunks=None, reps=3, mode="single"):
+        if mode not in ("single", "batched"):
+            raise ValueError("mode: 'single' or 'batched'")
+        self.mode = mode
+        suffix = "" if mode == "single" else "_batched"
         self.path = path or os.environ.get("LENTILS_TUNING_CACHE") or os.path.join(
-            DEFAULT_CACHE_DIR, f"{arch_name()}.json")
+            DEFAULT_CACHE_DIR, f"{arch_name()}{suffix}.json")
+        if tiles is None:
+            tiles = TILES if mode == "single" else BATCH_TILES
+        if chunks is None:
+            chunks = CHUNKS if mode == "single" else BATCH_CHUNKS
         self.tiles, self.chunks, self.reps = tuple(tiles), tuple(chunks), int(reps)
         self.cache = {}
         if os.path.exists(self.path):
@@ -70,7 +87,8 @@ class Autotuner:
         """(tile, chunk) for the class of this plan, tuning it on first use."""
         k = self.key(nu, nv, w2, nvis)
         if k not in self.cache:
-            self.cache[k] = self.tune(nu, nv, du, dv, w2, 2 ** nvis_bucket(nvis))
+            fn = self.tune if self.mode == "single" else self.tune_batched
+            self.cache[k] = fn(nu, nv, du, dv, w2, 2 ** nvis_bucket(nvis))
             self.tuned += 1
         c = self.cache[k]
         return int(c["tile"]), int(c["chunk"])
@@ -110,6 +128,47 @@ class Autotuner:
                         best = min(best, ev[0].elapsed_time(ev[1]))
                 results.append({"tile": T, "chunk": chunk, "ms": best})
                 plan.close()
+        best = min(results, key=lambda r: r["ms"])
+        return {"tile": best["tile"], "chunk": best["chunk"], "ms": best["ms"],
+                "candidates": results}
+
+    def tune_batched(self, nu, nv, du, dv, w2, nvis, nsamples=8, seed=0):
+        """Best (tile, chunk) for samples of this class inside the persistent sweep."""
+        from .sweep import BatchedSweep, draw_samples
+        rng = np.random.default_rng(seed)
+        n = nu // 2
+        samples = draw_samples(rng, nsamples, sizes=(n,), nvis_range=(nvis, nvis))
+        pix = 0.02
+        for smp in samples:
+            smp.tol = KB_ERROR[w2]
+            smp.pix = pix
+
+        class _Fixed:
+            def __init__(self, t, c):
+                self.t, self.tuned = (t, c), 0
+
+            def params(self, *a):
+                return self.t
+
+        results = []
+        for T in self.tiles:
+            if T > nu // 2 or T > nv // 2:
+                continue
+            for chunk in self.chunks:
+                sw = BatchedSweep(samples, tuner=_Fixed(T, chunk))
+                s = sw.stream
+                ev = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
+                sw.run()
+                best = float("inf")
+                for _ in range(self.reps):
+                    s.synchronize()
+                    ev[0].record(s)
+                    sw.run()
+                    ev[1].record(s)
+                    s.synchronize()
+                    best = min(best, ev[0].elapsed_time(ev[1]))
+                results.append({"tile": T, "chunk": chunk, "ms": best})
+                sw.close()
         best = min(results, key=lambda r: r["ms"])
         return {"tile": best["tile"], "chunk": best["chunk"], "ms": best["ms"],
                 "candidates": results}

@@ -4,7 +4,8 @@ whose operators run one lens model at a time).
 Each sample is a lens model (PEMD + external shear drawn from priors), an n x n image plane
 (pixel centres deflected to the source plane), and its own visibility set on the 2n x 2n
 r2c grid of that image; its KB width follows from its accuracy target (autotune.width_for)
-and its tile and work-item size from the autotuner. One run degrids every sample's grid,
+and its tile and work-item size from the autotuner (batched mode: timed inside the sweep
+kernel). One run degrids every sample's grid,
 grids every sample's visibilities and deflects every sample's pixel grid in one persistent
 kernel launch, replayed as a CUDA graph.
 """
@@ -71,12 +72,12 @@ class BatchedSweep:
     grid(vis_in[s]), beta_out[s] (n*n, 2) float32 source-plane positions of the pixel centres
     (x-major)."""
 
-    def __init__(self, samples, tuner=None, seed=1, tiles=(8, 16)):
+    def __init__(self, samples, tuner=None, seed=1):
         from .spaces import ImageSpace
         from .synthetic import padded_fourier_space, synth_uv
         self.samples = list(samples)
         self.uvw = []
-        self.tuner = tuner if tuner is not None else Autotuner(tiles=tiles)
+        self.tuner = tuner if tuner is not None else Autotuner(mode="batched")
         self.stream = torch.cuda.Stream()
         gen = torch.Generator(device="cuda").manual_seed(seed)
         self.plans, self.grid_in, self.vis_in = [], [], []

@@ -26,7 +26,7 @@ def sweep(tmp_path_factory):
     from lentils_gb300.autotune import Autotuner
     from lentils_gb300.sweep import BatchedSweep
     path = str(tmp_path_factory.mktemp("tune") / "cache.json")
-    tuner = Autotuner(path=path, tiles=(8, 16), chunks=(256, 1024), reps=1)
+    tuner = Autotuner(path=path, tiles=(8, 16), chunks=(256, 1024), reps=1, mode="batched")
     sw = BatchedSweep(_samples(np.random.default_rng(11)), tuner=tuner)
     tuner.save()
     return sw, tuner, path
@@ -38,7 +38,7 @@ def test_sweep_mixes_widths_and_tunes(sweep):
     widths = {s.info["w2"] for s in sw.samples}
     assert widths == {6, 8}
     assert tuner.tuned > 0
-    again = Autotuner(path=path, tiles=(8, 16), chunks=(256, 1024))
+    again = Autotuner(path=path, tiles=(8, 16), chunks=(256, 1024), mode="batched")
     for s in sw.samples:
         p = sw.plans[sw.samples.index(s)]
         assert again.params(p.nu, p.nv, 0, 0, s.info["w2"], s.nvis) == (s.info["tile"],
@@ -101,3 +101,17 @@ def test_sweep_against_oracle(sweep):
         lenses = GlobalLensModel(s.lenses).setup_raytracing(2.0)
         b_or = O.deflect(lenses, sw.pixel_points(k))
         assert np.max(np.abs(sw.beta_out[k].cpu().numpy() - b_or)) < 2e-6
+
+
+def test_single_plan_tuning(tmp_path):
+    """Single-plan mode: every (tile, chunk) candidate timed on its own plan; the cache
+    answers the same class without tuning again."""
+    from lentils_gb300.autotune import Autotuner
+    path = str(tmp_path / "single.json")
+    t = Autotuner(path=path, tiles=(8, 16), chunks=(256, 1024), reps=1)
+    p = t.params(128, 128, 2e4, 2e4, 8, 5000)
+    assert p in {(8, 256), (8, 1024), (16, 256), (16, 1024)} and t.tuned == 1
+    assert len(t.cache[t.key(128, 128, 8, 5000)]["candidates"]) == 4
+    t.save()
+    assert Autotuner(path=path).params(128, 128, 0, 0, 8, 5000) == p
+
