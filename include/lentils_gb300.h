@@ -424,6 +424,10 @@ int lentils_dot64(const double *a, const double *b, int n, double *out, void *st
  * ---------------------------------------------------------------------------------------- */
 int lentils_tc_gemm_bf16(const void *A, const void *B, float *C, int M, int N, int K,
                          int swap_lbo_sbo, int *err_dev, void *stream);
+/* Failure-path self-test of the bounded tensor-core waits: a kernel holding tensor memory
+ * waits on an mbarrier that nothing completes, gives up after poll_limit polls (1..2^20), sets
+ * *err_dev = 1, frees its tensor memory and returns; the context stays usable. */
+int lentils_tc_timeout_selftest(int *err_dev, int poll_limit, void *stream);
 
 /* ------------------------------------------------------------------------------------------
  * Batched lens-parameter sweep (no counterpart in the reference, whose operators run one lens

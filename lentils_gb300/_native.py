@@ -172,6 +172,7 @@ _SIGNATURES = [
     ("lentils_prior_gradient_apply64", c_int, [c_void_p, c_void_p, c_int, c_int, c_double,
                                                c_double, c_double, c_void_p]),
     ("lentils_dot64", c_int, [c_void_p, c_void_p, c_int, POINTER(c_double), c_void_p]),
+    ("lentils_tc_timeout_selftest", c_int, [c_void_p, c_int, c_void_p]),
     ("lentils_tc_gemm_bf16", c_int, [c_void_p, c_void_p, c_void_p, c_int, c_int, c_int, c_int,
                                      c_void_p, c_void_p]),
     ("lentils_unet_param_count", c_longlong, []),

@@ -35,11 +35,12 @@ __device__ __forceinline__ void fence_mbar_init()
 }
 
 // Waits until the barrier's phase with parity `parity` has completed. Returns false if the
-// wait gave up after kSpinLimit polls.
-__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity)
+// wait gave up after `limit` polls.
+__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity,
+                                          uint32_t limit = kSpinLimit)
 {
     const uint32_t addr = smem_u32(bar);
-    for (uint32_t i = 0; i < kSpinLimit; ++i) {
+    for (uint32_t i = 0; i < limit; ++i) {
         uint32_t done;
         asm volatile(
             "{\n\t.reg .pred p;\n\t"

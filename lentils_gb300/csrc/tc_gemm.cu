@@ -24,11 +24,45 @@ static int launch_tc_gemm(const void *A, const void *B, float *C, int M, int K, 
     return LENTILS_OK;
 }
 
+// Self-test of the bounded wait: one CTA allocates tensor memory, waits on an mbarrier that
+// nothing arrives on (with a short poll limit), records the timeout like the GEMM kernels do,
+// frees its tensor memory and returns.
+__global__ void __launch_bounds__(32) tc_timeout_selftest_kernel(int *err, uint32_t limit)
+{
+    using namespace tc;
+    __shared__ uint64_t bar;
+    __shared__ uint32_t tmem_base;
+    tmem_alloc(&tmem_base, 32);
+    tmem_relinquish();
+    if (threadIdx.x == 0) {
+        mbar_init(&bar, 1);
+        fence_mbar_init();
+    }
+    tc_fence_before();
+    __syncwarp();
+    tc_fence_after();
+    const bool ok = mbar_wait(&bar, 0, limit);  // phase 0 never completes
+    if (!ok && threadIdx.x == 0) atomicExch(err, 1);
+    tc_fence_before();
+    __syncwarp();
+    tmem_dealloc(tmem_base, 32);
+}
+
 }  // namespace lentils
 
 using namespace lentils;
 
 extern "C" {
+
+int lentils_tc_timeout_selftest(int *err_dev, int poll_limit, void *stream)
+{
+    clear_error();
+    if (!err_dev || poll_limit < 1 || poll_limit > (1 << 20))
+        return set_error(LENTILS_ERR_INVALID, "tc_timeout_selftest: bad arguments");
+    tc_timeout_selftest_kernel<<<1, 32, 0, (cudaStream_t)stream>>>(err_dev, (uint32_t)poll_limit);
+    LENTILS_CHECK_LAUNCH("tc_timeout_selftest_kernel");
+    return LENTILS_OK;
+}
 
 int lentils_tc_gemm_bf16(const void *A, const void *B, float *C, int M, int N, int K,
                          int swap_lbo_sbo, int *err_dev, void *stream)

@@ -26,3 +26,14 @@ def test_tc_gemm_bf16(native, M, N, K):
     ref = A.double() @ B.double().T
     rel = float(((C.double() - ref).abs().max() / ref.abs().max()).item())
     assert rel < 5e-6
+
+
+def test_bounded_wait_times_out_and_context_survives(native):
+    """A wait that nothing completes gives up after its poll limit: the kernel returns, sets
+    the error flag and frees its tensor memory; the next tensor-core GEMM runs normally."""
+    L = native.lib()
+    err = torch.zeros(1, dtype=torch.int32, device="cuda")
+    assert L.lentils_tc_timeout_selftest(ctypes.c_void_p(err.data_ptr()), 1000, None) == 0
+    torch.cuda.synchronize()
+    assert int(err.item()) == 1
+    test_tc_gemm_bf16(native, 128, 64, 64)
