@@ -36,23 +36,51 @@ __device__ __forceinline__ int core_offset(int row, int piece)
     return (row >> 3) * 1024 + piece * 128 + (row & 7) * 16;
 }
 
+// Piece i of thread t (128 threads) is row r = 16 i + 8 (t / 64) + t % 8, K-piece q = (t / 8) % 8:
+// its core-matrix offset is 2048 i + 16 t, so a warp's shared-memory stores are contiguous, and
+// eight consecutive threads take eight consecutive rows of one K-piece. All global loads of a
+// group are issued before its shared-memory stores (the loaders read through generic pointers,
+// which the compiler cannot separate from the stores), so a chunk costs one or two memory
+// round trips per thread instead of one per piece.
+template <int NP, class L>
+__device__ __forceinline__ void stage_rows(const L &ld, int r0, int kp0, int kp_end,
+                                           unsigned char *s)
+{
+    const int t = threadIdx.x;
+    const int rr = ((t >> 6) << 3) + (t & 7), q = (t >> 3) & 7, kp = kp0 + q;
+    constexpr int kGroup = NP < 8 ? NP : 8;
+#pragma unroll
+    for (int g = 0; g < NP; g += kGroup) {
+        uint4 v[kGroup];
+#pragma unroll
+        for (int i = 0; i < kGroup; ++i)
+            v[i] = (kp < kp_end) ? ld(r0 + 16 * (g + i) + rr, kp) : make_uint4(0, 0, 0, 0);
+#pragma unroll
+        for (int i = 0; i < kGroup; ++i)
+            *reinterpret_cast<uint4 *>(s + 2048 * (g + i) + 16 * t) = v[i];
+    }
+}
+
 template <int N, class LA, class LB>
 __device__ __forceinline__ void stage_chunk(const LA &la, const LB &lb, int m0, int n0, int kp0,
                                             int kp_end, unsigned char *sa, unsigned char *sb)
 {
-    for (int p = threadIdx.x; p < 128 * kPiecesPerChunk; p += blockDim.x) {
-        const int r = p >> 3, q = p & 7;
-        const int kp = kp0 + q;
-        const uint4 v = (kp < kp_end) ? la(m0 + r, kp) : make_uint4(0, 0, 0, 0);
-        *reinterpret_cast<uint4 *>(sa + core_offset(r, q)) = v;
-    }
-    for (int p = threadIdx.x; p < N * kPiecesPerChunk; p += blockDim.x) {
-        const int r = p >> 3, q = p & 7;
-        const int kp = kp0 + q;
-        const uint4 v = (kp < kp_end) ? lb(n0 + r, kp) : make_uint4(0, 0, 0, 0);
-        *reinterpret_cast<uint4 *>(sb + core_offset(r, q)) = v;
-    }
+    stage_rows<128 / 16>(la, m0, kp0, kp_end, sa);
+    stage_rows<N / 16>(lb, n0, kp0, kp_end, sb);
 }
+
+// Epilogues declare `static constexpr bool kRowPerLane = true` when each thread should call them
+// for its own row (an output of one column); the others are called through a shared-memory
+// transpose, 32 columns at a time, so the 32 lanes of a warp handle 32 consecutive columns of
+// one row and row-major stores coalesce.
+template <class EP, class = void>
+struct row_per_lane {
+    static constexpr bool value = false;
+};
+template <class EP>
+struct row_per_lane<EP, decltype((void)EP::kRowPerLane)> {
+    static constexpr bool value = EP::kRowPerLane;
+};
 
 // kpieces: total K / 8; kp_per_split: pieces handled by one blockIdx.z (multiple of 8)
 template <int N, class LA, class LB, class EP>
@@ -123,12 +151,31 @@ __global__ void __launch_bounds__(128)
     tc_fence_after();
     if (!ok && threadIdx.x == 0) atomicExch(err, 1);
     if (ok && nchunks > 0) {
-        const int row = warp * 32 + (threadIdx.x & 31);
-        for (int c0 = 0; c0 < N; c0 += 8) {
-            float v[8];
-            tmem_ld8(tmem + ((uint32_t)(warp * 32) << 16) + c0, v);
+        const int lane = threadIdx.x & 31;
+        const uint32_t taddr = tmem + ((uint32_t)(warp * 32) << 16);
+        if constexpr (row_per_lane<EP>::value || N % 32 != 0) {
+            for (int c0 = 0; c0 < N; c0 += 8) {
+                float v[8];
+                tmem_ld8(taddr + c0, v);
 #pragma unroll
-            for (int j = 0; j < 8; ++j) ep(m0 + row, n0 + c0 + j, v[j]);
+                for (int j = 0; j < 8; ++j) ep(m0 + warp * 32 + lane, n0 + c0 + j, v[j]);
+            }
+        } else {
+            // the staging buffers are free: every MMA that read them has completed
+            float *tr = reinterpret_cast<float *>(smem) + warp * (32 * 33);
+            for (int c0 = 0; c0 < N; c0 += 32) {
+#pragma unroll
+                for (int j = 0; j < 32; j += 8) {
+                    float v[8];
+                    tmem_ld8(taddr + c0 + j, v);
+#pragma unroll
+                    for (int i = 0; i < 8; ++i) tr[lane * 33 + j + i] = v[i];
+                }
+                __syncwarp();
+#pragma unroll 4
+                for (int r = 0; r < 32; ++r) ep(m0 + warp * 32 + r, n0 + c0 + lane, tr[r * 33 + lane]);
+                __syncwarp();
+            }
         }
     }
     tc_fence_before();

@@ -172,6 +172,7 @@ struct EpiAct {  // y[pixel][co] = bf16(relu?(v + bias))
 };
 
 struct EpiOut {  // out[pixel] = v + bias (channel 0 only), FP32
+    static constexpr bool kRowPerLane = true;
     float *out;
     const float *bias;
     int npix;
@@ -199,6 +200,24 @@ struct EpiAtomicF32 {  // g[row][col] += v
     }
 };
 
+struct EpiPartialF32 {  // slab blockIdx.z of g: g[z][row][col] = v (split-K partial sums)
+    float *g;
+    int rows, cols;
+    __device__ __forceinline__ void operator()(int r, int c, float v) const
+    {
+        if (r < rows && c < cols) g[((size_t)blockIdx.z * rows + r) * cols + c] = v;
+    }
+};
+
+// A forward layer whose output has fewer than kSplitMaxPix pixels (fewer than 64 row tiles of
+// 128) splits its K reduction over CTAs: each split writes an FP32 partial slab, and a second
+// kernel sums the slabs in a fixed order and applies bias / ReLU / BF16, so the result does not
+// depend on CTA timing. At batch 1 this turns the deep layers' long serial chunk chains (9-18
+// chunks on 2-8 CTAs) into a few chunks on many CTAs. The number of splits is at most
+// max(2, 128 / row tiles), so the slabs hold at most kSplitSlabPix pixels x 128 channels.
+constexpr int kSplitMaxPix = 64 * 128;
+constexpr int kSplitSlabPix = 2 * kSplitMaxPix;
+
 // -- elementwise kernels ----------------------------------------------------------------------------
 static int blocks_n(long long n)
 {
@@ -220,6 +239,21 @@ __global__ void make_input_kernel(const float *__restrict__ r, const float *__re
         v[1] = __float2bfloat16(d[p]);
         for (int i = 2; i < 8; ++i) v[i] = __float2bfloat16(0.f);
         *reinterpret_cast<uint4 *>(x0 + p * 8) = *reinterpret_cast<uint4 *>(v);
+    }
+}
+
+// y[pixel][c] = bf16(relu?(sum_z part[z][pixel][c] + bias)), slabs summed in order z = 0, 1, ...
+__global__ void finalize_act_kernel(const float *__restrict__ part, int nz,
+                                    const float *__restrict__ bias, bf16 *__restrict__ y,
+                                    long long n, int C, int relu)
+{
+    LENTILS_GRID_STRIDE(e, n)
+    {
+        float acc = part[e];
+        for (int z = 1; z < nz; ++z) acc += part[(size_t)z * n + e];
+        float v = acc + bias[e % C];
+        if (relu) v = fmaxf(v, 0.f);
+        y[e] = __float2bfloat16(v);
     }
 }
 
@@ -498,6 +532,7 @@ struct lentils_unet {
     lentils::bf16 *x0, *e1, *p1, *e2, *p2, *e3, *p3, *b, *u3, *c3, *u2, *c2, *u1, *c1;
     float *out;
     float *pscale;  // preconditioner scale (device)
+    float *splitk;  // FP32 partial slabs of split-K forward layers (kSplitSlabPix x 128)
     // gradients
     lentils::bf16 *dy_out, *d_c1, *d_u1, *d_c2, *d_u2, *d_c3, *d_u3, *d_b, *d_p3, *d_e3, *d_p2,
         *d_e2, *d_p1, *d_e1;
@@ -537,6 +572,18 @@ static int conv_gemm(const LA &la, const tc::RowMajorLoader &lb, const EP &ep, i
     return LENTILS_OK;
 }
 
+template <int N>
+static int conv_gemm_split(const ConvFwdA &la, const tc::RowMajorLoader &lb,
+                           const EpiPartialF32 &ep, int mtiles, int kp, int per, int nz, int *err,
+                           cudaStream_t s)
+{
+    auto kern = tc::gemm_kernel<N, ConvFwdA, tc::RowMajorLoader, EpiPartialF32>;
+    LENTILS_CUDA_TRY((gemm_smem_attr<N, ConvFwdA, tc::RowMajorLoader, EpiPartialF32>()));
+    kern<<<dim3(mtiles, 1, nz), 128, tc::GemmSmem<N>::kBytes, s>>>(la, lb, ep, kp, per, err);
+    LENTILS_CHECK_LAUNCH("conv gemm (split-K)");
+    return LENTILS_OK;
+}
+
 template <class LA, class EP>
 static int conv_gemm_n(int N, const LA &la, const tc::RowMajorLoader &lb, const EP &ep, int M,
                        int K, int *err, cudaStream_t s)
@@ -569,6 +616,27 @@ static int layer_forward(lentils_unet *net, int l, const bf16 *x, void *y, int B
     if (l == kNumLayers - 1) {
         EpiOut ep{(float *)y, net->b32[l], npix};
         return conv_gemm_n(c.cout_p, la, lb, ep, npix, K, net->err, s);
+    }
+    const int mtiles = (npix + 127) / 128;
+    const int kp = (K + 7) / 8, nchunks = (kp + 7) / 8;
+    const int split = std::min(nchunks, std::max(2, 128 / mtiles));
+    const int per = ((nchunks + split - 1) / split) * 8;  // pieces per split (whole chunks)
+    const int nz = (kp + per - 1) / per;
+    const long long n = (long long)npix * c.cout_p;
+    if (npix < kSplitMaxPix && nz > 1 && nz * n <= (long long)kSplitSlabPix * 128) {
+        EpiPartialF32 ep{net->splitk, npix, c.cout_p};
+        int st = LENTILS_OK;
+        switch (c.cout_p) {
+        case 32: st = conv_gemm_split<32>(la, lb, ep, mtiles, kp, per, nz, net->err, s); break;
+        case 64: st = conv_gemm_split<64>(la, lb, ep, mtiles, kp, per, nz, net->err, s); break;
+        case 128: st = conv_gemm_split<128>(la, lb, ep, mtiles, kp, per, nz, net->err, s); break;
+        default: return set_error(LENTILS_ERR_UNSUPPORTED, "split-K N=%d", c.cout_p);
+        }
+        if (st) return st;
+        finalize_act_kernel<<<blocks_n(n), 256, 0, s>>>(net->splitk, nz, net->b32[l], (bf16 *)y,
+                                                        n, c.cout_p, c.relu);
+        LENTILS_CHECK_LAUNCH("finalize_act_kernel");
+        return LENTILS_OK;
     }
     EpiAct ep{(bf16 *)y, net->b32[l], npix, c.cout_p, c.relu};
     return conv_gemm_n(c.cout_p, la, lb, ep, npix, K, net->err, s);
@@ -720,6 +788,9 @@ static int prepare_forward()
     LENTILS_CUDA_TRY((gemm_smem_attr<64, ConvFwdA, tc::RowMajorLoader, EpiAct>()));
     LENTILS_CUDA_TRY((gemm_smem_attr<128, ConvFwdA, tc::RowMajorLoader, EpiAct>()));
     LENTILS_CUDA_TRY((gemm_smem_attr<32, ConvFwdA, tc::RowMajorLoader, EpiOut>()));
+    LENTILS_CUDA_TRY((gemm_smem_attr<32, ConvFwdA, tc::RowMajorLoader, EpiPartialF32>()));
+    LENTILS_CUDA_TRY((gemm_smem_attr<64, ConvFwdA, tc::RowMajorLoader, EpiPartialF32>()));
+    LENTILS_CUDA_TRY((gemm_smem_attr<128, ConvFwdA, tc::RowMajorLoader, EpiPartialF32>()));
     return LENTILS_OK;
 }
 
@@ -854,6 +925,7 @@ int lentils_unet_create(lentils_unet **out, int H, int W, int max_batch, const f
     add((void **)&net->d_e1, b2 * np0 * 32);
     add((void **)&net->loss, sizeof(float));
     add((void **)&net->pscale, sizeof(float));
+    add((void **)&net->splitk, sizeof(float) * kSplitSlabPix * 128);
     add((void **)&net->err, sizeof(int));
     size_t total = 0;
     for (auto &p : parts) total += p.second;

@@ -41,7 +41,10 @@ def _cuda(*a):
     return [torch.as_tensor(v).cuda() for v in a]
 
 
-@pytest.mark.parametrize("B,H,W", [(1, 16, 16), (2, 32, 48), (3, 64, 64)])
+# (1, 16, 16) ... (2, 32, 48) run every layer through the split-K form (FP32 partial slabs summed
+# in order), (3, 64, 64) the full-resolution layers through the unsplit form, (1, 128, 128) is
+# the 128 x 128 source at batch 1 as the solver applies it (deep layers split, top ones not).
+@pytest.mark.parametrize("B,H,W", [(1, 16, 16), (2, 32, 48), (3, 64, 64), (1, 128, 128)])
 def test_unet_forward_matches_oracle(native, B, H, W):
     from lentils_gb300 import learned
     p, x, f, _ = _problem(10 + H, B, H, W)
@@ -53,6 +56,20 @@ def test_unet_forward_matches_oracle(native, B, H, W):
     ref_x = U.forward(p, x, f, emulate_bf16=False)
     assert _rel(out, ref_e) < REL_EMULATED
     assert _rel(out, ref_x) < REL_EXACT
+
+
+def test_unet_forward_is_deterministic(native):
+    """Split-K layers sum their partial slabs in a fixed order: repeated forwards at batch 1
+    (and at batch 4, same weights) give bit-identical outputs."""
+    from lentils_gb300 import learned
+    p, x, f, _ = _problem(77, 4, 128, 128)
+    net = learned.UNet(128, 128, max_batch=4, params=p)
+    xc, fc = _cuda(x, f)
+    for B in (1, 4):
+        outs = [net.forward(xc[:B], fc[:B]) for _ in range(4)]
+        for o in outs[1:]:
+            assert torch.equal(o, outs[0])
+    assert net.error_flag() == 0
 
 
 @pytest.mark.parametrize("B,H,W", [(1, 16, 16), (2, 32, 32)])
