@@ -356,7 +356,8 @@ def run_cg_bench(repeats=3):
     iterative refinement, CUDA-graph inner iterations), three ways, each the best of `repeats`
     solves after a warm-up solve: plain Jacobi-PCG; flexible CG with Jacobi directions and an
     8-direction A-orthogonalisation window; the same with the learned preconditioner
-    (committed weights, trained on the GPU by lentils_gb300.train_preconditioner)."""
+    (committed weights, trained on the GPU by lentils_gb300.train_preconditioner, used with the
+    deployment policy stored beside them)."""
     import ctypes
     import torch
     from lentils_gb300 import _native as N
@@ -367,15 +368,20 @@ def run_cg_bench(repeats=3):
     inv, _, _ = workloads.inversion()
     setup_s = time.perf_counter() - t0
     params, meta = T.load(T.DEFAULT_WEIGHTS)
+    pol = T.deploy_policy(meta)
     net = learned.UNet(workloads.SRC, workloads.SRC, max_batch=1, params=params)
-    net.set_jacobi_weight(0.3)
+    net.set_jacobi_weight(pol["jacobi_weight"])
     inner_tol = 1e-3
+
+    def learned_solve(target):
+        return lambda tol: target.solve_flexible(net, tol=tol, inner_tol=inner_tol,
+                                                 window=pol["window"],
+                                                 net_every=pol["net_every"])
     runs = {
         "plain_jacobi_pcg": lambda tol: inv.solve(tol=tol, inner_tol=inner_tol),
         "jacobi_fcg8": lambda tol: inv.solve_flexible(None, tol=tol, inner_tol=inner_tol,
                                                       window=8),
-        "learned_fcg8": lambda tol: inv.solve_flexible(net, tol=tol, inner_tol=inner_tol,
-                                                       window=8),
+        "learned_fcg8": learned_solve(inv),
     }
     out = {"workload": workloads.DESCRIPTION, "tol": 1e-6, "inner_tol": inner_tol,
            "setup_s": setup_s}
@@ -391,9 +397,9 @@ def run_cg_bench(repeats=3):
                      "solve_s": best["seconds"]}
         if name == "learned_fcg8":
             out[name].update({"net_iterations": best["net_iterations"],
-                              "fallback": best["fallback"], "jacobi_weight": 0.3,
+                              "fallback": best["fallback"], "policy": pol,
                               "training": {k: meta[k] for k in ("draws", "pairs", "steps",
-                                                                "loss")}})
+                                                                "loss") if k in meta}})
     # the same inversion with the dirty-beam data term (the reference's production form)
     t1 = time.perf_counter()
     inv_b = workloads.inversion(nufft=inv.nufft, data_term="bcb")[0]
@@ -402,8 +408,7 @@ def run_cg_bench(repeats=3):
         "bcb_plain_jacobi_pcg": lambda tol: inv_b.solve(tol=tol, inner_tol=inner_tol),
         "bcb_jacobi_fcg8": lambda tol: inv_b.solve_flexible(None, tol=tol, inner_tol=inner_tol,
                                                             window=8),
-        "bcb_learned_fcg8": lambda tol: inv_b.solve_flexible(net, tol=tol, inner_tol=inner_tol,
-                                                             window=8),
+        "bcb_learned_fcg8": learned_solve(inv_b),
     }
     for name, fn in runs_b.items():
         fn(1e-2)

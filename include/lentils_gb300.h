@@ -349,6 +349,8 @@ typedef struct {
     int use_graph;     /* capture one inner iteration in a CUDA graph and replay it        */
     int window;        /* lentils_fcg_solve: directions kept for A-orthogonalisation (1-8;
                           0 means 1); ignored by lentils_cg_solve                          */
+    int net_every;     /* lentils_fcg_solve with a network: it proposes every net_every-th
+                          direction (0 or 1: every one), the others are Jacobi directions  */
 } lentils_cg_options;
 
 typedef struct {

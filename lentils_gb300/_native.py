@@ -61,7 +61,7 @@ class GridDescC(Structure):
 class CGOptionsC(Structure):
     _fields_ = [("tol", c_double), ("inner_tol", c_double), ("max_outer", c_int),
                 ("max_inner", c_int), ("check_every", c_int), ("use_graph", c_int),
-                ("window", c_int)]
+                ("window", c_int), ("net_every", c_int)]
 
 
 class CGResultC(Structure):

@@ -899,8 +899,8 @@ int lentils_fcg_solve(lentils_normal_op *op, const double *b, double *x, const f
     double *r64 = nullptr, *ax64 = nullptr, *partial = nullptr, *scal = nullptr;
     FCGScalars *sc = nullptr;
     FCGWindow *win = nullptr;
-    cudaGraph_t graph = nullptr;
-    cudaGraphExec_t gexec = nullptr;
+    cudaGraph_t graph[2] = {nullptr, nullptr};  // one inner iteration: [0] Jacobi, [1] network
+    cudaGraphExec_t gexec[2] = {nullptr, nullptr};
     int st = LENTILS_OK;
     cudaError_t e = cudaMalloc(&e32, sizeof(float) * n);
     if (e == cudaSuccess) e = cudaMalloc(&r32, sizeof(float) * n);
@@ -931,11 +931,13 @@ int lentils_fcg_solve(lentils_normal_op *op, const double *b, double *x, const f
     if (!st && net) st = lentils_unet_features(inv_diag32, feat, n, stream);
     if (!st && net) st = unet_prepare(net);
     bool use_net = net != nullptr;  // false after a stagnation fallback
+    const int every = std::max(1, opt->net_every);
 
-    // direction step: z = M(r); d = z or the Jacobi direction; p = d - sum_j (d.Q[j] / pq[j]) P[j]
-    auto direction = [&](bool first) -> int {
-        float *zdir = use_net ? z32 : nullptr;
-        if (use_net) {
+    // direction step: z = M(r) (with_net) and d = z or the Jacobi direction;
+    // p = d - sum_j (d.Q[j] / pq[j]) P[j]
+    auto direction = [&](bool first, bool with_net) -> int {
+        float *zdir = with_net ? z32 : nullptr;
+        if (with_net) {
             if (int q = unet_precondition(net, r32, inv_diag32, feat, z32, s)) return q;
             fcg_descent_dots_kernel<<<kRedBlocks, 256, 0, s>>>(z32, r32, inv_diag32, n, partial);
             fcg_select_kernel<<<1, 256, 0, s>>>(partial, kRedBlocks, sc, 1);
@@ -948,7 +950,7 @@ int lentils_fcg_solve(lentils_normal_op *op, const double *b, double *x, const f
         cudaError_t le = cudaGetLastError();
         return le == cudaSuccess ? LENTILS_OK : cuda_status(le, "fcg direction");
     };
-    auto inner_iteration = [&]() -> int {
+    auto inner_iteration = [&](bool with_net) -> int {
         int q = lentils_normal_op_apply(op, p32, ap32, s);
         if (q) return q;
         fcg_dot2_kernel<<<kRedBlocks, 256, 0, s>>>(p32, ap32, r32, n, partial);
@@ -956,7 +958,7 @@ int lentils_fcg_solve(lentils_normal_op *op, const double *b, double *x, const f
         fcg_update_kernel<<<kRedBlocks, 256, 0, s>>>(e32, r32, p32, ap32, sc, n, partial);
         fcg_rr_kernel<<<1, 256, 0, s>>>(partial, kRedBlocks, sc, 0);
         fcg_store_kernel<<<nb(n), 256, 0, s>>>(p32, ap32, Pw, Qw, sc, win, n);
-        return direction(false);
+        return direction(false, with_net);
     };
 
     const auto t0 = std::chrono::steady_clock::now();
@@ -969,20 +971,29 @@ int lentils_fcg_solve(lentils_normal_op *op, const double *b, double *x, const f
             rel = (bnorm > 0) ? sqrt(host_dot64(r64, r64, n, partial, scal, s)) / bnorm : 0.0;
         }
     }
-    // one inner iteration captured as a graph (again after a fallback changes the iteration)
-    auto capture = [&]() -> int {
-        if (gexec) cudaGraphExecDestroy(gexec);
-        if (graph) cudaGraphDestroy(graph);
-        gexec = nullptr;
-        graph = nullptr;
+    // one inner iteration captured as a graph, with and/or without the network (again after a
+    // fallback changes the iteration)
+    auto capture_one = [&](int w) -> int {
         cudaError_t ce = cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal);
         if (ce != cudaSuccess) return cuda_status(ce, "cudaStreamBeginCapture");
-        const int q = inner_iteration();
-        ce = cudaStreamEndCapture(s, &graph);
+        const int q = inner_iteration(w == 1);
+        ce = cudaStreamEndCapture(s, &graph[w]);
         if (q) return q;
         if (ce != cudaSuccess) return cuda_status(ce, "cudaStreamEndCapture");
-        ce = cudaGraphInstantiate(&gexec, graph, 0);
+        ce = cudaGraphInstantiate(&gexec[w], graph[w], 0);
         return ce == cudaSuccess ? LENTILS_OK : cuda_status(ce, "cudaGraphInstantiate");
+    };
+    auto capture = [&]() -> int {
+        for (int w = 0; w < 2; ++w) {
+            if (gexec[w]) cudaGraphExecDestroy(gexec[w]);
+            if (graph[w]) cudaGraphDestroy(graph[w]);
+            gexec[w] = nullptr;
+            graph[w] = nullptr;
+        }
+        if (use_net)
+            if (int q = capture_one(1)) return q;
+        if (!use_net || every > 1) return capture_one(0);
+        return LENTILS_OK;
     };
     if (!st && opt->use_graph) st = capture();
     int outer = 0, inner_total = 0, fallback = 0;
@@ -992,20 +1003,22 @@ int lentils_fcg_solve(lentils_normal_op *op, const double *b, double *x, const f
         ++outer;
         fcg_start_kernel<<<kRedBlocks, 256, 0, s>>>(r64, r32, e32, p32, ap32, n, partial);
         fcg_rr_kernel<<<1, 256, 0, s>>>(partial, kRedBlocks, sc, 1);
-        if ((st = direction(true))) break;
+        if ((st = direction(true, use_net))) break;
         FCGScalars hs;
         int k = 0;
         double mark_rr = -1.0;
         int mark_k = 0;
         while (k < opt->max_inner) {
             for (int c = 0; c < check && k < opt->max_inner; ++c, ++k) {
-                if (gexec) {
-                    e = cudaGraphLaunch(gexec, s);
+                // the direction this iteration ends with is the (k + 2)-th of the inner solve
+                const int w = (use_net && (k + 1) % every == 0) ? 1 : 0;
+                if (gexec[w]) {
+                    e = cudaGraphLaunch(gexec[w], s);
                     if (e != cudaSuccess) {
                         st = cuda_status(e, "cudaGraphLaunch");
                         break;
                     }
-                } else if ((st = inner_iteration())) {
+                } else if ((st = inner_iteration(w == 1))) {
                     break;
                 }
             }
@@ -1029,7 +1042,7 @@ int lentils_fcg_solve(lentils_normal_op *op, const double *b, double *x, const f
                 use_net = false;
                 fallback = 1;
                 mark_k = k;
-                if (gexec && (st = capture())) break;
+                if (opt->use_graph && (st = capture())) break;
             }
         }
         inner_total += k;
@@ -1062,8 +1075,10 @@ int lentils_fcg_solve(lentils_normal_op *op, const double *b, double *x, const f
     res->inner_total = inner_total;
     res->rel_residual = rel;
     res->seconds = std::chrono::duration<double>(t1 - t0).count();
-    if (gexec) cudaGraphExecDestroy(gexec);
-    if (graph) cudaGraphDestroy(graph);
+    for (int w = 0; w < 2; ++w) {
+        if (gexec[w]) cudaGraphExecDestroy(gexec[w]);
+        if (graph[w]) cudaGraphDestroy(graph[w]);
+    }
     cudaFree(e32);
     cudaFree(r32);
     cudaFree(z32);

@@ -132,14 +132,15 @@ class SourceInversion:
         return x, info
 
     def solve_flexible(self, net=None, tol=1e-6, inner_tol=1e-2, max_outer=30, max_inner=5000,
-                       check_every=10, use_graph=True, x0=None, window=1):
+                       check_every=10, use_graph=True, x0=None, window=1, net_every=1):
         """Flexible CG with the learned preconditioner `net` (learned.UNet on the source grid;
         None: the same iteration with Jacobi directions only), inside the same FP64 iterative
-        refinement as solve(). Returns (x float64 CUDA tensor, info)."""
+        refinement as solve(); the network proposes every `net_every`-th direction. Returns
+        (x float64 CUDA tensor, info)."""
         x = torch.zeros(self.nsrc, dtype=torch.float64, device="cuda") if x0 is None else \
             torch.as_tensor(x0, dtype=torch.float64).reshape(-1).cuda().clone()
         opt = N.CGOptionsC(float(tol), float(inner_tol), int(max_outer), int(max_inner),
-                           int(check_every), 1 if use_graph else 0, int(window))
+                           int(check_every), 1 if use_graph else 0, int(window), int(net_every))
         res = N.CGResultC()
         torch.cuda.synchronize()
         N.check(N.lib().lentils_fcg_solve(

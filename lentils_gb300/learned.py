@@ -201,7 +201,7 @@ class UNet:
 
 
 # ------------------------------------------------------------------------------------------------
-# Training data: (residual, correction) pairs from plain Jacobi-CG trajectories
+# Training data: (residual, correction) pairs from Jacobi-CG and Jacobi flexible-CG trajectories
 # ------------------------------------------------------------------------------------------------
 def lens_draw(rng, centre=(0.0, 0.0), jitter=0.05):
     """A PEMD + external shear drawn from the sweep priors: b in [0.8, 1.6], axis ratio q in
@@ -269,6 +269,84 @@ def jacobi_cg_trajectory(inv, max_iter=8000, rtol=1e-6, check_every=50):
         if k % check_every == 0 and float(torch.linalg.vector_norm(r.double())) <= rtol * bn:
             break
     return xs[:k + 1]
+
+
+def fcg_trajectory(inv, window=8, net=None, max_iter=4000, rtol=1e-6, check_every=25):
+    """Truncated flexible CG on inv's normal equations from x = 0: the inner iteration of
+    lentils_fcg_solve without its restarts (FP32 operator and vectors, FP64 dot products). Each
+    direction p_k = d_k - sum_j (d_k . A p_j / p_j . A p_j) p_j over the last `window`
+    directions; d_k = net.precondition(r_k) where that is a descent direction (d.r > 0), else
+    the Jacobi direction dinv r_k (always, without a network). Returns the iterates xs
+    (K + 1, n), x_0 = 0, and the normalised A-directions q_k = A p_k / sqrt(p_k . A p_k)
+    (K, n): the direction taken after step k is made A-orthogonal to q_{k-m}, ..., q_{k-1},
+    m = min(k, window)."""
+    import ctypes as _ct
+    n = inv.nsrc
+    L = N.lib()
+    xs = torch.zeros((max_iter + 1, n), dtype=torch.float32, device="cuda")
+    qs = torch.zeros((max_iter, n), dtype=torch.float32, device="cuda")
+    b = inv.b.float()
+    dinv = inv.inv_diag32
+    bn = float(torch.linalg.vector_norm(inv.b))
+    sp = _ct.c_void_p(torch.cuda.current_stream().cuda_stream)
+    x = torch.zeros(n, dtype=torch.float32, device="cuda")
+    r = b.clone()
+    p = dinv * r
+    ring = []  # (p_j, A p_j, p_j . A p_j)
+    feat = features(dinv) if net is not None else None
+    k = 0
+    while k < max_iter:
+        ap = torch.empty_like(p)
+        N.check(L.lentils_normal_op_apply(inv.handle, _ptr(p), _ptr(ap), sp))
+        pap = torch.dot(p.double(), ap.double())
+        alpha = (torch.dot(p.double(), r.double()) / pap).float()
+        x.add_(alpha * p)
+        r.sub_(alpha * ap)
+        qs[k] = ap / pap.sqrt().float()
+        k += 1
+        xs[k] = x
+        ring.append((p, ap, pap))
+        if len(ring) > window:
+            ring.pop(0)
+        if k % check_every == 0 and float(torch.linalg.vector_norm(r.double())) <= rtol * bn:
+            break
+        d = dinv * r
+        if net is not None:
+            z = net.precondition(r, dinv, feat)
+            if float(torch.dot(z.double(), r.double())) > 0.0:
+                d = z
+        p = d.clone()
+        for pj, apj, papj in ring:
+            p.add_((-torch.dot(d.double(), apj.double()) / papj).float() * pj)
+    return xs[:k + 1], qs[:k]
+
+
+def window_pairs(inv, npairs, rng, window=8, net=None, max_iter=4000, tol_star=1e-9):
+    """(residual, correction, window) triples of one inversion along its flexible-CG trajectory
+    (fcg_trajectory, Jacobi or with `net`) at iterations drawn uniformly: the true FP64 residual
+    r_k = b - A x_k, the correction e_k = x* - x_k to the FP64-refined solution x*, and the
+    normalised A-directions the solver's next direction is made A-orthogonal to, zero-padded
+    to `window` rows. Returns float32 CUDA tensors (npairs, n), (npairs, n),
+    (npairs, window, n) and the trajectory length."""
+    import ctypes as _ct
+    x_star, _ = inv.solve(tol=tol_star, max_outer=60)
+    xs, qs = fcg_trajectory(inv, window=window, net=net, max_iter=max_iter)
+    K = xs.shape[0] - 1
+    idx = np.sort(rng.choice(K, size=min(npairs, K), replace=False))
+    L = N.lib()
+    sp = _ct.c_void_p(torch.cuda.current_stream().cuda_stream)
+    rs, es = [], []
+    Q = torch.zeros((idx.size, window, inv.nsrc), dtype=torch.float32, device="cuda")
+    ax = torch.empty(inv.nsrc, dtype=torch.float64, device="cuda")
+    for i, k in enumerate(idx.tolist()):
+        xk = xs[k].double()
+        N.check(L.lentils_normal_op_apply64(inv.handle, _ptr(xk), _ptr(ax), sp))
+        rs.append((inv.b - ax).float())
+        es.append((x_star - xk).float())
+        m = min(k, window)
+        if m:
+            Q[i, :m] = qs[k - m:k]
+    return torch.stack(rs), torch.stack(es), Q, K
 
 
 def trajectory_pairs(inv, npairs, rng, max_iter=8000, tol_star=1e-9):

@@ -134,21 +134,27 @@ def test_unet_precondition_form(native):
         assert _rel(z.cpu().numpy(), (gamma * u + s * out).cpu().numpy()) < 1e-5
 
 
-@pytest.mark.parametrize("with_net,window", [(False, 1), (True, 1), (False, 4), (True, 8)])
+@pytest.mark.parametrize("with_net,window,every",
+                         [(False, 1, 1), (True, 1, 1), (False, 4, 1), (True, 8, 1), (True, 8, 3)])
 @pytest.mark.parametrize("use_graph", [True, False])
-def test_flexible_cg_reaches_true_residual(native, with_net, window, use_graph):
-    """Flexible CG (Jacobi directions only, or an untrained network with the Jacobi fallback)
-    reaches a true FP64 relative residual of 1e-6, checked again with the oracle operator."""
+def test_flexible_cg_reaches_true_residual(native, with_net, window, every, use_graph):
+    """Flexible CG (Jacobi directions only, or an untrained network with the Jacobi fallback,
+    proposing every direction or every third) reaches a true FP64 relative residual of 1e-6,
+    checked again with the oracle operator."""
     import oracle as O
     from lentils_gb300 import learned
     from test_operators_gpu import _inversion, _oracle_normal
     rng = np.random.default_rng(29)
     inv, img, src, four, uvw, d = _inversion(rng, n_img=96, n_src=48, nvis=8000)
     net = learned.UNet(48, 48, max_batch=1, params=learned.init_params(3)) if with_net else None
-    x, info = inv.solve_flexible(net, tol=1e-6, use_graph=use_graph, window=window)
+    x, info = inv.solve_flexible(net, tol=1e-6, use_graph=use_graph, window=window,
+                                 net_every=every)
     assert info["converged"] == 1, info
     if not with_net:
         assert info["net_iterations"] == 0 and info["fallback"] == 0
+    elif every > 1 and not info["fallback"]:
+        # the network is offered one direction in `every` (plus the first of each inner solve)
+        assert info["net_iterations"] <= info["inner_total"] // every + 2 * info["outer"], info
     pts = inv.lens.source_points.cpu().numpy()
     A, rhs = _oracle_normal(img, src, four, uvw, pts, np.ones(uvw.shape[0]), 1e-2)
     b = rhs(d)
@@ -173,17 +179,27 @@ def test_unet_backward_external_gradient_matches_mse_path(native):
 
 def test_trained_network_gains_over_jacobi(native):
     """What the trained network (the committed weights, trained on the GPU by
-    train_preconditioner) gains over the method without it on the 128^2 source inversion:
-    on pairs from lens draws it was not trained on, its direction removes a larger share of the
-    A-norm error per line-search step than the Jacobi direction, and flexible CG with it needs
-    fewer iterations than plain Jacobi-CG to a true relative residual of 1e-6."""
+    train_preconditioner) gains over the method without it on the 128^2 source inversion,
+    used with the deployment policy stored beside it:
+    - on windowed flexible-CG pairs from lens draws it was not trained on, its direction (with
+      the Jacobi share it was trained with) removes a larger share of the A-norm error per step
+      than the Jacobi direction, after the A-orthogonalisation flexible CG applies;
+    - on the workload inversion, flexible CG with it needs at most a third of the iterations
+      of plain Jacobi-CG to a true relative residual of 1e-6;
+    - on held-out lens draws that gain does not carry over (plain Jacobi-CG is often as fast),
+      but the descent check and the stagnation fallback keep the solver within twice plain
+      Jacobi-CG's iterations."""
     from lentils_gb300 import learned, workloads
     from lentils_gb300 import train_preconditioner as T
+    from lentils_gb300.inversion import SourceInversion
     from lentils_gb300.operators import NUFFTOperator
     params, meta = T.load(T.DEFAULT_WEIGHTS)
+    pol = T.deploy_policy(meta)
+    g_train = float(meta.get("gamma", 0.0))
     vs, ims, srcs, uvw, _ = workloads.geometry()
     F = NUFFTOperator(vs, ims)
-    data = T.build_training_set(F, (vs, ims, srcs, uvw), 2, 40, 90210, log=lambda m: None)
+    data = T.build_training_set(F, (vs, ims, srcs, uvw), 2, 40, 90210, log=lambda m: None,
+                                window=pol["window"])
     net = learned.UNet(workloads.SRC, workloads.SRC, max_batch=16, params=params)
     fr_net, fr_jac = [], []
     for i in range(0, data["r"].shape[0] - 15, 16):
@@ -192,16 +208,28 @@ def test_trained_network_gains_over_jacobi(native):
         di = data["draw"][ids]
         x, f = learned.scaled_inputs(r, data["dinv"][di].view(-1, 128, 128),
                                      data["feat"][di].view(-1, 128, 128))
-        fr_net.append(T.energy_loss(data, ids, net.forward(x, f))[0])
-        fr_jac.append(T.energy_loss(data, ids, x)[0])
+        fr_net.append(T.window_energy_loss(data, ids, g_train * x + net.forward(x, f))[0])
+        fr_jac.append(T.window_energy_loss(data, ids, x)[0])
     fn, fj = float(torch.cat(fr_net).mean()), float(torch.cat(fr_jac).mean())
-    assert fn < fj - 0.05, (fn, fj)
+    assert fn < fj - 0.03, (fn, fj)
     del data
-    inv, _, _ = workloads.inversion(nufft=F)
     pnet = learned.UNet(workloads.SRC, workloads.SRC, max_batch=1, params=params)
-    pnet.set_jacobi_weight(0.3)
-    _, plain = inv.solve(tol=1e-6, inner_tol=1e-3)
-    _, lrn = inv.solve_flexible(pnet, tol=1e-6, inner_tol=1e-3, window=8)
-    assert plain["converged"] == 1 and lrn["converged"] == 1
-    assert lrn["net_iterations"] > 0
-    assert lrn["inner_total"] < plain["inner_total"], (lrn, plain)
+    pnet.set_jacobi_weight(pol["jacobi_weight"])
+    inv, _, _ = workloads.inversion(nufft=F)
+    rng = np.random.default_rng(4242)
+    problems = [inv]
+    for _ in range(2):
+        glm = learned.lens_draw(rng, centre=(0.25 * ims.dx, 0.25 * ims.dy))
+        d = workloads.simulate(F, ims, srcs, glm, learned.random_source(rng, srcs), rng)
+        problems.append(SourceInversion(vs, d, 1.0, ims, srcs, glm, workloads.Z_SRC,
+                                        workloads.LAMBDA, nufft=F))
+    for k, p in enumerate(problems):
+        _, plain = p.solve(tol=1e-6, inner_tol=1e-3)
+        _, lrn = p.solve_flexible(pnet, tol=1e-6, inner_tol=1e-3, window=pol["window"],
+                                  net_every=pol["net_every"])
+        assert plain["converged"] == 1 and lrn["converged"] == 1, (k, plain, lrn)
+        assert lrn["net_iterations"] > 0, (k, lrn)
+        if k == 0:
+            assert 3 * lrn["inner_total"] <= plain["inner_total"], (k, lrn, plain)
+        else:
+            assert lrn["inner_total"] <= 2 * plain["inner_total"] + 50, (k, lrn, plain)
