@@ -94,7 +94,7 @@ enum {
     LENTILS_ERR_NYQUIST = 2,      /* a visibility lies beyond the grid's Nyquist guard     */
     LENTILS_ERR_ALLOC = 3,        /* device or pinned-host allocation failed               */
     LENTILS_ERR_CUDA = 4,         /* a CUDA runtime / cuFFT call failed                    */
-    LENTILS_ERR_UNSUPPORTED = 5,  /* valid request this build does not implement           */
+    LENTILS_ERR_UNSUPPORTED = 5,  /* valid request the library does not implement         */
     LENTILS_ERR_TIMEOUT = 6,      /* a bounded device-side wait gave up                    */
     LENTILS_ERR_NONFINITE = 7,    /* NaN/Inf detected where the caller asked for a check   */
     LENTILS_ERR_NO_DEVICE = 8     /* no CUDA device visible                                */
@@ -535,7 +535,7 @@ int lentils_fcg_solve(lentils_normal_op *op, const double *b, double *x, const f
 /* ------------------------------------------------------------------------------------------
  * Gridding without device allocation. No counterpart in the reference: it exists for callers
  * that cannot call cudaMalloc -- code running where allocation is forbidden or impossible
- * (host callbacks and stream-ordered sections that must not synchronise, a memory budget that
+ * (host callbacks and stream-ordered sections that must not synchronise, device memory that
  * another framework's pool has already claimed, real-time pipelines that do not allocate after
  * start-up).
  *

@@ -2,7 +2,7 @@
 //
 // Who needs this: code that runs where allocating device memory is not allowed or not
 // possible -- inside a host callback or a CUDA stream-ordered section that must not
-// synchronise, under a memory budget that another framework's pool has already claimed in full,
+// synchronise, with device memory that another framework's pool has already claimed in full,
 // or in a long-running real-time pipeline that forbids allocation after start-up. Such a caller
 // owns its inputs and outputs in device memory and needs the visibilities gridded without the
 // plan object (lentils_plan_create allocates the plan arrays, its temporaries and the sort's

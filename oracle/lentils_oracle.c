@@ -2,7 +2,8 @@
  * CPU oracle: a plain-C restatement of the reference's FP64 hot path.
  *
  * TEST INFRASTRUCTURE ONLY. Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline /
- * reference arm may load this library, and only as the checker or the timed CPU baseline.
+ * reference arm may load this library, and only to compare results against or as the timed
+ * CPU baseline.
  * Nothing in lentils_gb300/ links, loads or calls it.
  *
  * Each function restates one reference routine (cited per function) with the same

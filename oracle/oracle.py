@@ -1,8 +1,8 @@
 """CPU oracle for the lensed visibility-operator chain.
 
 TEST INFRASTRUCTURE ONLY. Only ``tests/``, ``__graft_entry__.smoke()`` and ``bench.py``'s
-CPU-baseline / reference arm import this module, and only as the checker or the timed CPU
-baseline. The product package ``lentils_gb300`` never imports it.
+CPU-baseline / reference arm import this module, and only to compare results against or as the
+timed CPU baseline. The product package ``lentils_gb300`` never imports it.
 
 Two layers:
 

@@ -1,7 +1,7 @@
 """lentils_grid_noalloc: gridding for callers that cannot allocate device memory.
 
 Some callers cannot call cudaMalloc -- code running in a host callback or a stream-ordered
-section that must not synchronise, under a memory budget another framework's pool already
+section that must not synchronise, with device memory another framework's pool already
 holds, or in a real-time pipeline that does not allocate after start-up. For them
 lentils_grid_noalloc grids a bounded batch of visibilities from caller-owned device buffers
 with all working memory in a static device array. These tests call it through the C ABI and
