@@ -106,7 +106,7 @@ int lentils_last_error(void);
 const char *lentils_last_error_message(void);
 /* Library version as major*10000 + minor*100 + patch. */
 int lentils_version(void);
-/* Copy bytes from a device array to host memory (synchronous). */
+/* Copy bytes from a device array to host memory after all device work has finished. */
 int lentils_copy_to_host(void *dst, const void *src, long long bytes);
 /* Release a device array that an entry point allocated for the caller (cudaFree). */
 int lentils_device_free(void *ptr);
@@ -496,6 +496,7 @@ long long lentils_unet_param_count(void);
 int lentils_unet_create(lentils_unet **out, int H, int W, int max_batch, const float *init_params,
                         void *stream);
 int lentils_unet_destroy(lentils_unet *net);
+/* FP32 master parameters to host memory (waits for all device work first). */
 int lentils_unet_get_params(lentils_unet *net, float *host_out);
 int lentils_unet_set_params(lentils_unet *net, const float *host_in, void *stream);
 int lentils_unet_forward(lentils_unet *net, const float *r, const float *d, float *out, int B,

@@ -95,8 +95,10 @@ int lentils_dft_forward(const double *uvw, int nrows, const double *channels,
     if (!uvw || nrows < 0 || !channels || !im || !mask || !image || !vis || im->nx < 1 ||
         im->ny < 1)
         return set_error(LENTILS_ERR_INVALID, "dft_forward: bad arguments");
-    double ch = 0.0;
-    LENTILS_CUDA_TRY(cudaMemcpy(&ch, channels, sizeof(double), cudaMemcpyDeviceToHost));
+    double ch = 0.0;  // read on the caller's stream, after whatever wrote it there
+    LENTILS_CUDA_TRY(cudaMemcpyAsync(&ch, channels, sizeof(double), cudaMemcpyDeviceToHost,
+                                     (cudaStream_t)stream));
+    LENTILS_CUDA_TRY(cudaStreamSynchronize((cudaStream_t)stream));
     DftGeom g{im->nx, im->ny, im->xmin, im->ymin, im->dx, im->dy, ch};
     const int blocks = std::max(1, std::min((nrows + 127) / 128, 152 * 16));
     dft_forward_kernel<<<blocks, 128, 0, (cudaStream_t)stream>>>(uvw, nrows, g, mask, image,
@@ -113,8 +115,10 @@ int lentils_dft_adjoint(const double *uvw, int nrows, const double *channels,
     if (!uvw || nrows < 0 || !channels || !im || !mask || !image || !vis || im->nx < 1 ||
         im->ny < 1)
         return set_error(LENTILS_ERR_INVALID, "dft_adjoint: bad arguments");
-    double ch = 0.0;
-    LENTILS_CUDA_TRY(cudaMemcpy(&ch, channels, sizeof(double), cudaMemcpyDeviceToHost));
+    double ch = 0.0;  // read on the caller's stream, after whatever wrote it there
+    LENTILS_CUDA_TRY(cudaMemcpyAsync(&ch, channels, sizeof(double), cudaMemcpyDeviceToHost,
+                                     (cudaStream_t)stream));
+    LENTILS_CUDA_TRY(cudaStreamSynchronize((cudaStream_t)stream));
     DftGeom g{im->nx, im->ny, im->xmin, im->ymin, im->dx, im->dy, ch};
     const long long npix = (long long)im->nx * im->ny;
     const int blocks = (int)std::max(1LL, std::min((npix + 127) / 128, 152LL * 16));

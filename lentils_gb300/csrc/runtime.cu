@@ -172,13 +172,16 @@ int lentils_last_error(void) { return lentils::t_err; }
 const char *lentils_last_error_message(void) { return lentils::t_msg; }
 int lentils_version(void) { return 10000; }
 
-// copy `bytes` from a device array to host memory (synchronous)
+// copy `bytes` from a device array to host memory once all device work has finished (the
+// producer may have run on any stream, including a non-blocking one)
 int lentils_copy_to_host(void *dst, const void *src, long long bytes)
 {
     lentils::clear_error();
     if (bytes < 0 || (bytes > 0 && (!dst || !src)))
         return lentils::set_error(LENTILS_ERR_INVALID, "copy_to_host: bad arguments");
-    if (bytes) LENTILS_CUDA_TRY(cudaMemcpy(dst, src, (size_t)bytes, cudaMemcpyDeviceToHost));
+    if (!bytes) return LENTILS_OK;
+    LENTILS_CUDA_TRY(cudaDeviceSynchronize());
+    LENTILS_CUDA_TRY(cudaMemcpy(dst, src, (size_t)bytes, cudaMemcpyDeviceToHost));
     return LENTILS_OK;
 }
 

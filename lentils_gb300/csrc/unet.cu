@@ -981,6 +981,8 @@ int lentils_unet_get_params(lentils_unet *net, float *host_out)
 {
     clear_error();
     if (!net || !host_out) return set_error(LENTILS_ERR_INVALID, "unet_get_params: null");
+    // training steps may still be running on the caller's stream, whatever its flags
+    LENTILS_CUDA_TRY(cudaDeviceSynchronize());
     LENTILS_CUDA_TRY(cudaMemcpy(host_out, net->params, sizeof(float) * net->nparams, cudaMemcpyDeviceToHost));
     return LENTILS_OK;
 }
@@ -1080,6 +1082,7 @@ int lentils_unet_error_flag(lentils_unet *net, int *flag)
 {
     clear_error();
     if (!net || !flag) return set_error(LENTILS_ERR_INVALID, "unet_error_flag: null");
+    LENTILS_CUDA_TRY(cudaDeviceSynchronize());  // after every launch already issued
     LENTILS_CUDA_TRY(cudaMemcpy(flag, net->err, sizeof(int), cudaMemcpyDeviceToHost));
     return LENTILS_OK;
 }
