@@ -196,9 +196,12 @@ int lentils_plan_create(lentils_plan **plan, const lentils_grid_desc *grid, cons
 int lentils_plan_destroy(lentils_plan *plan);
 int lentils_plan_get_stats(const lentils_plan *plan, lentils_plan_stats *stats);
 /* Tuning: the gridding kernel's work split. 0 (default): lanes own window rows, 32/(2w)
- * visibilities side by side per warp, warp-private tiles; 1: lanes own taps, one visibility
- * per warp; 2: two visibilities per warp; 3: as 0 with one tile per CTA flushed by
- * shared-memory atomics. All give the same result up to FP32 summation order. */
+ * visibilities side by side per warp, warp-private tiles, the cell changes of each batch found
+ * once per batch (bit masks) and flush turns only for the groups that flush; 1: lanes own
+ * taps, one visibility per warp; 2: two visibilities per warp; 3: as 0 with one tile per CTA
+ * flushed by shared-memory atomics and cell changes checked at every step; 4: as 0 with cell
+ * changes checked at every step and flush turns for every group. All give the same result up
+ * to FP32 summation order. */
 int lentils_plan_set_grid_variant(lentils_plan *plan, int variant);
 
 /* Degrid: half-plane grid (c64, device) -> visibilities (c64, device, plan order, plan frame).

@@ -231,14 +231,14 @@ static int launch_degrid_t(const lentils_plan *p, const typename Prec<R>::C *gri
     return LENTILS_OK;
 }
 
-template <int W2, bool SHARED>
+template <int W2, bool SHARED, bool MASKED = false>
 __global__ void __launch_bounds__(kGridBatch)
     grid_rows_kernel(const float2 *__restrict__ vis, const uint2 *__restrict__ coords,
                      float2 *__restrict__ grid, const WorkItem *__restrict__ items,
                      const __grid_constant__ KBPoly kb, const GridGeom g)
 {
     extern __shared__ __align__(16) unsigned char smraw[];
-    grid_rows_item<W2, SHARED>(vis, coords, grid, items[blockIdx.x], kb, g, smraw);
+    grid_rows_item<W2, SHARED, MASKED>(vis, coords, grid, items[blockIdx.x], kb, g, smraw);
 }
 
 constexpr size_t kMaxGridSmem = 200 * 1024;
@@ -279,7 +279,7 @@ static int launch_grid_t(const lentils_plan *p, const typename Prec<R>::C *vis,
                          typename Prec<R>::C *grid, cudaStream_t s)
 {
     if constexpr (std::is_same<R, float>::value && (W2 % 2) == 0) {
-        if (p->grid_variant == 0 || p->grid_variant == 3) {
+        if (p->grid_variant == 0 || p->grid_variant == 3 || p->grid_variant == 4) {
             const GridGeom &g = p->geom;
             if (p->grid_variant == 3) {
                 const size_t smem = grid_rows_smem_bytes<W2, true>(g);
@@ -290,6 +290,13 @@ static int launch_grid_t(const lentils_plan *p, const typename Prec<R>::C *vis,
                 return LENTILS_OK;
             }
             const size_t smem = grid_rows_smem_bytes<W2, false>(g);
+            if (smem <= kMaxGridSmem && p->grid_variant == 0) {
+                if (int st = set_smem(grid_rows_kernel<W2, false, true>, smem)) return st;
+                grid_rows_kernel<W2, false, true><<<p->nitems, kGridBatch, smem, s>>>(
+                    vis, p->coords, grid, p->items, p->kb, g);
+                LENTILS_CHECK_LAUNCH("grid_rows_kernel");
+                return LENTILS_OK;
+            }
             if (smem <= kMaxGridSmem) {
                 if (int st = set_smem(grid_rows_kernel<W2, false>, smem)) return st;
                 grid_rows_kernel<W2, false><<<p->nitems, kGridBatch, smem, s>>>(

@@ -226,6 +226,7 @@ __device__ __forceinline__ void grid_flush_extended(const typename Prec<R>::C *s
 }
 
 constexpr int kGridBatch = 256;  // visibilities per weight batch (= threads per CTA)
+constexpr int kRowSkew = 8;      // floats between consecutive groups' weight rows
 
 // Row-owner gridding (the default for float). The work item's sorted visibilities are split
 // into NG = 8 warps x G contiguous ranges, one per group of 2w lanes (G = 32/(2w) groups per
@@ -241,8 +242,13 @@ constexpr int kGridBatch = 256;  // visibilities per weight batch (= threads per
 // shared-memory float atomics (collisions only where two groups' windows overlap), which
 // removes the turn-taking and the final summation of copies and needs an eighth of the tile
 // memory.
+// MASKED = true (warp-private tiles): each group reads its SHARE keys once per batch and marks
+// the steps where its cell changes in a bit mask; one warp OR of the masks gives the steps at
+// which any group flushes, so the fully unrolled step loop is plain loads and FMAs except at
+// those steps, and a flush takes turns only among the groups that need one (ballot), not all
+// G groups.
 // One work item by a CTA of kGridBatch threads; smraw: grid_rows_smem_bytes<W2, SHARED>(g).
-template <int W2, bool SHARED = false>
+template <int W2, bool SHARED = false, bool MASKED = false>
 __device__ __forceinline__ void grid_rows_item(const float2 *__restrict__ vis,
                                                const uint2 *__restrict__ coords,
                                                float2 *__restrict__ grid, const WorkItem &it,
@@ -259,7 +265,10 @@ __device__ __forceinline__ void grid_rows_item(const float2 *__restrict__ vis,
     const int E = g.E, S = g.stride;
     float2 *tiles = reinterpret_cast<float2 *>(smraw);  // NT x (E x S)
     const size_t tile_bytes = ((sizeof(float2) * (size_t)NT * E * S) + 15) & ~size_t(15);
-    float *rows = reinterpret_cast<float *>(smraw + tile_bytes);  // NG*SHARE x STR
+    // NG*SHARE rows of STR floats; group g's SHARE rows start kRowSkew*g floats later, so the
+    // G groups of a warp, which read their rows in the same instruction, hit different banks
+    // (SHARE*STR is a multiple of 32 words for W2 = 6 and 8)
+    float *rows = reinterpret_cast<float *>(smraw + tile_bytes);
     for (int e = threadIdx.x; e < NT * E * S; e += blockDim.x) tiles[e] = make_float2(0.f, 0.f);
 
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -278,6 +287,37 @@ __device__ __forceinline__ void grid_rows_item(const float2 *__restrict__ vis,
     for (int j = 0; j < W2; ++j) acc[j] = make_float2(0.f, 0.f);
     int cur = -1;
     const int nbatch = (L + SHARE - 1) / SHARE;
+    // add the accumulated taps of cell `cur` to this lane's window row of the warp's tile
+    auto flush_rows = [&]() {
+        float2 *p = mytile + ((cur >> 6) + 1 + ri) * S + (cur & 63) + 1;
+#pragma unroll
+        for (int j = 0; j < W2; ++j) {
+            float2 v = p[j];
+            v.x += acc[j].x;
+            v.y += acc[j].y;
+            p[j] = v;
+            acc[j] = make_float2(0.f, 0.f);
+        }
+    };
+    // accumulate one visibility row [wv | wu | x, key] into this lane's window row
+    auto consume = [&](const float *row) {
+        const float4 xk = reinterpret_cast<const float4 *>(row + 2 * W2)[0];
+        const float wui = row[W2 + ri];
+        const float2 t = make_float2(wui * xk.x, wui * xk.y);
+        float wv[W2];
+#pragma unroll
+        for (int q = 0; q < W2 / 4; ++q) {
+            const float4 v4 = reinterpret_cast<const float4 *>(row)[q];
+            wv[4 * q] = v4.x;
+            wv[4 * q + 1] = v4.y;
+            wv[4 * q + 2] = v4.z;
+            wv[4 * q + 3] = v4.w;
+        }
+#pragma unroll
+        for (int j = (W2 / 4) * 4; j < W2; ++j) wv[j] = row[j];
+#pragma unroll
+        for (int j = 0; j < W2; ++j) acc[j] = __ffma2_rn(f2(wv[j]), t, acc[j]);
+    };
     for (int b = 0; b <= nbatch; ++b) {
         __syncthreads();  // tiles zeroed / previous batch consumed
         if (b < nbatch && pg < NG) {
@@ -291,7 +331,7 @@ __device__ __forceinline__ void grid_rows_item(const float2 *__restrict__ vis,
                 float2 x = vis[it.begin + kv];
                 const float h = tap_parity(it, g, lu, lv) ? -0.5f : 0.5f;
                 x = make_float2(h * x.x, h * x.y);
-                float *row = rows + threadIdx.x * STR;
+                float *row = rows + threadIdx.x * STR + pg * kRowSkew;
                 float4 *row4 = reinterpret_cast<float4 *>(row);
 #pragma unroll
                 for (int q = 0; q < W2 / 4; ++q)
@@ -310,12 +350,44 @@ __device__ __forceinline__ void grid_rows_item(const float2 *__restrict__ vis,
         __syncthreads();
         // consume this batch's rows of my range; after the last batch flush what is left
         const int kfirst = rbeg + b * SHARE;
+        if constexpr (MASKED && !SHARED) {
+            const int nval = (lane_on && b < nbatch) ? max(0, min(SHARE, rend - kfirst)) : 0;
+            const float *rowg = rows + gid * (SHARE * STR + kRowSkew);
+            int keys[SHARE];
+            unsigned bm = 0;  // bit s: flush `cur` before consuming step s
+            int prev = cur;
+#pragma unroll
+            for (int st = 0; st < SHARE; ++st) {
+                keys[st] = (st < nval) ? __float_as_int(rowg[st * STR + 2 * W2 + 2]) : prev;
+                if (st < nval && prev >= 0 && keys[st] != prev) bm |= 1u << st;
+                prev = keys[st];
+            }
+            if (b == nbatch && lane_on && cur >= 0) bm = 1u;  // what is left after the last batch
+            const unsigned wm = __reduce_or_sync(0xffffffffu, bm);
+#pragma unroll
+            for (int st = 0; st < SHARE; ++st) {
+                if (wm & (1u << st)) {  // warp-uniform
+                    const bool need = (bm >> st) & 1u;
+                    unsigned gm = __ballot_sync(0xffffffffu, need);
+                    while (gm) {  // groups that flush here, one at a time
+                        const int g0 = (__ffs(gm) - 1) / W2;
+                        if (need && grp == g0) flush_rows();
+                        __syncwarp();
+                        gm &= ~(((1u << W2) - 1u) << (g0 * W2));
+                    }
+                }
+                if (st < nval) {
+                    cur = keys[st];
+                    consume(rowg + st * STR);
+                }
+            }
+        } else {
         for (int step = 0; step < SHARE; ++step) {
             const int k = kfirst + step;
             const bool valid = lane_on && b < nbatch && k < rend;
             float4 xk = make_float4(0.f, 0.f, 0.f, 0.f);
             int key = cur;
-            const float *row = rows + (gid * SHARE + step) * STR;
+            const float *row = rows + (gid * SHARE + step) * STR + gid * kRowSkew;
             if (valid) {
                 xk = reinterpret_cast<const float4 *>(row + 2 * W2)[0];
                 key = __float_as_int(xk.z);
@@ -334,38 +406,15 @@ __device__ __forceinline__ void grid_rows_item(const float2 *__restrict__ vis,
                 }
             } else if (__any_sync(0xffffffffu, need)) {
                 for (int hgrp = 0; hgrp < G; ++hgrp) {
-                    if (need && grp == hgrp) {
-                        float2 *p = mytile + ((cur >> 6) + 1 + ri) * S + (cur & 63) + 1;
-#pragma unroll
-                        for (int j = 0; j < W2; ++j) {
-                            float2 v = p[j];
-                            v.x += acc[j].x;
-                            v.y += acc[j].y;
-                            p[j] = v;
-                            acc[j] = make_float2(0.f, 0.f);
-                        }
-                    }
+                    if (need && grp == hgrp) flush_rows();
                     __syncwarp();
                 }
                 if (need) cur = -1;
             }
             if (!valid) continue;
             cur = key;
-            const float wui = row[W2 + ri];
-            const float2 t = make_float2(wui * xk.x, wui * xk.y);
-            float wv[W2];
-#pragma unroll
-            for (int q = 0; q < W2 / 4; ++q) {
-                const float4 v4 = reinterpret_cast<const float4 *>(row)[q];
-                wv[4 * q] = v4.x;
-                wv[4 * q + 1] = v4.y;
-                wv[4 * q + 2] = v4.z;
-                wv[4 * q + 3] = v4.w;
-            }
-#pragma unroll
-            for (int j = (W2 / 4) * 4; j < W2; ++j) wv[j] = row[j];
-#pragma unroll
-            for (int j = 0; j < W2; ++j) acc[j] = __ffma2_rn(f2(wv[j]), t, acc[j]);
+            consume(row);
+        }
         }
     }
     __syncthreads();
@@ -390,7 +439,8 @@ __host__ __device__ inline size_t grid_rows_smem_bytes(const GridGeom &g)
 {
     const size_t ntile = SHARED ? 1 : kGridBatch / 32;
     const size_t tile_bytes = ((sizeof(float2) * ntile * g.E * g.stride) + 15) & ~size_t(15);
-    return tile_bytes + sizeof(float) * (size_t)kGridBatch * (2 * W2 + 4);
+    const size_t ngroups = (kGridBatch / 32) * (32 / W2);
+    return tile_bytes + sizeof(float) * ((size_t)kGridBatch * (2 * W2 + 4) + ngroups * kRowSkew);
 }
 
 template <typename R>

@@ -633,8 +633,8 @@ int lentils_plan_destroy(lentils_plan *p)
 int lentils_plan_set_grid_variant(lentils_plan *p, int variant)
 {
     clear_error();
-    if (!p || variant < 0 || variant > 3)
-        return set_error(LENTILS_ERR_INVALID, "plan_set_grid_variant: variant 0, 1, 2 or 3");
+    if (!p || variant < 0 || variant > 4)
+        return set_error(LENTILS_ERR_INVALID, "plan_set_grid_variant: variant 0 to 4");
     p->grid_variant = variant;
     return LENTILS_OK;
 }

@@ -84,7 +84,7 @@ class GriddingPlan:
         return self._handle
 
     def set_grid_variant(self, variant):
-        """Visibilities per warp iteration in the gridding kernel (1 or 2); tuning only."""
+        """Work split of the gridding kernel (lentils_plan_set_grid_variant, 0-4); tuning only."""
         N.check(N.lib().lentils_plan_set_grid_variant(self._handle, int(variant)))
 
     @property

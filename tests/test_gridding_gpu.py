@@ -37,7 +37,7 @@ def gpu_grid(plan, vis_c128):
 
 @pytest.mark.parametrize("name", ["nufft_cfg0_w3", "nufft_odd_w4", "nufft_tiny_w1"])
 @pytest.mark.parametrize("tile,variant", [(0, 0), (8, 0), (64, 0), (0, 1), (32, 1), (0, 2),
-                                          (16, 2), (0, 3), (32, 3)])
+                                          (16, 2), (0, 3), (32, 3), (0, 4), (8, 4), (64, 4)])
 def test_plan_api_vs_golden(native, name, tile, variant):
     d, vis, four = load_nufft_golden(name)
     w, beta = int(d["wsup"]), float(d["beta"])
@@ -117,7 +117,7 @@ def test_heavy_bins_and_seams(native):
     seams[:, 0] = (rng.integers(-4, 4, 3000) * 16 + rng.uniform(-0.5, 0.5, 3000)) * four.du
     seams[:, 1] = (rng.uniform(-1.0, 1.0, 3000) * 4) * four.dv
     for uvw, variant in ((one_cell, 0), (seams, 0), (one_cell, 1), (seams, 1), (one_cell, 2),
-                         (seams, 2), (one_cell, 3), (seams, 3)):
+                         (seams, 2), (one_cell, 3), (seams, 3), (one_cell, 4), (seams, 4)):
         vis = O.VisGeom(uvw, [1.0])
         plan = make_plan(vis, four, w, beta, tile=16, chunk=512)
         plan.set_grid_variant(variant)
