@@ -318,17 +318,29 @@ __device__ __forceinline__ void grid_rows_item(const float2 *__restrict__ vis,
 #pragma unroll
         for (int j = 0; j < W2; ++j) acc[j] = __ffma2_rn(f2(wv[j]), t, acc[j]);
     };
+    // the producer's inputs for batch b + 1 are loaded while batch b is evaluated and consumed
+    uint2 cpre = make_uint2(0u, 0u);
+    float2 xpre = make_float2(0.f, 0.f);
+    auto prefetch = [&](int bb) {
+        const int kv = pbeg + bb * SHARE + pj;
+        if (bb < nbatch && pg < NG && kv < pend) {
+            cpre = coords[it.begin + kv];
+            xpre = vis[it.begin + kv];
+        }
+    };
+    prefetch(0);
     for (int b = 0; b <= nbatch; ++b) {
         __syncthreads();  // tiles zeroed / previous batch consumed
         if (b < nbatch && pg < NG) {
             const int kv = pbeg + b * SHARE + pj;
             if (kv < pend) {
-                const uint2 c = coords[it.begin + kv];
+                const uint2 c = cpre;
+                float2 x = xpre;
+                prefetch(b + 1);
                 const int lu = cell_of(c.x), lv = cell_of(c.y);
                 float wu[W2], wv[W2];
                 kb_weights<W2>(kb, c.x, wu);
                 kb_weights<W2>(kb, c.y, wv);
-                float2 x = vis[it.begin + kv];
                 const float h = tap_parity(it, g, lu, lv) ? -0.5f : 0.5f;
                 x = make_float2(h * x.x, h * x.y);
                 float *row = rows + threadIdx.x * STR + pg * kRowSkew;
