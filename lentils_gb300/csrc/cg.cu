@@ -28,6 +28,10 @@
 #include "unet.cuh"
 
 namespace lentils {
+int nufft_forward_scaled(lentils_nufft *op, const float *image, float *vis_plan,
+                         const float *vscale, void *stream);
+int nufft_forward_scaled64(lentils_nufft *op, const double *image, double *vis_plan,
+                           const double *vscale, void *stream);
 int bcb_apply32(lentils_bcb *op, const float *x, float *out, cudaStream_t s);
 int bcb_apply64(lentils_bcb *op, const double *x, double *out, cudaStream_t s);
 double bcb_centre(const lentils_bcb *op);
@@ -663,9 +667,9 @@ int lentils_normal_op_apply(lentils_normal_op *op, const float *s_in, float *out
     if (op->bcb) {
         if ((st = bcb_apply32(op->bcb, op->img32a, op->img32b, s))) return st;
     } else {
-        if ((st = lentils_nufft_forward(op->F, op->img32a, (float *)op->vis32, stream))) return st;
-        scale_vis_kernel<float2, float><<<nb(op->nvis), 256, 0, s>>>(op->vis32, op->w32, op->nvis);
-        LENTILS_CHECK_LAUNCH("scale_vis_kernel");
+        // C^-1 F L s, the data weights applied by the degridding kernel
+        if ((st = nufft_forward_scaled(op->F, op->img32a, (float *)op->vis32, op->w32, stream)))
+            return st;
         if ((st = lentils_nufft_adjoint(op->F, (const float *)op->vis32, op->img32b, stream)))
             return st;
     }
@@ -687,11 +691,9 @@ int lentils_normal_op_apply64(lentils_normal_op *op, const double *s_in, double 
     if (op->bcb) {
         if ((st = bcb_apply64(op->bcb, op->img64a, op->img64b, s))) return st;
     } else {
-        if ((st = lentils_nufft_forward64(op->F, op->img64a, (double *)op->vis64, stream)))
+        if ((st = nufft_forward_scaled64(op->F, op->img64a, (double *)op->vis64, op->w64,
+                                         stream)))
             return st;
-        scale_vis_kernel<double2, double><<<nb(op->nvis), 256, 0, s>>>(op->vis64, op->w64,
-                                                                        op->nvis);
-        LENTILS_CHECK_LAUNCH("scale_vis_kernel");
         if ((st = lentils_nufft_adjoint64(op->F, (const double *)op->vis64, op->img64b, stream)))
             return st;
     }

@@ -36,10 +36,10 @@ __global__ void __launch_bounds__(256)
     degrid_kernel(const typename Prec<R>::C *__restrict__ grid, const uint2 *__restrict__ coords,
                   typename Prec<R>::C *__restrict__ out, const WorkItem *__restrict__ items,
                   const __grid_constant__ typename Prec<R>::Table kb, const GridGeom g,
-                  const float2 *__restrict__ cres)
+                  const float2 *__restrict__ cres, const R *__restrict__ vscale)
 {
     extern __shared__ __align__(16) unsigned char smraw[];
-    degrid_item<W2, R>(grid, coords, out, items[blockIdx.x], kb, g, cres, smraw);
+    degrid_item<W2, R>(grid, coords, out, items[blockIdx.x], kb, g, cres, smraw, vscale);
 }
 
 
@@ -219,14 +219,14 @@ const KBPoly64 &table_of<double>(const lentils_plan *p) { return p->kb64; }
 
 template <int W2, typename R>
 static int launch_degrid_t(const lentils_plan *p, const typename Prec<R>::C *grid,
-                           typename Prec<R>::C *vis, cudaStream_t s)
+                           typename Prec<R>::C *vis, cudaStream_t s, const R *vscale)
 {
     const GridGeom &g = p->geom;
     const size_t smem = sizeof(typename Prec<R>::C) * (size_t)g.E * g.stride;
     if (int st = set_smem(degrid_kernel<W2, R>, smem)) return st;
     const float2 *cres = std::is_same<R, double>::value ? p->coords_res : nullptr;
     degrid_kernel<W2, R><<<p->nitems, 256, smem, s>>>(grid, p->coords, vis, p->items,
-                                                     table_of<R>(p), g, cres);
+                                                     table_of<R>(p), g, cres, vscale);
     LENTILS_CHECK_LAUNCH("degrid_kernel");
     return LENTILS_OK;
 }
@@ -312,18 +312,18 @@ static int launch_grid_t(const lentils_plan *p, const typename Prec<R>::C *vis,
 
 template <typename R>
 static int launch_degrid_r(const lentils_plan *p, const typename Prec<R>::C *grid,
-                           typename Prec<R>::C *vis, cudaStream_t s)
+                           typename Prec<R>::C *vis, cudaStream_t s, const R *vscale)
 {
     if (p->nitems == 0) return LENTILS_OK;
     switch (p->geom.w) {
-    case 1: return launch_degrid_t<2, R>(p, grid, vis, s);
-    case 2: return launch_degrid_t<4, R>(p, grid, vis, s);
-    case 3: return launch_degrid_t<6, R>(p, grid, vis, s);
-    case 4: return launch_degrid_t<8, R>(p, grid, vis, s);
-    case 5: return launch_degrid_t<10, R>(p, grid, vis, s);
-    case 6: return launch_degrid_t<12, R>(p, grid, vis, s);
-    case 7: return launch_degrid_t<14, R>(p, grid, vis, s);
-    case 8: return launch_degrid_t<16, R>(p, grid, vis, s);
+    case 1: return launch_degrid_t<2, R>(p, grid, vis, s, vscale);
+    case 2: return launch_degrid_t<4, R>(p, grid, vis, s, vscale);
+    case 3: return launch_degrid_t<6, R>(p, grid, vis, s, vscale);
+    case 4: return launch_degrid_t<8, R>(p, grid, vis, s, vscale);
+    case 5: return launch_degrid_t<10, R>(p, grid, vis, s, vscale);
+    case 6: return launch_degrid_t<12, R>(p, grid, vis, s, vscale);
+    case 7: return launch_degrid_t<14, R>(p, grid, vis, s, vscale);
+    case 8: return launch_degrid_t<16, R>(p, grid, vis, s, vscale);
     }
     return set_error(LENTILS_ERR_UNSUPPORTED, "degrid: w=%d", p->geom.w);
 }
@@ -346,9 +346,10 @@ static int launch_grid_r(const lentils_plan *p, const typename Prec<R>::C *vis,
     return set_error(LENTILS_ERR_UNSUPPORTED, "grid: w=%d", p->geom.w);
 }
 
-int launch_degrid(const lentils_plan *p, const float2 *grid, float2 *vis, cudaStream_t s)
+int launch_degrid(const lentils_plan *p, const float2 *grid, float2 *vis, cudaStream_t s,
+                  const float *vscale)
 {
-    return launch_degrid_r<float>(p, grid, vis, s);
+    return launch_degrid_r<float>(p, grid, vis, s, vscale);
 }
 
 int launch_grid(const lentils_plan *p, const float2 *vis, float2 *grid, cudaStream_t s)
@@ -356,9 +357,10 @@ int launch_grid(const lentils_plan *p, const float2 *vis, float2 *grid, cudaStre
     return launch_grid_r<float>(p, vis, grid, s);
 }
 
-int launch_degrid64(const lentils_plan *p, const double2 *grid, double2 *vis, cudaStream_t s)
+int launch_degrid64(const lentils_plan *p, const double2 *grid, double2 *vis, cudaStream_t s,
+                    const double *vscale)
 {
-    return launch_degrid_r<double>(p, grid, vis, s);
+    return launch_degrid_r<double>(p, grid, vis, s, vscale);
 }
 
 int launch_grid64(const lentils_plan *p, const double2 *vis, double2 *grid, cudaStream_t s)

@@ -100,6 +100,8 @@ __device__ __forceinline__ int tap_parity(const WorkItem &it, const GridGeom &g,
 }
 
 // Degridding of one work item by the whole CTA (any block size); smraw: E x stride cells.
+// vscale (optional, plan order): each output is multiplied by its factor (the data weights of
+// a normal operator, applied here instead of in a separate pass).
 template <int W2, typename R>
 __device__ __forceinline__ void degrid_item(const typename Prec<R>::C *__restrict__ grid,
                                             const uint2 *__restrict__ coords,
@@ -107,7 +109,8 @@ __device__ __forceinline__ void degrid_item(const typename Prec<R>::C *__restric
                                             const WorkItem &it,
                                             const typename Prec<R>::Table &kb, const GridGeom &g,
                                             const float2 *__restrict__ cres,
-                                            unsigned char *smraw)
+                                            unsigned char *smraw,
+                                            const R *__restrict__ vscale = nullptr)
 {
     using P = Prec<R>;
     using C = typename P::C;
@@ -165,6 +168,11 @@ __device__ __forceinline__ void degrid_item(const typename Prec<R>::C *__restric
         if (tap_parity(it, g, lu, lv)) {
             acc.x = -acc.x;
             acc.y = -acc.y;
+        }
+        if (vscale) {
+            const R sc = vscale[it.begin + k];
+            acc.x *= sc;
+            acc.y *= sc;
         }
         out[it.begin + k] = acc;
     }

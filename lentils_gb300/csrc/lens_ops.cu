@@ -165,16 +165,24 @@ __global__ void csr_transpose_fill_kernel(const int *__restrict__ ids, const int
     }
 }
 
+// src = L^T img from the transposed CSR: one warp per source node. Row lengths are very uneven
+// (no image pixel maps to most of the outer source grid; hundreds do near the critical curves),
+// so the lanes stride a row's entries (coalesced loads) and combine with shuffles.
 template <typename R>
 __global__ void lens_apply_t_kernel(const int *__restrict__ ptr, const int *__restrict__ row,
                                     const R *__restrict__ val, const R *__restrict__ img,
                                     R *__restrict__ src, int nsrc)
 {
-    for (long long j = blockIdx.x * (long long)blockDim.x + threadIdx.x; j < nsrc;
-         j += (long long)gridDim.x * blockDim.x) {
+    const int lane = threadIdx.x & 31;
+    const long long nwarps = ((long long)gridDim.x * blockDim.x) >> 5;
+    for (long long j = (blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5; j < nsrc;
+         j += nwarps) {
         R acc = (R)0;
-        for (int e = ptr[j]; e < ptr[j + 1]; ++e) acc += val[e] * img[row[e]];
-        src[j] = acc;
+        const int e1 = ptr[j + 1];
+        for (int e = ptr[j] + lane; e < e1; e += 32) acc += val[e] * img[row[e]];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+        if (lane == 0) src[j] = acc;
     }
 }
 
@@ -411,7 +419,7 @@ int lentils_lensop_apply_t(const lentils_lensop *op, const float *img, float *sr
 {
     clear_error();
     if (!op || !src || !img) return set_error(LENTILS_ERR_INVALID, "lensop_apply_t: null argument");
-    lens_apply_t_kernel<float><<<blocks_for(op->nsrc), 256, 0, (cudaStream_t)stream>>>(
+    lens_apply_t_kernel<float><<<blocks_for(32LL * op->nsrc), 256, 0, (cudaStream_t)stream>>>(
         op->t_ptr, op->t_row, op->t_val32, img, src, op->nsrc);
     LENTILS_CHECK_LAUNCH("lens_apply_t_kernel");
     return LENTILS_OK;
@@ -437,7 +445,7 @@ int lentils_lensop_apply_t64(const lentils_lensop *op, const double *img, double
     clear_error();
     if (!op || !src || !img)
         return set_error(LENTILS_ERR_INVALID, "lensop_apply_t64: null argument");
-    lens_apply_t_kernel<double><<<blocks_for(op->nsrc), 256, 0, (cudaStream_t)stream>>>(
+    lens_apply_t_kernel<double><<<blocks_for(32LL * op->nsrc), 256, 0, (cudaStream_t)stream>>>(
         op->t_ptr, op->t_row, op->t_val64, img, src, op->nsrc);
     LENTILS_CHECK_LAUNCH("lens_apply_t_kernel");
     return LENTILS_OK;

@@ -39,9 +39,15 @@ struct lentils_nufft {
 
 namespace lentils {
 
-int launch_degrid(const lentils_plan *p, const float2 *grid, float2 *vis, cudaStream_t s);
+int launch_degrid(const lentils_plan *p, const float2 *grid, float2 *vis, cudaStream_t s,
+                  const float *vscale = nullptr);
 int launch_grid(const lentils_plan *p, const float2 *vis, float2 *grid, cudaStream_t s);
-int launch_degrid64(const lentils_plan *p, const double2 *grid, double2 *vis, cudaStream_t s);
+int launch_degrid64(const lentils_plan *p, const double2 *grid, double2 *vis, cudaStream_t s,
+                    const double *vscale = nullptr);
+int nufft_forward_scaled(lentils_nufft *op, const float *image, float *vis_plan,
+                         const float *vscale, void *stream);
+int nufft_forward_scaled64(lentils_nufft *op, const double *image, double *vis_plan,
+                           const double *vscale, void *stream);
 int launch_grid64(const lentils_plan *p, const double2 *vis, double2 *grid, cudaStream_t s);
 
 static int cufft_status(cufftResult r, const char *what)
@@ -255,6 +261,24 @@ int lentils_nufft_destroy(lentils_nufft *op)
 
 int lentils_nufft_forward(lentils_nufft *op, const float *image, float *vis_plan, void *stream)
 {
+    return lentils::nufft_forward_scaled(op, image, vis_plan, nullptr, stream);
+}
+
+int lentils_nufft_forward64(lentils_nufft *op, const double *image, double *vis_plan,
+                            void *stream)
+{
+    return lentils::nufft_forward_scaled64(op, image, vis_plan, nullptr, stream);
+}
+
+}  // extern "C"
+
+namespace lentils {
+
+// The forward operator with each visibility multiplied by vscale (plan order; null: none),
+// folded into the degridding kernel's output.
+int nufft_forward_scaled(lentils_nufft *op, const float *image, float *vis_plan,
+                         const float *vscale, void *stream)
+{
     clear_error();
     if (!op || !op->have32 || !image || !vis_plan)
         return set_error(LENTILS_ERR_INVALID, "nufft_forward: bad arguments (FP32 not created?)");
@@ -264,8 +288,27 @@ int lentils_nufft_forward(lentils_nufft *op, const float *image, float *vis_plan
     LENTILS_CHECK_LAUNCH("apod_pad_kernel");
     LENTILS_CUFFT_TRY(cufftSetStream(op->r2c32, s));
     LENTILS_CUFFT_TRY(cufftExecR2C(op->r2c32, op->pad32, (cufftComplex *)op->grid32));
-    return launch_degrid(op->plan, op->grid32, (float2 *)vis_plan, s);
+    return launch_degrid(op->plan, op->grid32, (float2 *)vis_plan, s, vscale);
 }
+
+int nufft_forward_scaled64(lentils_nufft *op, const double *image, double *vis_plan,
+                           const double *vscale, void *stream)
+{
+    clear_error();
+    if (!op || !op->have64 || !image || !vis_plan)
+        return set_error(LENTILS_ERR_INVALID, "nufft_forward64: bad arguments (FP64 not created?)");
+    cudaStream_t s = (cudaStream_t)stream;
+    apod_pad_kernel<double><<<nblocks((long long)op->nu * op->nv), 256, 0, s>>>(
+        image, op->pad64, op->apx64, op->apy64, op->nx, op->ny, op->padx, op->pady, op->nu, op->nv);
+    LENTILS_CHECK_LAUNCH("apod_pad_kernel");
+    LENTILS_CUFFT_TRY(cufftSetStream(op->d2z64, s));
+    LENTILS_CUFFT_TRY(cufftExecD2Z(op->d2z64, op->pad64, (cufftDoubleComplex *)op->grid64));
+    return launch_degrid64(op->plan, op->grid64, (double2 *)vis_plan, s, vscale);
+}
+
+}  // namespace lentils
+
+extern "C" {
 
 int lentils_nufft_adjoint(lentils_nufft *op, const float *vis_plan, float *image, void *stream)
 {
@@ -286,21 +329,6 @@ int lentils_nufft_adjoint(lentils_nufft *op, const float *vis_plan, float *image
         op->pad32, image, op->apx32, op->apy32, op->nx, op->ny, op->padx, op->pady, op->nv);
     LENTILS_CHECK_LAUNCH("crop_apod_kernel");
     return LENTILS_OK;
-}
-
-int lentils_nufft_forward64(lentils_nufft *op, const double *image, double *vis_plan,
-                            void *stream)
-{
-    clear_error();
-    if (!op || !op->have64 || !image || !vis_plan)
-        return set_error(LENTILS_ERR_INVALID, "nufft_forward64: bad arguments (FP64 not created?)");
-    cudaStream_t s = (cudaStream_t)stream;
-    apod_pad_kernel<double><<<nblocks((long long)op->nu * op->nv), 256, 0, s>>>(
-        image, op->pad64, op->apx64, op->apy64, op->nx, op->ny, op->padx, op->pady, op->nu, op->nv);
-    LENTILS_CHECK_LAUNCH("apod_pad_kernel");
-    LENTILS_CUFFT_TRY(cufftSetStream(op->d2z64, s));
-    LENTILS_CUFFT_TRY(cufftExecD2Z(op->d2z64, op->pad64, (cufftDoubleComplex *)op->grid64));
-    return launch_degrid64(op->plan, op->grid64, (double2 *)vis_plan, s);
 }
 
 int lentils_nufft_adjoint64(lentils_nufft *op, const double *vis_plan, double *image,

@@ -332,7 +332,8 @@ int launch_to_plan_c64(const int *perm, const float2 *phase, const float2 *vu, f
 }
 
 // defined in gridding.cu
-int launch_degrid(const lentils_plan *p, const float2 *grid, float2 *vis, cudaStream_t s);
+int launch_degrid(const lentils_plan *p, const float2 *grid, float2 *vis, cudaStream_t s,
+                  const float *vscale = nullptr);
 int launch_grid(const lentils_plan *p, const float2 *vis, float2 *grid, cudaStream_t s);
 
 static int ilog2_exact(int v)
