@@ -449,6 +449,7 @@ def run_cg_bench(repeats=3):
         N.check(L.lentils_unet_precondition(net.handle, _ptr(s32), _ptr(dinv), _ptr(feat),
                                             _ptr(o32), sp))
     ev[4].record(inv.stream)
+    torch.cuda.synchronize()  # the dirty-beam timing below must not overlap the work above
     spb = ctypes.c_void_p(inv_b.stream.cuda_stream)
     for _ in range(3):
         N.check(L.lentils_normal_op_apply(inv_b.handle, _ptr(s32), _ptr(o32), spb))
