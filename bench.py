@@ -170,6 +170,52 @@ def time_cpu_gridder(O, use_ref, four, uvw, nsample, reps=1):
     return times
 
 
+class Ranks:
+    """Process-group plumbing of an N-GPU run: one process per GPU, launched by torchrun
+    (RANK / LOCAL_RANK / WORLD_SIZE / MASTER_* in the environment). Every rank runs its own
+    replica of the workload; the only collectives are the barriers around the timed region and
+    the maximum of the ranks' times."""
+
+    def __init__(self, backend="nccl"):
+        self.world = int(os.environ.get("WORLD_SIZE", "1"))
+        self.rank = int(os.environ.get("RANK", "0"))
+        self.local = int(os.environ.get("LOCAL_RANK", "0"))
+        self.backend = backend
+        if self.world > 1:
+            import torch.distributed as dist
+            dist.init_process_group(backend, init_method="env://")
+
+    def _device(self):
+        import torch
+        return torch.device("cuda", self.local) if self.backend == "nccl" else torch.device("cpu")
+
+    def barrier(self):
+        if self.world > 1:
+            import torch.distributed as dist
+            dist.barrier()
+
+    def max(self, x):
+        """The maximum of x over the ranks (x itself on one rank)."""
+        if self.world == 1:
+            return float(x)
+        import torch
+        import torch.distributed as dist
+        t = torch.tensor([float(x)], dtype=torch.float64, device=self._device())
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        return float(t.item())
+
+    def close(self):
+        if self.world > 1:
+            import torch.distributed as dist
+            dist.destroy_process_group()
+
+
+def whole_job_rate(world, units_per_rank, seconds):
+    """Whole-job throughput in millions of units per second: every rank processes
+    units_per_rank in `seconds` (the slowest rank's time)."""
+    return world * units_per_rank / seconds / 1e6
+
+
 def run_reference(args):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
@@ -207,13 +253,9 @@ def run_reference(args):
 def run_ours(args):
     import numpy as np
     import torch
-    import torch.distributed as dist
 
-    world = int(os.environ.get("WORLD_SIZE", "1"))
-    rank = int(os.environ.get("RANK", "0"))
-    local = int(os.environ.get("LOCAL_RANK", "0"))
-    if world > 1:
-        dist.init_process_group("nccl", init_method="env://")
+    ranks = Ranks("nccl")
+    world, rank, local = ranks.world, ranks.rank, ranks.local
     torch.cuda.set_device(local)
     dev = torch.device("cuda", local)
 
@@ -256,8 +298,7 @@ def run_ours(args):
     evs = [[torch.cuda.Event(enable_timing=True) for _ in range(3)] for _ in range(args.steps)]
     clocks = ClockSampler(local)
     clocks.start()
-    if world > 1:
-        dist.barrier()
+    ranks.barrier()
     torch.cuda.synchronize()
     t_start = torch.cuda.Event(enable_timing=True)
     t_end = torch.cuda.Event(enable_timing=True)
@@ -266,18 +307,14 @@ def run_ours(args):
         step(evs[k])
     t_end.record(stream)
     torch.cuda.synchronize()
-    if world > 1:
-        dist.barrier()
+    ranks.barrier()
     clk = clocks.stop()
     total_ms = t_start.elapsed_time(t_end)
     deg_ms = sum(e[0].elapsed_time(e[1]) for e in evs) / args.steps
     grd_ms = sum(e[1].elapsed_time(e[2]) for e in evs) / args.steps
-    if world > 1:
-        t = torch.tensor([total_ms], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        total_ms = float(t.item())
+    total_ms = ranks.max(total_ms)
     ms_per_step = total_ms / args.steps
-    value = world * nvis / (ms_per_step * 1e-3) / 1e6
+    value = whole_job_rate(world, nvis, ms_per_step * 1e-3)
 
     # roofline of the dominant kernel: algorithmic bytes = N*(8 B coords + 8 B vis) + G
     G = four.nu * four.half_nv * 8
@@ -308,12 +345,14 @@ def run_ours(args):
         e2e_step()
     e2e_steps = max(3, min(args.steps, 20))
     torch.cuda.synchronize()
+    ranks.barrier()
     t0 = time.perf_counter()
     for _ in range(e2e_steps):
         e2e_step()
     torch.cuda.synchronize()
-    e2e_s = (time.perf_counter() - t0) / e2e_steps
-    e2e_value = world * nvis / e2e_s / 1e6
+    e2e_s = ranks.max((time.perf_counter() - t0) / e2e_steps)
+    ranks.barrier()
+    e2e_value = whole_job_rate(world, nvis, e2e_s)
     h2d = G * 2 + nvis * 16
     d2h = nvis * 16 + G * 2
 
@@ -344,8 +383,7 @@ def run_ours(args):
         if not args.no_cpu_baseline:
             line["cpu_baseline"] = cpu_baseline(four, uvw)
         print(json.dumps(line))
-    if world > 1:
-        dist.destroy_process_group()
+    ranks.close()
     return 0
 
 
