@@ -284,61 +284,6 @@ struct FCGScalars {
     double pap, pr, alpha, beta, rr, rr0, use_net, fallbacks, net_iters, pad;
 };
 
-// partials of p.ap and p.r
-__global__ void __launch_bounds__(256)
-    fcg_dot2_kernel(const float *__restrict__ p, const float *__restrict__ ap,
-                    const float *__restrict__ r, int n, double *__restrict__ partial)
-{
-    __shared__ double sh[8];
-    double a = 0.0, b = 0.0;
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        a += (double)p[i] * (double)ap[i];
-        b += (double)p[i] * (double)r[i];
-    }
-    const double ta = block_sum(a, sh);
-    const double tb = block_sum(b, sh);
-    if (threadIdx.x == 0) {
-        partial[blockIdx.x] = ta;
-        partial[gridDim.x + blockIdx.x] = tb;
-    }
-}
-
-__global__ void fcg_alpha_kernel(const double *__restrict__ partial, int np, FCGScalars *sc)
-{
-    __shared__ double sh[8];
-    double a = 0.0, b = 0.0;
-    for (int i = threadIdx.x; i < np; i += blockDim.x) {
-        a += partial[i];
-        b += partial[np + i];
-    }
-    const double ta = block_sum(a, sh);
-    const double tb = block_sum(b, sh);
-    if (threadIdx.x == 0) {
-        sc->pap = ta;
-        sc->pr = tb;
-        sc->alpha = (ta != 0.0) ? tb / ta : 0.0;
-    }
-}
-
-// e += alpha p; r -= alpha ap; partials of r.r
-__global__ void __launch_bounds__(256)
-    fcg_update_kernel(float *__restrict__ e, float *__restrict__ r, const float *__restrict__ p,
-                      const float *__restrict__ ap, const FCGScalars *__restrict__ sc, int n,
-                      double *__restrict__ partial)
-{
-    __shared__ double sh[8];
-    const float alpha = (float)sc->alpha;
-    double rr = 0.0;
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        e[i] = fmaf(alpha, p[i], e[i]);
-        const float ri = fmaf(-alpha, ap[i], r[i]);
-        r[i] = ri;
-        rr += (double)ri * (double)ri;
-    }
-    const double t = block_sum(rr, sh);
-    if (threadIdx.x == 0) partial[blockIdx.x] = t;
-}
-
 __global__ void fcg_rr_kernel(const double *__restrict__ partial, int np, FCGScalars *sc, int start)
 {
     __shared__ double sh[8];
@@ -361,128 +306,6 @@ struct FCGWindow {
     int slot, count, m, pad;
 };
 
-// P[slot] = p, Q[slot] = ap, pq[slot] = p . ap (from the alpha step)
-__global__ void fcg_store_kernel(const float *__restrict__ p, const float *__restrict__ ap,
-                                 float *__restrict__ P, float *__restrict__ Q,
-                                 const FCGScalars *__restrict__ sc, FCGWindow *__restrict__ win,
-                                 int n)
-{
-    const int slot = win->slot;
-    float *ps = P + (size_t)slot * n;
-    float *qs = Q + (size_t)slot * n;
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        ps[i] = p[i];
-        qs[i] = ap[i];
-    }
-    if (blockIdx.x == 0 && threadIdx.x == 0) win->pq[slot] = sc->pap;
-}
-
-// partials of z.r and j.r, j = dinv r the Jacobi direction (z null: Jacobi only)
-__global__ void __launch_bounds__(256)
-    fcg_descent_dots_kernel(const float *__restrict__ z, const float *__restrict__ r,
-                            const float *__restrict__ dinv, int n, double *__restrict__ partial)
-{
-    __shared__ double sh[8];
-    double zr = 0.0;
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        const double ri = (double)r[i];
-        const double zi = z ? (double)z[i] : (double)dinv[i] * ri;
-        zr += zi * ri;
-    }
-    const double t = block_sum(zr, sh);
-    if (threadIdx.x == 0) partial[blockIdx.x] = t;
-}
-
-// the network's z is used where it is a descent direction (z . r > 0), else dinv r
-__global__ void fcg_select_kernel(const double *__restrict__ partial, int np, FCGScalars *sc,
-                                  int have_net)
-{
-    __shared__ double sh[8];
-    double a = 0.0;
-    for (int i = threadIdx.x; i < np; i += blockDim.x) a += partial[i];
-    const double zr = block_sum(a, sh);
-    if (threadIdx.x == 0) {
-        const bool net_ok = have_net && zr > 0.0 && zr < 1e300;
-        sc->use_net = net_ok ? 1.0 : 0.0;
-        if (have_net && !net_ok) sc->fallbacks += 1.0;
-        if (net_ok) sc->net_iters += 1.0;
-    }
-}
-
-// dir = z (network) or dinv r (Jacobi), written to d
-__global__ void fcg_dir_kernel(const float *__restrict__ z, const float *__restrict__ r,
-                               const float *__restrict__ dinv, const FCGScalars *__restrict__ sc,
-                               float *__restrict__ d, int n)
-{
-    const bool net = z && sc->use_net != 0.0;
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
-        d[i] = net ? z[i] : dinv[i] * r[i];
-}
-
-// partials of d . Q[j] for j < m (blocks x m)
-__global__ void __launch_bounds__(256)
-    fcg_window_dots_kernel(const float *__restrict__ d, const float *__restrict__ Q, int m, int n,
-                           double *__restrict__ partial)
-{
-    __shared__ double sh[8];
-    double acc[kMaxWindow];
-#pragma unroll
-    for (int j = 0; j < kMaxWindow; ++j) acc[j] = 0.0;
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        const double di = (double)d[i];
-#pragma unroll
-        for (int j = 0; j < kMaxWindow; ++j)
-            if (j < m) acc[j] += di * (double)Q[(size_t)j * n + i];
-    }
-    for (int j = 0; j < m; ++j) {
-        const double t = block_sum(acc[j], sh);
-        if (threadIdx.x == 0) partial[j * gridDim.x + blockIdx.x] = t;
-    }
-}
-
-// beta_j = -(d . Q[j]) / pq[j] over the stored directions (the one just stored included);
-// then the ring advances. first != 0 (start of an inner solve): no stored directions.
-__global__ void fcg_window_beta_kernel(const double *__restrict__ partial, int np,
-                                       FCGWindow *__restrict__ win, int first)
-{
-    __shared__ double sh[8];
-    const int m = win->m;
-    const int valid = first ? 0 : min(win->count + 1, m);
-    for (int j = 0; j < m; ++j) {
-        double a = 0.0;
-        if (j < valid)
-            for (int i = threadIdx.x; i < np; i += blockDim.x) a += partial[j * np + i];
-        const double t = block_sum(a, sh);
-        if (threadIdx.x == 0)
-            win->beta[j] = (j < valid && win->pq[j] != 0.0) ? -t / win->pq[j] : 0.0;
-    }
-    if (threadIdx.x == 0) {
-        if (first) {
-            win->count = 0;
-            win->slot = 0;
-        } else {
-            win->count = valid;
-            win->slot = (win->slot + 1) % m;
-        }
-    }
-}
-
-// p = d + sum_j beta_j P[j]
-__global__ void fcg_window_p_kernel(float *__restrict__ p, const float *__restrict__ d,
-                                    const float *__restrict__ P,
-                                    const FCGWindow *__restrict__ win, int n)
-{
-    __shared__ float beta[kMaxWindow];
-    const int m = win->m;
-    if (threadIdx.x < kMaxWindow) beta[threadIdx.x] = (threadIdx.x < m) ? (float)win->beta[threadIdx.x] : 0.f;
-    __syncthreads();
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        float v = d[i];
-        for (int j = 0; j < m; ++j) v = fmaf(beta[j], P[(size_t)j * n + i], v);
-        p[i] = v;
-    }
-}
-
 // start of an inner solve: r32 = (float) r64, e = p = ap = 0; partials of r.r
 __global__ void __launch_bounds__(256)
     fcg_start_kernel(const double *__restrict__ r64, float *__restrict__ r, float *__restrict__ e,
@@ -501,6 +324,210 @@ __global__ void __launch_bounds__(256)
     }
     const double t = block_sum(rr, sh);
     if (threadIdx.x == 0) partial[blockIdx.x] = t;
+}
+
+// -- fused flexible-CG steps: grid-wide passes whose last block finishes the reduction ----------
+// Each block writes its FP64 partials; the block that arrives last (atomic counter, reset by it
+// for the next replay) sums them in block order and derives the step's scalars, so one
+// iteration needs three launches besides the matvec instead of nine. Nothing waits on another
+// block. Per element the arithmetic is that of the separate kernels.
+constexpr int kFusedRows = 24;  // partial rows: K1 2, K2 1 + window, select 1 + 2 x window
+
+// thread 0 (after writing its block's partials) learns whether its block arrived last
+__device__ __forceinline__ bool arrive_last(unsigned *counter, int *flag)
+{
+    if (threadIdx.x == 0) {
+        __threadfence();
+        *flag = (atomicAdd(counter, 1u) == gridDim.x - 1) ? 1 : 0;
+    }
+    __syncthreads();
+    return *flag != 0;
+}
+
+// sum of row k of the partials, in block order (valid in thread 0 of the last block)
+__device__ __forceinline__ double sum_row(const double *part, int k, double *sh)
+{
+    double a = 0.0;
+    for (int i = threadIdx.x; i < (int)gridDim.x; i += blockDim.x) a += __ldcg(&part[k * gridDim.x + i]);
+    return block_sum(a, sh);
+}
+
+// K1: p.ap and p.r; the last block sets pap, pr and alpha = p.r / p.ap
+__global__ void __launch_bounds__(256)
+    fcg_alpha_fused_kernel(const float *__restrict__ p, const float *__restrict__ ap,
+                           const float *__restrict__ r, int n, double *__restrict__ part,
+                           unsigned *__restrict__ counter, FCGScalars *__restrict__ sc)
+{
+    __shared__ double sh[8];
+    __shared__ int last;
+    double a = 0.0, b = 0.0;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        a += (double)p[i] * (double)ap[i];
+        b += (double)p[i] * (double)r[i];
+    }
+    const double ta = block_sum(a, sh), tb = block_sum(b, sh);
+    if (threadIdx.x == 0) {
+        part[blockIdx.x] = ta;
+        part[gridDim.x + blockIdx.x] = tb;
+    }
+    if (!arrive_last(counter, &last)) return;
+    const double A = sum_row(part, 0, sh), B = sum_row(part, 1, sh);
+    if (threadIdx.x == 0) {
+        sc->pap = A;
+        sc->pr = B;
+        sc->alpha = (A != 0.0) ? B / A : 0.0;
+        *counter = 0u;
+    }
+}
+
+// beta_j = -(d.Q[j]) / pq[j] over the valid window entries, then the ring advances
+__device__ __forceinline__ void window_finish(const double *dots, int valid, int first,
+                                              FCGWindow *win)
+{
+    const int m = win->m;
+    for (int j = 0; j < kMaxWindow; ++j)
+        win->beta[j] = (j < valid && win->pq[j] != 0.0) ? -dots[j] / win->pq[j] : 0.0;
+    if (first) {
+        win->count = 0;
+        win->slot = 0;
+    } else {
+        win->count = valid;
+        win->slot = (win->slot + 1) % m;
+    }
+}
+
+// K2: e += alpha p, r -= alpha ap, r.r, P[slot] = p, Q[slot] = ap; with_dir: the window dots of
+// the Jacobi direction d = dinv r (not stored). The last block sets rr and pq[slot] and, with_dir,
+// the window coefficients.
+__global__ void __launch_bounds__(256)
+    fcg_update_fused_kernel(float *__restrict__ e, float *__restrict__ r,
+                            const float *__restrict__ p, const float *__restrict__ ap,
+                            float *__restrict__ P, float *__restrict__ Q,
+                            const float *__restrict__ dinv, int n, FCGScalars *__restrict__ sc,
+                            FCGWindow *__restrict__ win, double *__restrict__ part,
+                            unsigned *__restrict__ counter, int with_dir)
+{
+    __shared__ double sh[8];
+    __shared__ int last;
+    const float alpha = (float)sc->alpha;
+    const int slot = win->slot;
+    const int valid = with_dir ? min(win->count + 1, win->m) : 0;
+    float *ps = P + (size_t)slot * n;
+    float *qs = Q + (size_t)slot * n;
+    double rr = 0.0, acc[kMaxWindow];
+#pragma unroll
+    for (int j = 0; j < kMaxWindow; ++j) acc[j] = 0.0;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const float pi = p[i], api = ap[i];
+        e[i] = fmaf(alpha, pi, e[i]);
+        const float ri = fmaf(-alpha, api, r[i]);
+        r[i] = ri;
+        rr += (double)ri * (double)ri;
+        ps[i] = pi;
+        qs[i] = api;
+        if (valid > 0) {
+            const double di = (double)(dinv[i] * ri);
+#pragma unroll
+            for (int j = 0; j < kMaxWindow; ++j)
+                if (j < valid) acc[j] += di * (double)((j == slot) ? api : Q[(size_t)j * n + i]);
+        }
+    }
+    const double t = block_sum(rr, sh);
+    if (threadIdx.x == 0) part[blockIdx.x] = t;
+    for (int j = 0; j < valid; ++j) {
+        const double tj = block_sum(acc[j], sh);
+        if (threadIdx.x == 0) part[(1 + j) * gridDim.x + blockIdx.x] = tj;
+    }
+    if (!arrive_last(counter, &last)) return;
+    const double R = sum_row(part, 0, sh);
+    double dots[kMaxWindow];
+    for (int j = 0; j < valid; ++j) dots[j] = sum_row(part, 1 + j, sh);
+    if (threadIdx.x == 0) {
+        sc->rr = R;
+        win->pq[slot] = sc->pap;
+        if (with_dir) window_finish(dots, valid, 0, win);
+        *counter = 0u;
+    }
+}
+
+// The direction choice with the network's z (z may be null: Jacobi only): partials of z.r and
+// of the window dots of both candidates, z and d = dinv r; the last block keeps z where it
+// descends (z.r > 0; counted in sc), else d, and sets the window coefficients. first: start of
+// an inner solve (empty window).
+__global__ void __launch_bounds__(256)
+    fcg_select_fused_kernel(const float *__restrict__ z, const float *__restrict__ r,
+                            const float *__restrict__ dinv, const float *__restrict__ Q, int n,
+                            FCGScalars *__restrict__ sc, FCGWindow *__restrict__ win,
+                            double *__restrict__ part, unsigned *__restrict__ counter, int first)
+{
+    __shared__ double sh[8];
+    __shared__ int last;
+    const int valid = first ? 0 : min(win->count + 1, win->m);
+    double zr = 0.0, az[kMaxWindow], aj[kMaxWindow];
+#pragma unroll
+    for (int j = 0; j < kMaxWindow; ++j) az[j] = aj[j] = 0.0;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const float ri = r[i];
+        const double ji = (double)(dinv[i] * ri);
+        const double zi = z ? (double)z[i] : 0.0;
+        zr += zi * (double)ri;
+#pragma unroll
+        for (int j = 0; j < kMaxWindow; ++j)
+            if (j < valid) {
+                const double q = (double)Q[(size_t)j * n + i];
+                az[j] += zi * q;
+                aj[j] += ji * q;
+            }
+    }
+    const double t = block_sum(zr, sh);
+    if (threadIdx.x == 0) part[blockIdx.x] = t;
+    for (int j = 0; j < valid; ++j) {
+        const double a = block_sum(az[j], sh), b = block_sum(aj[j], sh);
+        if (threadIdx.x == 0) {
+            part[(1 + j) * gridDim.x + blockIdx.x] = a;
+            part[(1 + kMaxWindow + j) * gridDim.x + blockIdx.x] = b;
+        }
+    }
+    if (!arrive_last(counter, &last)) return;
+    const double ZR = sum_row(part, 0, sh);
+    __shared__ int use_z;
+    if (threadIdx.x == 0) {
+        const bool ok = z && ZR > 0.0 && ZR < 1e300;
+        if (z) {
+            sc->use_net = ok ? 1.0 : 0.0;
+            if (ok) sc->net_iters += 1.0;
+            else sc->fallbacks += 1.0;
+        } else {
+            sc->use_net = 0.0;
+        }
+        use_z = ok ? 1 : 0;
+    }
+    __syncthreads();
+    double dots[kMaxWindow];
+    for (int j = 0; j < valid; ++j) dots[j] = sum_row(part, (use_z ? 1 : 1 + kMaxWindow) + j, sh);
+    if (threadIdx.x == 0) {
+        window_finish(dots, valid, first, win);
+        *counter = 0u;
+    }
+}
+
+// K3: p = d + sum_j beta_j P[j], d = z where the network's direction was kept, else dinv r
+__global__ void __launch_bounds__(256)
+    fcg_p_fused_kernel(float *__restrict__ p, const float *__restrict__ z,
+                       const float *__restrict__ r, const float *__restrict__ dinv,
+                       const float *__restrict__ P, const FCGScalars *__restrict__ sc,
+                       const FCGWindow *__restrict__ win, int n)
+{
+    __shared__ float beta[kMaxWindow];
+    const int m = win->m;
+    if (threadIdx.x < kMaxWindow) beta[threadIdx.x] = (threadIdx.x < m) ? (float)win->beta[threadIdx.x] : 0.f;
+    __syncthreads();
+    const bool zdir = z && sc->use_net != 0.0;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        float v = zdir ? z[i] : dinv[i] * r[i];
+        for (int j = 0; j < m; ++j) v = fmaf(beta[j], P[(size_t)j * n + i], v);
+        p[i] = v;
+    }
 }
 
 static double host_dot64(const double *a, const double *b, int n, double *partial, double *out,
@@ -897,8 +924,10 @@ int lentils_fcg_solve(lentils_normal_op *op, const double *b, double *x, const f
     const int n = op->nsrc;
     const int m = std::min(kMaxWindow, std::max(1, opt->window));
     float *e32 = nullptr, *r32 = nullptr, *z32 = nullptr, *p32 = nullptr, *ap32 = nullptr,
-          *feat = nullptr, *d32 = nullptr, *Pw = nullptr, *Qw = nullptr;
-    double *r64 = nullptr, *ax64 = nullptr, *partial = nullptr, *scal = nullptr;
+          *feat = nullptr, *Pw = nullptr, *Qw = nullptr;
+    double *r64 = nullptr, *ax64 = nullptr, *partial = nullptr, *scal = nullptr,
+           *fpart = nullptr;
+    unsigned *counter = nullptr;
     FCGScalars *sc = nullptr;
     FCGWindow *win = nullptr;
     cudaGraph_t graph[2] = {nullptr, nullptr};  // one inner iteration: [0] Jacobi, [1] network
@@ -910,12 +939,14 @@ int lentils_fcg_solve(lentils_normal_op *op, const double *b, double *x, const f
     if (e == cudaSuccess) e = cudaMalloc(&p32, sizeof(float) * n);
     if (e == cudaSuccess) e = cudaMalloc(&ap32, sizeof(float) * n);
     if (e == cudaSuccess) e = cudaMalloc(&feat, sizeof(float) * n);
-    if (e == cudaSuccess) e = cudaMalloc(&d32, sizeof(float) * n);
     if (e == cudaSuccess) e = cudaMalloc(&Pw, sizeof(float) * n * m);
     if (e == cudaSuccess) e = cudaMalloc(&Qw, sizeof(float) * n * m);
     if (e == cudaSuccess) e = cudaMalloc(&r64, sizeof(double) * n);
     if (e == cudaSuccess) e = cudaMalloc(&ax64, sizeof(double) * n);
     if (e == cudaSuccess) e = cudaMalloc(&partial, sizeof(double) * kMaxWindow * kRedBlocks);
+    if (e == cudaSuccess) e = cudaMalloc(&fpart, sizeof(double) * kFusedRows * kRedBlocks);
+    if (e == cudaSuccess) e = cudaMalloc(&counter, sizeof(unsigned));
+    if (e == cudaSuccess) e = cudaMemsetAsync(counter, 0, sizeof(unsigned), s);
     if (e == cudaSuccess) e = cudaMalloc(&scal, sizeof(double) * 2);
     if (e == cudaSuccess) e = cudaMalloc(&sc, sizeof(FCGScalars));
     if (e == cudaSuccess) e = cudaMalloc(&win, sizeof(FCGWindow));
@@ -939,28 +970,27 @@ int lentils_fcg_solve(lentils_normal_op *op, const double *b, double *x, const f
     // p = d - sum_j (d.Q[j] / pq[j]) P[j]
     auto direction = [&](bool first, bool with_net) -> int {
         float *zdir = with_net ? z32 : nullptr;
-        if (with_net) {
+        if (with_net)
             if (int q = unet_precondition(net, r32, inv_diag32, feat, z32, s)) return q;
-            fcg_descent_dots_kernel<<<kRedBlocks, 256, 0, s>>>(z32, r32, inv_diag32, n, partial);
-            fcg_select_kernel<<<1, 256, 0, s>>>(partial, kRedBlocks, sc, 1);
-        }
-        fcg_dir_kernel<<<nb(n), 256, 0, s>>>(zdir, r32, inv_diag32, sc, d32, n);
-        if (!first)
-            fcg_window_dots_kernel<<<kRedBlocks, 256, 0, s>>>(d32, Qw, m, n, partial);
-        fcg_window_beta_kernel<<<1, 256, 0, s>>>(partial, kRedBlocks, win, first ? 1 : 0);
-        fcg_window_p_kernel<<<nb(n), 256, 0, s>>>(p32, d32, Pw, win, n);
+        fcg_select_fused_kernel<<<kRedBlocks, 256, 0, s>>>(zdir, r32, inv_diag32, Qw, n, sc, win,
+                                                            fpart, counter, first ? 1 : 0);
+        fcg_p_fused_kernel<<<nb(n), 256, 0, s>>>(p32, zdir, r32, inv_diag32, Pw, sc, win, n);
         cudaError_t le = cudaGetLastError();
         return le == cudaSuccess ? LENTILS_OK : cuda_status(le, "fcg direction");
     };
+    // one inner iteration: ap = A p; alpha; the updates, ring store and (Jacobi direction) the
+    // window coefficients in one pass; then p -- three launches besides the matvec
     auto inner_iteration = [&](bool with_net) -> int {
         int q = lentils_normal_op_apply(op, p32, ap32, s);
         if (q) return q;
-        fcg_dot2_kernel<<<kRedBlocks, 256, 0, s>>>(p32, ap32, r32, n, partial);
-        fcg_alpha_kernel<<<1, 256, 0, s>>>(partial, kRedBlocks, sc);
-        fcg_update_kernel<<<kRedBlocks, 256, 0, s>>>(e32, r32, p32, ap32, sc, n, partial);
-        fcg_rr_kernel<<<1, 256, 0, s>>>(partial, kRedBlocks, sc, 0);
-        fcg_store_kernel<<<nb(n), 256, 0, s>>>(p32, ap32, Pw, Qw, sc, win, n);
-        return direction(false, with_net);
+        fcg_alpha_fused_kernel<<<kRedBlocks, 256, 0, s>>>(p32, ap32, r32, n, fpart, counter, sc);
+        fcg_update_fused_kernel<<<kRedBlocks, 256, 0, s>>>(e32, r32, p32, ap32, Pw, Qw,
+                                                            inv_diag32, n, sc, win, fpart,
+                                                            counter, with_net ? 0 : 1);
+        if (with_net) return direction(false, true);
+        fcg_p_fused_kernel<<<nb(n), 256, 0, s>>>(p32, nullptr, r32, inv_diag32, Pw, sc, win, n);
+        cudaError_t le = cudaGetLastError();
+        return le == cudaSuccess ? LENTILS_OK : cuda_status(le, "fcg step");
     };
 
     const auto t0 = std::chrono::steady_clock::now();
@@ -1087,7 +1117,8 @@ int lentils_fcg_solve(lentils_normal_op *op, const double *b, double *x, const f
     cudaFree(p32);
     cudaFree(ap32);
     cudaFree(feat);
-    cudaFree(d32);
+    cudaFree(fpart);
+    cudaFree(counter);
     cudaFree(Pw);
     cudaFree(Qw);
     cudaFree(win);
