@@ -541,6 +541,22 @@ static double host_dot64(const double *a, const double *b, int n, double *partia
     return h;
 }
 
+// r = b - A x in FP64. A zero x (the usual start) needs no matvec, whose FP64 form costs
+// about twenty FP32 ones: r = b.
+static int initial_residual(lentils_normal_op *op, const double *b, const double *x,
+                            double *ax64, double *r64, int n, double *partial, double *scal,
+                            cudaStream_t s)
+{
+    if (host_dot64(x, x, n, partial, scal, s) == 0.0) {
+        LENTILS_CUDA_TRY(cudaMemcpyAsync(r64, b, sizeof(double) * n, cudaMemcpyDeviceToDevice, s));
+        return LENTILS_OK;
+    }
+    if (int st = lentils_normal_op_apply64(op, x, ax64, s)) return st;
+    sub_kernel<<<nb(n), 256, 0, s>>>(b, ax64, r64, n);
+    LENTILS_CHECK_LAUNCH("sub_kernel");
+    return LENTILS_OK;
+}
+
 }  // namespace lentils
 
 using namespace lentils;
@@ -819,12 +835,10 @@ int lentils_cg_solve(lentils_normal_op *op, const double *b, double *x, const fl
     double bnorm = 0.0, rel = 0.0;
     if (!st) {
         bnorm = sqrt(host_dot64(b, b, n, partial, scal, s));
-        // r = b - A x
-        st = lentils_normal_op_apply64(op, x, ax64, s);
-        if (!st) {
-            sub_kernel<<<nb(n), 256, 0, s>>>(b, ax64, r64, n);
+        // r = b - A x (the FP64 matvec is skipped for the zero initial guess: r = b)
+        st = initial_residual(op, b, x, ax64, r64, n, partial, scal, s);
+        if (!st)
             rel = (bnorm > 0) ? sqrt(host_dot64(r64, r64, n, partial, scal, s)) / bnorm : 0.0;
-        }
     }
     if (!st && opt->use_graph) {
         // capture one inner iteration
@@ -997,11 +1011,9 @@ int lentils_fcg_solve(lentils_normal_op *op, const double *b, double *x, const f
     double bnorm = 0.0, rel = 0.0;
     if (!st) {
         bnorm = sqrt(host_dot64(b, b, n, partial, scal, s));
-        st = lentils_normal_op_apply64(op, x, ax64, s);
-        if (!st) {
-            sub_kernel<<<nb(n), 256, 0, s>>>(b, ax64, r64, n);
+        st = initial_residual(op, b, x, ax64, r64, n, partial, scal, s);
+        if (!st)
             rel = (bnorm > 0) ? sqrt(host_dot64(r64, r64, n, partial, scal, s)) / bnorm : 0.0;
-        }
     }
     // one inner iteration captured as a graph, with and/or without the network (again after a
     // fallback changes the iteration)
