@@ -125,7 +125,7 @@ def load_peaks():
 
 # DRAM bytes (read + write) per launch of the two kernels on this workload, from one ncu capture
 # of this command (dram__bytes_read.sum + dram__bytes_write.sum, tile 16, chunk 4096).
-TRAFFIC = {"degrid_kernel": 121055232, "grid_rows_kernel": 168015104}
+TRAFFIC = {"degrid_kernel": 120944128, "grid_rows_kernel": 167198976}
 
 
 def cpu_reference_lib():
