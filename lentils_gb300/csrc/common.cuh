@@ -70,10 +70,13 @@ struct KBPoly {
     float edge;  // weight of the extra tap at argument +w (only when f == 0): -1/(2w)
 };
 
-// The same table in FP64 (for the double-precision operator used by the refinement residual):
-// cd[k][i] is coefficient k (highest degree first) of tap i.
+// The same table in FP64 (for the double-precision operator used by the refinement residual),
+// in the even/odd form of the FP32 table: for tap i < w, P_i(t) = E_i(t^2) + t O_i(t^2) with
+// ce[k][i] / co[k][i] the coefficients of E_i / O_i (highest power of t^2 first); tap
+// 2w-1-i is -P_i(-t) = t O_i(t^2) - E_i(t^2).
 struct KBPoly64 {
-    double cd[kPolyCoef][kMaxTaps];
+    double ce[kHalfCoef][kMaxW];
+    double co[kHalfCoef][kMaxW];
     double edge;
 };
 

@@ -82,13 +82,18 @@ __device__ __forceinline__ void kb_weights(const KBPoly64 &kb, uint32_t word, do
                                            float res)
 {
     const double f = (double)(word & kFracMask) * (1.0 / (double)(1u << kFracBits)) + (double)res;
-    const double t = 2.0 * f - 1.0;
+    const double t = 2.0 * f - 1.0, u = t * t;
+    // taps i and 2w-1-i from the even and odd parts of P_i (half the FMAs of one Horner per tap)
 #pragma unroll
-    for (int i = 0; i < W2; ++i) {
-        double acc = kb.cd[0][i];
+    for (int i = 0; i < W2 / 2; ++i) {
+        double e = kb.ce[0][i], o = kb.co[0][i];
 #pragma unroll
-        for (int k = 1; k < kPolyCoef; ++k) acc = ::fma(acc, t, kb.cd[k][i]);
-        wt[i] = acc;
+        for (int k = 1; k < kHalfCoef; ++k) {
+            e = ::fma(e, u, kb.ce[k][i]);
+            o = ::fma(o, u, kb.co[k][i]);
+        }
+        wt[i] = ::fma(t, o, e);
+        wt[W2 - 1 - i] = ::fma(t, o, -e);
     }
     if (word & kTopOffBit) wt[W2 - 1] = 0.0;
 }

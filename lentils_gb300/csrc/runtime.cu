@@ -111,8 +111,12 @@ void kb_poly_build(int w, double beta, KBPoly *out, double *fit_err, KBPoly64 *o
             // reflected tap 2w-1-i: P(t) = -P_i(-t)
             mono_all[2 * w - 1 - i][d] = ((d & 1) ? 1.0 : -1.0) * mono[d];
         }
-        // FP32 even/odd table (highest power of t^2 first)
+        // even/odd tables, FP32 and FP64 (highest power of t^2 first)
         for (int k = 0; k < kHalfCoef; ++k) {
+            if (out64) {
+                out64->ce[k][i] = mono[2 * (kHalfCoef - 1 - k)];
+                out64->co[k][i] = mono[2 * (kHalfCoef - 1 - k) + 1];
+            }
             const float e = (float)mono[2 * (kHalfCoef - 1 - k)];
             const float o = (float)mono[2 * (kHalfCoef - 1 - k) + 1];
             if (i & 1) {
@@ -126,8 +130,6 @@ void kb_poly_build(int w, double beta, KBPoly *out, double *fit_err, KBPoly64 *o
     }
     for (int i = 0; i < 2 * w; ++i) {
         const double sgn = (i & 1) ? -1.0 : 1.0;
-        if (out64)
-            for (int k = 0; k < n; ++k) out64->cd[k][i] = mono_all[i][n - 1 - k];
         if (fit_err) {
             for (int s = 0; s <= 400; ++s) {
                 const double t = -1.0 + s / 200.0;
