@@ -407,7 +407,8 @@ int lentils_normal_op_rhs_image64(lentils_normal_op *op, const double *d_img, do
 
 /* Iterative refinement: outer FP64 residuals r = b - A x, inner Jacobi-preconditioned CG with
  * the FP32 operator (inv_diag32 may be NULL for no preconditioner). x (f64, device) holds the
- * initial guess and receives the solution. */
+ * initial guess and receives the solution; an all-zero guess starts from r = b without an FP64
+ * matvec. */
 int lentils_cg_solve(lentils_normal_op *op, const double *b, double *x, const float *inv_diag32,
                      const lentils_cg_options *opt, lentils_cg_result *res, void *stream);
 /* lambda R^T R s of the 'gradient' prior (R = forward differences of
@@ -526,11 +527,13 @@ int lentils_unet_features(const float *dinv, float *feat, int n, void *stream);
 /* z = M(r) for one H x W residual (device FP32), the preconditioner form above */
 int lentils_unet_precondition(lentils_unet *net, const float *r, const float *dinv,
                               const float *feat, float *z, void *stream);
-/* Truncated flexible CG (each new direction A-orthogonalised against the last opt->window
- * directions: p = d - sum_j (d . A p_j) / (p_j . A p_j) p_j) on the normal equations with the learned preconditioner inside the same FP64 iterative refinement as
- * lentils_cg_solve. Where the network's direction is not a descent direction (z . r <= 0)
- * that iteration uses the Jacobi direction instead; if the inner residual has not halved over
- * the last 20 checks (20 * check_every iterations), the solve continues as plain Jacobi-CG
+/* Truncated flexible CG on the normal equations, inside the same FP64 iterative refinement as
+ * lentils_cg_solve: each new direction is A-orthogonalised against the last opt->window
+ * directions, p = d - sum_j (d . A p_j) / (p_j . A p_j) p_j. With the learned preconditioner,
+ * d is the network's direction on every opt->net_every-th iteration and the Jacobi direction
+ * otherwise. Where the network's direction is not a descent direction (z . r <= 0), that
+ * iteration uses the Jacobi direction instead. If the inner residual has not halved over the
+ * last 20 checks (20 * check_every iterations), the solve continues as plain Jacobi-CG
  * (res->fallback = 1). net = NULL runs the same iteration with Jacobi only. */
 int lentils_fcg_solve(lentils_normal_op *op, const double *b, double *x, const float *inv_diag32,
                       lentils_unet *net, const lentils_cg_options *opt, lentils_cg_result *res,
