@@ -355,6 +355,11 @@ def run_ours(args):
     e2e_value = whole_job_rate(world, nvis, e2e_s)
     h2d = G * 2 + nvis * 16
     d2h = nvis * 16 + G * 2
+    dropin = None if args.no_dropin else time_dropin(four, uvw, grid_h, vis_h, ranks)
+    del grid_h, vis_h, vis_o, grid_o
+
+    # accuracy of the timed outputs against the FP64 operator on the same inputs
+    parity = fp64_parity(plan, grid_in, vis_in, vis_out, grid_out)
 
     if rank == 0:
         line = {
@@ -372,12 +377,16 @@ def run_ours(args):
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h, "ms_per_step": e2e_s * 1e3,
                     "api": "lentils_degrid_host + lentils_grid_host (pinned c128, row order)"},
+            "parity": parity,
+            "e2e_dropin": dropin,
             "plan": {"build_s": plan_s, "items": st["nitems"], "tile": st["tile"],
                      "heaviest_tile_vis": st["heaviest_tile_vis"]},
             "clocks": clk,
         }
+        if not args.no_deflect:
+            line["deflect"] = run_deflect_bench(peak, cpu=not args.no_cpu_baseline)
         if not args.no_cg:
-            line["cg"] = run_cg_bench()
+            line["cg"] = run_cg_bench(cpu=not (args.no_cpu_baseline or args.no_cpu_cg))
         if not args.no_sweep:
             line["sweep"] = run_sweep_bench(peak, args.sweep_samples)
         if not args.no_cpu_baseline:
@@ -387,9 +396,160 @@ def run_ours(args):
     return 0
 
 
+def fp64_parity(plan, grid_in, vis_in, vis_out, grid_out):
+    """Relative L2 of the timed FP32 outputs (the last step's degrid and grid, all 1e7
+    visibilities and the whole half-plane grid) against the FP64 operator (lentils_degrid64 /
+    lentils_grid64: FP64 coordinates, weights and accumulation, pinned to the oracle at this
+    size by tests/test_gridding_gpu.py::test_full_size_fp32_vs_oracle) on the same inputs."""
+    import torch
+
+    def rel(a, b):
+        a = a.to(torch.complex128).reshape(-1)
+        b = b.reshape(-1)
+        return float(torch.linalg.vector_norm(a - b) / torch.linalg.vector_norm(b))
+    v64 = plan.degrid64(grid_in.to(torch.complex128))
+    e_deg = rel(vis_out, v64)
+    del v64
+    g64 = plan.grid64(vis_in.to(torch.complex128))
+    e_grid = rel(grid_out, g64)
+    del g64
+    torch.cuda.synchronize()
+    return {"degrid_rel_l2": e_deg, "grid_rel_l2": e_grid, "bar": 1e-5,
+            "against": "FP64 degrid/grid on the GPU (lentils_degrid64/lentils_grid64) of the "
+                       "same inputs, all 1e7 visibilities",
+            "accumulation": "plain FP32 (register runs, shared tiles, float2 atomics)"}
+
+
+def time_dropin(four, uvw, grid_h, vis_h, ranks, steps=5):
+    """The reference's own call path: grid_cpu FORWARD then ADJOINT with the reference's
+    by-value structs and host complex128 buffers, as GriddingOperator._matrixfree_forward /
+    _transpose make them (fourier_operators.py:85-93: fresh numpy zeros for each output), the
+    uv binning kept by the drop-in's plan cache after the first call. Also with page-locked
+    buffers (torch pinned tensors), which the kernels read and write directly."""
+    import numpy as np
+    import torch
+    from lentils_gb300 import _native as N
+    from lentils_gb300.spaces import VisibilitySpace
+    L = N.lib()
+    vs = VisibilitySpace(channels=[1.0], uvcoords=uvw)
+    gs = N.FourierSpaceC(four.nu, four.nv, four.half_nv, 1, 1, four.du, four.dv, four.gcx,
+                         four.gcy, None)
+    g_np, v_np = grid_h.numpy().copy(), vis_h.numpy().copy()
+    nvis = v_np.size
+
+    def call(vis, grid, direction):
+        L.grid_cpu(vs, ctypes.c_void_p(vis), gs, ctypes.c_void_p(grid), WSUP, BETA, direction)
+        N.check_last()
+
+    def pageable():
+        v = np.zeros(nvis, dtype=np.complex128)
+        call(v.ctypes.data, g_np.ctypes.data, 0)
+        g = np.zeros(g_np.shape, dtype=np.complex128)
+        call(v_np.ctypes.data, g.ctypes.data, 1)
+
+    vo = torch.zeros(nvis, dtype=torch.complex128, pin_memory=True)
+    go = torch.zeros(g_np.shape, dtype=torch.complex128, pin_memory=True)
+
+    def pinned():
+        vo.zero_()
+        call(vo.data_ptr(), grid_h.data_ptr(), 0)
+        go.zero_()
+        call(vis_h.data_ptr(), go.data_ptr(), 1)
+
+    out = {"api": "grid_cpu(FORWARD) + grid_cpu(ADJOINT), reference structs and signature",
+           "unit": UNIT, "cache_mode": 1}
+    t0 = time.perf_counter()
+    pageable()  # first call: binning (plan cache miss)
+    out["first_call_s"] = time.perf_counter() - t0
+    for name, fn in (("pageable", pageable), ("pinned", pinned)):
+        fn()
+        ranks.barrier()
+        t0 = time.perf_counter()
+        for _ in range(steps):
+            fn()
+        dt = ranks.max((time.perf_counter() - t0) / steps)
+        out[name] = {"value": whole_job_rate(ranks.world, nvis, dt), "ms_per_step": dt * 1e3}
+    out["note"] = ("pageable: fresh numpy zeros per output, staged through device copies "
+                   "(the reference caller's buffers); pinned: outputs zeroed on the host, kernels "
+                   "address the page-locked buffers directly")
+    L.lentils_dropin_cache_clear()
+    return out
+
+
+def run_deflect_bench(peak, cpu=True, steps=10, warmup=3):
+    """PEMD + external-shear deflection (the CG workload's lens: b=1.2", q=0.7, gamma=2,
+    shear 0.05 at 20 deg) in FP32 on the GPU: the 512^2 pixel grid of one image (262,144
+    points, L2-resident, one launch) and 256 such grids offset by sub-pixel shifts (6.7e7
+    points, 1.07 GB streamed) -- the roofline case, 16 algorithmic bytes per point (8 B in,
+    8 B out). Error of the FP32 output against the FP64 path (lentils_deflect_f64io, pinned to
+    the compiled reference by tests/test_deflect_gpu.py). Beside it the reference's serial
+    deflect_points on the host (FP64, one thread as shipped)."""
+    import numpy as np
+    import torch
+    from lentils_gb300 import _native as N
+    from lentils_gb300 import workloads as WL
+    lenses = np.ascontiguousarray(WL.lens_model().setup_raytracing(WL.Z_SRC))
+    L = N.lib()
+    half = 0.5 * WL.IMG * WL.PIX
+    c = -half + WL.PIX * (np.arange(WL.IMG) + 0.5)
+    pts = np.stack(np.meshgrid(c, c, indexing="ij"), axis=-1).reshape(-1, 2)
+    s = torch.cuda.current_stream()
+    sp = ctypes.c_void_p(s.cuda_stream)
+    lp = ctypes.c_void_p(lenses.ctypes.data)
+    out = {"workload": "PEMD b=1.2 q=0.7 gamma=2 + shear (0.05, 20 deg); 512^2 pixel centres "
+                       "(0.01\") per image", "bytes_per_point": 16}
+    shifts = np.random.default_rng(SEED + 5).uniform(-0.5, 0.5, (256, 2)) * WL.PIX
+    for name, nimg in (("one_image", 1), ("256_images", 256)):
+        p = pts[None] if nimg == 1 else pts[None] + shifts[:, None, :]
+        p32 = torch.as_tensor(p.reshape(-1, 2).astype(np.float32)).cuda()
+        o32 = torch.empty_like(p32)
+        n = p32.shape[0]
+        for _ in range(warmup):
+            N.check(L.lentils_deflect_f32(lp, len(lenses), ctypes.c_void_p(p32.data_ptr()),
+                                          ctypes.c_void_p(o32.data_ptr()), n, sp))
+        ev = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
+        torch.cuda.synchronize()
+        ev[0].record(s)
+        for _ in range(steps):
+            N.check(L.lentils_deflect_f32(lp, len(lenses), ctypes.c_void_p(p32.data_ptr()),
+                                          ctypes.c_void_p(o32.data_ptr()), n, sp))
+        ev[1].record(s)
+        torch.cuda.synchronize()
+        ms = ev[0].elapsed_time(ev[1]) / steps
+        achieved = 16.0 * n / (ms * 1e-3) / 1e9
+        r = {"points": n, "ms_per_launch": ms, "mpts_per_s": n / (ms * 1e-3) / 1e6,
+             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                          "frac": achieved / peak}}
+        # error against the FP64 path on the same (FP32-rounded) input points
+        p64 = p32.double()
+        o64 = torch.empty_like(p64)
+        N.check(L.lentils_deflect_f64io(lp, len(lenses), ctypes.c_void_p(p64.data_ptr()),
+                                        ctypes.c_void_p(o64.data_ptr()), n, sp))
+        torch.cuda.synchronize()
+        a32, a64 = (p64 - o32.double()), (p64 - o64)
+        r["alpha_rel_l2_vs_fp64"] = float(torch.linalg.vector_norm(a32 - a64)
+                                          / torch.linalg.vector_norm(a64))
+        r["max_abs_err_arcsec"] = float((o32.double() - o64).abs().max())
+        out[name] = r
+        del p32, o32, p64, o64
+    if cpu:
+        O, _ = cpu_reference_lib()
+        use_ref = O.ref_available()
+        reps, t = 0, 0.0
+        while t < 3.0:
+            t0 = time.perf_counter()
+            O.deflect(lenses, pts, use_ref=use_ref)
+            t += time.perf_counter() - t0
+            reps += 1
+        out["cpu_baseline"] = {"value": reps * pts.shape[0] / t / 1e6, "unit": "Mpts/s",
+                               "cores": 1, "kind": "reference" if use_ref else "port",
+                               "sample": f"{reps} x 512^2 points, FP64, serial as shipped"}
+    return out
+
+
 # CG source inversion (512^2 image plane, 128^2 source grid, 2e6 visibilities, PEMD b=1.2",
 # q=0.7, gamma=2.0 + external shear (0.05, 20 deg), lambda=1e-2 gradient prior, sigma=1).
-def run_cg_bench(repeats=3):
+def run_cg_bench(repeats=3, cpu=True):
     """CG source inversion to a true FP64 relative residual of 1e-6 (FP32 operator inside FP64
     iterative refinement, CUDA-graph inner iterations), three ways, each the best of `repeats`
     solves after a warm-up solve: plain Jacobi-PCG; flexible CG with Jacobi directions and an
@@ -403,7 +563,7 @@ def run_cg_bench(repeats=3):
     from lentils_gb300 import train_preconditioner as T
     from lentils_gb300.gridding import _ptr
     t0 = time.perf_counter()
-    inv, _, _ = workloads.inversion()
+    inv, _, geom = workloads.inversion()
     setup_s = time.perf_counter() - t0
     params, meta = T.load(T.DEFAULT_WEIGHTS)
     pol = T.deploy_policy(meta)
@@ -500,6 +660,129 @@ def run_cg_bench(repeats=3):
                 "matvec64_ms": ev[2].elapsed_time(ev[3]),
                 "precondition_ms": ev[3].elapsed_time(ev[4]) / 10,
                 "bcb_matvec32_ms": ev[5].elapsed_time(ev[6]) / 10})
+    out["gpu_fp64_jacobi_pcg"] = fp64_pcg(inv)
+    out["bcb_gpu_fp64_jacobi_pcg"] = fp64_pcg(inv_b)
+    if cpu:
+        out["cpu_cg"] = cpu_cg_baseline(inv, geom)
+    return out
+
+
+def fp64_pcg(inv, tol=1e-6, maxiter=5000):
+    """Plain Jacobi-PCG entirely in FP64 on the GPU: the FP64 operator
+    (lentils_normal_op_apply64) every iteration and FP64 vectors (torch), no refinement loop.
+    Its iteration count is what exact-arithmetic CG needs, free of the conjugacy the FP32
+    inner solves lose; its time is what that costs with the FP64 operator."""
+    import torch
+    from lentils_gb300 import _native as N
+    from lentils_gb300.gridding import _ptr
+    L = N.lib()
+    s = inv.stream
+    sp = ctypes.c_void_p(s.cuda_stream)
+    b = inv.b
+    dinv = inv.inv_diag
+    ap = torch.empty_like(b)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    with torch.cuda.stream(s):
+        x = torch.zeros_like(b)
+        r = b.clone()
+        z = dinv * r
+        p = z.clone()
+        rz = torch.dot(r, z)
+        bn = float(torch.linalg.vector_norm(b))
+        it = 0
+        while it < maxiter:
+            N.check(L.lentils_normal_op_apply64(inv.handle, _ptr(p), _ptr(ap), sp))
+            alpha = rz / torch.dot(p, ap)
+            x.add_(alpha * p)
+            r.sub_(alpha * ap)
+            it += 1
+            if it % 10 == 0 and float(torch.linalg.vector_norm(r)) <= tol * bn:
+                break
+            z = dinv * r
+            rz_new = torch.dot(r, z)
+            p.mul_(rz_new / rz).add_(z)
+            rz = rz_new
+        N.check(L.lentils_normal_op_apply64(inv.handle, _ptr(x), _ptr(ap), sp))
+        true_res = float(torch.linalg.vector_norm(b - ap)) / bn
+    s.synchronize()
+    return {"iterations": it, "solve_s": time.perf_counter() - t0, "rel_residual_fp64": true_res,
+            "converged": true_res <= 1.5 * tol}
+
+
+class _Budget(Exception):
+    pass
+
+
+def cpu_cg_baseline(inv, geom, budget_s=60.0):
+    """The reference's CG on the host: scipy cg(rtol=1e-6) on the oracle's FP64 restatement of
+    the normal equations of this inversion, as lentils/tests/solver_tests.py:77-114 runs it --
+    the dirty-beam data term (data_base.py:115-172) with, in turn, the Jacobi preconditioner
+    and the reference's own preconditioner (splu of reg + wtsum L^T L, solver_tests.py:103-106).
+    FFTs and sparse products are single-threaded as in the reference (scipy defaults). The
+    visibility-form operator (NUFFT degrid + grid of the 2e6 visibilities every iteration, the
+    gridder on all host cores) is timed per application and scaled by the Jacobi iteration
+    count, and says so."""
+    import numpy as np
+    import scipy.sparse.linalg as sla
+    from lentils_gb300 import workloads as WL
+    O, _ = cpu_reference_lib()
+    vs, ims, srcs, uvw = geom
+    img = O.ImageGeom((ims.nx, ims.ny), [(ims.xmin, ims.xmax), (ims.ymin, ims.ymax)])
+    src = O.ImageGeom((srcs.nx, srcs.ny), [(srcs.xmin, srcs.xmax), (srcs.ymin, srcs.ymax)])
+    pts = inv.lens.source_points.cpu().numpy().astype(np.float64)
+    w = inv.weights_user
+    cores = int(os.environ.get("OMP_NUM_THREADS", os.cpu_count() or 1))
+    t0 = time.perf_counter()
+    A, rhs, M, R = O.normal_operator_bcb(img, src, uvw, pts, w, WL.LAMBDA)
+    b = rhs(inv.data_user)
+    out = {"operator": "oracle FP64 restatement, dirty-beam data term", "tol": 1e-6,
+           "fft_threads": 1, "setup_s": time.perf_counter() - t0,
+           "setup_note": f"dirty beam and right-hand side by the C gridder on {cores} threads"}
+    n = b.size
+    Aop = sla.LinearOperator((n, n), matvec=A, dtype=np.float64)
+    dinv = O.jacobi_inverse_diagonal(M, R, w)
+    t0 = time.perf_counter()
+    wsum = float(np.sum(np.abs(w)))
+    lu = sla.splu((R + wsum * (M.T @ M)).tocsc())
+    splu_s = time.perf_counter() - t0
+    pcs = {"jacobi": sla.LinearOperator((n, n), matvec=lambda r: dinv * r, dtype=np.float64),
+           "reference_splu": sla.LinearOperator((n, n), matvec=lu.solve, dtype=np.float64)}
+    bn = float(np.linalg.norm(b))
+    for name, pc in pcs.items():
+        it = [0]
+        t0 = time.perf_counter()
+
+        def cb(_xk):
+            it[0] += 1
+            if time.perf_counter() - t0 > budget_s:
+                raise _Budget()
+        try:
+            x, _ = sla.cg(Aop, b, rtol=1e-6, atol=0.0, maxiter=20000, M=pc, callback=cb)
+            done = True
+        except _Budget:
+            x, done = None, False
+        dt = time.perf_counter() - t0
+        r = {"iterations": it[0], "solve_s": dt, "s_per_iteration": dt / max(1, it[0]),
+             "cores": 1}
+        if done:
+            r["rel_residual_fp64"] = float(np.linalg.norm(b - A(x)) / bn)
+        else:
+            r["stopped"] = f"time budget {budget_s} s reached"
+        if name == "reference_splu":
+            r["factorisation_s"] = splu_s
+        out[name] = r
+    # the visibility-form operator per application (two CPU gridder passes of 2e6 vis)
+    Av, _, _, _ = O.normal_operator(img, src, uvw, pts, w, WL.LAMBDA)
+    xs = np.random.default_rng(SEED).normal(size=n)
+    Av(xs)
+    t0 = time.perf_counter()
+    Av(xs)
+    mv = time.perf_counter() - t0
+    out["visibility_form"] = {"s_per_matvec": mv, "cores": cores,
+                              "extrapolated_solve_s": mv * out["jacobi"]["iterations"],
+                              "note": "per-application time x the Jacobi iteration count of the "
+                                      "dirty-beam solve (the two forms agree to ~1e-6)"}
     return out
 
 
@@ -580,17 +863,39 @@ def run_sweep_bench(peak, nsamples=256, steps=10, warmup=3):
             "setup_s": setup_s, "autotuned_classes": sw.tuner.tuned}
 
 
+def _omp_threads(n):
+    """Set the OpenMP thread count of this (calling) thread for the CPU gridder's parallel
+    loops (libgomp, which the compiled gridder links)."""
+    try:
+        ctypes.CDLL("libgomp.so.1").omp_set_num_threads(int(n))
+        return True
+    except (OSError, AttributeError):
+        return False
+
+
 def cpu_baseline(four, uvw):
-    """The reference's CPU gridder on all host cores over a bounded sample (~10 s)."""
+    """The reference's CPU gridder on all host cores over a bounded sample (~10 s), and on one
+    thread over a smaller one (~5 s)."""
     O, use_ref = cpu_reference_lib()
     cores = int(os.environ.get("OMP_NUM_THREADS", os.cpu_count() or 1))
     cal = 20000
     rate = cal / time_cpu_gridder(O, use_ref, four, uvw, cal)[0]
     nsample = int(max(20000, min(2_000_000, rate * 10.0)))
     t = time_cpu_gridder(O, use_ref, four, uvw, nsample)[0]
-    return {"value": nsample / t / 1e6, "unit": UNIT, "cores": cores,
-            "kind": "reference" if use_ref else "port",
-            "sample": f"{nsample} random visibilities of the 1e7 set, full grid, degrid+grid"}
+    out = {"value": nsample / t / 1e6, "unit": UNIT, "cores": cores,
+           "kind": "reference" if use_ref else "port",
+           "sample": f"{nsample} random visibilities of the 1e7 set, full grid, degrid+grid"}
+    if _omp_threads(1):
+        try:
+            cal1 = 4000
+            rate1 = cal1 / time_cpu_gridder(O, use_ref, four, uvw, cal1)[0]
+            n1 = int(max(4000, min(500_000, rate1 * 5.0)))
+            t1 = time_cpu_gridder(O, use_ref, four, uvw, n1)[0]
+            out["one_thread"] = {"value": n1 / t1 / 1e6, "unit": UNIT, "cores": 1,
+                                 "sample": f"{n1} random visibilities, degrid+grid"}
+        finally:
+            _omp_threads(cores)
+    return out
 
 
 def main():
@@ -603,6 +908,9 @@ def main():
     ap.add_argument("--no-cg", action="store_true")
     ap.add_argument("--no-sweep", action="store_true")
     ap.add_argument("--sweep-samples", type=int, default=256)
+    ap.add_argument("--no-deflect", action="store_true")
+    ap.add_argument("--no-dropin", action="store_true")
+    ap.add_argument("--no-cpu-cg", action="store_true")
     args = ap.parse_args()
     os.environ.setdefault("OMP_NUM_THREADS", str(os.cpu_count() or 1))
     if args.impl == "reference":

@@ -132,6 +132,18 @@ int lentils_kb_poly_ncoef(void);
 void grid_cpu(lentils_visibility_space visspace, double *vis, lentils_fourier_space gspace,
               double *grid, int wsup, double kb_beta, int direction);
 
+/* The uv binning of grid_cpu is cached: the reference calls grid_cpu on every operator
+ * application with the same visibility space (fourier_operators.py:85-93), so the plan
+ * (lentils_plan_create) is kept for up to 4 uv sets, keyed by device, uv address, nrows,
+ * channels, grid geometry, wsup, beta and a digest of the uv contents. Mode 1 (default)
+ * digests 4096 evenly spaced rows plus the last; mode 2 digests every row (about 30 ms per
+ * 1e7 rows); mode 0 bins on every call. A caller that rewrites a uv buffer in place between
+ * calls must use mode 2 or call lentils_dropin_cache_clear. No counterpart in the reference
+ * (its grid_cpu has no set-up to keep). grid_cpu calls are serialised by one lock. */
+int lentils_dropin_cache_mode(int mode);
+int lentils_dropin_cache_clear(void);
+int lentils_dropin_cache_size(void);
+
 /* Lens equation beta = theta - sum_l alpha_l(theta) for npoints interleaved (x, y) points.
  * Replaces deflect_points, lentils/backend/deflect.c:60-66. With want_deriv != 0 it also does
  * what the reference does with its single deriv pointer: deriv[0..11] += the PEMD parameter
@@ -554,7 +566,8 @@ int lentils_fcg_solve(lentils_normal_op *op, const double *b, double *x, const f
  * lentils_noalloc_scratch_bytes() (about 7.3 MB) that every GPU loading this library holds
  * until the process exits. Larger batches are rejected with LENTILS_ERR_INVALID; grid them in
  * several calls. The first call on a device looks the array's address up (set-up, once per
- * device); make that first call before any stream capture. Calls share the array: calls whose
+ * device and CUDA context: again after cudaDeviceReset or a re-created primary context); make
+ * that first call before any stream capture. Calls share the array: calls whose
  * GPU work overlaps race and corrupt each other's results, so order them on one stream. The
  * call does not synchronise the stream; the guard of fourier_operators.py:77-80 is not applied
  * (as grid_cpu), and non-finite coordinates are skipped.

@@ -100,6 +100,9 @@ _SIGNATURES = [
                         c_int]),
     ("deflect_points", None, [GlobalLensModelC, c_void_p, c_int, c_void_p, c_int, c_void_p]),
     ("grad_matrix_findiff_csr", None, [ImageSpaceC, c_void_p, c_void_p, c_void_p]),
+    ("lentils_dropin_cache_mode", c_int, [c_int]),
+    ("lentils_dropin_cache_clear", c_int, []),
+    ("lentils_dropin_cache_size", c_int, []),
     ("lentils_plan_create", c_int, [POINTER(c_void_p), POINTER(GridDescC), c_void_p, c_int,
                                     c_void_p, c_int, c_int, c_void_p]),
     ("lentils_plan_destroy", c_int, [c_void_p]),

@@ -4,6 +4,9 @@
 // and printed to stderr, since the reference's signatures have no error channel.
 #include <stdio.h>
 
+#include <mutex>
+#include <vector>
+
 #include "common.cuh"
 
 namespace lentils {
@@ -60,17 +63,101 @@ __global__ void grad_csr_kernel(int nx, int ny, double dx, double dy, int *rows,
     }
 }
 
-int grid_cpu_impl(lentils_visibility_space vs, double *vis, lentils_fourier_space gs,
-                  double *grid, int wsup, double beta, int direction)
+// ---------------------------------------------------------------------------------------
+// Plan cache of the drop-in grid_cpu.
+//
+// The reference calls grid_cpu on every operator application with the same visibility space
+// (GriddingOperator._matrixfree_forward/_transpose, fourier_operators.py:85-93), so binning the
+// uv set (lentils_plan_create: FP64 coordinates, radix sort, device arrays) on every call would
+// cost more than the gridding itself. Plans are kept, least recently used first out, keyed by
+// the device, the uv buffer's address, nrows, the channel values, the grid geometry (nu, nv,
+// du, dv, gcx, gcy), wsup and beta, and a digest of the uv contents:
+//   mode 1 (default): the digest covers 4096 rows spread evenly over the buffer plus its last
+//                     row -- microseconds, and it catches a new uv set at a reused address;
+//   mode 2:           the digest covers every byte of uv (about 30 ms per 1e7 rows);
+//   mode 0:           no cache: every call bins the uv set anew.
+// A caller that rewrites a uv buffer in place between calls, keeping the sampled rows, must
+// use mode 2 or clear the cache (lentils_dropin_cache_clear). Calls are serialised by one
+// mutex, since a cached plan's staging buffers are shared.
+// ---------------------------------------------------------------------------------------
+constexpr int kCacheSlots = 4;
+constexpr int kDigestRows = 4096;
+
+struct CachedPlan {
+    int device;
+    const double *uv;
+    int nrows;
+    std::vector<double> chans;
+    int nu, nv;
+    double du, dv, gcx, gcy;
+    int wsup;
+    double beta;
+    unsigned long long digest;
+    unsigned long long last_use;
+    lentils_plan *plan;
+};
+
+std::mutex g_cache_mu;
+std::vector<CachedPlan> g_cache;
+unsigned long long g_tick = 0;
+int g_cache_mode = 1;
+
+unsigned long long mix_word(unsigned long long h, unsigned long long x)
 {
-    if (direction != 0 && direction != 1)
-        return set_error(LENTILS_ERR_INVALID, "grid_cpu: direction %d (0 or 1)", direction);
-    if (vs.nrows < 0 || vs.nchannels < 1 || !vis || !grid)
-        return set_error(LENTILS_ERR_INVALID, "grid_cpu: bad visibility space or buffers");
-    if (gs.half_nv != gs.nv / 2 + 1)
-        return set_error(LENTILS_ERR_UNSUPPORTED, "grid_cpu: half_nv=%d, expected nv/2+1",
-                         gs.half_nv);
-    if (vs.nrows == 0) return LENTILS_OK;
+    h ^= x + 0x9e3779b97f4a7c15ull + (h << 6) + (h >> 2);
+    return h * 0x100000001b3ull;
+}
+
+unsigned long long uv_digest(const double *uv, int nrows, int mode)
+{
+    unsigned long long h = 0xcbf29ce484222325ull ^ (unsigned long long)nrows;
+    auto row = [&](long long r) {
+        unsigned long long w[3];
+        memcpy(w, uv + 3 * r, sizeof(w));
+        h = mix_word(mix_word(mix_word(h, w[0]), w[1]), w[2]);
+    };
+    if (mode == 2 || nrows <= kDigestRows) {
+        for (long long r = 0; r < nrows; ++r) row(r);
+    } else {
+        for (long long k = 0; k < kDigestRows; ++k) row(k * (long long)nrows / kDigestRows);
+        row(nrows - 1);
+    }
+    return h;
+}
+
+void destroy_cached(CachedPlan &c)
+{
+    int cur = -1;
+    cudaGetDevice(&cur);
+    if (cur != c.device) cudaSetDevice(c.device);
+    lentils_plan_destroy(c.plan);
+    if (cur >= 0 && cur != c.device) cudaSetDevice(cur);
+    c.plan = nullptr;
+}
+
+// The plan for this call: a cached one when every key matches, else a new one (cached unless
+// mode 0). *owned is set when the caller must destroy the returned plan itself.
+int cached_plan(const lentils_visibility_space &vs, const lentils_fourier_space &gs, int wsup,
+                double beta, lentils_plan **out, bool *owned)
+{
+    int dev = 0;
+    LENTILS_CUDA_TRY(cudaGetDevice(&dev));
+    *owned = false;
+    const unsigned long long dig = g_cache_mode ? uv_digest(vs.uv, vs.nrows, g_cache_mode) : 0;
+    if (g_cache_mode) {
+        for (CachedPlan &c : g_cache) {
+            if (c.device == dev && c.uv == vs.uv && c.nrows == vs.nrows &&
+                (int)c.chans.size() == vs.nchannels &&
+                memcmp(c.chans.data(), vs.channels, sizeof(double) * vs.nchannels) == 0 &&
+                c.nu == gs.nu && c.nv == gs.nv && c.du == gs.du && c.dv == gs.dv &&
+                c.gcx == gs.gcx && c.gcy == gs.gcy && c.wsup == wsup && c.beta == beta &&
+                c.digest == dig) {
+                c.last_use = ++g_tick;
+                *out = c.plan;
+                return LENTILS_OK;
+            }
+        }
+    }
     lentils_grid_desc gd;
     memset(&gd, 0, sizeof(gd));
     gd.nu = gs.nu;
@@ -82,11 +169,71 @@ int grid_cpu_impl(lentils_visibility_space vs, double *vis, lentils_fourier_spac
     gd.wsup = wsup;
     gd.kb_beta = beta;
     lentils_plan *plan = nullptr;
-    int st = lentils_plan_create(&plan, &gd, vs.uv, vs.nrows, vs.channels, vs.nchannels, 0,
-                                 nullptr);
+    if (int st = lentils_plan_create(&plan, &gd, vs.uv, vs.nrows, vs.channels, vs.nchannels, 0,
+                                     nullptr))
+        return st;
+    if (!g_cache_mode) {
+        *out = plan;
+        *owned = true;
+        return LENTILS_OK;
+    }
+    for (size_t i = 0; i < g_cache.size();) {  // same buffer, other contents: stale
+        if (g_cache[i].device == dev && g_cache[i].uv == vs.uv) {
+            destroy_cached(g_cache[i]);
+            g_cache.erase(g_cache.begin() + i);
+        } else {
+            ++i;
+        }
+    }
+    if ((int)g_cache.size() >= kCacheSlots) {  // evict the least recently used plan
+        size_t lru = 0;
+        for (size_t i = 1; i < g_cache.size(); ++i)
+            if (g_cache[i].last_use < g_cache[lru].last_use) lru = i;
+        destroy_cached(g_cache[lru]);
+        g_cache.erase(g_cache.begin() + lru);
+    }
+    CachedPlan c;
+    c.device = dev;
+    c.uv = vs.uv;
+    c.nrows = vs.nrows;
+    c.chans.assign(vs.channels, vs.channels + vs.nchannels);
+    c.nu = gs.nu;
+    c.nv = gs.nv;
+    c.du = gs.du;
+    c.dv = gs.dv;
+    c.gcx = gs.gcx;
+    c.gcy = gs.gcy;
+    c.wsup = wsup;
+    c.beta = beta;
+    c.digest = dig;
+    c.last_use = ++g_tick;
+    c.plan = plan;
+    g_cache.push_back(c);
+    *out = plan;
+    return LENTILS_OK;
+}
+
+int grid_cpu_impl(lentils_visibility_space vs, double *vis, lentils_fourier_space gs,
+                  double *grid, int wsup, double beta, int direction)
+{
+    if (direction != 0 && direction != 1)
+        return set_error(LENTILS_ERR_INVALID, "grid_cpu: direction %d (0 or 1)", direction);
+    if (vs.nrows < 0 || vs.nchannels < 1 || !vis || !grid)
+        return set_error(LENTILS_ERR_INVALID, "grid_cpu: bad visibility space or buffers");
+    if (vs.nrows > 0 && (!vs.uv || !vs.channels))
+        return set_error(LENTILS_ERR_INVALID, "grid_cpu: null uv or channels");
+    if (gs.half_nv != gs.nv / 2 + 1)
+        return set_error(LENTILS_ERR_UNSUPPORTED, "grid_cpu: half_nv=%d, expected nv/2+1",
+                         gs.half_nv);
+    if (vs.nrows == 0) return LENTILS_OK;
+    std::lock_guard<std::mutex> lock(g_cache_mu);
+    lentils_plan *plan = nullptr;
+    bool owned = false;
+    int st = cached_plan(vs, gs, wsup, beta, &plan, &owned);
     if (st) return st;
     if (direction == 0) st = lentils_degrid_host(plan, grid, vis, 1, nullptr);
     else st = lentils_grid_host(plan, vis, grid, 1, nullptr);
+    if (!owned) return st;
     const int code = st ? lentils_last_error() : LENTILS_OK;
     char msg[512] = {0};
     if (st) strncpy(msg, lentils_last_error_message(), sizeof(msg) - 1);
@@ -175,6 +322,35 @@ void grid_cpu(lentils_visibility_space vs, double *vis, lentils_fourier_space gs
 {
     clear_error();
     if (grid_cpu_impl(vs, vis, gs, grid, wsup, kb_beta, direction)) report("grid_cpu");
+}
+
+int lentils_dropin_cache_mode(int mode)
+{
+    clear_error();
+    if (mode < 0 || mode > 2)
+        return set_error(LENTILS_ERR_INVALID, "dropin_cache_mode: %d (0, 1 or 2)", mode);
+    std::lock_guard<std::mutex> lock(g_cache_mu);
+    if (mode != g_cache_mode) {  // digests of another mode do not compare
+        for (CachedPlan &c : g_cache) destroy_cached(c);
+        g_cache.clear();
+    }
+    g_cache_mode = mode;
+    return LENTILS_OK;
+}
+
+int lentils_dropin_cache_clear(void)
+{
+    clear_error();
+    std::lock_guard<std::mutex> lock(g_cache_mu);
+    for (CachedPlan &c : g_cache) destroy_cached(c);
+    g_cache.clear();
+    return LENTILS_OK;
+}
+
+int lentils_dropin_cache_size(void)
+{
+    std::lock_guard<std::mutex> lock(g_cache_mu);
+    return (int)g_cache.size();
 }
 
 void deflect_points(lentils_global_lens_model glm, double *p_in, int npoints, double *p_out,

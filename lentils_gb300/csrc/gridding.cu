@@ -104,6 +104,7 @@ __global__ void __launch_bounds__(kGridBatch)
     static_assert(!PRIV || V == 1, "private warp tiles need a warp-uniform flush (V == 1)");
     extern __shared__ __align__(16) unsigned char smraw[];
     const WorkItem it = items[blockIdx.x];
+    if (it.count == 0) return;  // padding item (block-uniform): nothing to clear or flush
     const int E = g.E, S = g.stride;
     const int ntile = PRIV ? NW : 1;
     C *tiles = reinterpret_cast<C *>(smraw);  // ntile x (E x S) extended tiles

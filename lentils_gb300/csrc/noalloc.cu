@@ -21,6 +21,7 @@
 // contents (everything that must start at zero is cleared on the stream by each call). Calls
 // whose GPU work overlaps -- on different streams, or from different host threads without
 // ordering -- race on the array and corrupt each other's results; order them on one stream.
+#include <cuda.h>  // driver types for the context lookup (entry points fetched at run time)
 #include <cub/cub.cuh>
 
 #include <algorithm>
@@ -57,12 +58,50 @@ constexpr size_t kNoAllocScratchBytes = kOffSort + kNoAllocSortBytes;  // about 
 // The scratch array. Every GPU that loads this library holds it until the process exits.
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
 
-// Device address of g_noalloc_scratch per device, looked up once per device with that device
-// current. (In host code the symbol names a host-side stand-in, not device memory; only the
-// address returned by cudaGetSymbolAddress may be handed to kernels.)
+// Device address of g_noalloc_scratch, looked up with the device current. (In host code the
+// symbol names a host-side stand-in, not device memory; only the address returned by
+// cudaGetSymbolAddress may be handed to kernels.) The address belongs to the CUDA context the
+// module was loaded into: after cudaDeviceReset, or when the primary context is released and
+// created again, the module is loaded anew and the array may sit elsewhere. So the cached
+// address is kept per device together with the unique ID of the context it was looked up in
+// (cuCtxGetId), and looked up again whenever the current context's ID differs.
 constexpr int kMaxDevices = 64;
-static void *g_scratch_dev[kMaxDevices] = {nullptr};
+struct ScratchAddr {
+    unsigned long long ctx_id;
+    void *ptr;
+};
+static ScratchAddr g_scratch_dev[kMaxDevices] = {};
 static std::mutex g_scratch_mu;
+
+using PfnCtxGetCurrent = CUresult (*)(CUcontext *);
+using PfnCtxGetId = CUresult (*)(CUcontext, unsigned long long *);
+
+// The current context's unique ID through driver entry points fetched from the runtime (the
+// library does not link libcuda); 0 when no context is current yet.
+static int current_context_id(unsigned long long *id)
+{
+    static PfnCtxGetCurrent get_current = nullptr;
+    static PfnCtxGetId get_id = nullptr;
+    if (!get_current || !get_id) {
+        void *f1 = nullptr, *f2 = nullptr;
+        cudaDriverEntryPointQueryResult q1 = cudaDriverEntryPointSymbolNotFound, q2 = q1;
+        LENTILS_CUDA_TRY(cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f1, 12000,
+                                                          cudaEnableDefault, &q1));
+        LENTILS_CUDA_TRY(cudaGetDriverEntryPointByVersion("cuCtxGetId", &f2, 12000,
+                                                          cudaEnableDefault, &q2));
+        if (q1 != cudaDriverEntryPointSuccess || q2 != cudaDriverEntryPointSuccess || !f1 || !f2)
+            return set_error(LENTILS_ERR_CUDA, "grid_noalloc: driver context queries unavailable");
+        get_current = (PfnCtxGetCurrent)f1;
+        get_id = (PfnCtxGetId)f2;
+    }
+    CUcontext ctx = nullptr;
+    if (get_current(&ctx) != CUDA_SUCCESS)
+        return set_error(LENTILS_ERR_CUDA, "grid_noalloc: cuCtxGetCurrent failed");
+    *id = 0;
+    if (ctx && get_id(ctx, id) != CUDA_SUCCESS)
+        return set_error(LENTILS_ERR_CUDA, "grid_noalloc: cuCtxGetId failed");
+    return LENTILS_OK;
+}
 
 static int scratch_for_current_device(unsigned char **out)
 {
@@ -71,14 +110,20 @@ static int scratch_for_current_device(unsigned char **out)
     if (dev < 0 || dev >= kMaxDevices)
         return set_error(LENTILS_ERR_UNSUPPORTED, "grid_noalloc: device ordinal %d", dev);
     std::lock_guard<std::mutex> lock(g_scratch_mu);
-    if (!g_scratch_dev[dev]) {
+    unsigned long long id = 0;
+    if (int st = current_context_id(&id)) return st;
+    ScratchAddr &a = g_scratch_dev[dev];
+    if (id == 0 || !a.ptr || a.ctx_id != id) {
+        // set-up for this device and context: also makes the device's primary context current
         void *ptr = nullptr;
         const cudaError_t e = cudaGetSymbolAddress(&ptr, g_noalloc_scratch);
         if (e != cudaSuccess) return cuda_status(e, "cudaGetSymbolAddress(g_noalloc_scratch)");
         if (!ptr) return set_error(LENTILS_ERR_CUDA, "grid_noalloc: null scratch address");
-        g_scratch_dev[dev] = ptr;
+        if (int st = current_context_id(&id)) return st;
+        a.ctx_id = id;
+        a.ptr = ptr;
     }
-    *out = (unsigned char *)g_scratch_dev[dev];
+    *out = (unsigned char *)a.ptr;
     return LENTILS_OK;
 }
 
@@ -226,8 +271,10 @@ int lentils_grid_noalloc(const lentils_grid_desc *gd, const double *uvw, int nro
     void *sort_tmp = (void *)(scr + kOffSort);
 
     cudaStream_t s = (cudaStream_t)stream;
+    // a non-finite coordinate gets the key 0xffffffff and is counted in no tile; the tile
+    // field is sized for ntiles + 1 values so that key sorts after every real tile's cells
     int tile_bits = 1;
-    while ((1 << tile_bits) < ntiles) ++tile_bits;
+    while ((1 << tile_bits) < ntiles + 1) ++tile_bits;
     const int key_bits = std::min(32, 2 * logT + tile_bits);
     size_t sort_bytes = 0;
     LENTILS_CUDA_TRY(cub::DeviceRadixSort::SortPairs(nullptr, sort_bytes, keys_in, keys_out, idx,

@@ -121,6 +121,27 @@ class GriddingPlan:
         N.check(N.lib().lentils_grid(self._handle, _ptr(vis), _ptr(out), _stream_ptr(stream)))
         return out
 
+    def degrid64(self, grid, out=None, stream=None):
+        """FP64 degridding (the double-precision operator): half-plane grid complex128 ->
+        plan-order visibilities complex128 (overwrites)."""
+        assert grid.dtype == torch.complex128 and grid.numel() == self.nu * self.half_nv
+        grid = grid.contiguous()
+        if out is None:
+            out = torch.empty(self.nvis, dtype=torch.complex128, device=grid.device)
+        N.check(N.lib().lentils_degrid64(self._handle, _ptr(grid), _ptr(out),
+                                         _stream_ptr(stream)))
+        return out
+
+    def grid64(self, vis, out=None, stream=None):
+        """FP64 gridding: plan-order visibilities complex128 -> a fresh half-plane grid
+        complex128 (or accumulated into `out`)."""
+        assert vis.dtype == torch.complex128 and vis.numel() == self.nvis
+        vis = vis.contiguous()
+        if out is None:
+            out = torch.zeros((self.nu, self.half_nv), dtype=torch.complex128, device=vis.device)
+        N.check(N.lib().lentils_grid64(self._handle, _ptr(vis), _ptr(out), _stream_ptr(stream)))
+        return out
+
     def to_plan(self, vis_user, out=None, stream=None):
         """Reference row order (complex128 or complex64 CUDA tensor) -> plan order c64."""
         v = vis_user.contiguous().reshape(-1)

@@ -88,6 +88,9 @@ class SourceInversion:
                                                _ptr(self.inv_diag32), sp))
         self.stream.synchronize()
         self.strength = float(strength)
+        # the problem as given (reference row order), for residual checks by callers
+        self.data_user = np.ascontiguousarray(data, dtype=np.complex128).reshape(-1)
+        self.weights_user = w_user
 
     @property
     def handle(self):

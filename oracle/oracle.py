@@ -93,10 +93,22 @@ def build_port(quiet=True):
         raise RuntimeError("oracle build failed:\n" + out.stdout + out.stderr)
 
 
-def build_ref(ref_root="/root/reference"):
+def reference_root():
+    """Root of a Lentils checkout (the directory holding lentils/backend): the environment
+    variable LENTILS_REFERENCE, else a checkout named ``reference`` beside this repository;
+    None when neither exists."""
+    for cand in (os.environ.get("LENTILS_REFERENCE"),
+                 os.path.join(os.path.dirname(os.path.dirname(HERE)), "reference")):
+        if cand and os.path.isdir(os.path.join(cand, "lentils", "backend")):
+            return cand
+    return None
+
+
+def build_ref(ref_root=None):
     """Compile the reference's own nufft.c / deflect.c into oracle/_ref (only where the
     reference sources exist). Returns True when both libraries are present afterwards."""
-    if os.path.isdir(os.path.join(ref_root, "lentils", "backend")):
+    ref_root = ref_root or reference_root()
+    if ref_root:
         subprocess.run(["make", "-C", HERE, "ref", f"REF={ref_root}"], capture_output=True,
                        text=True)
     return ref_available()
@@ -622,6 +634,59 @@ def bilinear_lens_matrix(src_points, img_mask, src: ImageGeom):
     mat = sps.csr_matrix((vals.reshape(-1), (np.repeat(rows, 4), cols.reshape(-1))),
                          shape=(p.shape[0], src.nx * src.ny))
     return mat
+
+
+def normal_operator(img: ImageGeom, src: ImageGeom, uvw, src_points, weights, lam, wsup=4,
+                    beta=None):
+    """The FP64 normal equations of the CG source inversion, visibility form:
+    A s = M^T F^T C^-1 F M s + lam R^T R s and rhs(d) = M^T F^T C^-1 d, with M the bilinear
+    lens matrix, F the NUFFT (NufftOracle) and C^-1 = diag(weights); restates
+    lhs = lensop.T * (nufft.T * C^-1 * nufft) * lensop + reg_op (solver_tests.py:97-99,
+    operator_base.py:116-175, data_base.py:36-44). Returns (A, rhs, M, R)."""
+    vis = VisGeom(uvw, [1.0])
+    ora = NufftOracle(vis, img, 2, wsup, beta)
+    M = bilinear_lens_matrix(src_points, img.mask, src)
+    R = regulariser(src, lam)
+    w = np.asarray(weights, dtype=np.float64)
+
+    def A(s):
+        return M.T @ ora.adjoint(w * ora.forward((M @ s).reshape(img.shape))).reshape(-1) + R @ s
+
+    def rhs(d):
+        return M.T @ ora.adjoint(w * d).reshape(-1)
+    return A, rhs, M, R
+
+
+def normal_operator_bcb(img: ImageGeom, src: ImageGeom, uvw, src_points, weights, lam,
+                        wsup=4, beta=None):
+    """The same normal equations with the dirty-beam data term, the reference's production
+    form: A s = M^T BCB(M s) + lam R^T R s with BCB the blurred covariance (bcb_apply of the
+    dirty beam), rhs(d) = M^T (dirty image F^T C^-1 d) (data_base.py:115-172,
+    solver_tests.py:97-99). Returns (A, rhs, M, R)."""
+    vis = VisGeom(uvw, [1.0])
+    w = np.asarray(weights, dtype=np.float64)
+    beam = dirty_beam(vis, img, w, wsup, beta)
+    ora = NufftOracle(vis, img, 2, wsup, beta)
+    M = bilinear_lens_matrix(src_points, img.mask, src)
+    R = regulariser(src, lam)
+
+    def A(s):
+        return M.T @ bcb_apply(beam, img, (M @ s).reshape(img.shape)).reshape(-1) + R @ s
+
+    def rhs(d):
+        return M.T @ ora.adjoint(w * d).reshape(-1)
+    return A, rhs, M, R
+
+
+def jacobi_inverse_diagonal(M, R, weights):
+    """1 / diag(wsum M^T M + R^T R) with wsum the sum of the data weights (the dirty beam's
+    peak): the diagonal of the matrix whose factorisation the reference's radio CG uses as its
+    preconditioner, reg_op + wtsum * L^T L (solver_tests.py:103-106)."""
+    wsum = float(np.sum(np.abs(weights)))
+    d = wsum * np.asarray(M.multiply(M).sum(axis=0)).reshape(-1) + R.diagonal()
+    out = np.zeros_like(d)
+    out[d > 0] = 1.0 / d[d > 0]
+    return out
 
 
 def max_relative_error(a, b):

@@ -93,16 +93,7 @@ def test_lens_and_prior_vs_oracle(native):
 
 
 def _oracle_normal(img, src, four, uvw, pts, w, lam, wsup=4):
-    vis = O.VisGeom(uvw, [1.0])
-    ora = O.NufftOracle(vis, img, 2, wsup)
-    M = O.bilinear_lens_matrix(pts, img.mask, src)
-    R = O.regulariser(src, lam)
-
-    def A(s):
-        return M.T @ ora.adjoint(w * ora.forward((M @ s).reshape(img.shape))).reshape(-1) + R @ s
-
-    def rhs(d):
-        return M.T @ ora.adjoint(w * d).reshape(-1)
+    A, rhs, _, _ = O.normal_operator(img, src, uvw, pts, w, lam, wsup)
     return A, rhs
 
 
@@ -154,6 +145,18 @@ def test_cg_reaches_true_residual(native, use_graph):
     b = rhs(d)
     xs = x.cpu().numpy()
     assert np.linalg.norm(b - A(xs)) / np.linalg.norm(b) < 1.5e-6
+    # the learned flexible-CG solve as the benchmark runs it (committed weights and policy)
+    from lentils_gb300 import learned
+    from lentils_gb300 import train_preconditioner as T
+    params, meta = T.load(T.DEFAULT_WEIGHTS)
+    pol = T.deploy_policy(meta)
+    net = learned.UNet(WL.SRC, WL.SRC, max_batch=1, params=params)
+    net.set_jacobi_weight(pol["jacobi_weight"])
+    x, info = inv.solve_flexible(net, tol=1e-6, inner_tol=1e-3, window=pol["window"],
+                                 net_every=pol["net_every"])
+    assert info["converged"] == 1 and info["rel_residual"] <= 1e-6, info
+    xs = x.cpu().numpy()
+    assert np.linalg.norm(b - A(xs)) / np.linalg.norm(b) < 1.5e-6
 
 
 def test_cg_warm_start(native):
@@ -173,3 +176,42 @@ def test_cg_warm_start(native):
         assert float(torch.linalg.vector_norm(x_half - x_ref)) / scale < 1e-2
         _, info = solve(tol=1e-6, x0=x_ref)
         assert info["converged"] == 1 and info["inner_total"] == 0 and info["outer"] == 0, info
+
+
+def test_workload_normal_operator_and_cg_vs_oracle(native):
+    """The benchmarked CG inversion at full size (512^2 image, 128^2 source, 2e6 visibilities,
+    PEMD + shear): the GPU deflection against the oracle's, the FP64 normal operator
+    (lentils_normal_op_apply64) against the oracle's FP64 operator on a random source, the
+    right-hand side, and the benchmarked solve's answer, whose true relative residual is
+    recomputed with the oracle's operator (exact Kaiser-Bessel weights, scipy FFTs)."""
+    from lentils_gb300 import workloads as WL
+    inv, F, (vs, ims, srcs, uvw) = WL.inversion()
+    img = O.ImageGeom((ims.nx, ims.ny), [(ims.xmin, ims.xmax), (ims.ymin, ims.ymax)])
+    src = O.ImageGeom((srcs.nx, srcs.ny), [(srcs.xmin, srcs.xmax), (srcs.ymin, srcs.ymax)])
+    c = 0.25 * WL.PIX
+    lenses = O.lens_array([O.pemd_cpars(1.2, 0.0, 0.7, c, c, 0.5),
+                           O.shear_cpars(c, c, 0.05, 20.0)])
+    pts = inv.lens.source_points.cpu().numpy()
+    assert np.max(np.abs(pts - O.deflect(lenses, img.points().reshape(-1, 2)))) < 2e-6
+    A, rhs, _, _ = O.normal_operator(img, src, uvw, pts, inv.weights_user, WL.LAMBDA)
+    rng = np.random.default_rng(5)
+    s = rng.normal(size=src.nx * src.ny)
+    assert O.rel_l2(inv.apply(s), A(s)) < 1e-9
+    b = rhs(inv.data_user)
+    assert O.rel_l2(inv.b.cpu().numpy(), b) < 1e-9
+    x, info = inv.solve(tol=1e-6, inner_tol=1e-3)
+    assert info["converged"] == 1 and info["rel_residual"] <= 1e-6, info
+    xs = x.cpu().numpy()
+    assert np.linalg.norm(b - A(xs)) / np.linalg.norm(b) < 1.5e-6
+    # the learned flexible-CG solve as the benchmark runs it (committed weights and policy)
+    from lentils_gb300 import learned
+    from lentils_gb300 import train_preconditioner as T
+    params, meta = T.load(T.DEFAULT_WEIGHTS)
+    pol = T.deploy_policy(meta)
+    net = learned.UNet(WL.SRC, WL.SRC, max_batch=1, params=params)
+    net.set_jacobi_weight(pol["jacobi_weight"])
+    x, info = inv.solve_flexible(net, tol=1e-6, inner_tol=1e-3, window=pol["window"],
+                                 net_every=pol["net_every"])
+    assert info["converged"] == 1 and info["rel_residual"] <= 1e-6, info
+    xs = x.cpu().numpy()
+    assert np.linalg.norm(b - A(xs)) / np.linalg.norm(b) < 1.5e-6

@@ -6,6 +6,7 @@ import os
 import numpy as np
 import pytest
 
+import oracle as O
 from lentils_gb300 import uvfits
 
 
@@ -48,14 +49,17 @@ def test_roundtrip_reference_rules(tmp_path, combine):
     assert np.array_equal(mask, exp(m))
 
 
-REF = os.path.join("/root/reference", "lentils", "tests", "data_radio_2d")
+def _ref_data(name):
+    root = O.reference_root()
+    return None if root is None else os.path.join(root, "lentils", "tests", "data_radio_2d",
+                                                  name)
 
 
 @pytest.mark.parametrize("name", ["input/j0751_small_snr1x.uvfits",
                                   "new_mock/j0751_lwmp_nopos_nosub_0.000000_tiny.uvfits"])
 def test_reference_files(name):
-    path = os.path.join(REF, name)
-    if not os.path.exists(path):
+    path = _ref_data(name)
+    if path is None or not os.path.exists(path):
         pytest.skip("reference data not present")
     space, data, sigma, mask = uvfits.load_uvfits(path)
     hdus = uvfits.read_hdus(path)

@@ -79,3 +79,37 @@ def test_noalloc_rejects_batches_beyond_its_fixed_size(native):
     assert st == 1
     assert b"maximum" in N.lib().lentils_last_error_message()
     assert float(grid.abs().sum()) == 0.0
+
+
+def test_noalloc_skips_nonfinite_rows_on_power_of_two_tile_count(native):
+    """Rows with non-finite coordinates are skipped: on a 1024 x 1024 grid with 16-cell tiles
+    (4096 tiles, a power of two) the result equals the plan path run without those rows, so the
+    skipped rows' sort keys cannot fall into the last tile's range."""
+    from lentils_gb300.gridding import GriddingPlan
+    N = native
+    four, uvw, chans, vis = _case(4, (512, 512), [(-5.12, 5.12), (-5.12, 5.12)], [1.0], 4,
+                                  20000)
+    assert (four.nu // 16) * (four.nv // 16) == 4096
+    bad = np.array([5, 777, 19998])
+    uvw_nan = uvw.copy()
+    uvw_nan[bad[0], 0] = np.nan
+    uvw_nan[bad[1], 1] = np.inf
+    uvw_nan[bad[2], :2] = np.nan
+    # a cluster in the last cell of the last tile (the top corner of the canonical window,
+    # grid coordinates 511.x), whose keys would equal a skipped row's key if the key's tile
+    # field had no room above the last tile
+    off = np.random.default_rng(5).uniform(0.1, 0.6, (50, 2))
+    uvw_nan[10:60, 0] = (four.nu // 2 - 1 + off[:, 0]) * four.du
+    uvw_nan[10:60, 1] = -(four.nv // 2 - 1 + off[:, 1]) * four.dv
+    w, beta = 4, O.kb_beta(4)
+    got = torch.zeros((four.nu, four.half_nv), dtype=torch.complex64, device="cuda")
+    vis_t = torch.as_tensor(vis.astype(np.complex64)).cuda()
+    assert _grid_noalloc(N, four, w, beta, torch.as_tensor(uvw_nan).cuda(),
+                         torch.as_tensor(chans).cuda(), vis_t, got) == 0, \
+        N.lib().lentils_last_error_message()
+    keep = np.setdiff1d(np.arange(uvw.shape[0]), bad)
+    plan = GriddingPlan(uvw_nan[keep], chans, four.nu, four.nv, four.du, four.dv, four.gcx,
+                        four.gcy, w, beta)
+    want = plan.grid(plan.to_plan(vis_t[torch.as_tensor(keep).cuda()]))
+    torch.cuda.synchronize()
+    assert O.rel_l2(got.cpu().numpy(), want.cpu().numpy()) < REL_L2_FP32
