@@ -212,9 +212,14 @@ int lentils_plan_get_stats(const lentils_plan *plan, lentils_plan_stats *stats);
  * once per batch (bit masks) and flush turns only for the groups that flush; 1: lanes own
  * taps, one visibility per warp; 2: two visibilities per warp; 3: as 0 with one tile per CTA
  * flushed by shared-memory atomics and cell changes checked at every step; 4: as 0 with cell
- * changes checked at every step and flush turns for every group. All give the same result up
- * to FP32 summation order. */
+ * changes checked at every step and flush turns for every group; 5: as 0 with flushes by
+ * shared-memory atomics, no turns; 6: as 5 into one tile per CTA; 7: as 0 with compensated
+ * (Kahan) register sums. All give the same result up to FP32 summation order. */
 int lentils_plan_set_grid_variant(lentils_plan *plan, int variant);
+/* Tuning: the degridding kernel's shared-memory layout for even 2w. 0 (default): the staged
+ * tile holds overlapping column pairs (16-byte loads, two taps each); 1: one cell per
+ * element. Identical results. */
+int lentils_plan_set_degrid_variant(lentils_plan *plan, int variant);
 
 /* Degrid: half-plane grid (c64, device) -> visibilities (c64, device, plan order, plan frame).
  * vis_plan is OVERWRITTEN. */

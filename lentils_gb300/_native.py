@@ -108,6 +108,7 @@ _SIGNATURES = [
     ("lentils_plan_destroy", c_int, [c_void_p]),
     ("lentils_plan_get_stats", c_int, [c_void_p, POINTER(PlanStatsC)]),
     ("lentils_plan_set_grid_variant", c_int, [c_void_p, c_int]),
+    ("lentils_plan_set_degrid_variant", c_int, [c_void_p, c_int]),
     ("lentils_degrid", c_int, [c_void_p, c_void_p, c_void_p, c_void_p]),
     ("lentils_grid", c_int, [c_void_p, c_void_p, c_void_p, c_void_p]),
     ("lentils_vis_to_plan", c_int, [c_void_p, c_void_p, c_int, c_void_p, c_void_p]),

@@ -218,11 +218,28 @@ const KBPoly &table_of<float>(const lentils_plan *p) { return p->kb; }
 template <>
 const KBPoly64 &table_of<double>(const lentils_plan *p) { return p->kb64; }
 
+template <int W2>
+__global__ void degrid_pair_kernel(const float2 *__restrict__ grid,
+                                   const uint2 *__restrict__ coords, float2 *__restrict__ out,
+                                   const WorkItem *__restrict__ items,
+                                   const __grid_constant__ KBPoly kb, const GridGeom g,
+                                   const float *__restrict__ vscale);
+
 template <int W2, typename R>
 static int launch_degrid_t(const lentils_plan *p, const typename Prec<R>::C *grid,
                            typename Prec<R>::C *vis, cudaStream_t s, const R *vscale)
 {
     const GridGeom &g = p->geom;
+    if constexpr (std::is_same<R, float>::value && (W2 % 2) == 0) {
+        if (p->degrid_variant == 0) {
+            const size_t smem = degrid_pair_smem_bytes(g);
+            if (int st = set_smem(degrid_pair_kernel<W2>, smem)) return st;
+            degrid_pair_kernel<W2><<<p->nitems, 256, smem, s>>>(grid, p->coords, vis, p->items,
+                                                                p->kb, g, vscale);
+            LENTILS_CHECK_LAUNCH("degrid_pair_kernel");
+            return LENTILS_OK;
+        }
+    }
     const size_t smem = sizeof(typename Prec<R>::C) * (size_t)g.E * g.stride;
     if (int st = set_smem(degrid_kernel<W2, R>, smem)) return st;
     const float2 *cres = std::is_same<R, double>::value ? p->coords_res : nullptr;
@@ -232,14 +249,26 @@ static int launch_degrid_t(const lentils_plan *p, const typename Prec<R>::C *gri
     return LENTILS_OK;
 }
 
-template <int W2, bool SHARED, bool MASKED = false>
+template <int W2, bool SHARED, bool MASKED = false, bool ATOMIC = false, bool KAHAN = false>
 __global__ void __launch_bounds__(kGridBatch)
     grid_rows_kernel(const float2 *__restrict__ vis, const uint2 *__restrict__ coords,
                      float2 *__restrict__ grid, const WorkItem *__restrict__ items,
                      const __grid_constant__ KBPoly kb, const GridGeom g)
 {
     extern __shared__ __align__(16) unsigned char smraw[];
-    grid_rows_item<W2, SHARED, MASKED>(vis, coords, grid, items[blockIdx.x], kb, g, smraw);
+    grid_rows_item<W2, SHARED, MASKED, ATOMIC, KAHAN>(vis, coords, grid, items[blockIdx.x], kb,
+                                                      g, smraw);
+}
+
+template <int W2>
+__global__ void __launch_bounds__(256)
+    degrid_pair_kernel(const float2 *__restrict__ grid, const uint2 *__restrict__ coords,
+                       float2 *__restrict__ out, const WorkItem *__restrict__ items,
+                       const __grid_constant__ KBPoly kb, const GridGeom g,
+                       const float *__restrict__ vscale)
+{
+    extern __shared__ __align__(16) unsigned char smraw[];
+    degrid_item_pair<W2>(grid, coords, out, items[blockIdx.x], kb, g, smraw, vscale);
 }
 
 constexpr size_t kMaxGridSmem = 200 * 1024;
@@ -280,6 +309,35 @@ static int launch_grid_t(const lentils_plan *p, const typename Prec<R>::C *vis,
                          typename Prec<R>::C *grid, cudaStream_t s)
 {
     if constexpr (std::is_same<R, float>::value && (W2 % 2) == 0) {
+        if (p->grid_variant == 7) {  // compensated register sums
+            const GridGeom &g = p->geom;
+            const size_t smem = grid_rows_smem_bytes<W2, false>(g);
+            if (smem > kMaxGridSmem)
+                return set_error(LENTILS_ERR_UNSUPPORTED, "grid variant 7: tile too large");
+            if (int st = set_smem(grid_rows_kernel<W2, false, true, false, true>, smem)) return st;
+            grid_rows_kernel<W2, false, true, false, true><<<p->nitems, kGridBatch, smem, s>>>(
+                vis, p->coords, grid, p->items, p->kb, g);
+            LENTILS_CHECK_LAUNCH("grid_rows_kernel");
+            return LENTILS_OK;
+        }
+        if (p->grid_variant == 5 || p->grid_variant == 6) {  // atomic flushes
+            const GridGeom &g = p->geom;
+            if (p->grid_variant == 6) {
+                const size_t smem = grid_rows_smem_bytes<W2, true>(g);
+                if (int st = set_smem(grid_rows_kernel<W2, true, true, true>, smem)) return st;
+                grid_rows_kernel<W2, true, true, true><<<p->nitems, kGridBatch, smem, s>>>(
+                    vis, p->coords, grid, p->items, p->kb, g);
+            } else {
+                const size_t smem = grid_rows_smem_bytes<W2, false>(g);
+                if (smem > kMaxGridSmem)
+                    return set_error(LENTILS_ERR_UNSUPPORTED, "grid variant 5: tile too large");
+                if (int st = set_smem(grid_rows_kernel<W2, false, true, true>, smem)) return st;
+                grid_rows_kernel<W2, false, true, true><<<p->nitems, kGridBatch, smem, s>>>(
+                    vis, p->coords, grid, p->items, p->kb, g);
+            }
+            LENTILS_CHECK_LAUNCH("grid_rows_kernel");
+            return LENTILS_OK;
+        }
         if (p->grid_variant == 0 || p->grid_variant == 3 || p->grid_variant == 4) {
             const GridGeom &g = p->geom;
             if (p->grid_variant == 3) {

@@ -183,6 +183,102 @@ __device__ __forceinline__ void degrid_item(const typename Prec<R>::C *__restric
     }
 }
 
+// Degridding with the extended tile staged as overlapping column pairs: element (a, b) of
+// the shared array holds (G[a][b], G[a][b+1]) as one float4, so a visibility's 2w taps along v
+// are w 16-byte loads instead of 2w 8-byte loads. Threads of a warp take consecutive sorted
+// visibilities, which mostly share a cell or sit in neighbouring ones; their loads are then
+// broadcasts or adjacent 16-byte words, so halving the load instructions also halves the
+// shared-memory wavefronts that bound this kernel. Same arithmetic, in the same order, as
+// degrid_item<W2, float>. smraw: degrid_pair_smem_bytes(g).
+template <int W2>
+__device__ __forceinline__ void degrid_item_pair(const float2 *__restrict__ grid,
+                                                 const uint2 *__restrict__ coords,
+                                                 float2 *__restrict__ out, const WorkItem &it,
+                                                 const KBPoly &kb, const GridGeom &g,
+                                                 unsigned char *smraw,
+                                                 const float *__restrict__ vscale = nullptr)
+{
+    static_assert((W2 % 2) == 0, "pairs of taps");
+    float4 *sm = reinterpret_cast<float4 *>(smraw);
+    constexpr int w = W2 / 2;
+    const int a0 = it.tu * g.T - g.Hu - w;
+    const int b0 = it.tv * g.T - g.Hv - w;
+    const int E = g.E, S = g.stride;  // S odd: rows 4 words apart modulo 32 banks
+    for (int e = threadIdx.x; e < E * E; e += blockDim.x) {
+        const int ea = e / E, eb = e - ea * E;
+        int au = wrap_index(a0 + ea, g.nu);
+        int bv = wrap_index(b0 + eb, g.nv);
+        float2 val;
+        if (bv >= g.half_nv) {
+            au = (g.nu - au) % g.nu;
+            bv = g.nv - bv;
+            val = grid[(long long)au * g.half_nv + bv];
+            val.y = -val.y;
+        } else {
+            val = grid[(long long)au * g.half_nv + bv];
+        }
+        float2 *row = reinterpret_cast<float2 *>(sm + ea * S);
+        row[2 * eb] = val;                       // (a, b).xy
+        if (eb > 0) row[2 * eb - 1] = val;       // (a, b-1).zw
+        if (eb == E - 1) row[2 * eb + 1] = make_float2(0.f, 0.f);
+    }
+    __syncthreads();
+
+    for (int k = threadIdx.x; k < it.count; k += blockDim.x) {
+        const uint2 c = coords[it.begin + k];
+        const int lu = cell_of(c.x), lv = cell_of(c.y);
+        float wu[W2], wv[W2];
+        kb_weights<W2>(kb, c.x, wu);
+        kb_weights<W2>(kb, c.y, wv);
+        const float4 *p = sm + (lu + 1) * S + (lv + 1);
+        float2 acc = make_float2(0.f, 0.f);
+#pragma unroll
+        for (int i = 0; i < W2; ++i) {
+            float2 r = make_float2(0.f, 0.f);
+#pragma unroll
+            for (int m = 0; m < W2 / 2; ++m) {
+                const float4 q = p[i * S + 2 * m];
+                r = __ffma2_rn(f2(wv[2 * m]), make_float2(q.x, q.y), r);
+                r = __ffma2_rn(f2(wv[2 * m + 1]), make_float2(q.z, q.w), r);
+            }
+            acc = __ffma2_rn(f2(wu[i]), r, acc);
+        }
+        if ((c.x | c.y) & kExtraTapBit) {
+            const float eu = (c.x & kExtraTapBit) ? kb.edge : 0.f;
+            const float ev = (c.y & kExtraTapBit) ? kb.edge : 0.f;
+            const float4 *q = sm + lu * S + lv;
+            float2 r = make_float2(0.f, 0.f);
+            for (int j = 0; j < W2; ++j) {
+                const float4 t = q[j + 1];
+                r = __ffma2_rn(f2(wv[j]), make_float2(t.x, t.y), r);
+            }
+            r = __ffma2_rn(f2(ev), make_float2(q[0].x, q[0].y), r);
+            acc = __ffma2_rn(f2(eu), r, acc);
+            float2 cs = make_float2(0.f, 0.f);
+            for (int i = 0; i < W2; ++i) {
+                const float4 t = q[(i + 1) * S];
+                cs = __ffma2_rn(f2(wu[i]), make_float2(t.x, t.y), cs);
+            }
+            acc = __ffma2_rn(f2(ev), cs, acc);
+        }
+        if (tap_parity(it, g, lu, lv)) {
+            acc.x = -acc.x;
+            acc.y = -acc.y;
+        }
+        if (vscale) {
+            const float sc = vscale[it.begin + k];
+            acc.x *= sc;
+            acc.y *= sc;
+        }
+        out[it.begin + k] = acc;
+    }
+}
+
+__host__ __device__ inline size_t degrid_pair_smem_bytes(const GridGeom &g)
+{
+    return sizeof(float4) * (size_t)g.E * g.stride;
+}
+
 // Extra taps of one visibility (rare): added to shared memory directly.
 template <int W2, typename R>
 __device__ __forceinline__ void grid_extra_taps(typename Prec<R>::C *sm, int S, int lu, int lv,
@@ -261,7 +357,13 @@ constexpr int kRowSkew = 8;      // floats between consecutive groups' weight ro
 // those steps, and a flush takes turns only among the groups that need one (ballot), not all
 // G groups.
 // One work item by a CTA of kGridBatch threads; smraw: grid_rows_smem_bytes<W2, SHARED>(g).
-template <int W2, bool SHARED = false, bool MASKED = false>
+// ATOMIC = true (with MASKED): a group that needs a flush adds its rows with shared-memory
+// float atomics at once, without waiting for its turn, into the warp's copy (or the CTA's one
+// tile when SHARED).
+// KAHAN = true (with MASKED): the register sums of a run are compensated (Kahan): each tap
+// keeps the rounding error of its running sum and the flush adds the corrected sum.
+template <int W2, bool SHARED = false, bool MASKED = false, bool ATOMIC = false,
+          bool KAHAN = false>
 __device__ __forceinline__ void grid_rows_item(const float2 *__restrict__ vis,
                                                const uint2 *__restrict__ coords,
                                                float2 *__restrict__ grid, const WorkItem &it,
@@ -296,8 +398,11 @@ __device__ __forceinline__ void grid_rows_item(const float2 *__restrict__ vis,
     const int pbeg = min(it.count, pg * L), pend = min(it.count, pbeg + L);
 
     float2 acc[W2];
+    float2 cmp[KAHAN ? W2 : 1];  // Kahan: rounding error of each running sum (acc - cmp is exact)
 #pragma unroll
     for (int j = 0; j < W2; ++j) acc[j] = make_float2(0.f, 0.f);
+#pragma unroll
+    for (int j = 0; j < (KAHAN ? W2 : 1); ++j) cmp[j] = make_float2(0.f, 0.f);
     int cur = -1;
     const int nbatch = (L + SHARE - 1) / SHARE;
     // add the accumulated taps of cell `cur` to this lane's window row of the warp's tile
@@ -305,10 +410,21 @@ __device__ __forceinline__ void grid_rows_item(const float2 *__restrict__ vis,
         float2 *p = mytile + ((cur >> 6) + 1 + ri) * S + (cur & 63) + 1;
 #pragma unroll
         for (int j = 0; j < W2; ++j) {
-            float2 v = p[j];
-            v.x += acc[j].x;
-            v.y += acc[j].y;
-            p[j] = v;
+            if constexpr (KAHAN) {
+                p[j] = __fadd2_rn(p[j], __fadd2_rn(acc[j], make_float2(-cmp[j].x, -cmp[j].y)));
+                cmp[j] = make_float2(0.f, 0.f);
+            } else {
+                p[j] = __fadd2_rn(p[j], acc[j]);
+            }
+            acc[j] = make_float2(0.f, 0.f);
+        }
+    };
+    auto flush_rows_atomic = [&]() {
+        float2 *p = mytile + ((cur >> 6) + 1 + ri) * S + (cur & 63) + 1;
+#pragma unroll
+        for (int j = 0; j < W2; ++j) {
+            atomicAdd(&p[j].x, acc[j].x);
+            atomicAdd(&p[j].y, acc[j].y);
             acc[j] = make_float2(0.f, 0.f);
         }
     };
@@ -328,8 +444,19 @@ __device__ __forceinline__ void grid_rows_item(const float2 *__restrict__ vis,
         }
 #pragma unroll
         for (int j = (W2 / 4) * 4; j < W2; ++j) wv[j] = row[j];
+        if constexpr (KAHAN) {
 #pragma unroll
-        for (int j = 0; j < W2; ++j) acc[j] = __ffma2_rn(f2(wv[j]), t, acc[j]);
+            for (int j = 0; j < W2; ++j) {
+                const float2 y = __ffma2_rn(f2(wv[j]), t, make_float2(-cmp[j].x, -cmp[j].y));
+                const float2 sum = __fadd2_rn(acc[j], y);
+                cmp[j] = __fadd2_rn(__fadd2_rn(sum, make_float2(-acc[j].x, -acc[j].y)),
+                                    make_float2(-y.x, -y.y));
+                acc[j] = sum;
+            }
+        } else {
+#pragma unroll
+            for (int j = 0; j < W2; ++j) acc[j] = __ffma2_rn(f2(wv[j]), t, acc[j]);
+        }
     };
     // the producer's inputs for batch b + 1 are loaded while batch b is evaluated and consumed
     uint2 cpre = make_uint2(0u, 0u);
@@ -375,7 +502,7 @@ __device__ __forceinline__ void grid_rows_item(const float2 *__restrict__ vis,
         __syncthreads();
         // consume this batch's rows of my range; after the last batch flush what is left
         const int kfirst = rbeg + b * SHARE;
-        if constexpr (MASKED && !SHARED) {
+        if constexpr (MASKED && (ATOMIC || !SHARED)) {
             const int nval = (lane_on && b < nbatch) ? max(0, min(SHARE, rend - kfirst)) : 0;
             const float *rowg = rows + gid * (SHARE * STR + kRowSkew);
             int keys[SHARE];
@@ -391,7 +518,9 @@ __device__ __forceinline__ void grid_rows_item(const float2 *__restrict__ vis,
             const unsigned wm = __reduce_or_sync(0xffffffffu, bm);
 #pragma unroll
             for (int st = 0; st < SHARE; ++st) {
-                if (wm & (1u << st)) {  // warp-uniform
+                if constexpr (ATOMIC) {
+                    if ((bm >> st) & 1u) flush_rows_atomic();
+                } else if (wm & (1u << st)) {  // warp-uniform
                     const bool need = (bm >> st) & 1u;
                     unsigned gm = __ballot_sync(0xffffffffu, need);
                     while (gm) {  // groups that flush here, one at a time

@@ -605,6 +605,7 @@ int lentils_plan_create(lentils_plan **out, const lentils_grid_desc *gd, const d
     p->nchannels = nchannels;
     p->has_phase = (gd->gcx != 0.0 || gd->gcy != 0.0) ? 1 : 0;
     p->grid_variant = 0;
+    p->degrid_variant = 0;
     kb_poly_build(g.w, gd->kb_beta, &p->kb, nullptr, &p->kb64);
 
     int st = LENTILS_OK;
@@ -634,9 +635,18 @@ int lentils_plan_destroy(lentils_plan *p)
 int lentils_plan_set_grid_variant(lentils_plan *p, int variant)
 {
     clear_error();
-    if (!p || variant < 0 || variant > 4)
-        return set_error(LENTILS_ERR_INVALID, "plan_set_grid_variant: variant 0 to 4");
+    if (!p || variant < 0 || variant > 7)
+        return set_error(LENTILS_ERR_INVALID, "plan_set_grid_variant: variant 0 to 7");
     p->grid_variant = variant;
+    return LENTILS_OK;
+}
+
+int lentils_plan_set_degrid_variant(lentils_plan *p, int variant)
+{
+    clear_error();
+    if (!p || variant < 0 || variant > 1)
+        return set_error(LENTILS_ERR_INVALID, "plan_set_degrid_variant: variant 0 or 1");
+    p->degrid_variant = variant;
     return LENTILS_OK;
 }
 

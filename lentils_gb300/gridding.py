@@ -84,8 +84,13 @@ class GriddingPlan:
         return self._handle
 
     def set_grid_variant(self, variant):
-        """Work split of the gridding kernel (lentils_plan_set_grid_variant, 0-4); tuning only."""
+        """Work split of the gridding kernel (lentils_plan_set_grid_variant, 0-6); tuning only."""
         N.check(N.lib().lentils_plan_set_grid_variant(self._handle, int(variant)))
+
+    def set_degrid_variant(self, variant):
+        """Shared-memory layout of the degridding kernel (lentils_plan_set_degrid_variant, 0 or
+        1); tuning only, identical results."""
+        N.check(N.lib().lentils_plan_set_degrid_variant(self._handle, int(variant)))
 
     @property
     def stats(self):

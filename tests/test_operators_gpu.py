@@ -145,18 +145,6 @@ def test_cg_reaches_true_residual(native, use_graph):
     b = rhs(d)
     xs = x.cpu().numpy()
     assert np.linalg.norm(b - A(xs)) / np.linalg.norm(b) < 1.5e-6
-    # the learned flexible-CG solve as the benchmark runs it (committed weights and policy)
-    from lentils_gb300 import learned
-    from lentils_gb300 import train_preconditioner as T
-    params, meta = T.load(T.DEFAULT_WEIGHTS)
-    pol = T.deploy_policy(meta)
-    net = learned.UNet(WL.SRC, WL.SRC, max_batch=1, params=params)
-    net.set_jacobi_weight(pol["jacobi_weight"])
-    x, info = inv.solve_flexible(net, tol=1e-6, inner_tol=1e-3, window=pol["window"],
-                                 net_every=pol["net_every"])
-    assert info["converged"] == 1 and info["rel_residual"] <= 1e-6, info
-    xs = x.cpu().numpy()
-    assert np.linalg.norm(b - A(xs)) / np.linalg.norm(b) < 1.5e-6
 
 
 def test_cg_warm_start(native):
