@@ -15,6 +15,8 @@
 #include <algorithm>
 
 #include "common.cuh"
+#include <type_traits>
+
 #include "deflect_device.cuh"
 
 namespace lentils {
@@ -24,6 +26,24 @@ __global__ void __launch_bounds__(256)
     deflect_kernel(const P *__restrict__ pin, P *__restrict__ pout, long long n,
                    const __grid_constant__ DevLensSet lenses, int accumulate)
 {
+    if constexpr (std::is_same<P, float2>::value) {  // FP32 points: FP32 arithmetic only
+        for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+             i += (long long)gridDim.x * blockDim.x) {
+            const float2 v = pin[i];
+            float axs = 0.f, ays = 0.f;
+            for (int l = 0; l < lenses.n; ++l) {
+                const DevLens &L = lenses.l[l];
+                float ax, ay;
+                lens_alpha(L, offset_f32(v.x, L.x0h, L.x0l), offset_f32(v.y, L.y0h, L.y0l),
+                           ax, ay);
+                axs += ax;
+                ays += ay;
+            }
+            const float2 base = accumulate ? pout[i] : v;
+            pout[i] = make_float2(base.x - axs, base.y - ays);
+        }
+        return;
+    }
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
          i += (long long)gridDim.x * blockDim.x) {
         double x, y;
@@ -59,6 +79,10 @@ int build_lens(const lentils_mass_model &m, DevLens &L)
     L.type = (int)m.type;
     L.x0 = p[0];
     L.y0 = p[1];
+    L.x0h = (float)p[0];
+    L.x0l = (float)(p[0] - (double)L.x0h);
+    L.y0h = (float)p[1];
+    L.y0l = (float)(p[1] - (double)L.y0h);
     if (m.type == 0) {
         const double t = 2.0 * p[7];
         const double q = p[2];

@@ -15,6 +15,8 @@ struct DevLens {
     int type;
     int order;    // multipoles: highest order
     double x0, y0;
+    float x0h, x0l, y0h, y0l;  // the centre as FP32 pairs: x0 = x0h + x0l to ~2^-48 relative
+    float gxh, gxl, gyh, gyl;  // batched sweep: its sample's pixel-grid origin minus the centre
     // PEMD
     float q, cth, sth, t, bnorm2, bnorm, qp;  // qp = (1-q^2)/q^2
     float an[kSeriesTerms];
@@ -30,6 +32,18 @@ struct DevLensSet {
     int n;
     DevLens l[kMaxLensesPerLaunch];
 };
+
+// x - (hi + lo) for FP32 x and a pair (hi, lo), rounded once: Knuth's two-sum gives
+// x - hi = s + e exactly, then s + (e - lo). Exact offsets from a lens centre matter near the
+// centre, where the angle of the offset sets the direction of the deflection; this keeps the
+// FP32 path off the FP64 units, which on GB300 run at a small fraction of the FP32 rate.
+__device__ __forceinline__ float offset_f32(float x, float hi, float lo)
+{
+    const float s = x - hi;
+    const float bp = s - x;
+    const float e = (x - (s - bp)) + (-hi - bp);
+    return s + (e - lo);
+}
 
 __device__ __forceinline__ float2 cmul(float2 a, float2 b)
 {

@@ -55,18 +55,34 @@ __device__ __forceinline__ void deflect_chunk(const SweepSampleDev &s,
     const long long npix = (long long)s.nx * s.ny;
     const long long p0 = (long long)chunk * kDeflectChunk;
     const long long p1 = min(npix, p0 + kDeflectChunk);
+    // positions x0 + i dx in FP32 pairs (hi + lo), so the pixel loop stays off the FP64 units:
+    // the offset from a lens centre, (x0 - xc) + i dx with x0 - xc a pair made on the host, is
+    // formed with an exact product error (fma) and a two-sum, rounded once
+    const float dxh = (float)s.dx, dxl = (float)(s.dx - (double)dxh);
+    const float dyh = (float)s.dy, dyl = (float)(s.dy - (double)dyh);
+    const float xh = (float)s.x0, xl = (float)(s.x0 - (double)xh);
+    const float yh = (float)s.y0, yl = (float)(s.y0 - (double)yh);
+    auto pair_sum = [](float ch, float cl, float k, float dh, float dl) {  // (ch+cl) + k(dh+dl)
+        const float pr = k * dh;
+        const float pe = fmaf(k, dh, -pr);
+        const float sm = ch + pr;
+        const float bp = sm - ch;
+        const float e = (ch - (sm - bp)) + (pr - bp);
+        return sm + ((e + pe) + fmaf(k, dl, cl));
+    };
     for (long long p = p0 + threadIdx.x; p < p1; p += blockDim.x) {
         const int i = (int)(p / s.ny), j = (int)(p - (long long)i * s.ny);
-        const double x = s.x0 + i * s.dx, y = s.y0 + j * s.dy;
         float axs = 0.f, ays = 0.f;
         for (int l = 0; l < s.nlenses; ++l) {
             const DevLens &L = lenses[s.lens0 + l];
             float ax, ay;
-            lens_alpha(L, (float)(x - L.x0), (float)(y - L.y0), ax, ay);
+            lens_alpha(L, pair_sum(L.gxh, L.gxl, (float)i, dxh, dxl),
+                       pair_sum(L.gyh, L.gyl, (float)j, dyh, dyl), ax, ay);
             axs += ax;
             ays += ay;
         }
-        s.beta_out[p] = make_float2((float)(x - (double)axs), (float)(y - (double)ays));
+        s.beta_out[p] = make_float2(pair_sum(xh, xl, (float)i, dxh, dxl) - axs,
+                                    pair_sum(yh, yl, (float)j, dyh, dyl) - ays);
     }
 }
 
@@ -193,6 +209,11 @@ int lentils_sweep_create(lentils_sweep **out, const lentils_sweep_sample *in, in
         for (int l = 0; l < a.nlenses && !st; ++l) {
             DevLens L;
             st = build_lens(a.lenses[l], L);
+            const double gx = a.x0 - L.x0, gy = a.y0 - L.y0;
+            L.gxh = (float)gx;
+            L.gxl = (float)(gx - (double)L.gxh);
+            L.gyh = (float)gy;
+            L.gyl = (float)(gy - (double)L.gyh);
             hl.push_back(L);
         }
         if (st) break;

@@ -69,3 +69,27 @@ def test_reference_files(name):
     assert np.all(np.isfinite(data)) and np.all(np.isfinite(space.uvw))
     assert np.all(sigma[mask] > 0) and np.all(sigma[~mask] == 0)
     assert space.channels[0] == pytest.approx(h["CRVAL4"], rel=1e-6)
+
+
+@pytest.mark.parametrize("combine", [False, True])
+@pytest.mark.parametrize("name", ["input/j0751_small_snr1x.uvfits",
+                                  "new_mock/j0751_lwmp_nopos_nosub_0.000000_tiny.uvfits"])
+def test_reference_files_element_wise(name, combine):
+    """The reference's own uvfits files, loaded by lentils_gb300.uvfits and by an independent
+    decoder of the FITS random-groups standard (tests/uvfits_decode.py, numpy structured
+    records) with the reference loader's rules applied: uvw, channel frequencies, data, mask
+    bit for bit; sigma to the FP32 rounding of the weights the file stores (the reference
+    takes weight^-1/2 of the FP32 column)."""
+    import uvfits_decode as D
+    path = _ref_data(name)
+    if path is None or not os.path.exists(path):
+        pytest.skip("reference data not present")
+    space, data, sigma, mask = uvfits.load_uvfits(path, combine_stokes=combine)
+    uvw, chans, d2, s2, m2 = D.decode(path, combine_stokes=combine)
+    assert np.array_equal(space.uvw, uvw)
+    assert np.array_equal(space.channels, chans)
+    assert data.shape == d2.shape and np.array_equal(data, d2)
+    assert np.array_equal(mask, m2)
+    assert 0 < mask.sum() <= mask.size
+    assert np.all(sigma[~mask] == 0)
+    assert np.allclose(sigma[mask], s2[mask], rtol=2e-7, atol=0)
