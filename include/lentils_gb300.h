@@ -214,11 +214,13 @@ int lentils_plan_get_stats(const lentils_plan *plan, lentils_plan_stats *stats);
  * flushed by shared-memory atomics and cell changes checked at every step; 4: as 0 with cell
  * changes checked at every step and flush turns for every group; 5: as 0 with flushes by
  * shared-memory atomics, no turns; 6: as 5 into one tile per CTA; 7: as 0 with compensated
- * (Kahan) register sums. All give the same result up to FP32 summation order. */
+ * (Kahan) register sums; 8 (2w dividing 32): as 0 with the flush steps found by the producer
+ * lanes (one warp ballot per batch) instead of per-lane key checks. All give the same result
+ * up to FP32 summation order. */
 int lentils_plan_set_grid_variant(lentils_plan *plan, int variant);
-/* Tuning: the degridding kernel's shared-memory layout for even 2w. 0 (default): the staged
- * tile holds overlapping column pairs (16-byte loads, two taps each); 1: one cell per
- * element. Identical results. */
+/* Tuning: the degridding kernel's shared-memory layout. 0 (default): one cell per element;
+ * 1 (even 2w): the staged tile holds overlapping column pairs (16-byte loads, two taps each).
+ * Identical results. */
 int lentils_plan_set_degrid_variant(lentils_plan *plan, int variant);
 
 /* Degrid: half-plane grid (c64, device) -> visibilities (c64, device, plan order, plan frame).

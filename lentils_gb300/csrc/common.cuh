@@ -131,7 +131,7 @@ struct lentils_plan {
     int heaviest_tile;
     int has_phase;
     int grid_variant;     // work split of the gridding kernel (lentils_plan_set_grid_variant)
-    int degrid_variant;   // shared-memory layout of the degridding kernel (0 pairs, 1 single)
+    int degrid_variant;   // shared-memory layout of the degridding kernel (0 single, 1 pairs)
     // plan-order arrays
     uint2 *coords;        // fixed-point tile-relative (u, v)
     float2 *coords_res;   // g - q*2^-24 per axis (exact in FP64, stored FP32): FP64 kernels only

@@ -231,7 +231,7 @@ static int launch_degrid_t(const lentils_plan *p, const typename Prec<R>::C *gri
 {
     const GridGeom &g = p->geom;
     if constexpr (std::is_same<R, float>::value && (W2 % 2) == 0) {
-        if (p->degrid_variant == 0) {
+        if (p->degrid_variant == 1) {
             const size_t smem = degrid_pair_smem_bytes(g);
             if (int st = set_smem(degrid_pair_kernel<W2>, smem)) return st;
             degrid_pair_kernel<W2><<<p->nitems, 256, smem, s>>>(grid, p->coords, vis, p->items,
@@ -258,6 +258,16 @@ __global__ void __launch_bounds__(kGridBatch)
     extern __shared__ __align__(16) unsigned char smraw[];
     grid_rows_item<W2, SHARED, MASKED, ATOMIC, KAHAN>(vis, coords, grid, items[blockIdx.x], kb,
                                                       g, smraw);
+}
+
+template <int W2>
+__global__ void __launch_bounds__(kGridBatch)
+    grid_ballot_kernel(const float2 *__restrict__ vis, const uint2 *__restrict__ coords,
+                       float2 *__restrict__ grid, const WorkItem *__restrict__ items,
+                       const __grid_constant__ KBPoly kb, const GridGeom g)
+{
+    extern __shared__ __align__(16) unsigned char smraw[];
+    grid_rows_item_ballot<W2>(vis, coords, grid, items[blockIdx.x], kb, g, smraw);
 }
 
 template <int W2>
@@ -309,6 +319,19 @@ static int launch_grid_t(const lentils_plan *p, const typename Prec<R>::C *vis,
                          typename Prec<R>::C *grid, cudaStream_t s)
 {
     if constexpr (std::is_same<R, float>::value && (W2 % 2) == 0) {
+        if constexpr (32 % W2 == 0) {
+            if (p->grid_variant == 8) {  // flush steps from the producers' ballot
+                const GridGeom &g = p->geom;
+                const size_t smem = grid_rows_smem_bytes<W2, false>(g);
+                if (smem > kMaxGridSmem)
+                    return set_error(LENTILS_ERR_UNSUPPORTED, "grid variant 8: tile too large");
+                if (int st = set_smem(grid_ballot_kernel<W2>, smem)) return st;
+                grid_ballot_kernel<W2><<<p->nitems, kGridBatch, smem, s>>>(
+                    vis, p->coords, grid, p->items, p->kb, g);
+                LENTILS_CHECK_LAUNCH("grid_ballot_kernel");
+                return LENTILS_OK;
+            }
+        }
         if (p->grid_variant == 7) {  // compensated register sums
             const GridGeom &g = p->geom;
             const size_t smem = grid_rows_smem_bytes<W2, false>(g);

@@ -588,6 +588,167 @@ __device__ __forceinline__ void grid_rows_item(const float2 *__restrict__ vis,
     grid_flush_extended<W2, float>(tiles, grid, it, g);
 }
 
+// Row-owner gridding with the flush steps found by the producers. Same data flow as
+// grid_rows_item<W2, false, true> (warp-private tiles, producer rows in shared memory, lane i
+// of a group of 2w lanes owning window row i), for 2w dividing 32, where the producer threads
+// of a group's rows and the group's consumer lanes are the same lanes of one warp (row st of
+// group g is produced by lane g*2w + st). Each producer compares its row's cell with the row
+// before (a shuffle; the first row with the group's last cell of the previous batch), and one
+// warp ballot hands every consumer lane the steps at which its group must flush. Rows past the
+// end of a range carry x = 0 and never flush, so the consumers run every step unconditionally
+// and read no keys; the cell to flush is read from the row before the flush step. Flushes take
+// turns among the groups that flush at the same step, as in grid_rows_item.
+template <int W2>
+__device__ __forceinline__ void grid_rows_item_ballot(const float2 *__restrict__ vis,
+                                                      const uint2 *__restrict__ coords,
+                                                      float2 *__restrict__ grid,
+                                                      const WorkItem &it, const KBPoly &kb,
+                                                      const GridGeom &g, unsigned char *smraw)
+{
+    static_assert(32 % W2 == 0, "groups must tile a warp");
+    constexpr int STR = 2 * W2 + 4;
+    constexpr int G = 32 / W2;              // groups per warp
+    constexpr int NW = kGridBatch / 32;
+    constexpr int NG = NW * G;
+    constexpr int SHARE = kGridBatch / NG;  // == W2: rows per group and batch
+    static_assert(SHARE == W2, "one producer lane per row of its own group");
+    const int E = g.E, S = g.stride;
+    float2 *tiles = reinterpret_cast<float2 *>(smraw);
+    const size_t tile_bytes = ((sizeof(float2) * (size_t)NW * E * S) + 15) & ~size_t(15);
+    float *rows = reinterpret_cast<float *>(smraw + tile_bytes);
+    for (int e = threadIdx.x; e < NW * E * S; e += blockDim.x) tiles[e] = make_float2(0.f, 0.f);
+
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    float2 *mytile = tiles + warp * E * S;
+    const int grp = lane / W2, ri = lane - grp * W2;  // consumer: group, window row
+    const int gid = warp * G + grp;                    // this lane's range (also as producer)
+    const int L = (it.count + NG - 1) / NG;
+    const int rbeg = min(it.count, gid * L), rend = min(it.count, rbeg + L);
+    const int nbatch = (L + SHARE - 1) / SHARE;
+    const unsigned gmask = ((1u << W2) - 1u) << (grp * W2);
+    // this group's rows: row st at rowg + st * STR
+    const float *rowg = rows + gid * (SHARE * STR + kRowSkew);
+    float *myrow = rows + gid * (SHARE * STR + kRowSkew) + ri * STR;  // produced by this lane
+
+    float2 acc[W2];
+#pragma unroll
+    for (int j = 0; j < W2; ++j) acc[j] = make_float2(0.f, 0.f);
+    int plast = -1;  // cell of the group's last valid row so far (-1: none)
+    auto flush_to = [&](int cell) {
+        float2 *p = mytile + ((cell >> 6) + 1 + ri) * S + (cell & 63) + 1;
+#pragma unroll
+        for (int j = 0; j < W2; ++j) {
+            p[j] = __fadd2_rn(p[j], acc[j]);
+            acc[j] = make_float2(0.f, 0.f);
+        }
+    };
+    auto consume = [&](const float *row) {
+        const float2 x = reinterpret_cast<const float2 *>(row + 2 * W2)[0];
+        const float wui = row[W2 + ri];
+        const float2 t = make_float2(wui * x.x, wui * x.y);
+        float wv[W2];
+#pragma unroll
+        for (int q = 0; q < W2 / 4; ++q) {
+            const float4 v4 = reinterpret_cast<const float4 *>(row)[q];
+            wv[4 * q] = v4.x;
+            wv[4 * q + 1] = v4.y;
+            wv[4 * q + 2] = v4.z;
+            wv[4 * q + 3] = v4.w;
+        }
+#pragma unroll
+        for (int j = (W2 / 4) * 4; j < W2; ++j) wv[j] = row[j];
+#pragma unroll
+        for (int j = 0; j < W2; ++j) acc[j] = __ffma2_rn(f2(wv[j]), t, acc[j]);
+    };
+    uint2 cpre = make_uint2(0u, 0u);
+    float2 xpre = make_float2(0.f, 0.f);
+    auto prefetch = [&](int bb) {
+        const int kv = rbeg + bb * SHARE + ri;
+        if (bb < nbatch && kv < rend) {
+            cpre = coords[it.begin + kv];
+            xpre = vis[it.begin + kv];
+        }
+    };
+    prefetch(0);
+    for (int b = 0; b < nbatch; ++b) {
+        __syncthreads();  // tiles zeroed / previous batch consumed
+        // produce row ri of this group: weights, value, cell; x = 0 past the range's end
+        const int kv = rbeg + b * SHARE + ri;
+        const bool valid = kv < rend;
+        int key = -1;
+        {
+            const uint2 c = cpre;
+            float2 x = xpre;
+            prefetch(b + 1);
+            const int lu = cell_of(c.x), lv = cell_of(c.y);
+            float wu[W2], wv[W2];
+            kb_weights<W2>(kb, c.x, wu);
+            kb_weights<W2>(kb, c.y, wv);
+            const float h = valid ? (tap_parity(it, g, lu, lv) ? -0.5f : 0.5f) : 0.f;
+            x = make_float2(h * x.x, h * x.y);
+            float4 *row4 = reinterpret_cast<float4 *>(myrow);
+#pragma unroll
+            for (int q = 0; q < W2 / 4; ++q)
+                row4[q] = make_float4(wv[4 * q], wv[4 * q + 1], wv[4 * q + 2], wv[4 * q + 3]);
+#pragma unroll
+            for (int j = (W2 / 4) * 4; j < W2; ++j) myrow[j] = wv[j];
+#pragma unroll
+            for (int i = 0; i < W2; ++i) myrow[W2 + i] = wu[i];
+            key = valid ? ((lu << 6) | lv) : -1;
+            reinterpret_cast<float4 *>(myrow + 2 * W2)[0] =
+                make_float4(x.x, x.y, __int_as_float(key), 0.f);
+            if (valid && ((c.x | c.y) & kExtraTapBit))  // rare: straight into the warp's tile
+                grid_extra_taps<W2, float>(mytile, S, lu, lv, c, wu, wv, kb.edge, x);
+        }
+        // flush steps: row st flushes the group's accumulated cell when its cell differs from
+        // the cell of the row before it (valid rows are a prefix of each group's rows)
+        const int up = __shfl_up_sync(0xffffffffu, key, 1);
+        const int cell0 = plast;  // the cell a flush at step 0 leaves
+        const int prev = (ri == 0) ? plast : up;
+        const unsigned flags = __ballot_sync(0xffffffffu, valid && prev >= 0 && key != prev);
+        const unsigned nvalid = __popc(__ballot_sync(0xffffffffu, valid) & gmask);
+        const int lastkey = __shfl_sync(0xffffffffu, key, grp * W2 + max((int)nvalid, 1) - 1);
+        if (nvalid) plast = lastkey;
+        unsigned wm = 0;  // steps at which any group of the warp flushes
+#pragma unroll
+        for (int q = 0; q < G; ++q) wm |= flags >> (q * W2);
+        wm &= (1u << W2) - 1u;
+        const unsigned bm = (flags >> (grp * W2)) & ((1u << W2) - 1u);
+        __syncthreads();
+#pragma unroll
+        for (int st = 0; st < SHARE; ++st) {
+            if (wm & (1u << st)) {  // warp-uniform
+                const bool need = (bm >> st) & 1u;
+                unsigned gm = __ballot_sync(0xffffffffu, need);
+                while (gm) {  // groups that flush here, one at a time
+                    const int g0 = (__ffs(gm) - 1) / W2;
+                    if (need && grp == g0)  // the cell being left: the row before's
+                        flush_to(st > 0 ? __float_as_int(rowg[(st - 1) * STR + 2 * W2 + 2])
+                                        : cell0);
+                    __syncwarp();
+                    gm &= ~(((1u << W2) - 1u) << (g0 * W2));
+                }
+            }
+            consume(rowg + st * STR);
+        }
+    }
+    // what is left: every group with a non-empty range flushes its last cell, in turn
+#pragma unroll
+    for (int g0 = 0; g0 < G; ++g0) {
+        if (grp == g0 && plast >= 0) flush_to(plast);
+        __syncwarp();
+    }
+    __syncthreads();
+    for (int e = threadIdx.x; e < E * S; e += blockDim.x) {  // sum the warps' copies
+        float2 a = tiles[e];
+#pragma unroll
+        for (int q = 1; q < NW; ++q) a = __fadd2_rn(a, tiles[q * E * S + e]);
+        tiles[e] = a;
+    }
+    __syncthreads();
+    grid_flush_extended<W2, float>(tiles, grid, it, g);
+}
+
 template <int W2, bool SHARED = false>
 __host__ __device__ inline size_t grid_rows_smem_bytes(const GridGeom &g)
 {

@@ -635,8 +635,8 @@ int lentils_plan_destroy(lentils_plan *p)
 int lentils_plan_set_grid_variant(lentils_plan *p, int variant)
 {
     clear_error();
-    if (!p || variant < 0 || variant > 7)
-        return set_error(LENTILS_ERR_INVALID, "plan_set_grid_variant: variant 0 to 7");
+    if (!p || variant < 0 || variant > 8)
+        return set_error(LENTILS_ERR_INVALID, "plan_set_grid_variant: variant 0 to 8");
     p->grid_variant = variant;
     return LENTILS_OK;
 }

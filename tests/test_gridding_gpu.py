@@ -37,6 +37,7 @@ def gpu_grid(plan, vis_c128):
 
 @pytest.mark.parametrize("name", ["nufft_cfg0_w3", "nufft_odd_w4", "nufft_tiny_w1"])
 @pytest.mark.parametrize("tile,variant", [(0, 0), (8, 0), (64, 0), (0, 1), (32, 1), (0, 2),
+                                          (0, 5), (0, 6), (0, 7), (0, 8), (8, 8), (64, 8),
                                           (16, 2), (0, 3), (32, 3), (0, 4), (8, 4), (64, 4)])
 def test_plan_api_vs_golden(native, name, tile, variant):
     d, vis, four = load_nufft_golden(name)
@@ -47,6 +48,20 @@ def test_plan_api_vs_golden(native, name, tile, variant):
     assert O.rel_l2(v, d["vis_out"] - d["vis_acc0"]) < REL_L2_FP32
     g = gpu_grid(plan, d["vis_in"])
     assert O.rel_l2(g, d["grid_out"] - d["grid_acc0"]) < REL_L2_FP32
+
+
+@pytest.mark.parametrize("name", ["nufft_cfg0_w3", "nufft_odd_w4", "nufft_tiny_w1"])
+@pytest.mark.parametrize("tile", [0, 8, 64])
+def test_degrid_layouts_vs_golden(native, name, tile):
+    """Both shared-memory layouts of the degridding kernel give the same bits."""
+    d, vis, four = load_nufft_golden(name)
+    w, beta = int(d["wsup"]), float(d["beta"])
+    plan = make_plan(vis, four, w, beta, tile=tile)
+    v0 = gpu_degrid(plan, d["grid_in"])
+    plan.set_degrid_variant(1)
+    v1 = gpu_degrid(plan, d["grid_in"])
+    assert np.array_equal(v0, v1)
+    assert O.rel_l2(v1, d["vis_out"] - d["vis_acc0"]) < REL_L2_FP32
 
 
 @pytest.mark.parametrize("name", ["nufft_cfg0_w3", "nufft_odd_w4", "nufft_tiny_w1"])
