@@ -662,16 +662,23 @@ def run_cg_bench(repeats=3, cpu=True):
                 "bcb_matvec32_ms": ev[5].elapsed_time(ev[6]) / 10})
     out["gpu_fp64_jacobi_pcg"] = fp64_pcg(inv)
     out["bcb_gpu_fp64_jacobi_pcg"] = fp64_pcg(inv_b)
+    out["gpu_mixed_jacobi_pcg"] = fp64_pcg(inv, operator32=True)
+    out["bcb_gpu_mixed_jacobi_pcg"] = fp64_pcg(inv_b, operator32=True)
+    lr = out["learned_fcg8"]["solve_s"]
+    out["learned_vs_mixed_pcg_time"] = out["gpu_mixed_jacobi_pcg"]["solve_s"] / lr
+    out["learned_vs_mixed_pcg_iterations"] = (out["gpu_mixed_jacobi_pcg"]["iterations"]
+                                              / max(1, out["learned_fcg8"]["inner_iterations"]))
     if cpu:
         out["cpu_cg"] = cpu_cg_baseline(inv, geom)
     return out
 
 
-def fp64_pcg(inv, tol=1e-6, maxiter=5000):
-    """Plain Jacobi-PCG entirely in FP64 on the GPU: the FP64 operator
-    (lentils_normal_op_apply64) every iteration and FP64 vectors (torch), no refinement loop.
-    Its iteration count is what exact-arithmetic CG needs, free of the conjugacy the FP32
-    inner solves lose; its time is what that costs with the FP64 operator."""
+def fp64_pcg(inv, tol=1e-6, maxiter=5000, operator32=False):
+    """Plain Jacobi-PCG with FP64 vectors on the GPU (torch vector operations, no refinement
+    loop, no restarts): the FP64 operator (lentils_normal_op_apply64) every iteration, or with
+    operator32 the FP32 operator (lentils_normal_op_apply) on the FP32-rounded direction.
+    Its iteration count is what CG needs without the conjugacy that FP32 inner vectors and
+    restarts lose; the answer's true residual is recomputed with the FP64 operator."""
     import torch
     from lentils_gb300 import _native as N
     from lentils_gb300.gridding import _ptr
@@ -691,8 +698,15 @@ def fp64_pcg(inv, tol=1e-6, maxiter=5000):
         rz = torch.dot(r, z)
         bn = float(torch.linalg.vector_norm(b))
         it = 0
+        p32 = torch.empty(p.shape, dtype=torch.float32, device=p.device)
+        ap32 = torch.empty_like(p32)
         while it < maxiter:
-            N.check(L.lentils_normal_op_apply64(inv.handle, _ptr(p), _ptr(ap), sp))
+            if operator32:
+                p32.copy_(p)
+                N.check(L.lentils_normal_op_apply(inv.handle, _ptr(p32), _ptr(ap32), sp))
+                ap.copy_(ap32)
+            else:
+                N.check(L.lentils_normal_op_apply64(inv.handle, _ptr(p), _ptr(ap), sp))
             alpha = rz / torch.dot(p, ap)
             x.add_(alpha * p)
             r.sub_(alpha * ap)

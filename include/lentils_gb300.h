@@ -208,15 +208,16 @@ int lentils_plan_create(lentils_plan **plan, const lentils_grid_desc *grid, cons
 int lentils_plan_destroy(lentils_plan *plan);
 int lentils_plan_get_stats(const lentils_plan *plan, lentils_plan_stats *stats);
 /* Tuning: the gridding kernel's work split. 0 (default): lanes own window rows, 32/(2w)
- * visibilities side by side per warp, warp-private tiles, the cell changes of each batch found
- * once per batch (bit masks) and flush turns only for the groups that flush; 1: lanes own
- * taps, one visibility per warp; 2: two visibilities per warp; 3: as 0 with one tile per CTA
- * flushed by shared-memory atomics and cell changes checked at every step; 4: as 0 with cell
- * changes checked at every step and flush turns for every group; 5: as 0 with flushes by
- * shared-memory atomics, no turns; 6: as 5 into one tile per CTA; 7: as 0 with compensated
- * (Kahan) register sums; 8 (2w dividing 32): as 0 with the flush steps found by the producer
- * lanes (one warp ballot per batch) instead of per-lane key checks. All give the same result
- * up to FP32 summation order. */
+ * visibilities side by side per warp, warp-private tiles, flushes taking turns only among the
+ * groups that flush; the flush steps are found by the lanes that produce the batch's rows (one
+ * warp ballot per batch); 1: lanes own taps, one visibility
+ * per warp; 2: two visibilities per warp; 3: as 8 with one tile per CTA flushed by
+ * shared-memory atomics and cell changes checked at every step; 4: as 8 with cell changes
+ * checked at every step and flush turns for every group; 5: as 8 with flushes by shared-memory
+ * atomics, no turns; 6: as 5 into one tile per CTA; 7: as 8 with compensated (Kahan) register
+ * sums; 8: as 0 with every consumer lane reading its group's cell keys and marking the
+ * batch's flush steps itself. Tiles too large for the warp-private copies fall back to 1. All
+ * give the same result up to FP32 summation order. */
 int lentils_plan_set_grid_variant(lentils_plan *plan, int variant);
 /* Tuning: the degridding kernel's shared-memory layout. 0 (default): one cell per element;
  * 1 (even 2w): the staged tile holds overlapping column pairs (16-byte loads, two taps each).

@@ -319,15 +319,14 @@ static int launch_grid_t(const lentils_plan *p, const typename Prec<R>::C *vis,
                          typename Prec<R>::C *grid, cudaStream_t s)
 {
     if constexpr (std::is_same<R, float>::value && (W2 % 2) == 0) {
-        if constexpr (32 % W2 == 0) {
-            if (p->grid_variant == 8) {  // flush steps from the producers' ballot
-                const GridGeom &g = p->geom;
-                const size_t smem = grid_rows_smem_bytes<W2, false>(g);
-                if (smem > kMaxGridSmem)
-                    return set_error(LENTILS_ERR_UNSUPPORTED, "grid variant 8: tile too large");
+        {
+            // the default: flush steps from the producers' ballot (warp-private tiles; larger
+            // tiles than fit in shared memory fall through to grid_kernel)
+            const size_t smem = grid_rows_smem_bytes<W2, false>(p->geom);
+            if (p->grid_variant == 0 && smem <= kMaxGridSmem) {
                 if (int st = set_smem(grid_ballot_kernel<W2>, smem)) return st;
                 grid_ballot_kernel<W2><<<p->nitems, kGridBatch, smem, s>>>(
-                    vis, p->coords, grid, p->items, p->kb, g);
+                    vis, p->coords, grid, p->items, p->kb, p->geom);
                 LENTILS_CHECK_LAUNCH("grid_ballot_kernel");
                 return LENTILS_OK;
             }
@@ -335,8 +334,7 @@ static int launch_grid_t(const lentils_plan *p, const typename Prec<R>::C *vis,
         if (p->grid_variant == 7) {  // compensated register sums
             const GridGeom &g = p->geom;
             const size_t smem = grid_rows_smem_bytes<W2, false>(g);
-            if (smem > kMaxGridSmem)
-                return set_error(LENTILS_ERR_UNSUPPORTED, "grid variant 7: tile too large");
+            if (smem > kMaxGridSmem) return launch_grid_tv<W2, 1, R>(p, vis, grid, s);
             if (int st = set_smem(grid_rows_kernel<W2, false, true, false, true>, smem)) return st;
             grid_rows_kernel<W2, false, true, false, true><<<p->nitems, kGridBatch, smem, s>>>(
                 vis, p->coords, grid, p->items, p->kb, g);
@@ -352,8 +350,7 @@ static int launch_grid_t(const lentils_plan *p, const typename Prec<R>::C *vis,
                     vis, p->coords, grid, p->items, p->kb, g);
             } else {
                 const size_t smem = grid_rows_smem_bytes<W2, false>(g);
-                if (smem > kMaxGridSmem)
-                    return set_error(LENTILS_ERR_UNSUPPORTED, "grid variant 5: tile too large");
+                if (smem > kMaxGridSmem) return launch_grid_tv<W2, 1, R>(p, vis, grid, s);
                 if (int st = set_smem(grid_rows_kernel<W2, false, true, true>, smem)) return st;
                 grid_rows_kernel<W2, false, true, true><<<p->nitems, kGridBatch, smem, s>>>(
                     vis, p->coords, grid, p->items, p->kb, g);
@@ -361,7 +358,8 @@ static int launch_grid_t(const lentils_plan *p, const typename Prec<R>::C *vis,
             LENTILS_CHECK_LAUNCH("grid_rows_kernel");
             return LENTILS_OK;
         }
-        if (p->grid_variant == 0 || p->grid_variant == 3 || p->grid_variant == 4) {
+        if (p->grid_variant == 0 || p->grid_variant == 3 || p->grid_variant == 4 ||
+            p->grid_variant == 8) {
             const GridGeom &g = p->geom;
             if (p->grid_variant == 3) {
                 const size_t smem = grid_rows_smem_bytes<W2, true>(g);
@@ -372,7 +370,7 @@ static int launch_grid_t(const lentils_plan *p, const typename Prec<R>::C *vis,
                 return LENTILS_OK;
             }
             const size_t smem = grid_rows_smem_bytes<W2, false>(g);
-            if (smem <= kMaxGridSmem && p->grid_variant == 0) {
+            if (smem <= kMaxGridSmem && (p->grid_variant == 0 || p->grid_variant == 8)) {
                 if (int st = set_smem(grid_rows_kernel<W2, false, true>, smem)) return st;
                 grid_rows_kernel<W2, false, true><<<p->nitems, kGridBatch, smem, s>>>(
                     vis, p->coords, grid, p->items, p->kb, g);

@@ -588,16 +588,17 @@ __device__ __forceinline__ void grid_rows_item(const float2 *__restrict__ vis,
     grid_flush_extended<W2, float>(tiles, grid, it, g);
 }
 
-// Row-owner gridding with the flush steps found by the producers. Same data flow as
-// grid_rows_item<W2, false, true> (warp-private tiles, producer rows in shared memory, lane i
-// of a group of 2w lanes owning window row i), for 2w dividing 32, where the producer threads
-// of a group's rows and the group's consumer lanes are the same lanes of one warp (row st of
-// group g is produced by lane g*2w + st). Each producer compares its row's cell with the row
-// before (a shuffle; the first row with the group's last cell of the previous batch), and one
-// warp ballot hands every consumer lane the steps at which its group must flush. Rows past the
-// end of a range carry x = 0 and never flush, so the consumers run every step unconditionally
-// and read no keys; the cell to flush is read from the row before the flush step. Flushes take
-// turns among the groups that flush at the same step, as in grid_rows_item.
+// Row-owner gridding with the flush steps found by the producers (the default). Same data
+// flow as grid_rows_item<W2, false, true> -- warp-private tiles, producer rows in shared
+// memory, lane i of a group of 2w lanes owning window row i -- but each group's rows are
+// produced by the group's own lanes (row st by lane g*2w + st; G = 32/(2w) groups per warp, so
+// SHARE = 2w rows per group and batch, and the 32 - G*2w lanes left over idle). Each producer
+// compares its row's cell with the row before it (a shuffle; the first row with the group's
+// last cell of the previous batch), and one warp ballot hands every consumer lane the steps at
+// which its group must flush. Rows past the end of a range carry x = 0 and never flush, so the
+// consumers run every step unconditionally and read no keys; the cell to flush is read from
+// the row before the flush step. Flushes take turns among the groups that flush at the same
+// step, as in grid_rows_item. smraw: grid_rows_smem_bytes<W2, false>(g).
 template <int W2>
 __device__ __forceinline__ void grid_rows_item_ballot(const float2 *__restrict__ vis,
                                                       const uint2 *__restrict__ coords,
@@ -605,13 +606,12 @@ __device__ __forceinline__ void grid_rows_item_ballot(const float2 *__restrict__
                                                       const WorkItem &it, const KBPoly &kb,
                                                       const GridGeom &g, unsigned char *smraw)
 {
-    static_assert(32 % W2 == 0, "groups must tile a warp");
     constexpr int STR = 2 * W2 + 4;
     constexpr int G = 32 / W2;              // groups per warp
     constexpr int NW = kGridBatch / 32;
     constexpr int NG = NW * G;
-    constexpr int SHARE = kGridBatch / NG;  // == W2: rows per group and batch
-    static_assert(SHARE == W2, "one producer lane per row of its own group");
+    constexpr int SHARE = W2;               // rows per group and batch, one per lane
+    static_assert(NG * SHARE <= kGridBatch, "rows fit the batch");
     const int E = g.E, S = g.stride;
     float2 *tiles = reinterpret_cast<float2 *>(smraw);
     const size_t tile_bytes = ((sizeof(float2) * (size_t)NW * E * S) + 15) & ~size_t(15);
@@ -619,15 +619,16 @@ __device__ __forceinline__ void grid_rows_item_ballot(const float2 *__restrict__
     for (int e = threadIdx.x; e < NW * E * S; e += blockDim.x) tiles[e] = make_float2(0.f, 0.f);
 
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const bool lane_on = lane < G * W2;
     float2 *mytile = tiles + warp * E * S;
-    const int grp = lane / W2, ri = lane - grp * W2;  // consumer: group, window row
+    const int grp = lane_on ? lane / W2 : G - 1;      // consumer: group, window row
+    const int ri = lane_on ? lane - grp * W2 : 0;
     const int gid = warp * G + grp;                    // this lane's range (also as producer)
     const int L = (it.count + NG - 1) / NG;
-    const int rbeg = min(it.count, gid * L), rend = min(it.count, rbeg + L);
+    const int rbeg = min(it.count, gid * L), rend = lane_on ? min(it.count, rbeg + L) : rbeg;
     const int nbatch = (L + SHARE - 1) / SHARE;
     const unsigned gmask = ((1u << W2) - 1u) << (grp * W2);
-    // this group's rows: row st at rowg + st * STR
-    const float *rowg = rows + gid * (SHARE * STR + kRowSkew);
+    const float *rowg = rows + gid * (SHARE * STR + kRowSkew);  // row st at rowg + st * STR
     float *myrow = rows + gid * (SHARE * STR + kRowSkew) + ri * STR;  // produced by this lane
 
     float2 acc[W2];
@@ -686,17 +687,19 @@ __device__ __forceinline__ void grid_rows_item_ballot(const float2 *__restrict__
             kb_weights<W2>(kb, c.y, wv);
             const float h = valid ? (tap_parity(it, g, lu, lv) ? -0.5f : 0.5f) : 0.f;
             x = make_float2(h * x.x, h * x.y);
-            float4 *row4 = reinterpret_cast<float4 *>(myrow);
+            if (lane_on) {
+                float4 *row4 = reinterpret_cast<float4 *>(myrow);
 #pragma unroll
-            for (int q = 0; q < W2 / 4; ++q)
-                row4[q] = make_float4(wv[4 * q], wv[4 * q + 1], wv[4 * q + 2], wv[4 * q + 3]);
+                for (int q = 0; q < W2 / 4; ++q)
+                    row4[q] = make_float4(wv[4 * q], wv[4 * q + 1], wv[4 * q + 2], wv[4 * q + 3]);
 #pragma unroll
-            for (int j = (W2 / 4) * 4; j < W2; ++j) myrow[j] = wv[j];
+                for (int j = (W2 / 4) * 4; j < W2; ++j) myrow[j] = wv[j];
 #pragma unroll
-            for (int i = 0; i < W2; ++i) myrow[W2 + i] = wu[i];
-            key = valid ? ((lu << 6) | lv) : -1;
-            reinterpret_cast<float4 *>(myrow + 2 * W2)[0] =
-                make_float4(x.x, x.y, __int_as_float(key), 0.f);
+                for (int i = 0; i < W2; ++i) myrow[W2 + i] = wu[i];
+                key = valid ? ((lu << 6) | lv) : -1;
+                reinterpret_cast<float4 *>(myrow + 2 * W2)[0] =
+                    make_float4(x.x, x.y, __int_as_float(key), 0.f);
+            }
             if (valid && ((c.x | c.y) & kExtraTapBit))  // rare: straight into the warp's tile
                 grid_extra_taps<W2, float>(mytile, S, lu, lv, c, wu, wv, kb.edge, x);
         }
@@ -713,7 +716,7 @@ __device__ __forceinline__ void grid_rows_item_ballot(const float2 *__restrict__
 #pragma unroll
         for (int q = 0; q < G; ++q) wm |= flags >> (q * W2);
         wm &= (1u << W2) - 1u;
-        const unsigned bm = (flags >> (grp * W2)) & ((1u << W2) - 1u);
+        const unsigned bm = lane_on ? (flags >> (grp * W2)) & ((1u << W2) - 1u) : 0u;
         __syncthreads();
 #pragma unroll
         for (int st = 0; st < SHARE; ++st) {
@@ -729,13 +732,13 @@ __device__ __forceinline__ void grid_rows_item_ballot(const float2 *__restrict__
                     gm &= ~(((1u << W2) - 1u) << (g0 * W2));
                 }
             }
-            consume(rowg + st * STR);
+            if (lane_on) consume(rowg + st * STR);
         }
     }
     // what is left: every group with a non-empty range flushes its last cell, in turn
 #pragma unroll
     for (int g0 = 0; g0 < G; ++g0) {
-        if (grp == g0 && plast >= 0) flush_to(plast);
+        if (lane_on && grp == g0 && plast >= 0) flush_to(plast);
         __syncwarp();
     }
     __syncthreads();

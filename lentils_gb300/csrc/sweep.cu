@@ -119,9 +119,9 @@ __global__ void __launch_bounds__(kGridBatch, 3)
         const WorkItem it = s.items[d.index];
         if (d.kind == kSweepGrid) {
             if (s.w2 == 8)
-                grid_rows_item<8, false, true>(s.vis_in, s.coords, s.grid_out, it, kb, g, smraw);
+                grid_rows_item_ballot<8>(s.vis_in, s.coords, s.grid_out, it, kb, g, smraw);
             else
-                grid_rows_item<6, false, true>(s.vis_in, s.coords, s.grid_out, it, kb, g, smraw);
+                grid_rows_item_ballot<6>(s.vis_in, s.coords, s.grid_out, it, kb, g, smraw);
         } else {
             if (s.w2 == 8) degrid_item<8, float>(s.grid_in, s.coords, s.vis_out, it, kb, g, nullptr, smraw);
             else degrid_item<6, float>(s.grid_in, s.coords, s.vis_out, it, kb, g, nullptr, smraw);
