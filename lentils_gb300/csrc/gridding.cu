@@ -322,7 +322,7 @@ static int launch_grid_t(const lentils_plan *p, const typename Prec<R>::C *vis,
         {
             // the default: flush steps from the producers' ballot (warp-private tiles; larger
             // tiles than fit in shared memory fall through to grid_kernel)
-            const size_t smem = grid_rows_smem_bytes<W2, false>(p->geom);
+            const size_t smem = grid_ballot_smem_bytes<W2>(p->geom);
             if (p->grid_variant == 0 && smem <= kMaxGridSmem) {
                 if (int st = set_smem(grid_ballot_kernel<W2>, smem)) return st;
                 grid_ballot_kernel<W2><<<p->nitems, kGridBatch, smem, s>>>(

@@ -336,6 +336,17 @@ __device__ __forceinline__ void grid_flush_extended(const typename Prec<R>::C *s
 
 constexpr int kGridBatch = 256;  // visibilities per weight batch (= threads per CTA)
 constexpr int kRowSkew = 8;      // floats between consecutive groups' weight rows
+template <int W2>
+constexpr int kBallotRowStride = 2 * W2 + 8;  // floats per row of the ballot gridder
+// Floats between consecutive groups' rows in the ballot gridder: the groups of a warp read
+// their rows in the same instruction, so group g's rows start 8g (4g when more than four
+// groups share a warp) banks later, modulo 32.
+template <int W2>
+constexpr int ballot_group_skew()
+{
+    const int want = (32 / W2 <= 4) ? 8 : 4;
+    return ((want - (W2 * kBallotRowStride<W2>) % 32) % 32 + 32) % 32;
+}
 
 // Row-owner gridding (the default for float). The work item's sorted visibilities are split
 // into NG = 8 warps x G contiguous ranges, one per group of 2w lanes (G = 32/(2w) groups per
@@ -598,7 +609,12 @@ __device__ __forceinline__ void grid_rows_item(const float2 *__restrict__ vis,
 // which its group must flush. Rows past the end of a range carry x = 0 and never flush, so the
 // consumers run every step unconditionally and read no keys; the cell to flush is read from
 // the row before the flush step. Flushes take turns among the groups that flush at the same
-// step, as in grid_rows_item. smraw: grid_rows_smem_bytes<W2, false>(g).
+// step, as in grid_rows_item.
+// The register sums pair taps rather than real and imaginary parts: accr[q] holds the real
+// parts of taps 2q and 2q+1, acci[q] their imaginary parts, so a packed FMA takes the two
+// taps' v-weights straight from the row (an aligned pair) and the value's real or imaginary
+// part, which the producer stores twice, (re, re, im, im): no operand is duplicated per tap.
+// smraw: grid_ballot_smem_bytes<W2>(g).
 template <int W2>
 __device__ __forceinline__ void grid_rows_item_ballot(const float2 *__restrict__ vis,
                                                       const uint2 *__restrict__ coords,
@@ -606,7 +622,8 @@ __device__ __forceinline__ void grid_rows_item_ballot(const float2 *__restrict__
                                                       const WorkItem &it, const KBPoly &kb,
                                                       const GridGeom &g, unsigned char *smraw)
 {
-    constexpr int STR = 2 * W2 + 4;
+    static_assert((W2 % 2) == 0, "taps in pairs");
+    constexpr int STR = kBallotRowStride<W2>;  // [wv | wu | re re im im | key, 3 pad]
     constexpr int G = 32 / W2;              // groups per warp
     constexpr int NW = kGridBatch / 32;
     constexpr int NG = NW * G;
@@ -628,38 +645,51 @@ __device__ __forceinline__ void grid_rows_item_ballot(const float2 *__restrict__
     const int rbeg = min(it.count, gid * L), rend = lane_on ? min(it.count, rbeg + L) : rbeg;
     const int nbatch = (L + SHARE - 1) / SHARE;
     const unsigned gmask = ((1u << W2) - 1u) << (grp * W2);
-    const float *rowg = rows + gid * (SHARE * STR + kRowSkew);  // row st at rowg + st * STR
-    float *myrow = rows + gid * (SHARE * STR + kRowSkew) + ri * STR;  // produced by this lane
+    constexpr int GSTR = SHARE * STR + ballot_group_skew<W2>();  // floats per group of rows
+    const float *rowg = rows + gid * GSTR;  // row st at rowg + st * STR
+    float *myrow = rows + gid * GSTR + ri * STR;  // produced by this lane
 
-    float2 acc[W2];
+    float2 accr[W2 / 2], acci[W2 / 2];
 #pragma unroll
-    for (int j = 0; j < W2; ++j) acc[j] = make_float2(0.f, 0.f);
+    for (int q = 0; q < W2 / 2; ++q) {
+        accr[q] = make_float2(0.f, 0.f);
+        acci[q] = make_float2(0.f, 0.f);
+    }
     int plast = -1;  // cell of the group's last valid row so far (-1: none)
     auto flush_to = [&](int cell) {
         float2 *p = mytile + ((cell >> 6) + 1 + ri) * S + (cell & 63) + 1;
 #pragma unroll
-        for (int j = 0; j < W2; ++j) {
-            p[j] = __fadd2_rn(p[j], acc[j]);
-            acc[j] = make_float2(0.f, 0.f);
+        for (int q = 0; q < W2 / 2; ++q) {
+            float2 a = p[2 * q], b = p[2 * q + 1];
+            a.x += accr[q].x;
+            a.y += acci[q].x;
+            b.x += accr[q].y;
+            b.y += acci[q].y;
+            p[2 * q] = a;
+            p[2 * q + 1] = b;
+            accr[q] = make_float2(0.f, 0.f);
+            acci[q] = make_float2(0.f, 0.f);
         }
     };
     auto consume = [&](const float *row) {
-        const float2 x = reinterpret_cast<const float2 *>(row + 2 * W2)[0];
+        const float4 xx = reinterpret_cast<const float4 *>(row + 2 * W2)[0];  // re re im im
         const float wui = row[W2 + ri];
-        const float2 t = make_float2(wui * x.x, wui * x.y);
-        float wv[W2];
+        const float2 w2 = make_float2(wui, wui);
+        const float2 tr = __fmul2_rn(w2, make_float2(xx.x, xx.y));
+        const float2 ti = __fmul2_rn(w2, make_float2(xx.z, xx.w));
 #pragma unroll
         for (int q = 0; q < W2 / 4; ++q) {
             const float4 v4 = reinterpret_cast<const float4 *>(row)[q];
-            wv[4 * q] = v4.x;
-            wv[4 * q + 1] = v4.y;
-            wv[4 * q + 2] = v4.z;
-            wv[4 * q + 3] = v4.w;
+            accr[2 * q] = __ffma2_rn(make_float2(v4.x, v4.y), tr, accr[2 * q]);
+            acci[2 * q] = __ffma2_rn(make_float2(v4.x, v4.y), ti, acci[2 * q]);
+            accr[2 * q + 1] = __ffma2_rn(make_float2(v4.z, v4.w), tr, accr[2 * q + 1]);
+            acci[2 * q + 1] = __ffma2_rn(make_float2(v4.z, v4.w), ti, acci[2 * q + 1]);
         }
-#pragma unroll
-        for (int j = (W2 / 4) * 4; j < W2; ++j) wv[j] = row[j];
-#pragma unroll
-        for (int j = 0; j < W2; ++j) acc[j] = __ffma2_rn(f2(wv[j]), t, acc[j]);
+        if constexpr ((W2 % 4) != 0) {  // the last pair of taps
+            const float2 v2 = reinterpret_cast<const float2 *>(row)[W2 / 2 - 1];
+            accr[W2 / 2 - 1] = __ffma2_rn(v2, tr, accr[W2 / 2 - 1]);
+            acci[W2 / 2 - 1] = __ffma2_rn(v2, ti, acci[W2 / 2 - 1]);
+        }
     };
     uint2 cpre = make_uint2(0u, 0u);
     float2 xpre = make_float2(0.f, 0.f);
@@ -697,8 +727,8 @@ __device__ __forceinline__ void grid_rows_item_ballot(const float2 *__restrict__
 #pragma unroll
                 for (int i = 0; i < W2; ++i) myrow[W2 + i] = wu[i];
                 key = valid ? ((lu << 6) | lv) : -1;
-                reinterpret_cast<float4 *>(myrow + 2 * W2)[0] =
-                    make_float4(x.x, x.y, __int_as_float(key), 0.f);
+                reinterpret_cast<float4 *>(myrow + 2 * W2)[0] = make_float4(x.x, x.x, x.y, x.y);
+                myrow[2 * W2 + 4] = __int_as_float(key);
             }
             if (valid && ((c.x | c.y) & kExtraTapBit))  // rare: straight into the warp's tile
                 grid_extra_taps<W2, float>(mytile, S, lu, lv, c, wu, wv, kb.edge, x);
@@ -726,7 +756,7 @@ __device__ __forceinline__ void grid_rows_item_ballot(const float2 *__restrict__
                 while (gm) {  // groups that flush here, one at a time
                     const int g0 = (__ffs(gm) - 1) / W2;
                     if (need && grp == g0)  // the cell being left: the row before's
-                        flush_to(st > 0 ? __float_as_int(rowg[(st - 1) * STR + 2 * W2 + 2])
+                        flush_to(st > 0 ? __float_as_int(rowg[(st - 1) * STR + 2 * W2 + 4])
                                         : cell0);
                     __syncwarp();
                     gm &= ~(((1u << W2) - 1u) << (g0 * W2));
@@ -750,6 +780,16 @@ __device__ __forceinline__ void grid_rows_item_ballot(const float2 *__restrict__
     }
     __syncthreads();
     grid_flush_extended<W2, float>(tiles, grid, it, g);
+}
+
+template <int W2>
+__host__ __device__ inline size_t grid_ballot_smem_bytes(const GridGeom &g)
+{
+    const size_t tile_bytes =
+        ((sizeof(float2) * (kGridBatch / 32) * g.E * g.stride) + 15) & ~size_t(15);
+    const size_t ngroups = (kGridBatch / 32) * (32 / W2);
+    return tile_bytes +
+           sizeof(float) * (ngroups * ((size_t)W2 * kBallotRowStride<W2> + ballot_group_skew<W2>()));
 }
 
 template <int W2, bool SHARED = false>

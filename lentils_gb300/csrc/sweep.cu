@@ -247,7 +247,7 @@ int lentils_sweep_create(lentils_sweep **out, const lentils_sweep_sample *in, in
         sw->zero.push_back({d.grid_out, gbytes});
         sw->total_vis += p->nvis;
         sw->algorithmic_bytes += 2.0 * (16.0 * (double)p->nvis + (double)gbytes);
-        smem = std::max(smem, w2 == 8 ? grid_rows_smem_bytes<8>(p->geom) : grid_rows_smem_bytes<6>(p->geom));
+        smem = std::max(smem, w2 == 8 ? grid_ballot_smem_bytes<8>(p->geom) : grid_ballot_smem_bytes<6>(p->geom));
         smem = std::max(smem, degrid_smem_bytes<float>(p->geom));
         std::vector<WorkItem> hitems(p->nitems);
         if (p->nitems > 0) {
