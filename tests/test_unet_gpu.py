@@ -177,18 +177,22 @@ def test_unet_backward_external_gradient_matches_mse_path(native):
     assert _rel(g_ext, g_mse) < 1e-3
 
 
-def test_trained_network_gains_over_jacobi(native):
+def test_trained_network_in_flexible_cg(native):
     """What the trained network (the committed weights, trained on the GPU by
-    train_preconditioner) gains over the method without it on the 128^2 source inversion,
-    used with the deployment policy stored beside it:
-    - on windowed flexible-CG pairs from lens draws it was not trained on, its direction (with
-      the Jacobi share it was trained with) removes a larger share of the A-norm error per step
-      than the Jacobi direction, after the A-orthogonalisation flexible CG applies;
-    - on the workload inversion, flexible CG with it needs at most a third of the iterations
-      of plain Jacobi-CG to a true relative residual of 1e-6;
-    - on held-out lens draws that gain does not carry over (plain Jacobi-CG is often as fast),
-      but the descent check and the stagnation fallback keep the solver within twice plain
-      Jacobi-CG's iterations."""
+    train_preconditioner) gains, and does not gain, on the 128^2 source inversion, used with
+    the deployment policy stored beside it. The fair comparison is flexible CG with the same
+    8-direction window and Jacobi directions only: in exact arithmetic that is Jacobi-PCG, and
+    it needs about the iterations of Jacobi-PCG with FP64 vectors.
+    - Per step, on windowed flexible-CG pairs from lens draws it was not trained on, its
+      direction (with the Jacobi share it was trained with) removes a larger share of the
+      A-norm error than the Jacobi direction, after the A-orthogonalisation flexible CG applies.
+    - On the workload inversion the learned solver stays within 1.5x of Jacobi flexible CG's
+      iterations, and both windowed solvers need at most a third of the iterations of plain
+      Jacobi-CG with FP32 inner solves (which lose conjugacy).
+    - On held-out lens draws the per-step gain does not carry over: the learned solver can
+      need more than twice the iterations of Jacobi flexible CG. The descent check and the
+      stagnation fallback keep it within twice plain Jacobi-CG's iterations, and every solve
+      reaches the true relative residual of 1e-6."""
     from lentils_gb300 import learned, workloads
     from lentils_gb300 import train_preconditioner as T
     from lentils_gb300.inversion import SourceInversion
@@ -224,12 +228,17 @@ def test_trained_network_gains_over_jacobi(native):
         problems.append(SourceInversion(vs, d, 1.0, ims, srcs, glm, workloads.Z_SRC,
                                         workloads.LAMBDA, nufft=F))
     for k, p in enumerate(problems):
-        _, plain = p.solve(tol=1e-6, inner_tol=1e-3)
+        _, jac = p.solve_flexible(None, tol=1e-6, inner_tol=1e-3, window=pol["window"])
         _, lrn = p.solve_flexible(pnet, tol=1e-6, inner_tol=1e-3, window=pol["window"],
                                   net_every=pol["net_every"])
-        assert plain["converged"] == 1 and lrn["converged"] == 1, (k, plain, lrn)
+        _, plain = p.solve(tol=1e-6, inner_tol=1e-3)
+        for info in (jac, lrn, plain):
+            assert info["converged"] == 1 and info["rel_residual"] <= 1e-6, (k, jac, lrn, plain)
         assert lrn["net_iterations"] > 0, (k, lrn)
+        assert jac["inner_total"] <= plain["inner_total"], (k, jac, plain)
         if k == 0:
-            assert 3 * lrn["inner_total"] <= plain["inner_total"], (k, lrn, plain)
+            assert lrn["inner_total"] <= 1.5 * jac["inner_total"], (k, lrn, jac)
+            assert 3 * max(lrn["inner_total"], jac["inner_total"]) <= plain["inner_total"], \
+                (lrn, jac, plain)
         else:
             assert lrn["inner_total"] <= 2 * plain["inner_total"] + 50, (k, lrn, plain)
