@@ -207,20 +207,26 @@ int lentils_plan_create(lentils_plan **plan, const lentils_grid_desc *grid, cons
                         void *stream);
 int lentils_plan_destroy(lentils_plan *plan);
 int lentils_plan_get_stats(const lentils_plan *plan, lentils_plan_stats *stats);
-/* Tuning: the gridding kernel's work split. 0 (default): lanes own window rows, 32/(2w)
- * visibilities side by side per warp, warp-private tiles, flushes taking turns only among the
- * groups that flush; the flush steps are found by the lanes that produce the batch's rows (one
- * warp ballot per batch); 1: lanes own taps, one visibility
- * per warp; 2: two visibilities per warp; 3: as 8 with one tile per CTA flushed by
- * shared-memory atomics and cell changes checked at every step; 4: as 8 with cell changes
- * checked at every step and flush turns for every group; 5: as 8 with flushes by shared-memory
- * atomics, no turns; 6: as 5 into one tile per CTA; 7: as 8 with compensated (Kahan) register
- * sums; 8: as 0 with every consumer lane reading its group's cell keys and marking the
- * batch's flush steps itself. Tiles too large for the warp-private copies fall back to 1. All
- * give the same result up to FP32 summation order. */
+/* Tuning: the gridding kernel's work split. Every form gives the same result up to FP32
+ * summation order.
+ *  0 (default): lanes own window rows: 32/(2w) visibilities side by side per warp, each lane
+ *     summing its 2w + 1 taps in registers while its group's sorted visibilities stay in one
+ *     pair of cells (lu, 2m), (lu, 2m + 1); weights produced by the group's own lanes, warp-
+ *     local batches, warp-private tiles, flushes taking turns only among the groups that
+ *     flush, 4 warps per CTA;
+ *  1: lanes own taps, one visibility per warp; 2: two visibilities per warp;
+ *  3: as 8 with one tile per CTA flushed by shared-memory atomics, cell changes checked at
+ *     every step; 4: as 8 with cell changes checked at every step and flush turns for every
+ *     group; 5: as 8 with flushes by shared-memory atomics; 6: as 5 into one tile per CTA;
+ *  7: as 8 with compensated (Kahan) register sums; 8: row owners with a CTA-wide weight batch
+ *     and per-group flush masks; 9: as 0 with one-cell windows, CTA barriers per batch and
+ *     8 warps per CTA; 10: as 0 with one-cell windows; 11: as 0 with 8 warps per CTA.
+ * Tiles too large for the warp-private copies fall back to 8, then to 1. */
 int lentils_plan_set_grid_variant(lentils_plan *plan, int variant);
-/* Tuning: the degridding kernel's shared-memory layout. 0 (default): one cell per element;
- * 1 (even 2w): the staged tile holds overlapping column pairs (16-byte loads, two taps each).
+/* Tuning: the degridding kernel's form. 0 (default): a thread takes up to 4 sorted visibilities
+ * of one cell and reads each window row from shared memory once for all of them (2w <= 8;
+ * wider kernels use 2); 1 (even 2w): one visibility per thread, the staged tile holding
+ * overlapping column pairs (16-byte loads, two taps each); 2: one visibility per thread.
  * Identical results. */
 int lentils_plan_set_degrid_variant(lentils_plan *plan, int variant);
 

@@ -139,6 +139,13 @@ struct lentils_plan {
     int *iperm;           // user index -> plan index (host-buffer forms)
     float2 *phase;        // s * e^{-i phi} per visibility (plan order)
     lentils::WorkItem *items;
+    // same-cell chunks (degridding): runs of visibilities in one cell, cut into pieces of at
+    // most chunk_k; chunk c covers plan indices [chunk_begin[c], chunk_begin[c + 1]), and work
+    // item i covers chunks [item_chunks[i].x, item_chunks[i].y). Null when not built.
+    int *chunk_begin;
+    int2 *item_chunks;
+    int chunk_k;
+    long long nchunks;
     long long device_bytes;
     // staging for the host-buffer forms (allocated on first use)
     void *stage_vis64;    // nvis c128

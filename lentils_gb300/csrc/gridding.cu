@@ -24,6 +24,7 @@
 // (2w regular taps) plus, when g is (within FP64) an integer, floor(g)-w at argument +w. The
 // plan records that extra tap, and the rare exclusion of the top tap, as flag bits decided in
 // FP64; the extra tap (weight I0(0)/(2w)) runs on a separate, rarely taken path.
+#include <algorithm>
 #include <type_traits>
 
 #include "common.cuh"
@@ -225,11 +226,37 @@ __global__ void degrid_pair_kernel(const float2 *__restrict__ grid,
                                    const __grid_constant__ KBPoly kb, const GridGeom g,
                                    const float *__restrict__ vscale);
 
+constexpr int kChunkThreads = 128;
+
+template <int W2, int K>
+__global__ void __launch_bounds__(kChunkThreads, 4)
+    degrid_chunk_kernel(const float2 *__restrict__ grid, const uint2 *__restrict__ coords,
+                        float2 *__restrict__ out, const WorkItem *__restrict__ items,
+                        const int2 *__restrict__ item_chunks, const int *__restrict__ chunk_begin,
+                        const __grid_constant__ KBPoly kb, const GridGeom g,
+                        const float *__restrict__ vscale)
+{
+    extern __shared__ __align__(16) unsigned char smraw[];
+    degrid_item_chunks<W2, K>(grid, coords, out, items[blockIdx.x], item_chunks[blockIdx.x],
+                              chunk_begin, kb, g, smraw, vscale);
+}
+
 template <int W2, typename R>
 static int launch_degrid_t(const lentils_plan *p, const typename Prec<R>::C *grid,
                            typename Prec<R>::C *vis, cudaStream_t s, const R *vscale)
 {
     const GridGeom &g = p->geom;
+    if constexpr (std::is_same<R, float>::value && W2 <= 8) {
+        if (p->degrid_variant == 0 && p->chunk_begin && p->chunk_k == 4) {  // the default
+            const size_t smem = sizeof(float2) * (size_t)g.E * g.stride;
+            if (int st = set_smem(degrid_chunk_kernel<W2, 4>, smem)) return st;
+            degrid_chunk_kernel<W2, 4><<<p->nitems, kChunkThreads, smem, s>>>(
+                grid, p->coords, vis, p->items, p->item_chunks, p->chunk_begin, p->kb, g,
+                vscale);
+            LENTILS_CHECK_LAUNCH("degrid_chunk_kernel");
+            return LENTILS_OK;
+        }
+    }
     if constexpr (std::is_same<R, float>::value && (W2 % 2) == 0) {
         if (p->degrid_variant == 1) {
             const size_t smem = degrid_pair_smem_bytes(g);
@@ -270,6 +297,58 @@ __global__ void __launch_bounds__(kGridBatch)
     grid_rows_item_ballot<W2>(vis, coords, grid, items[blockIdx.x], kb, g, smraw);
 }
 
+constexpr size_t kMaxGridSmem = 200 * 1024;
+
+template <int W2, int NW>
+__global__ void __launch_bounds__(NW * 32)
+    grid_local_kernel(const float2 *__restrict__ vis, const uint2 *__restrict__ coords,
+                      float2 *__restrict__ grid, const WorkItem *__restrict__ items,
+                      const __grid_constant__ KBPoly kb, const GridGeom g)
+{
+    extern __shared__ __align__(16) unsigned char smraw[];
+    grid_rows_item_local<W2, NW>(vis, coords, grid, items[blockIdx.x], kb, g, smraw);
+}
+
+template <int W2, int NW, bool NARROW>
+__global__ void __launch_bounds__(NW * 32)
+    grid_pairs_kernel(const float2 *__restrict__ vis, const uint2 *__restrict__ coords,
+                      float2 *__restrict__ grid, const WorkItem *__restrict__ items,
+                      const __grid_constant__ KBPoly kb, const GridGeom g)
+{
+    extern __shared__ __align__(16) unsigned char smraw[];
+    grid_rows_item_pairs<W2, NW, NARROW>(vis, coords, grid, items[blockIdx.x], kb, g, smraw);
+}
+
+template <int W2, int NW, bool NARROW = false>
+static int launch_grid_pairs(const lentils_plan *p, const float2 *vis, float2 *grid,
+                             cudaStream_t s, bool *done)
+{
+    *done = false;
+    const size_t smem = grid_pairs_smem_bytes<W2, NW>(p->geom);
+    if (smem > kMaxGridSmem) return LENTILS_OK;
+    if (int st = set_smem(grid_pairs_kernel<W2, NW, NARROW>, smem)) return st;
+    grid_pairs_kernel<W2, NW, NARROW><<<p->nitems, NW * 32, smem, s>>>(
+        vis, p->coords, grid, p->items, p->kb, p->geom);
+    LENTILS_CHECK_LAUNCH("grid_pairs_kernel");
+    *done = true;
+    return LENTILS_OK;
+}
+
+template <int W2, int NW>
+static int launch_grid_local(const lentils_plan *p, const float2 *vis, float2 *grid,
+                             cudaStream_t s, bool *done)
+{
+    *done = false;
+    const size_t smem = grid_local_smem_bytes<W2, NW>(p->geom);
+    if (smem > kMaxGridSmem) return LENTILS_OK;
+    if (int st = set_smem(grid_local_kernel<W2, NW>, smem)) return st;
+    grid_local_kernel<W2, NW><<<p->nitems, NW * 32, smem, s>>>(vis, p->coords, grid, p->items,
+                                                              p->kb, p->geom);
+    LENTILS_CHECK_LAUNCH("grid_local_kernel");
+    *done = true;
+    return LENTILS_OK;
+}
+
 template <int W2>
 __global__ void __launch_bounds__(256)
     degrid_pair_kernel(const float2 *__restrict__ grid, const uint2 *__restrict__ coords,
@@ -281,7 +360,6 @@ __global__ void __launch_bounds__(256)
     degrid_item_pair<W2>(grid, coords, out, items[blockIdx.x], kb, g, smraw, vscale);
 }
 
-constexpr size_t kMaxGridSmem = 200 * 1024;
 
 template <int W2, int V, bool PRIV, typename R>
 static size_t grid_smem_bytes(const GridGeom &g)
@@ -319,11 +397,28 @@ static int launch_grid_t(const lentils_plan *p, const typename Prec<R>::C *vis,
                          typename Prec<R>::C *grid, cudaStream_t s)
 {
     if constexpr (std::is_same<R, float>::value && (W2 % 2) == 0) {
-        {
-            // the default: flush steps from the producers' ballot (warp-private tiles; larger
-            // tiles than fit in shared memory fall through to grid_kernel)
+        if (p->grid_variant == 0 || p->grid_variant == 11) {
+            // the default: column-pair register windows, warp-local batches, 4 warps per CTA
+            // (tiles too large for the warp-private copies fall through)
+            bool done = false;
+            const int st = p->grid_variant == 0
+                               ? launch_grid_pairs<W2, 4>(p, vis, grid, s, &done)
+                               : launch_grid_pairs<W2, 8>(p, vis, grid, s, &done);
+            if (st || done) return st;
+        }
+        if (p->grid_variant == 10) {
+            bool done = false;
+            const int st = launch_grid_local<W2, 4>(p, vis, grid, s, &done);
+            if (st || done) return st;
+        }
+        if (p->grid_variant == 12) {
+            bool done = false;
+            const int st = launch_grid_pairs<W2, 4, true>(p, vis, grid, s, &done);
+            if (st || done) return st;
+        }
+        if (p->grid_variant == 9) {  // flush steps from the producers' ballot, CTA barriers
             const size_t smem = grid_ballot_smem_bytes<W2>(p->geom);
-            if (p->grid_variant == 0 && smem <= kMaxGridSmem) {
+            if (smem <= kMaxGridSmem) {
                 if (int st = set_smem(grid_ballot_kernel<W2>, smem)) return st;
                 grid_ballot_kernel<W2><<<p->nitems, kGridBatch, smem, s>>>(
                     vis, p->coords, grid, p->items, p->kb, p->geom);

@@ -104,22 +104,15 @@ __device__ __forceinline__ int tap_parity(const WorkItem &it, const GridGeom &g,
     return (it.tu * g.T - g.Hu + lu - g.w + 1 + it.tv * g.T - g.Hv + lv - g.w + 1) & 1;
 }
 
-// Degridding of one work item by the whole CTA (any block size); smraw: E x stride cells.
-// vscale (optional, plan order): each output is multiplied by its factor (the data weights of
-// a normal operator, applied here instead of in a separate pass).
+// The work item's extended tile (T + 2w cells square, row stride g.stride) gathered from the
+// stored half-plane grid by the whole CTA, with the wrap and the Hermitian fold applied
+// (folded cells conjugated), so that the degridding loops read a plain full-plane patch.
 template <int W2, typename R>
-__device__ __forceinline__ void degrid_item(const typename Prec<R>::C *__restrict__ grid,
-                                            const uint2 *__restrict__ coords,
-                                            typename Prec<R>::C *__restrict__ out,
-                                            const WorkItem &it,
-                                            const typename Prec<R>::Table &kb, const GridGeom &g,
-                                            const float2 *__restrict__ cres,
-                                            unsigned char *smraw,
-                                            const R *__restrict__ vscale = nullptr)
+__device__ __forceinline__ void stage_extended_tile(const typename Prec<R>::C *__restrict__ grid,
+                                                    const WorkItem &it, const GridGeom &g,
+                                                    typename Prec<R>::C *sm)
 {
-    using P = Prec<R>;
-    using C = typename P::C;
-    C *sm = reinterpret_cast<C *>(smraw);
+    using C = typename Prec<R>::C;
     constexpr int w = W2 / 2;
     const int a0 = it.tu * g.T - g.Hu - w;  // canonical index of extended row 0
     const int b0 = it.tv * g.T - g.Hv - w;
@@ -139,6 +132,26 @@ __device__ __forceinline__ void degrid_item(const typename Prec<R>::C *__restric
         }
         sm[ea * S + eb] = val;
     }
+}
+
+// Degridding of one work item by the whole CTA (any block size); smraw: E x stride cells.
+// vscale (optional, plan order): each output is multiplied by its factor (the data weights of
+// a normal operator, applied here instead of in a separate pass).
+template <int W2, typename R>
+__device__ __forceinline__ void degrid_item(const typename Prec<R>::C *__restrict__ grid,
+                                            const uint2 *__restrict__ coords,
+                                            typename Prec<R>::C *__restrict__ out,
+                                            const WorkItem &it,
+                                            const typename Prec<R>::Table &kb, const GridGeom &g,
+                                            const float2 *__restrict__ cres,
+                                            unsigned char *smraw,
+                                            const R *__restrict__ vscale = nullptr)
+{
+    using P = Prec<R>;
+    using C = typename P::C;
+    C *sm = reinterpret_cast<C *>(smraw);
+    const int S = g.stride;
+    stage_extended_tile<W2, R>(grid, it, g, sm);
     __syncthreads();
 
     for (int k = threadIdx.x; k < it.count; k += blockDim.x) {
@@ -271,6 +284,141 @@ __device__ __forceinline__ void degrid_item_pair(const float2 *__restrict__ grid
             acc.y *= sc;
         }
         out[it.begin + k] = acc;
+    }
+}
+
+template <int W2, int K>
+__device__ __forceinline__ void degrid_chunks_from_tile(const uint2 *__restrict__ coords,
+                                                        float2 *__restrict__ out,
+                                                        const WorkItem &it, int2 crange,
+                                                        const int *__restrict__ chunk_begin,
+                                                        const KBPoly &kb, const GridGeom &g,
+                                                        const float2 *sm,
+                                                        const float *__restrict__ vscale);
+
+// Degridding by same-cell chunks (the default for float, 2w <= 8). A thread takes one chunk:
+// up to K consecutive sorted visibilities of one cell (the plan's chunk_begin). It evaluates
+// the K visibilities' weights, then reads each of the 2w rows of the cell's window from the
+// staged tile once, into registers, and applies it to all K visibilities. So a tap is read
+// from shared memory once per chunk instead of once per visibility: (2w)^2 / K loads per
+// visibility slot, where the per-visibility kernel's shared-memory reads bound its time.
+// Slots past the chunk's end repeat its last visibility and are not stored. Per visibility the
+// arithmetic, and its order, is that of degrid_item<W2, float>: the results are identical.
+template <int W2, int K>
+__device__ __forceinline__ void degrid_item_chunks(const float2 *__restrict__ grid,
+                                                   const uint2 *__restrict__ coords,
+                                                   float2 *__restrict__ out, const WorkItem &it,
+                                                   int2 crange,
+                                                   const int *__restrict__ chunk_begin,
+                                                   const KBPoly &kb, const GridGeom &g,
+                                                   unsigned char *smraw,
+                                                   const float *__restrict__ vscale = nullptr)
+{
+    float2 *sm = reinterpret_cast<float2 *>(smraw);
+    stage_extended_tile<W2, float>(grid, it, g, sm);
+    __syncthreads();
+    degrid_chunks_from_tile<W2, K>(coords, out, it, crange, chunk_begin, kb, g, sm, vscale);
+}
+
+// The same-cell chunks of one work item from its extended tile, already staged in sm. The
+// coordinates of a thread's next chunk and the bounds of the one after are loaded while this
+// one is evaluated.
+template <int W2, int K>
+__device__ __forceinline__ void degrid_chunks_from_tile(const uint2 *__restrict__ coords,
+                                                        float2 *__restrict__ out,
+                                                        const WorkItem &it, int2 crange,
+                                                        const int *__restrict__ chunk_begin,
+                                                        const KBPoly &kb, const GridGeom &g,
+                                                        const float2 *sm,
+                                                        const float *__restrict__ vscale)
+{
+    const int S = g.stride;
+    const int B = blockDim.x;
+    // chunk c + B's bounds were loaded one iteration ago and its coordinates are loaded now;
+    // chunk c + 2B's bounds are loaded now: no load waits on another within an iteration
+    int nb0 = 0, nb1 = 1, fb0 = 0, fb1 = 1;
+    uint2 ncs[K];
+    auto load_coords = [&](int cc) {
+        if (cc < crange.y) {
+#pragma unroll
+            for (int q = 0; q < K; ++q) ncs[q] = coords[nb0 + min(q, nb1 - nb0 - 1)];
+        }
+    };
+    auto load_bounds = [&](int cc) {
+        if (cc < crange.y) {
+            fb0 = chunk_begin[cc];
+            fb1 = chunk_begin[cc + 1];
+        }
+    };
+    const int c0 = crange.x + (int)threadIdx.x;
+    load_bounds(c0);
+    nb0 = fb0;
+    nb1 = fb1;
+    load_coords(c0);
+    load_bounds(c0 + B);
+    for (int c = c0; c < crange.y; c += B) {
+        const int b0 = nb0;
+        const int n = nb1 - nb0;
+        uint2 cs[K];
+#pragma unroll
+        for (int q = 0; q < K; ++q) cs[q] = ncs[q];
+        nb0 = fb0;
+        nb1 = fb1;
+        load_coords(c + B);
+        load_bounds(c + 2 * B);
+        const int lu = cell_of(cs[0].x), lv = cell_of(cs[0].y);
+        float wu[K][W2], wv[K][W2];
+#pragma unroll
+        for (int q = 0; q < K; ++q) {
+            kb_weights<W2>(kb, cs[q].x, wu[q]);
+            kb_weights<W2>(kb, cs[q].y, wv[q]);
+        }
+        const float2 *p = sm + (lu + 1) * S + (lv + 1);
+        float2 acc[K];
+#pragma unroll
+        for (int q = 0; q < K; ++q) acc[q] = make_float2(0.f, 0.f);
+#pragma unroll
+        for (int i = 0; i < W2; ++i) {
+            float2 row[W2];
+#pragma unroll
+            for (int j = 0; j < W2; ++j) row[j] = p[i * S + j];
+#pragma unroll
+            for (int q = 0; q < K; ++q) {
+                float2 r = make_float2(0.f, 0.f);
+#pragma unroll
+                for (int j = 0; j < W2; ++j) r = __ffma2_rn(f2(wv[q][j]), row[j], r);
+                acc[q] = __ffma2_rn(f2(wu[q][i]), r, acc[q]);
+            }
+        }
+        const bool neg = tap_parity(it, g, lu, lv);
+#pragma unroll
+        for (int q = 0; q < K; ++q) {
+            if (q >= n) break;
+            const uint2 cq = cs[q];
+            float2 a = acc[q];
+            if ((cq.x | cq.y) & kExtraTapBit) {
+                const float eu = (cq.x & kExtraTapBit) ? kb.edge : 0.f;
+                const float ev = (cq.y & kExtraTapBit) ? kb.edge : 0.f;
+                const float2 *e = sm + lu * S + lv;
+                float2 r = make_float2(0.f, 0.f);
+                for (int j = 0; j < W2; ++j) r = __ffma2_rn(f2(wv[q][j]), e[j + 1], r);
+                r = __ffma2_rn(f2(ev), e[0], r);
+                a = __ffma2_rn(f2(eu), r, a);
+                float2 cs2 = make_float2(0.f, 0.f);
+                for (int i = 0; i < W2; ++i) cs2 = __ffma2_rn(f2(wu[q][i]), e[(i + 1) * S], cs2);
+                a = __ffma2_rn(f2(ev), cs2, a);
+            }
+            if (neg) {
+                a.x = -a.x;
+                a.y = -a.y;
+            }
+            if (vscale) {
+                const float sc = vscale[b0 + q];
+                a.x *= sc;
+                a.y *= sc;
+            }
+            out[b0 + q] = a;
+        }
     }
 }
 
@@ -780,6 +928,512 @@ __device__ __forceinline__ void grid_rows_item_ballot(const float2 *__restrict__
     }
     __syncthreads();
     grid_flush_extended<W2, float>(tiles, grid, it, g);
+}
+
+// Tile stride of the warp-local gridder, in float2: at least E + 1 (a flush of a window at an
+// odd column reads and writes one cell past it) and 2 modulo 4, so that a row's 16-byte
+// alignment depends on its column alone and the 8 rows a group flushes at once, 2S = 4 (mod 8)
+// words apart, fall in distinct 16-byte bank quads.
+__host__ __device__ inline int grid_local_stride(int E)
+{
+    const int s = E + 1;
+    return s + ((2 - (s & 3)) & 3);
+}
+template <int W2>
+constexpr int kLocalRowStride = 2 * W2 + 4;  // [wv | wu | re, im, key, pad]
+template <int W2>
+constexpr int local_group_skew()
+{
+    const int want = (32 / W2 <= 4) ? 8 : 4;
+    return ((want - (W2 * kLocalRowStride<W2>) % 32) % 32 + 32) % 32;
+}
+
+// Row-owner gridding with warp-local synchronisation (the default for float). The data flow
+// of grid_rows_item_ballot -- lane i of a group of 2w lanes owns window row i and sums its 2w
+// taps in registers while the group's sorted visibilities stay in one cell; the group's rows
+// [wv | wu | x, key] are produced by the group's own lanes; the flush steps come from one warp
+// ballot per batch -- with these differences:
+// * producers and consumers of a row are lanes of one warp, so a batch needs two __syncwarp
+//   and no CTA barrier: warps run their batches independently and wait for each other only
+//   at the end of the work item, when the warp-private tiles are summed;
+// * each tap's sum is one (re, im) register pair, updated by a packed FMA with the scalar
+//   v-weight, and added to the tile by packed adds;
+// * the tile stride makes a flushed window row 16-byte aligned or one cell off it, so a flush
+//   is w (aligned) or w + 1 (odd column) 16-byte read-modify-writes per lane, not 2w 8-byte
+//   ones.
+// Flushes take turns among the groups of a warp that flush at the same step, as before.
+// smraw: grid_local_smem_bytes<W2>(g).
+template <int W2, int NW = 8>
+__device__ __forceinline__ void grid_rows_item_local(const float2 *__restrict__ vis,
+                                                     const uint2 *__restrict__ coords,
+                                                     float2 *__restrict__ grid,
+                                                     const WorkItem &it, const KBPoly &kb,
+                                                     const GridGeom &gin, unsigned char *smraw)
+{
+    static_assert((W2 % 2) == 0, "taps in pairs");
+    constexpr int STR = kLocalRowStride<W2>;
+    constexpr int G = 32 / W2;
+    constexpr int NG = NW * G;
+    constexpr int SHARE = W2;
+    static_assert((STR % 4) == 0, "rows stay 16-byte aligned");
+    GridGeom g = gin;
+    g.stride = grid_local_stride(g.E);
+    const int E = g.E, S = g.stride;
+    float2 *tiles = reinterpret_cast<float2 *>(smraw);
+    const size_t tile_bytes = ((sizeof(float2) * (size_t)NW * E * S) + 15) & ~size_t(15);
+    float *rows = reinterpret_cast<float *>(smraw + tile_bytes);
+
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    float2 *mytile = tiles + warp * E * S;
+    {
+        float4 *t4 = reinterpret_cast<float4 *>(mytile);  // E*S even, base 16-byte aligned
+        for (int e = lane; e < (E * S) / 2; e += 32) t4[e] = make_float4(0.f, 0.f, 0.f, 0.f);
+    }
+    const bool lane_on = lane < G * W2;
+    const int grp = lane_on ? lane / W2 : G - 1;
+    const int ri = lane_on ? lane - grp * W2 : 0;
+    const int gid = warp * G + grp;
+    const int L = (it.count + NG - 1) / NG;
+    const int rbeg = min(it.count, gid * L), rend = lane_on ? min(it.count, rbeg + L) : rbeg;
+    const int nbatch = (L + SHARE - 1) / SHARE;
+    const unsigned gmask = ((1u << W2) - 1u) << (grp * W2);
+    constexpr int GSTR = SHARE * STR + local_group_skew<W2>();
+    const float *rowg = rows + gid * GSTR;
+    float *myrow = rows + gid * GSTR + ri * STR;
+
+    float2 acc[W2];
+#pragma unroll
+    for (int j = 0; j < W2; ++j) acc[j] = make_float2(0.f, 0.f);
+    int plast = -1;
+    auto flush_to = [&](int cell) {
+        const int lv = cell & 63;
+        float2 *p = mytile + ((cell >> 6) + 1 + ri) * S + lv + 1;
+        if (lv & 1) {  // lv + 1 even: the row segment starts on a 16-byte boundary
+            float4 *p4 = reinterpret_cast<float4 *>(p);
+#pragma unroll
+            for (int q = 0; q < W2 / 2; ++q) {
+                float4 f = p4[q];
+                const float2 a = __fadd2_rn(make_float2(f.x, f.y), acc[2 * q]);
+                const float2 b = __fadd2_rn(make_float2(f.z, f.w), acc[2 * q + 1]);
+                p4[q] = make_float4(a.x, a.y, b.x, b.y);
+            }
+        } else {  // one cell off: w + 1 pairs starting at the cell before
+            float4 *p4 = reinterpret_cast<float4 *>(p - 1);
+            {
+                const float4 f = p4[0];
+                const float2 b = __fadd2_rn(make_float2(f.z, f.w), acc[0]);
+                p4[0] = make_float4(f.x, f.y, b.x, b.y);
+            }
+#pragma unroll
+            for (int q = 1; q < W2 / 2; ++q) {
+                const float4 f = p4[q];
+                const float2 a = __fadd2_rn(make_float2(f.x, f.y), acc[2 * q - 1]);
+                const float2 b = __fadd2_rn(make_float2(f.z, f.w), acc[2 * q]);
+                p4[q] = make_float4(a.x, a.y, b.x, b.y);
+            }
+            {
+                const float4 f = p4[W2 / 2];
+                const float2 a = __fadd2_rn(make_float2(f.x, f.y), acc[W2 - 1]);
+                p4[W2 / 2] = make_float4(a.x, a.y, f.z, f.w);
+            }
+        }
+#pragma unroll
+        for (int j = 0; j < W2; ++j) acc[j] = make_float2(0.f, 0.f);
+    };
+    // one row's values: value (re, im) and cell, this lane's u-weight, the v-weights
+    struct RowVals {
+        float4 xk;
+        float wui;
+        float wv[W2];
+    };
+    auto load_row = [&](const float *row, RowVals &r) {
+        r.xk = reinterpret_cast<const float4 *>(row + 2 * W2)[0];  // re im key pad
+        r.wui = row[W2 + ri];
+#pragma unroll
+        for (int q = 0; q < W2 / 4; ++q) {
+            const float4 v4 = reinterpret_cast<const float4 *>(row)[q];
+            r.wv[4 * q] = v4.x;
+            r.wv[4 * q + 1] = v4.y;
+            r.wv[4 * q + 2] = v4.z;
+            r.wv[4 * q + 3] = v4.w;
+        }
+        if constexpr ((W2 % 4) != 0) {
+            const float2 v2 = reinterpret_cast<const float2 *>(row)[W2 / 2 - 1];
+            r.wv[W2 - 2] = v2.x;
+            r.wv[W2 - 1] = v2.y;
+        }
+    };
+    auto consume = [&](const RowVals &r) {
+        const float2 t = __fmul2_rn(make_float2(r.wui, r.wui), make_float2(r.xk.x, r.xk.y));
+#pragma unroll
+        for (int j = 0; j < W2; ++j) acc[j] = __ffma2_rn(f2(r.wv[j]), t, acc[j]);
+    };
+    uint2 cpre = make_uint2(0u, 0u);
+    float2 xpre = make_float2(0.f, 0.f);
+    auto prefetch = [&](int bb) {
+        const int kv = rbeg + bb * SHARE + ri;
+        if (bb < nbatch && kv < rend) {
+            cpre = coords[it.begin + kv];
+            xpre = vis[it.begin + kv];
+        }
+    };
+    prefetch(0);
+    for (int b = 0; b < nbatch; ++b) {
+        __syncwarp();  // tile zeroed / the warp's previous batch consumed
+        const int kv = rbeg + b * SHARE + ri;
+        const bool valid = kv < rend;
+        int key = -1;
+        {
+            const uint2 c = cpre;
+            float2 x = xpre;
+            prefetch(b + 1);
+            const int lu = cell_of(c.x), lv = cell_of(c.y);
+            float wt[2 * W2];  // [wv | wu], stored as 16-byte pieces
+            float wu[W2], wv[W2];
+            kb_weights<W2>(kb, c.x, wu);
+            kb_weights<W2>(kb, c.y, wv);
+#pragma unroll
+            for (int j = 0; j < W2; ++j) {
+                wt[j] = wv[j];
+                wt[W2 + j] = wu[j];
+            }
+            const float h = valid ? (tap_parity(it, g, lu, lv) ? -0.5f : 0.5f) : 0.f;
+            x = make_float2(h * x.x, h * x.y);
+            if (lane_on) {
+                float4 *row4 = reinterpret_cast<float4 *>(myrow);
+#pragma unroll
+                for (int q = 0; q < W2 / 2; ++q)
+                    row4[q] = make_float4(wt[4 * q], wt[4 * q + 1], wt[4 * q + 2], wt[4 * q + 3]);
+                key = valid ? ((lu << 6) | lv) : -1;
+                row4[W2 / 2] = make_float4(x.x, x.y, __int_as_float(key), 0.f);
+            }
+            if (valid && ((c.x | c.y) & kExtraTapBit))
+                grid_extra_taps<W2, float>(mytile, S, lu, lv, c, wu, wv, kb.edge, x);
+        }
+        const int up = __shfl_up_sync(0xffffffffu, key, 1);
+        const int cell0 = plast;
+        const int prev = (ri == 0) ? plast : up;
+        const unsigned flags = __ballot_sync(0xffffffffu, valid && prev >= 0 && key != prev);
+        const unsigned nvalid = __popc(__ballot_sync(0xffffffffu, valid) & gmask);
+        const int lastkey = __shfl_sync(0xffffffffu, key, grp * W2 + max((int)nvalid, 1) - 1);
+        if (nvalid) plast = lastkey;
+        unsigned wm = 0;
+#pragma unroll
+        for (int q = 0; q < G; ++q) wm |= flags >> (q * W2);
+        wm &= (1u << W2) - 1u;
+        const unsigned bm = lane_on ? (flags >> (grp * W2)) & ((1u << W2) - 1u) : 0u;
+        __syncwarp();  // the warp's rows are written
+        // rows are read one step ahead of their use (a flush writes only the tile)
+        RowVals cur;
+        if (lane_on) load_row(rowg, cur);
+        int lastcell = cell0;  // the cell of the row consumed last
+#pragma unroll
+        for (int st = 0; st < SHARE; ++st) {
+            RowVals nxt;
+            if (st + 1 < SHARE && lane_on) load_row(rowg + (st + 1) * STR, nxt);
+            if (wm & (1u << st)) {  // warp-uniform
+                const bool need = (bm >> st) & 1u;
+                unsigned gm = __ballot_sync(0xffffffffu, need);
+                while (gm) {  // groups that flush here, one at a time
+                    const int g0 = (__ffs(gm) - 1) / W2;
+                    if (need && grp == g0) flush_to(lastcell);
+                    __syncwarp();
+                    gm &= ~(((1u << W2) - 1u) << (g0 * W2));
+                }
+            }
+            if (lane_on) {
+                consume(cur);
+                lastcell = __float_as_int(cur.xk.z);
+            }
+            if (st + 1 < SHARE) cur = nxt;
+        }
+    }
+#pragma unroll
+    for (int g0 = 0; g0 < G; ++g0) {
+        if (lane_on && grp == g0 && plast >= 0) flush_to(plast);
+        __syncwarp();
+    }
+    __syncthreads();
+    {
+        float4 *t4 = reinterpret_cast<float4 *>(tiles);
+        const int n4 = (E * S) / 2;
+        for (int e = threadIdx.x; e < n4; e += blockDim.x) {  // sum the warps' copies
+            float4 a = t4[e];
+#pragma unroll
+            for (int q = 1; q < NW; ++q) {
+                const float4 bq = t4[q * n4 + e];
+                a.x += bq.x;
+                a.y += bq.y;
+                a.z += bq.z;
+                a.w += bq.w;
+            }
+            t4[e] = a;
+        }
+    }
+    __syncthreads();
+    grid_flush_extended<W2, float>(tiles, grid, it, g);
+}
+
+// Column-pair windows for the warp-local row-owner gridder. The register window of a group
+// spans 2w + 1 columns: the cells (lu, 2m) and (lu, 2m + 1) share it, a visibility in the odd
+// cell adding its 2w taps one column further right. The producer writes the v-weights into the
+// window's 2w + 1 slots at that offset (zero in the other slot), so the consumers run one more
+// packed FMA per visibility and flush only when the pair of cells changes: on the 1e7-
+// visibility workload 0.050 instead of 0.087 flushes per visibility.
+template <int W2>
+constexpr int kPairWinPad = ((W2 + 1) + 3) & ~3;  // window slots, padded to 16 bytes
+// Floats per row [window | re im key pad | wu], a multiple of 4 with an odd number of 16-byte
+// words, so that the 8 rows a group's producers write in one 16-byte store fall in distinct
+// bank quads.
+template <int W2>
+constexpr int pair_row_stride()
+{
+    const int s = (kPairWinPad<W2> + 4 + W2 + 3) & ~3;
+    return ((s / 4) % 2) ? s : s + 4;
+}
+template <int W2>
+constexpr int kPairRowStride = pair_row_stride<W2>();
+template <int W2>
+constexpr int pair_group_skew()
+{
+    const int want = (32 / W2 <= 4) ? 8 : 4;
+    return ((want - (W2 * kPairRowStride<W2>) % 32) % 32 + 32) % 32;
+}
+
+// As grid_rows_item_local, with column-pair windows. smraw: grid_pairs_smem_bytes<W2, NW>(g).
+// NARROW: the consumers read a row with 8-byte loads (and the flushed cell from the producers'
+// registers) instead of 16-byte loads.
+template <int W2, int NW = 8, bool NARROW = false>
+__device__ __forceinline__ void grid_rows_item_pairs(const float2 *__restrict__ vis,
+                                                     const uint2 *__restrict__ coords,
+                                                     float2 *__restrict__ grid,
+                                                     const WorkItem &it, const KBPoly &kb,
+                                                     const GridGeom &gin, unsigned char *smraw)
+{
+    static_assert((W2 % 2) == 0, "even kernel width");
+    constexpr int WC = W2 + 1;              // window columns
+    constexpr int WCP = kPairWinPad<W2>;
+    constexpr int STR = kPairRowStride<W2>;
+    constexpr int G = 32 / W2;
+    constexpr int NG = NW * G;
+    constexpr int SHARE = W2;
+    GridGeom g = gin;
+    g.stride = grid_local_stride(g.E);
+    const int E = g.E, S = g.stride;
+    float2 *tiles = reinterpret_cast<float2 *>(smraw);
+    const size_t tile_bytes = ((sizeof(float2) * (size_t)NW * E * S) + 15) & ~size_t(15);
+    float *rows = reinterpret_cast<float *>(smraw + tile_bytes);
+
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    float2 *mytile = tiles + warp * E * S;
+    {
+        float4 *t4 = reinterpret_cast<float4 *>(mytile);
+        for (int e = lane; e < (E * S) / 2; e += 32) t4[e] = make_float4(0.f, 0.f, 0.f, 0.f);
+    }
+    const bool lane_on = lane < G * W2;
+    const int grp = lane_on ? lane / W2 : G - 1;
+    const int ri = lane_on ? lane - grp * W2 : 0;
+    const int gid = warp * G + grp;
+    const int L = (it.count + NG - 1) / NG;
+    const int rbeg = min(it.count, gid * L), rend = lane_on ? min(it.count, rbeg + L) : rbeg;
+    const int nbatch = (L + SHARE - 1) / SHARE;
+    const unsigned gmask = ((1u << W2) - 1u) << (grp * W2);
+    constexpr int GSTR = SHARE * STR + pair_group_skew<W2>();
+    const float *rowg = rows + gid * GSTR;
+    float *myrow = rows + gid * GSTR + ri * STR;
+
+    float2 acc[WC];
+#pragma unroll
+    for (int j = 0; j < WC; ++j) acc[j] = make_float2(0.f, 0.f);
+    int plast = -1;
+    // window of key `cell` (row lu, even base column): columns base+1 .. base+WC of the tile
+    // row, one float2 past a 16-byte boundary (S even, base + 1 odd)
+    auto flush_to = [&](int cell) {
+        float4 *p4 = reinterpret_cast<float4 *>(mytile + ((cell >> 6) + 1 + ri) * S + (cell & 63));
+        {
+            const float4 f = p4[0];
+            const float2 b = __fadd2_rn(make_float2(f.z, f.w), acc[0]);
+            p4[0] = make_float4(f.x, f.y, b.x, b.y);
+        }
+#pragma unroll
+        for (int q = 1; q <= W2 / 2; ++q) {
+            const float4 f = p4[q];
+            const float2 a = __fadd2_rn(make_float2(f.x, f.y), acc[2 * q - 1]);
+            const float2 b = __fadd2_rn(make_float2(f.z, f.w), acc[2 * q]);
+            p4[q] = make_float4(a.x, a.y, b.x, b.y);
+        }
+#pragma unroll
+        for (int j = 0; j < WC; ++j) acc[j] = make_float2(0.f, 0.f);
+    };
+    struct RowVals {
+        float4 xk;
+        float wui;
+        float wv[WC];
+    };
+    auto load_row = [&](const float *row, RowVals &r) {
+        r.wui = row[WCP + 4 + ri];
+        if constexpr (NARROW) {
+            const float2 x2 = reinterpret_cast<const float2 *>(row + WCP)[0];  // re im
+            r.xk = make_float4(x2.x, x2.y, 0.f, 0.f);
+#pragma unroll
+            for (int q = 0; q < WC / 2; ++q) {
+                const float2 v2 = reinterpret_cast<const float2 *>(row)[q];
+                r.wv[2 * q] = v2.x;
+                r.wv[2 * q + 1] = v2.y;
+            }
+            if constexpr ((WC % 2) != 0) r.wv[WC - 1] = row[WC - 1];
+        } else {
+            r.xk = reinterpret_cast<const float4 *>(row + WCP)[0];  // re im key pad
+#pragma unroll
+            for (int q = 0; q < WCP / 4; ++q) {
+                const float4 v4 = reinterpret_cast<const float4 *>(row)[q];
+                if (4 * q < WC) r.wv[4 * q] = v4.x;
+                if (4 * q + 1 < WC) r.wv[4 * q + 1] = v4.y;
+                if (4 * q + 2 < WC) r.wv[4 * q + 2] = v4.z;
+                if (4 * q + 3 < WC) r.wv[4 * q + 3] = v4.w;
+            }
+        }
+    };
+    auto consume = [&](const RowVals &r) {
+        const float2 t = __fmul2_rn(make_float2(r.wui, r.wui), make_float2(r.xk.x, r.xk.y));
+#pragma unroll
+        for (int j = 0; j < WC; ++j) acc[j] = __ffma2_rn(f2(r.wv[j]), t, acc[j]);
+    };
+    uint2 cpre = make_uint2(0u, 0u);
+    float2 xpre = make_float2(0.f, 0.f);
+    auto prefetch = [&](int bb) {
+        const int kv = rbeg + bb * SHARE + ri;
+        if (bb < nbatch && kv < rend) {
+            cpre = coords[it.begin + kv];
+            xpre = vis[it.begin + kv];
+        }
+    };
+    prefetch(0);
+    for (int b = 0; b < nbatch; ++b) {
+        __syncwarp();
+        const int kv = rbeg + b * SHARE + ri;
+        const bool valid = kv < rend;
+        int key = -1;
+        {
+            const uint2 c = cpre;
+            float2 x = xpre;
+            prefetch(b + 1);
+            const int lu = cell_of(c.x), lv = cell_of(c.y);
+            float wu[W2], wv[W2];
+            kb_weights<W2>(kb, c.x, wu);
+            kb_weights<W2>(kb, c.y, wv);
+            const float h = valid ? (tap_parity(it, g, lu, lv) ? -0.5f : 0.5f) : 0.f;
+            x = make_float2(h * x.x, h * x.y);
+            if (lane_on) {
+                const bool odd = lv & 1;
+                float win[WCP];  // the v-weights at the cell's offset in its pair window
+#pragma unroll
+                for (int m = 0; m < WCP; ++m) {
+                    const float e0 = (m < W2) ? wv[m] : 0.f;
+                    const float e1 = (m >= 1 && m <= W2) ? wv[m - 1] : 0.f;
+                    win[m] = odd ? e1 : e0;
+                }
+                float4 *row4 = reinterpret_cast<float4 *>(myrow);
+#pragma unroll
+                for (int q = 0; q < WCP / 4; ++q)
+                    row4[q] = make_float4(win[4 * q], win[4 * q + 1], win[4 * q + 2], win[4 * q + 3]);
+                key = valid ? ((lu << 6) | (lv & ~1)) : -1;
+                row4[WCP / 4] = make_float4(x.x, x.y, __int_as_float(key), 0.f);
+                float *wrow = myrow + WCP + 4;  // 16-byte aligned
+#pragma unroll
+                for (int q = 0; q < W2 / 4; ++q)
+                    reinterpret_cast<float4 *>(wrow)[q] =
+                        make_float4(wu[4 * q], wu[4 * q + 1], wu[4 * q + 2], wu[4 * q + 3]);
+                if constexpr ((W2 % 4) != 0)
+                    reinterpret_cast<float2 *>(wrow)[W2 / 2 - 1] = make_float2(wu[W2 - 2], wu[W2 - 1]);
+            }
+            if (valid && ((c.x | c.y) & kExtraTapBit))
+                grid_extra_taps<W2, float>(mytile, S, lu, lv, c, wu, wv, kb.edge, x);
+        }
+        const int up = __shfl_up_sync(0xffffffffu, key, 1);
+        const int cell0 = plast;
+        const int prev = (ri == 0) ? plast : up;
+        const unsigned flags = __ballot_sync(0xffffffffu, valid && prev >= 0 && key != prev);
+        const unsigned nvalid = __popc(__ballot_sync(0xffffffffu, valid) & gmask);
+        const int lastkey = __shfl_sync(0xffffffffu, key, grp * W2 + max((int)nvalid, 1) - 1);
+        if (nvalid) plast = lastkey;
+        unsigned wm = 0;
+#pragma unroll
+        for (int q = 0; q < G; ++q) wm |= flags >> (q * W2);
+        wm &= (1u << W2) - 1u;
+        const unsigned bm = lane_on ? (flags >> (grp * W2)) & ((1u << W2) - 1u) : 0u;
+        __syncwarp();
+        RowVals cur;
+        if (lane_on) load_row(rowg, cur);
+        int lastcell = cell0;
+#pragma unroll
+        for (int st = 0; st < SHARE; ++st) {
+            RowVals nxt;
+            if (st + 1 < SHARE && lane_on) load_row(rowg + (st + 1) * STR, nxt);
+            if (wm & (1u << st)) {
+                const bool need = (bm >> st) & 1u;
+                int fcell = lastcell;  // the cell of the group's row before this step
+                if constexpr (NARROW)
+                    fcell = (st > 0) ? __shfl_sync(0xffffffffu, key, grp * W2 + st - 1) : cell0;
+                unsigned gm = __ballot_sync(0xffffffffu, need);
+                while (gm) {
+                    const int g0 = (__ffs(gm) - 1) / W2;
+                    if (need && grp == g0) flush_to(fcell);
+                    __syncwarp();
+                    gm &= ~(((1u << W2) - 1u) << (g0 * W2));
+                }
+            }
+            if (lane_on) {
+                consume(cur);
+                if constexpr (!NARROW) lastcell = __float_as_int(cur.xk.z);
+            }
+            if (st + 1 < SHARE) cur = nxt;
+        }
+    }
+#pragma unroll
+    for (int g0 = 0; g0 < G; ++g0) {
+        if (lane_on && grp == g0 && plast >= 0) flush_to(plast);
+        __syncwarp();
+    }
+    __syncthreads();
+    {
+        float4 *t4 = reinterpret_cast<float4 *>(tiles);
+        const int n4 = (E * S) / 2;
+        for (int e = threadIdx.x; e < n4; e += blockDim.x) {
+            float4 a = t4[e];
+#pragma unroll
+            for (int q = 1; q < NW; ++q) {
+                const float4 bq = t4[q * n4 + e];
+                a.x += bq.x;
+                a.y += bq.y;
+                a.z += bq.z;
+                a.w += bq.w;
+            }
+            t4[e] = a;
+        }
+    }
+    __syncthreads();
+    grid_flush_extended<W2, float>(tiles, grid, it, g);
+}
+
+template <int W2, int NW = 8>
+__host__ __device__ inline size_t grid_pairs_smem_bytes(const GridGeom &g)
+{
+    const size_t tile_bytes =
+        ((sizeof(float2) * NW * g.E * grid_local_stride(g.E)) + 15) & ~size_t(15);
+    const size_t ngroups = (size_t)NW * (32 / W2);
+    return tile_bytes +
+           sizeof(float) * (ngroups * ((size_t)W2 * kPairRowStride<W2> + pair_group_skew<W2>()));
+}
+
+template <int W2, int NW = 8>
+__host__ __device__ inline size_t grid_local_smem_bytes(const GridGeom &g)
+{
+    const size_t tile_bytes =
+        ((sizeof(float2) * NW * g.E * grid_local_stride(g.E)) + 15) & ~size_t(15);
+    const size_t ngroups = (size_t)NW * (32 / W2);
+    return tile_bytes +
+           sizeof(float) * (ngroups * ((size_t)W2 * kLocalRowStride<W2> + local_group_skew<W2>()));
 }
 
 template <int W2>

@@ -332,6 +332,57 @@ int launch_to_plan_c64(const int *perm, const float2 *phase, const float2 *vu, f
 }
 
 // defined in gridding.cu
+// Same-cell chunks. mark[k] = k where a run of equal sort keys (one cell of one tile) or a
+// work item starts, else 0; an inclusive max-scan then gives every visibility the start of its
+// run, and a chunk starts every chunk_k visibilities from there.
+__global__ void run_start_kernel(const unsigned *__restrict__ keys, int *__restrict__ mark,
+                                 long long n)
+{
+    for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < n;
+         k += (long long)gridDim.x * blockDim.x)
+        mark[k] = (k == 0 || keys[k] != keys[k - 1]) ? (int)k : 0;
+}
+
+__global__ void item_start_kernel(const WorkItem *__restrict__ items, int nitems,
+                                  int *__restrict__ mark)
+{
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nitems; i += gridDim.x * blockDim.x)
+        mark[items[i].begin] = items[i].begin;
+}
+
+__global__ void chunk_start_kernel(const int *__restrict__ last, int *__restrict__ cflag,
+                                   long long n, int K)
+{
+    for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < n;
+         k += (long long)gridDim.x * blockDim.x)
+        cflag[k] = ((k - last[k]) % K == 0) ? 1 : 0;
+}
+
+__global__ void chunk_write_kernel(const int *__restrict__ cflag, const int *__restrict__ cidx,
+                                   int *__restrict__ chunk_begin, long long n)
+{
+    for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < n;
+         k += (long long)gridDim.x * blockDim.x) {
+        if (cflag[k]) chunk_begin[cidx[k]] = (int)k;
+        if (k == n - 1) chunk_begin[cidx[k] + cflag[k]] = (int)n;  // end of the last chunk
+    }
+}
+
+__global__ void item_chunk_kernel(const WorkItem *__restrict__ items, int nitems,
+                                  const int *__restrict__ cidx, long long n, int nchunks,
+                                  int2 *__restrict__ out)
+{
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nitems; i += gridDim.x * blockDim.x) {
+        const WorkItem it = items[i];
+        const long long end = (long long)it.begin + it.count;
+        out[i] = make_int2(cidx[it.begin], end < n ? cidx[end] : nchunks);
+    }
+}
+
+struct MaxInt {
+    __device__ int operator()(int a, int b) const { return a > b ? a : b; }
+};
+
 int launch_degrid(const lentils_plan *p, const float2 *grid, float2 *vis, cudaStream_t s,
                   const float *vscale = nullptr);
 int launch_grid(const lentils_plan *p, const float2 *vis, float2 *grid, cudaStream_t s);
@@ -365,6 +416,8 @@ static void free_plan_arrays(lentils_plan *p)
     cudaFree(p->phase);
     cudaFree(p->coords_res);
     cudaFree(p->items);
+    cudaFree(p->chunk_begin);
+    cudaFree(p->item_chunks);
     cudaFree(p->stage_vis64);
     cudaFree(p->stage_grid64);
     cudaFree(p->stage_vis32);
@@ -386,6 +439,54 @@ struct DevTemps {
         return st;
     }
 };
+
+// Visibilities per same-cell chunk of the degridding kernel for half-width w (0: none). The
+// chunk's weights stay in registers, 4 * 2 * 2w floats; wider kernels keep one visibility per
+// thread.
+static int chunk_width(int w) { return w <= 4 ? 4 : 0; }
+
+// Builds p->chunk_begin / p->item_chunks from the sorted keys (after p->items is on the
+// device). Synchronises once, for the chunk count.
+static int build_chunks(lentils_plan *p, const unsigned *keys_sorted, DevTemps &tmp,
+                        cudaStream_t s)
+{
+    const long long n = p->nvis;
+    const int K = chunk_width(p->geom.w);
+    int *mark, *last, *cflag, *cidx;
+    int st;
+    if ((st = tmp.alloc(&mark, n))) return st;
+    if ((st = tmp.alloc(&last, n))) return st;
+    if ((st = tmp.alloc(&cflag, n))) return st;
+    if ((st = tmp.alloc(&cidx, n))) return st;
+    run_start_kernel<<<grid_blocks(n), 256, 0, s>>>(keys_sorted, mark, n);
+    LENTILS_CHECK_LAUNCH("run_start_kernel");
+    item_start_kernel<<<grid_blocks(p->nitems), 256, 0, s>>>(p->items, p->nitems, mark);
+    LENTILS_CHECK_LAUNCH("item_start_kernel");
+    size_t b1 = 0, b2 = 0;
+    LENTILS_CUDA_TRY(cub::DeviceScan::InclusiveScan(nullptr, b1, mark, last, MaxInt(), n, s));
+    LENTILS_CUDA_TRY(cub::DeviceScan::ExclusiveSum(nullptr, b2, cflag, cidx, n, s));
+    unsigned char *temp;
+    if ((st = tmp.alloc(&temp, std::max(b1, b2)))) return st;
+    LENTILS_CUDA_TRY(cub::DeviceScan::InclusiveScan(temp, b1, mark, last, MaxInt(), n, s));
+    chunk_start_kernel<<<grid_blocks(n), 256, 0, s>>>(last, cflag, n, K);
+    LENTILS_CHECK_LAUNCH("chunk_start_kernel");
+    LENTILS_CUDA_TRY(cub::DeviceScan::ExclusiveSum(temp, b2, cflag, cidx, n, s));
+    int tail[2] = {0, 0};
+    LENTILS_CUDA_TRY(cudaMemcpyAsync(&tail[0], cidx + n - 1, sizeof(int), cudaMemcpyDeviceToHost, s));
+    LENTILS_CUDA_TRY(cudaMemcpyAsync(&tail[1], cflag + n - 1, sizeof(int), cudaMemcpyDeviceToHost, s));
+    LENTILS_CUDA_TRY(cudaStreamSynchronize(s));
+    const long long nchunks = (long long)tail[0] + tail[1];
+    if ((st = dev_alloc(&p->chunk_begin, (size_t)nchunks + 1, &p->device_bytes))) return st;
+    if ((st = dev_alloc(&p->item_chunks, (size_t)p->nitems, &p->device_bytes))) return st;
+    chunk_write_kernel<<<grid_blocks(n), 256, 0, s>>>(cflag, cidx, p->chunk_begin, n);
+    LENTILS_CHECK_LAUNCH("chunk_write_kernel");
+    item_chunk_kernel<<<grid_blocks(p->nitems), 256, 0, s>>>(p->items, p->nitems, cidx, n,
+                                                             (int)nchunks, p->item_chunks);
+    LENTILS_CHECK_LAUNCH("item_chunk_kernel");
+    p->chunk_k = K;
+    p->nchunks = nchunks;
+    return LENTILS_OK;
+}
 
 static int plan_build(lentils_plan *p, const double *uvw, const double *chans, int flags,
                       cudaStream_t s)
@@ -497,6 +598,8 @@ static int plan_build(lentils_plan *p, const double *uvw, const double *chans, i
     if (!items.empty())
         LENTILS_CUDA_TRY(cudaMemcpyAsync(p->items, items.data(), sizeof(WorkItem) * items.size(),
                                          cudaMemcpyHostToDevice, s));
+    if (chunk_width(g.w) > 0 && !items.empty())
+        if ((st = build_chunks(p, keys_sorted, tmp, s))) return st;
     LENTILS_CUDA_TRY(cudaStreamSynchronize(s));
     return LENTILS_OK;
 }
@@ -635,8 +738,8 @@ int lentils_plan_destroy(lentils_plan *p)
 int lentils_plan_set_grid_variant(lentils_plan *p, int variant)
 {
     clear_error();
-    if (!p || variant < 0 || variant > 8)
-        return set_error(LENTILS_ERR_INVALID, "plan_set_grid_variant: variant 0 to 8");
+    if (!p || variant < 0 || variant > 12)
+        return set_error(LENTILS_ERR_INVALID, "plan_set_grid_variant: variant 0 to 12");
     p->grid_variant = variant;
     return LENTILS_OK;
 }
@@ -644,8 +747,8 @@ int lentils_plan_set_grid_variant(lentils_plan *p, int variant)
 int lentils_plan_set_degrid_variant(lentils_plan *p, int variant)
 {
     clear_error();
-    if (!p || variant < 0 || variant > 1)
-        return set_error(LENTILS_ERR_INVALID, "plan_set_degrid_variant: variant 0 or 1");
+    if (!p || variant < 0 || variant > 2)
+        return set_error(LENTILS_ERR_INVALID, "plan_set_degrid_variant: variant 0 to 2");
     p->degrid_variant = variant;
     return LENTILS_OK;
 }

@@ -84,12 +84,13 @@ class GriddingPlan:
         return self._handle
 
     def set_grid_variant(self, variant):
-        """Work split of the gridding kernel (lentils_plan_set_grid_variant, 0-6); tuning only."""
+        """Work split of the gridding kernel (lentils_plan_set_grid_variant, 0-11); tuning only,
+        equal results up to FP32 summation order."""
         N.check(N.lib().lentils_plan_set_grid_variant(self._handle, int(variant)))
 
     def set_degrid_variant(self, variant):
-        """Shared-memory layout of the degridding kernel (lentils_plan_set_degrid_variant, 0 or
-        1); tuning only, identical results."""
+        """Form of the degridding kernel (lentils_plan_set_degrid_variant, 0-2); tuning only,
+        identical results."""
         N.check(N.lib().lentils_plan_set_degrid_variant(self._handle, int(variant)))
 
     @property

@@ -38,7 +38,9 @@ def gpu_grid(plan, vis_c128):
 @pytest.mark.parametrize("name", ["nufft_cfg0_w3", "nufft_odd_w4", "nufft_tiny_w1"])
 @pytest.mark.parametrize("tile,variant", [(0, 0), (8, 0), (64, 0), (0, 1), (32, 1), (0, 2),
                                           (0, 5), (0, 6), (0, 7), (0, 8), (8, 8), (64, 8),
-                                          (16, 2), (0, 3), (32, 3), (0, 4), (8, 4), (64, 4)])
+                                          (16, 2), (0, 3), (32, 3), (0, 4), (8, 4), (64, 4),
+                                          (0, 9), (8, 9), (64, 9), (0, 10), (32, 10),
+                                          (0, 11), (8, 11), (64, 11), (0, 12), (8, 12)])
 def test_plan_api_vs_golden(native, name, tile, variant):
     d, vis, four = load_nufft_golden(name)
     w, beta = int(d["wsup"]), float(d["beta"])
@@ -53,15 +55,18 @@ def test_plan_api_vs_golden(native, name, tile, variant):
 @pytest.mark.parametrize("name", ["nufft_cfg0_w3", "nufft_odd_w4", "nufft_tiny_w1"])
 @pytest.mark.parametrize("tile", [0, 8, 64])
 def test_degrid_layouts_vs_golden(native, name, tile):
-    """Both shared-memory layouts of the degridding kernel give the same bits."""
+    """Every form of the degridding kernel (same-cell chunks, the paired-column shared tile,
+    one visibility per thread) gives the same bits."""
     d, vis, four = load_nufft_golden(name)
     w, beta = int(d["wsup"]), float(d["beta"])
     plan = make_plan(vis, four, w, beta, tile=tile)
+    plan.set_degrid_variant(0)
     v0 = gpu_degrid(plan, d["grid_in"])
-    plan.set_degrid_variant(1)
-    v1 = gpu_degrid(plan, d["grid_in"])
-    assert np.array_equal(v0, v1)
-    assert O.rel_l2(v1, d["vis_out"] - d["vis_acc0"]) < REL_L2_FP32
+    for variant in (1, 2):
+        plan.set_degrid_variant(variant)
+        v1 = gpu_degrid(plan, d["grid_in"])
+        assert np.array_equal(v0, v1), variant
+        assert O.rel_l2(v1, d["vis_out"] - d["vis_acc0"]) < REL_L2_FP32
 
 
 @pytest.mark.parametrize("name", ["nufft_cfg0_w3", "nufft_odd_w4", "nufft_tiny_w1"])
@@ -170,7 +175,9 @@ def test_heavy_bins_and_seams(native):
     seams[:, 0] = (rng.integers(-4, 4, 3000) * 16 + rng.uniform(-0.5, 0.5, 3000)) * four.du
     seams[:, 1] = (rng.uniform(-1.0, 1.0, 3000) * 4) * four.dv
     for uvw, variant in ((one_cell, 0), (seams, 0), (one_cell, 1), (seams, 1), (one_cell, 2),
-                         (seams, 2), (one_cell, 3), (seams, 3), (one_cell, 4), (seams, 4)):
+                         (seams, 2), (one_cell, 3), (seams, 3), (one_cell, 4), (seams, 4),
+                         (one_cell, 9), (seams, 9), (one_cell, 10), (seams, 10),
+                         (one_cell, 11), (seams, 11), (one_cell, 12), (seams, 12)):
         vis = O.VisGeom(uvw, [1.0])
         plan = make_plan(vis, four, w, beta, tile=16, chunk=512)
         plan.set_grid_variant(variant)
