@@ -127,7 +127,9 @@ def load_peaks():
 # launch on this workload from one ncu capture of the same plan (dram__bytes_read.sum +
 # dram__bytes_write.sum, tile 16, chunk 4096).
 DEGRID_KERNEL, GRID_KERNEL = "degrid_chunk_kernel", "grid_pairs_kernel"
-TRAFFIC = {DEGRID_KERNEL: None, GRID_KERNEL: None}
+TRAFFIC = {DEGRID_KERNEL: 130845440, GRID_KERNEL: 167329792}
+# FP32 lanes: 152 SMs x 128 FMA per clock x 2 FLOP at the 2.07 GHz maximum SM clock (nominal).
+FP32_PEAK_TFLOPS = 152 * 128 * 2 * 2.07e9 / 1e12
 
 
 def cpu_reference_lib():
@@ -375,7 +377,8 @@ def run_ours(args):
                          "frac": achieved / peak, "traffic": traffic, "kernel": dominant,
                          "peak_source": peak_kind,
                          "algorithmic_bytes_per_launch": alg_bytes,
-                         "pair_frac": 2 * alg_bytes / ((deg_ms + grd_ms) * 1e-3) / 1e9 / peak},
+                         "pair_frac": 2 * alg_bytes / ((deg_ms + grd_ms) * 1e-3) / 1e9 / peak,
+                         "fp32_taps": fp32_taps_roofline(nvis, deg_ms, grd_ms)},
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h, "ms_per_step": e2e_s * 1e3,
                     "api": "lentils_degrid_host + lentils_grid_host (pinned c128, row order)"},
@@ -396,6 +399,18 @@ def run_ours(args):
         print(json.dumps(line))
     ranks.close()
     return 0
+
+
+def fp32_taps_roofline(nvis, deg_ms, grd_ms):
+    """The tap arithmetic of both kernels against the nominal FP32 rate: each visibility is
+    (2w)^2 complex-by-real multiply-adds per direction (4 FLOP each), weights not counted."""
+    flop = 4 * (2 * WSUP) ** 2
+    out = {"flop_per_vis": flop, "peak_tflops": FP32_PEAK_TFLOPS,
+           "peak_source": "nominal: 152 SMs x 128 FP32 FMA/clock x 2 FLOP x 2.07 GHz"}
+    for name, ms in (("degrid", deg_ms), ("grid", grd_ms)):
+        t = nvis * flop / (ms * 1e-3) / 1e12
+        out[name] = {"achieved_tflops": t, "frac": t / FP32_PEAK_TFLOPS}
+    return out
 
 
 def fp64_parity(plan, grid_in, vis_in, vis_out, grid_out):
@@ -804,9 +819,10 @@ def cpu_cg_baseline(inv, geom, budget_s=60.0):
 
 
 SWEEP_SEED = SEED + 3
+SWEEP_FORM = 0  # lentils_sweep_create flags: the sweep kernel's item functions
 
 
-def run_sweep_bench(peak, nsamples=256, steps=10, warmup=3):
+def run_sweep_bench(peak, nsamples=256, steps=10, warmup=3, form=SWEEP_FORM):
     """Batched uneven lens-parameter sweep: 256 PEMD + shear samples from the priors, image
     sizes from {128, 256, 384, 512}^2 (0.02" pixels), visibility counts log-uniform in
     [1e5, 2e6] (uv density ~ 1/|uv| to 0.45 of Nyquist), per-sample KB width from the accuracy
@@ -819,7 +835,7 @@ def run_sweep_bench(peak, nsamples=256, steps=10, warmup=3):
     from lentils_gb300.sweep import BatchedSweep, draw_samples
     samples = draw_samples(np.random.default_rng(SWEEP_SEED), nsamples)
     t0 = time.perf_counter()
-    sw = BatchedSweep(samples)
+    sw = BatchedSweep(samples, form=form)
     setup_s = time.perf_counter() - t0
     if sw.tuner.tuned:
         try:
@@ -877,7 +893,7 @@ def run_sweep_bench(peak, nsamples=256, steps=10, warmup=3):
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak,
                          "unit": "GB/s", "frac": achieved / peak,
                          "algorithmic_bytes_per_run": st["algorithmic_bytes"]},
-            "setup_s": setup_s, "autotuned_classes": sw.tuner.tuned}
+            "kernel_form": form, "setup_s": setup_s, "autotuned_classes": sw.tuner.tuned}
 
 
 def _omp_threads(n):

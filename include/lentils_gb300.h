@@ -451,11 +451,13 @@ int lentils_dot64(const double *a, const double *b, int n, double *out, void *st
  * BF16 tensor-core GEMM (tcgen05, FP32 accumulation in tensor memory): C = A * B^T with A
  * (M x K) and B (N x K) row-major BF16 and C (M x N) row-major FP32, all device pointers; N in
  * {32, 64, 128, 256}, K a multiple of 8. The core of the learned preconditioner's kernels,
- * exposed for testing. swap_lbo_sbo = 0. *err_dev (device int) is set to 1 if a bounded
- * wait on the tensor core gave up (the result is then invalid).
+ * exposed for testing. form 0: the threads stage each K chunk and then the tensor core runs it
+ * (double-buffered); form 1: the pipelined kernel (operands copied by cp.async into a ring of
+ * chunks, the MMAs issued by a thread of a fifth warp). *err_dev (device int) is set to 1 if a
+ * bounded wait on the tensor core gave up (the result is then invalid).
  * ---------------------------------------------------------------------------------------- */
 int lentils_tc_gemm_bf16(const void *A, const void *B, float *C, int M, int N, int K,
-                         int swap_lbo_sbo, int *err_dev, void *stream);
+                         int form, int *err_dev, void *stream);
 /* Failure-path self-test of the bounded tensor-core waits: a kernel holding tensor memory
  * waits on an mbarrier that nothing completes, gives up after poll_limit polls (1..2^20), sets
  * *err_dev = 1, frees its tensor memory and returns; the context stays usable. */
@@ -497,6 +499,12 @@ typedef struct {
     long long total_pixels;
     double algorithmic_bytes; /* per run: 2 x (16 B per visibility + grid) + 8 B per pixel */
 } lentils_sweep_stats;
+/* flags & LENTILS_SWEEP_FORM_MASK: the form of the sweep kernel's items. 0: the ballot gridder
+ * and one visibility per degridding thread, three CTAs per SM; 1: the column-pair gridder and
+ * same-cell chunk degridding, two CTAs per SM; 2: the column-pair gridder and one visibility
+ * per degridding thread, two CTAs per SM. Tuning only: equal results up to FP32 summation
+ * order in the grids, identical visibilities. */
+#define LENTILS_SWEEP_FORM_MASK 3
 int lentils_sweep_create(lentils_sweep **sweep, const lentils_sweep_sample *samples, int n,
                          int flags, void *stream);
 int lentils_sweep_destroy(lentils_sweep *sweep);
@@ -545,6 +553,9 @@ int lentils_unet_train_step(lentils_unet *net, const float *r, const float *d, c
 int lentils_unet_backward(lentils_unet *net, const float *dout, int B, float lr,
                           float *grad_host, void *stream);
 /* gamma of the preconditioner form (default 0) */
+/* Tuning: 0 (default) runs the convolution GEMMs whose operands are plain gathers (forward;
+ * data gradient of a layer without ReLU) on the pipelined kernel, 1 on the staged kernel. */
+int lentils_unet_set_gemm_form(lentils_unet *net, int form);
 int lentils_unet_set_jacobi_weight(lentils_unet *net, float gamma);
 /* 1 if a bounded tensor-core wait gave up since creation (results then invalid) */
 int lentils_unet_error_flag(lentils_unet *net, int *flag);

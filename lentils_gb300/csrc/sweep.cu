@@ -39,6 +39,8 @@ struct SweepSampleDev {
     int nitems;
     const uint2 *coords;
     const WorkItem *items;
+    const int *chunk_begin;   // same-cell chunks (null: not built)
+    const int2 *item_chunks;
     const float2 *grid_in;
     float2 *vis_out;
     const float2 *vis_in;
@@ -86,9 +88,12 @@ __device__ __forceinline__ void deflect_chunk(const SweepSampleDev &s,
     }
 }
 
-// Three CTAs per SM (80 registers, a few bytes of spill) beat two at 128 registers: the items
-// are latency-bound and the third CTA hides the staging loads.
-__global__ void __launch_bounds__(kGridBatch, 3)
+// FORM 0: the ballot gridder and one visibility per degridding thread, three CTAs per SM (80
+// registers, a few bytes of spill). FORM 1: the column-pair gridder and same-cell chunk
+// degridding, two CTAs per SM (128 registers). FORM 2: the column-pair gridder and one
+// visibility per degridding thread, two CTAs per SM.
+template <int FORM>
+__global__ void __launch_bounds__(kGridBatch, FORM == 0 ? 3 : 2)
     sweep_kernel(const SweepSampleDev *__restrict__ samples, const SweepWork *__restrict__ work,
                  int nwork, const DevLens *__restrict__ lenses, int *__restrict__ counter)
 {
@@ -117,14 +122,34 @@ __global__ void __launch_bounds__(kGridBatch, 3)
         }
         __syncthreads();
         const WorkItem it = s.items[d.index];
-        if (d.kind == kSweepGrid) {
-            if (s.w2 == 8)
-                grid_rows_item_ballot<8>(s.vis_in, s.coords, s.grid_out, it, kb, g, smraw);
-            else
-                grid_rows_item_ballot<6>(s.vis_in, s.coords, s.grid_out, it, kb, g, smraw);
+        if constexpr (FORM != 0) {
+            if (d.kind == kSweepGrid) {
+                if (s.w2 == 8)
+                    grid_rows_item_pairs<8, 8>(s.vis_in, s.coords, s.grid_out, it, kb, g, smraw);
+                else
+                    grid_rows_item_pairs<6, 8>(s.vis_in, s.coords, s.grid_out, it, kb, g, smraw);
+            } else if constexpr (FORM == 1) {
+                const int2 cr = s.item_chunks[d.index];
+                if (s.w2 == 8)
+                    degrid_item_chunks<8, 4>(s.grid_in, s.coords, s.vis_out, it, cr,
+                                             s.chunk_begin, kb, g, smraw);
+                else
+                    degrid_item_chunks<6, 4>(s.grid_in, s.coords, s.vis_out, it, cr,
+                                             s.chunk_begin, kb, g, smraw);
+            } else {
+                if (s.w2 == 8) degrid_item<8, float>(s.grid_in, s.coords, s.vis_out, it, kb, g, nullptr, smraw);
+                else degrid_item<6, float>(s.grid_in, s.coords, s.vis_out, it, kb, g, nullptr, smraw);
+            }
         } else {
-            if (s.w2 == 8) degrid_item<8, float>(s.grid_in, s.coords, s.vis_out, it, kb, g, nullptr, smraw);
-            else degrid_item<6, float>(s.grid_in, s.coords, s.vis_out, it, kb, g, nullptr, smraw);
+            if (d.kind == kSweepGrid) {
+                if (s.w2 == 8)
+                    grid_rows_item_ballot<8>(s.vis_in, s.coords, s.grid_out, it, kb, g, smraw);
+                else
+                    grid_rows_item_ballot<6>(s.vis_in, s.coords, s.grid_out, it, kb, g, smraw);
+            } else {
+                if (s.w2 == 8) degrid_item<8, float>(s.grid_in, s.coords, s.vis_out, it, kb, g, nullptr, smraw);
+                else degrid_item<6, float>(s.grid_in, s.coords, s.vis_out, it, kb, g, nullptr, smraw);
+            }
         }
     }
 }
@@ -135,6 +160,7 @@ struct lentils_sweep {
     int nsamples;
     int nwork;
     int blocks;
+    int form;  // sweep_kernel<form>
     size_t smem;
     long long total_vis, total_pixels;
     double algorithmic_bytes;
@@ -159,13 +185,37 @@ static void sweep_free(lentils_sweep *sw)
     cudaFree(sw->counter);
 }
 
+static cudaError_t sweep_set_smem(int form, int smem)
+{
+    const cudaFuncAttribute a = cudaFuncAttributeMaxDynamicSharedMemorySize;
+    if (form == 1) return cudaFuncSetAttribute(sweep_kernel<1>, a, smem);
+    if (form == 2) return cudaFuncSetAttribute(sweep_kernel<2>, a, smem);
+    return cudaFuncSetAttribute(sweep_kernel<0>, a, smem);
+}
+
+static cudaError_t sweep_occupancy(int form, int *per_sm, size_t smem)
+{
+    if (form == 1)
+        return cudaOccupancyMaxActiveBlocksPerMultiprocessor(per_sm, sweep_kernel<1>, kGridBatch, smem);
+    if (form == 2)
+        return cudaOccupancyMaxActiveBlocksPerMultiprocessor(per_sm, sweep_kernel<2>, kGridBatch, smem);
+    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(per_sm, sweep_kernel<0>, kGridBatch, smem);
+}
+
 static int sweep_enqueue(lentils_sweep *sw, cudaStream_t s)
 {
     LENTILS_CUDA_TRY(cudaMemsetAsync(sw->counter, 0, sizeof(int), s));
     for (auto &z : sw->zero) LENTILS_CUDA_TRY(cudaMemsetAsync(z.first, 0, z.second, s));
     if (sw->nwork > 0) {
-        sweep_kernel<<<sw->blocks, kGridBatch, sw->smem, s>>>(sw->samples, sw->work, sw->nwork,
-                                                             sw->lenses, sw->counter);
+        if (sw->form == 1)
+            sweep_kernel<1><<<sw->blocks, kGridBatch, sw->smem, s>>>(
+                sw->samples, sw->work, sw->nwork, sw->lenses, sw->counter);
+        else if (sw->form == 2)
+            sweep_kernel<2><<<sw->blocks, kGridBatch, sw->smem, s>>>(
+                sw->samples, sw->work, sw->nwork, sw->lenses, sw->counter);
+        else
+            sweep_kernel<0><<<sw->blocks, kGridBatch, sw->smem, s>>>(
+                sw->samples, sw->work, sw->nwork, sw->lenses, sw->counter);
         LENTILS_CHECK_LAUNCH("sweep_kernel");
     }
     return LENTILS_OK;
@@ -185,6 +235,11 @@ int lentils_sweep_create(lentils_sweep **out, const lentils_sweep_sample *in, in
     std::vector<std::pair<double, SweepWork>> items;
     lentils_sweep *sw = new (std::nothrow) lentils_sweep();
     if (!sw) return set_error(LENTILS_ERR_ALLOC, "sweep_create: host allocation");
+    sw->form = flags & LENTILS_SWEEP_FORM_MASK;
+    if (sw->form > 2) {
+        delete sw;
+        return set_error(LENTILS_ERR_INVALID, "sweep_create: kernel form %d (0 to 2)", flags & 3);
+    }
     size_t smem = 0;
     int st = LENTILS_OK;
     for (int k = 0; k < n && !st; ++k) {
@@ -239,6 +294,12 @@ int lentils_sweep_create(lentils_sweep **out, const lentils_sweep_sample *in, in
         d.nitems = p->nitems;
         d.coords = p->coords;
         d.items = p->items;
+        d.chunk_begin = p->chunk_begin;
+        d.item_chunks = p->item_chunks;
+        if (sw->form == 1 && p->nitems > 0 && (!p->chunk_begin || p->chunk_k != 4)) {
+            st = set_error(LENTILS_ERR_UNSUPPORTED, "sweep_create: sample %d: no chunks", k);
+            break;
+        }
         d.grid_in = reinterpret_cast<const float2 *>(a.grid_in);
         d.vis_out = reinterpret_cast<float2 *>(a.vis_out);
         d.vis_in = reinterpret_cast<const float2 *>(a.vis_in);
@@ -247,7 +308,12 @@ int lentils_sweep_create(lentils_sweep **out, const lentils_sweep_sample *in, in
         sw->zero.push_back({d.grid_out, gbytes});
         sw->total_vis += p->nvis;
         sw->algorithmic_bytes += 2.0 * (16.0 * (double)p->nvis + (double)gbytes);
-        smem = std::max(smem, w2 == 8 ? grid_ballot_smem_bytes<8>(p->geom) : grid_ballot_smem_bytes<6>(p->geom));
+        if (sw->form != 0)
+            smem = std::max(smem, w2 == 8 ? grid_pairs_smem_bytes<8, 8>(p->geom)
+                                          : grid_pairs_smem_bytes<6, 8>(p->geom));
+        else
+            smem = std::max(smem, w2 == 8 ? grid_ballot_smem_bytes<8>(p->geom)
+                                          : grid_ballot_smem_bytes<6>(p->geom));
         smem = std::max(smem, degrid_smem_bytes<float>(p->geom));
         std::vector<WorkItem> hitems(p->nitems);
         if (p->nitems > 0) {
@@ -292,13 +358,11 @@ int lentils_sweep_create(lentils_sweep **out, const lentils_sweep_sample *in, in
         e = cudaMemcpyAsync(sw->work, hw.data(), sizeof(SweepWork) * hw.size(), cudaMemcpyHostToDevice, s);
     if (e == cudaSuccess && !hl.empty())
         e = cudaMemcpyAsync(sw->lenses, hl.data(), sizeof(DevLens) * hl.size(), cudaMemcpyHostToDevice, s);
-    if (e == cudaSuccess)
-        e = cudaFuncSetAttribute(sweep_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sw->smem);
+    if (e == cudaSuccess) e = sweep_set_smem(sw->form, (int)sw->smem);
     int per_sm = 0, nsm = 0, dev = 0;
     if (e == cudaSuccess) e = cudaGetDevice(&dev);
     if (e == cudaSuccess) e = cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
-    if (e == cudaSuccess)
-        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, sweep_kernel, kGridBatch, sw->smem);
+    if (e == cudaSuccess) e = sweep_occupancy(sw->form, &per_sm, sw->smem);
     if (e == cudaSuccess) e = cudaStreamSynchronize(s);
     if (e != cudaSuccess) {
         st = cuda_status(e, "sweep_create");
@@ -307,7 +371,6 @@ int lentils_sweep_create(lentils_sweep **out, const lentils_sweep_sample *in, in
         return st;
     }
     sw->blocks = std::max(1, std::min(sw->nwork, std::max(1, per_sm) * nsm));
-    (void)flags;
     *out = sw;
     return LENTILS_OK;
 }

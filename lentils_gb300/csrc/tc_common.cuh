@@ -54,6 +54,26 @@ __device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity,
     return false;
 }
 
+__device__ __forceinline__ void mbar_arrive(uint64_t *bar)
+{
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
+
+// -- cp.async (16 bytes, zero-filled when src_bytes == 0) ---------------------------------------
+__device__ __forceinline__ void cp_async16(void *dst_smem, const void *src, uint32_t src_bytes)
+{
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"(smem_u32(dst_smem)),
+                 "l"(src), "r"(src_bytes)
+                 : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait_group()
+{
+    asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
+
 // -- fences ------------------------------------------------------------------------------------
 // make generic-proxy shared-memory writes visible to the tensor core (async proxy)
 __device__ __forceinline__ void fence_async_smem()

@@ -1,4 +1,4 @@
-// BF16 tensor-core GEMM entry point (tcgen05, FP32 accumulation in TMEM) on the generic kernel
+// BF16 tensor-core GEMM entry point (tcgen05, FP32 accumulation in TMEM) on the generic kernels
 // of tc_gemm.cuh -- the core of the learned preconditioner's convolutions, exposed for tests:
 //   C[M x N] (f32, row-major) = A[M x K] (bf16, row-major) * B[N x K]^T (bf16, row-major)
 #include "common.cuh"
@@ -7,18 +7,27 @@
 namespace lentils {
 
 template <int N>
-static int launch_tc_gemm(const void *A, const void *B, float *C, int M, int K, int *err,
-                          cudaStream_t s)
+static int launch_tc_gemm(const void *A, const void *B, float *C, int M, int K, int form,
+                          int *err, cudaStream_t s)
 {
     using namespace tc;
-    const size_t smem = GemmSmem<N>::kBytes;
     RowMajorLoader la{(const __nv_bfloat16 *)A, M, K, K};
     RowMajorLoader lb{(const __nv_bfloat16 *)B, N, K, K};
     StoreF32 ep{C, M, N, N};
-    auto kern = gemm_kernel<N, RowMajorLoader, RowMajorLoader, StoreF32>;
-    LENTILS_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     const int kpieces = (K + 7) / 8;
     dim3 grid((M + 127) / 128, 1, 1);
+    if (form == 1) {
+        constexpr int kStages = 3;
+        const size_t smem = PipeSmem<N, kStages>::kBytes;
+        auto kern = gemm_pipe_kernel<N, kStages, RowMajorLoader, RowMajorLoader, StoreF32>;
+        LENTILS_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        kern<<<grid, kPipeThreads, smem, s>>>(la, lb, ep, kpieces, kpieces, err);
+        LENTILS_CHECK_LAUNCH("tc gemm_pipe_kernel");
+        return LENTILS_OK;
+    }
+    const size_t smem = GemmSmem<N>::kBytes;
+    auto kern = gemm_kernel<N, RowMajorLoader, RowMajorLoader, StoreF32>;
+    LENTILS_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     kern<<<grid, 128, smem, s>>>(la, lb, ep, kpieces, kpieces, err);
     LENTILS_CHECK_LAUNCH("tc gemm_kernel");
     return LENTILS_OK;
@@ -65,17 +74,17 @@ int lentils_tc_timeout_selftest(int *err_dev, int poll_limit, void *stream)
 }
 
 int lentils_tc_gemm_bf16(const void *A, const void *B, float *C, int M, int N, int K,
-                         int swap_lbo_sbo, int *err_dev, void *stream)
+                         int form, int *err_dev, void *stream)
 {
     clear_error();
-    if (!A || !B || !C || !err_dev || M < 1 || K < 8 || (K % 8) != 0 || swap_lbo_sbo != 0)
+    if (!A || !B || !C || !err_dev || M < 1 || K < 8 || (K % 8) != 0 || form < 0 || form > 1)
         return set_error(LENTILS_ERR_INVALID, "tc_gemm_bf16: bad arguments");
     cudaStream_t s = (cudaStream_t)stream;
     switch (N) {
-    case 32: return launch_tc_gemm<32>(A, B, C, M, K, err_dev, s);
-    case 64: return launch_tc_gemm<64>(A, B, C, M, K, err_dev, s);
-    case 128: return launch_tc_gemm<128>(A, B, C, M, K, err_dev, s);
-    case 256: return launch_tc_gemm<256>(A, B, C, M, K, err_dev, s);
+    case 32: return launch_tc_gemm<32>(A, B, C, M, K, form, err_dev, s);
+    case 64: return launch_tc_gemm<64>(A, B, C, M, K, form, err_dev, s);
+    case 128: return launch_tc_gemm<128>(A, B, C, M, K, form, err_dev, s);
+    case 256: return launch_tc_gemm<256>(A, B, C, M, K, form, err_dev, s);
     }
     return set_error(LENTILS_ERR_UNSUPPORTED, "tc_gemm_bf16: N=%d", N);
 }

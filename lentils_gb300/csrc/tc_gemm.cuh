@@ -183,6 +183,165 @@ __global__ void __launch_bounds__(128)
     if (warp == 0) tmem_dealloc(tmem, ncols);
 }
 
+// -- pipelined form ------------------------------------------------------------------------------
+// The same GEMM with the operand staging taken off the tensor core's critical path. Loaders
+// give the ADDRESS of each 16-byte piece (`const void *LA::ptr(int m, int kpiece)`, null for a
+// zero piece). 160 threads: warps 0-3 copy the pieces straight into a ring of STAGES shared-
+// memory chunks with cp.async (no register staging), STAGES - 1 chunks ahead, and afterwards
+// run the epilogue; warp 4 owns the tensor memory and one of its threads issues the MMAs.
+// Chunk c is handed over through two mbarriers: `full` (128 producer arrivals, each after the
+// thread's copies of c have landed and been fenced for the async proxy) and `empty` (the
+// tcgen05.commit of the MMAs that read it). Waits are bounded; on a timeout *err is set, the
+// loops stop, and the kernel waits (bounded) for its MMAs before it frees tensor memory.
+constexpr int kPipeThreads = 160;
+
+template <int N, int STAGES>
+struct PipeSmem {
+    static constexpr int kStageBytes = GemmSmem<N>::kStageBytes;
+    static constexpr int kBytes = STAGES * kStageBytes;
+};
+
+template <int NP, class L>
+__device__ __forceinline__ void stage_rows_async(const L &ld, int r0, int kp0, int kp_end,
+                                                 unsigned char *s)
+{
+    const int t = threadIdx.x;
+    const int rr = ((t >> 6) << 3) + (t & 7), q = (t >> 3) & 7, kp = kp0 + q;
+#pragma unroll
+    for (int i = 0; i < NP; ++i) {
+        const void *src = (kp < kp_end) ? ld.ptr(r0 + 16 * i + rr, kp) : nullptr;
+        cp_async16(s + 2048 * i + 16 * t, src ? src : ld.base(), src ? 16u : 0u);
+    }
+}
+
+template <int N, int STAGES, class LA, class LB, class EP>
+__global__ void __launch_bounds__(kPipeThreads)
+    gemm_pipe_kernel(const LA la, const LB lb, const EP ep, int kpieces, int kp_per_split,
+                     int *err)
+{
+    static_assert(N % 16 == 0 && N >= 32 && N <= 256, "N");
+    static_assert(STAGES >= 2, "stages");
+    extern __shared__ __align__(1024) unsigned char smem[];
+    __shared__ uint64_t full[STAGES], empty[STAGES], done;
+    __shared__ uint32_t tmem_base;
+    __shared__ int abort_flag;
+    constexpr uint32_t ncols = (N <= 32) ? 32 : (N <= 64) ? 64 : (N <= 128) ? 128 : 256;
+    constexpr int L = STAGES - 1;  // chunks in flight ahead of the one handed over
+    const int m0 = blockIdx.x * 128;
+    const int n0 = blockIdx.y * N;
+    const int kp_begin = blockIdx.z * kp_per_split;
+    const int kp_end = min(kpieces, kp_begin + kp_per_split);
+    const int warp = threadIdx.x >> 5;
+    const int nchunks =
+        (kp_end > kp_begin) ? (kp_end - kp_begin + kPiecesPerChunk - 1) / kPiecesPerChunk : 0;
+
+    if (warp == 4) {
+        tmem_alloc(&tmem_base, ncols);
+        tmem_relinquish();
+    }
+    if (threadIdx.x == 0) {
+        for (int i = 0; i < STAGES; ++i) {
+            mbar_init(&full[i], 128);
+            mbar_init(&empty[i], 1);
+        }
+        mbar_init(&done, 1);
+        abort_flag = 0;
+        fence_mbar_init();
+    }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = tmem_base;
+    bool ok = true;
+
+    if (warp < 4) {  // producers
+        for (int ch = 0; ch < nchunks + L; ++ch) {
+            if (ch < nchunks) {
+                const int st = ch % STAGES;
+                if (ch >= STAGES) {
+                    if (!mbar_wait(&empty[st], ((ch / STAGES) - 1) & 1)) {
+                        ok = false;
+                        break;
+                    }
+                }
+                unsigned char *sa = smem + st * PipeSmem<N, STAGES>::kStageBytes;
+                const int kp0 = kp_begin + ch * kPiecesPerChunk;
+                stage_rows_async<128 / 16>(la, m0, kp0, kp_end, sa);
+                stage_rows_async<N / 16>(lb, n0, kp0, kp_end, sa + kATileBytes);
+            }
+            cp_async_commit();
+            if (ch >= L) {  // chunk ch - L has landed: hand it to the tensor core
+                cp_async_wait_group<L>();
+                fence_async_smem();
+                mbar_arrive(&full[(ch - L) % STAGES]);
+            }
+            if (*(volatile int *)&abort_flag) {
+                ok = false;
+                break;
+            }
+        }
+        cp_async_wait_all();
+        if (!ok) atomicExch(&abort_flag, 1);
+    } else if (threadIdx.x == 128) {  // the MMA issuer
+        constexpr uint32_t idesc = idesc_bf16_f32(128, N);
+        for (int ch = 0; ch < nchunks; ++ch) {
+            const int st = ch % STAGES;
+            if (!mbar_wait(&full[st], (ch / STAGES) & 1) || *(volatile int *)&abort_flag) {
+                ok = false;
+                break;
+            }
+            tc_fence_after();
+            unsigned char *sa = smem + st * PipeSmem<N, STAGES>::kStageBytes;
+            unsigned char *sb = sa + kATileBytes;
+#pragma unroll
+            for (int k = 0; k < kChunkK / 16; ++k) {
+                const uint64_t ad = smem_desc(smem_u32(sa) + k * 256, 128, 1024);
+                const uint64_t bd = smem_desc(smem_u32(sb) + k * 256, 128, 1024);
+                mma_bf16(tmem, ad, bd, idesc, (ch > 0 || k > 0) ? 1u : 0u);
+            }
+            mma_commit(&empty[st]);
+        }
+        if (!ok) atomicExch(&abort_flag, 1);
+        mma_commit(&done);  // arrives once every MMA issued above has completed
+    }
+    // every MMA has completed once `done` fires (bounded wait; on a timeout nothing is read)
+    const bool fin = mbar_wait(&done, 0);
+    tc_fence_after();
+    __syncthreads();
+    const bool good = fin && !*(volatile int *)&abort_flag && nchunks > 0;
+    if (threadIdx.x == 0 && (!fin || *(volatile int *)&abort_flag)) atomicExch(err, 1);
+    if (good && warp < 4) {
+        const int lane = threadIdx.x & 31;
+        const uint32_t taddr = tmem + ((uint32_t)(warp * 32) << 16);
+        if constexpr (row_per_lane<EP>::value || N % 32 != 0) {
+            for (int c0 = 0; c0 < N; c0 += 8) {
+                float v[8];
+                tmem_ld8(taddr + c0, v);
+#pragma unroll
+                for (int j = 0; j < 8; ++j) ep(m0 + warp * 32 + lane, n0 + c0 + j, v[j]);
+            }
+        } else {
+            float *tr = reinterpret_cast<float *>(smem) + warp * (32 * 33);
+            for (int c0 = 0; c0 < N; c0 += 32) {
+#pragma unroll
+                for (int j = 0; j < 32; j += 8) {
+                    float v[8];
+                    tmem_ld8(taddr + c0 + j, v);
+#pragma unroll
+                    for (int i = 0; i < 8; ++i) tr[lane * 33 + j + i] = v[i];
+                }
+                __syncwarp();
+#pragma unroll 4
+                for (int r = 0; r < 32; ++r) ep(m0 + warp * 32 + r, n0 + c0 + lane, tr[r * 33 + lane]);
+                __syncwarp();
+            }
+        }
+    }
+    tc_fence_before();
+    __syncthreads();
+    if (warp == 4) tmem_dealloc(tmem, ncols);
+}
+
 // -- loaders / epilogues for plain row-major GEMMs ----------------------------------------------
 struct RowMajorLoader {  // rows x K bf16, leading dimension ld (multiple of 8)
     const __nv_bfloat16 *p;
@@ -193,6 +352,13 @@ struct RowMajorLoader {  // rows x K bf16, leading dimension ld (multiple of 8)
         if (r >= rows || k >= K) return make_uint4(0, 0, 0, 0);
         return *reinterpret_cast<const uint4 *>(p + (size_t)r * ld + k);
     }
+    __device__ __forceinline__ const void *ptr(int r, int kp) const
+    {
+        const int k = kp * 8;
+        if (r >= rows || k >= K) return nullptr;
+        return p + (size_t)r * ld + k;
+    }
+    __device__ __forceinline__ const void *base() const { return p; }
 };
 
 struct StoreF32 {  // D -> row-major FP32 (M x N), bounds checked

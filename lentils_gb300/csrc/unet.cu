@@ -74,6 +74,19 @@ struct ConvFwdA {
         if (hh < 0 || hh >= H || ww < 0 || ww >= W) return make_uint4(0, 0, 0, 0);
         return *reinterpret_cast<const uint4 *>(x + ((size_t)(n * H + hh) * W + ww) * C + c);
     }
+    // the same piece's address (null: a zero piece), for the cp.async pipeline
+    __device__ __forceinline__ const void *ptr(int p, int kp) const
+    {
+        const int k = kp * 8;
+        const int t = k / C, c = k - t * C;
+        if (p >= npix || t >= ks * ks) return nullptr;
+        const int hw = H * W;
+        const int n = p / hw, r = p - n * hw, h = r / W, w = r - h * W;
+        const int hh = h + t / ks - ks / 2, ww = w + t % ks - ks / 2;
+        if (hh < 0 || hh >= H || ww < 0 || ww >= W) return nullptr;
+        return x + ((size_t)(n * H + hh) * W + ww) * C + c;
+    }
+    __device__ __forceinline__ const void *base() const { return x; }
 };
 
 __device__ __forceinline__ uint4 relu_mask(uint4 g, uint4 y)
@@ -105,6 +118,19 @@ struct ConvBwdDataA {
         if (!y) return g;
         return relu_mask(g, *reinterpret_cast<const uint4 *>(y + off));
     }
+    // address of the unmasked piece (y must be null: the pipeline copies bytes as they are)
+    __device__ __forceinline__ const void *ptr(int p, int kp) const
+    {
+        const int k = kp * 8;
+        const int t = k / C, c = k - t * C;
+        if (p >= npix || t >= ks * ks) return nullptr;
+        const int hw = H * W;
+        const int n = p / hw, r = p - n * hw, h = r / W, w = r - h * W;
+        const int hh = h - (t / ks - ks / 2), ww = w - (t % ks - ks / 2);
+        if (hh < 0 || hh >= H || ww < 0 || ww >= W) return nullptr;
+        return dy + ((size_t)(n * H + hh) * W + ww) * C + c;
+    }
+    __device__ __forceinline__ const void *base() const { return dy; }
 };
 
 // weight gradient, A side: row = output channel, piece = 8 pixels of the masked gradient
@@ -157,6 +183,41 @@ struct ConvBwdWB {
     }
 };
 
+// Weight gradient on transposed operands (the pipelined form): the GEMM rows are the (tap,
+// input channel) pairs and the columns the output channels, K runs over pixels, and both
+// operands are read as 16-byte pieces of 8 consecutive pixels from pixel-major copies made per
+// layer: xT[s][c][p] = x[p + s - 1][c] within the image row (zero across its ends), for the
+// three column shifts s of a 3 x 3 tap (one copy, s = 1, for 1 x 1), and dyT[co][p] = the
+// ReLU-masked output gradient. A tap's row shift is then a whole-row pixel offset, so a piece
+// is one aligned 16-byte load, or zero when the shifted row leaves the image.
+struct ConvWgXT {
+    const bf16 *xT;  // [3 or 1][C][npix]
+    int npix, H, W, C, ks;
+    __device__ __forceinline__ const void *ptr(int kk, int kp) const
+    {
+        const int t = kk / C, c = kk - t * C;
+        const int p0 = kp * 8;
+        if (t >= ks * ks || p0 >= npix) return nullptr;
+        const int dh = t / ks - ks / 2, dw = t % ks - ks / 2;
+        const int h = (p0 / W) % H;
+        if (h + dh < 0 || h + dh >= H) return nullptr;
+        return xT + ((size_t)(dw + ks / 2) * C + c) * npix + p0 + dh * W;
+    }
+    __device__ __forceinline__ const void *base() const { return xT; }
+};
+
+struct ConvWgDyT {
+    const bf16 *dyT;  // [C][npix]
+    int npix, C;
+    __device__ __forceinline__ const void *ptr(int co, int kp) const
+    {
+        const int p0 = kp * 8;
+        if (co >= C || p0 >= npix) return nullptr;
+        return dyT + (size_t)co * npix + p0;
+    }
+    __device__ __forceinline__ const void *base() const { return dyT; }
+};
+
 // -- epilogues -------------------------------------------------------------------------------------
 struct EpiAct {  // y[pixel][co] = bf16(relu?(v + bias))
     bf16 *y;
@@ -197,6 +258,15 @@ struct EpiAtomicF32 {  // g[row][col] += v
     __device__ __forceinline__ void operator()(int r, int c, float v) const
     {
         if (r < rows && c < cols && v != 0.f) atomicAdd(&g[(size_t)r * cols + c], v);
+    }
+};
+
+struct EpiAtomicF32T {  // g[col][row] += v (the weight gradient from its transposed GEMM)
+    float *g;
+    int rows, cols;  // rows = taps * cin_p (GEMM rows), cols = cout_p
+    __device__ __forceinline__ void operator()(int r, int c, float v) const
+    {
+        if (r < rows && c < cols && v != 0.f) atomicAdd(&g[(size_t)c * rows + r], v);
     }
 };
 
@@ -391,6 +461,58 @@ __global__ void bias_grad_kernel(const bf16 *__restrict__ dy, const bf16 *__rest
     if (c < creal) atomicAdd(&db[c], acc);
 }
 
+// Operands of the pipelined backward pass of a layer, from its output gradient dy and output y
+// (ReLU mask; null: none), C channels, pixels p0 .. p0 + 63 per block of 256 threads:
+// dym[p][c] = masked dy (pixel-major, for the data gradient) and dyT[c][p] (for the weight
+// gradient). C <= 128.
+__global__ void __launch_bounds__(256)
+    grad_prep_kernel(const bf16 *__restrict__ dy, const bf16 *__restrict__ y,
+                     bf16 *__restrict__ dym, bf16 *__restrict__ dyT, int npix, int C)
+{
+    __shared__ bf16 tile[64][129];
+    const int p0 = blockIdx.x * 64;
+    for (int e = threadIdx.x; e < 64 * C; e += blockDim.x) {
+        const int i = e / C, c = e - i * C, p = p0 + i;
+        bf16 v = __float2bfloat16(0.f);
+        if (p < npix) {
+            const size_t o = (size_t)p * C + c;
+            v = dy[o];
+            if (y && !(bf(y[o]) > 0.f)) v = __float2bfloat16(0.f);
+            dym[o] = v;
+        }
+        tile[i][c] = v;
+    }
+    __syncthreads();
+    for (int e = threadIdx.x; e < 64 * C; e += blockDim.x) {
+        const int c = e / 64, i = e - c * 64, p = p0 + i;
+        if (p < npix) dyT[(size_t)c * npix + p] = tile[i][c];
+    }
+}
+
+// xT[s][c][p] = x[p + s - shift0][c] when that pixel is in p's image row, else 0, for the
+// nshift column shifts s (3 for a 3 x 3 kernel: -1, 0, +1; 1 for 1 x 1: 0). C <= 128.
+__global__ void __launch_bounds__(256)
+    shift_transpose_kernel(const bf16 *__restrict__ x, bf16 *__restrict__ xT, int npix, int W,
+                           int C, int nshift)
+{
+    __shared__ bf16 tile[66][129];  // pixels p0 - 1 .. p0 + 64
+    const int p0 = blockIdx.x * 64;
+    for (int e = threadIdx.x; e < 66 * C; e += blockDim.x) {
+        const int i = e / C, c = e - i * C, p = p0 - 1 + i;
+        tile[i][c] = (p >= 0 && p < npix) ? x[(size_t)p * C + c] : __float2bfloat16(0.f);
+    }
+    __syncthreads();
+    const int half = nshift / 2;
+    for (int e = threadIdx.x; e < nshift * 64 * C; e += blockDim.x) {
+        const int sc = e / 64, i = e - sc * 64;  // sc = shift * C + c
+        const int sh = sc / C, c = sc - sh * C, p = p0 + i;
+        if (p >= npix) continue;
+        const int dw = sh - half, w = p % W;
+        const bf16 v = (w + dw >= 0 && w + dw < W) ? tile[i + 1 + dw][c] : __float2bfloat16(0.f);
+        xT[((size_t)sh * C + c) * npix + p] = v;
+    }
+}
+
 // Adam step on a flat parameter vector; bias correction folded into the step size
 __global__ void adam_kernel(float *__restrict__ w, const float *__restrict__ g,
                             float *__restrict__ m, float *__restrict__ v, long long n, float lr,
@@ -519,6 +641,7 @@ __global__ void __launch_bounds__(1024)
 // ------------------------------------------------------------------------------------------------
 struct lentils_unet {
     int H, W, maxB;
+    int gemm_form;        // 0: pipelined convolution GEMMs (cp.async ring), 1: synchronous staging
     float jacobi_weight;  // gamma of the preconditioner form
     long long nparams;
     // per layer
@@ -536,6 +659,8 @@ struct lentils_unet {
     // gradients
     lentils::bf16 *dy_out, *d_c1, *d_u1, *d_c2, *d_u2, *d_c3, *d_u3, *d_b, *d_p3, *d_e3, *d_p2,
         *d_e2, *d_p1, *d_e1;
+    // operands of the pipelined backward pass (sized for the largest layer)
+    lentils::bf16 *dym, *dyT, *xT;
     float *loss;
     int *err;
     void *block;  // single allocation backing everything above
@@ -559,41 +684,80 @@ static cudaError_t gemm_smem_attr()
     return e;
 }
 
-template <int N, class LA, class EP>
-static int conv_gemm(const LA &la, const tc::RowMajorLoader &lb, const EP &ep, int M, int K,
-                     int *err, cudaStream_t s)
+// stages of the pipelined convolution GEMM (tc::gemm_pipe_kernel)
+constexpr int kConvStages = 3;
+
+template <int N, class LA, class LB, class EP>
+static cudaError_t gemm_pipe_smem_attr()
 {
-    auto kern = tc::gemm_kernel<N, LA, tc::RowMajorLoader, EP>;
-    const size_t smem = tc::GemmSmem<N>::kBytes;
-    LENTILS_CUDA_TRY((gemm_smem_attr<N, LA, tc::RowMajorLoader, EP>()));
-    const int kp = (K + 7) / 8;
-    kern<<<dim3((M + 127) / 128, 1, 1), 128, smem, s>>>(la, lb, ep, kp, kp, err);
+    static const cudaError_t e = cudaFuncSetAttribute(
+        tc::gemm_pipe_kernel<N, kConvStages, LA, LB, EP>,
+        cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tc::PipeSmem<N, kConvStages>::kBytes);
+    return e;
+}
+
+// One convolution GEMM over grid (mtiles, 1, nz) with kp_per_split pieces per split; pipe
+// selects tc::gemm_pipe_kernel (operands copied by cp.async; the loader must give addresses).
+template <int N, class LA, class EP>
+static int conv_gemm_launch(const LA &la, const tc::RowMajorLoader &lb, const EP &ep,
+                            int mtiles, int kp, int per, int nz, bool pipe, int *err,
+                            cudaStream_t s)
+{
+    if (pipe) {
+        auto kern = tc::gemm_pipe_kernel<N, kConvStages, LA, tc::RowMajorLoader, EP>;
+        LENTILS_CUDA_TRY((gemm_pipe_smem_attr<N, LA, tc::RowMajorLoader, EP>()));
+        kern<<<dim3(mtiles, 1, nz), tc::kPipeThreads, tc::PipeSmem<N, kConvStages>::kBytes, s>>>(
+            la, lb, ep, kp, per, err);
+    } else {
+        auto kern = tc::gemm_kernel<N, LA, tc::RowMajorLoader, EP>;
+        LENTILS_CUDA_TRY((gemm_smem_attr<N, LA, tc::RowMajorLoader, EP>()));
+        kern<<<dim3(mtiles, 1, nz), 128, tc::GemmSmem<N>::kBytes, s>>>(la, lb, ep, kp, per, err);
+    }
     LENTILS_CHECK_LAUNCH("conv gemm");
     return LENTILS_OK;
 }
 
+template <int N, class LA, class EP>
+static int conv_gemm(const LA &la, const tc::RowMajorLoader &lb, const EP &ep, int M, int K,
+                     bool pipe, int *err, cudaStream_t s)
+{
+    const int kp = (K + 7) / 8;
+    return conv_gemm_launch<N>(la, lb, ep, (M + 127) / 128, kp, kp, 1, pipe, err, s);
+}
+
 template <int N>
 static int conv_gemm_split(const ConvFwdA &la, const tc::RowMajorLoader &lb,
-                           const EpiPartialF32 &ep, int mtiles, int kp, int per, int nz, int *err,
-                           cudaStream_t s)
+                           const EpiPartialF32 &ep, int mtiles, int kp, int per, int nz, bool pipe,
+                           int *err, cudaStream_t s)
 {
-    auto kern = tc::gemm_kernel<N, ConvFwdA, tc::RowMajorLoader, EpiPartialF32>;
-    LENTILS_CUDA_TRY((gemm_smem_attr<N, ConvFwdA, tc::RowMajorLoader, EpiPartialF32>()));
-    kern<<<dim3(mtiles, 1, nz), 128, tc::GemmSmem<N>::kBytes, s>>>(la, lb, ep, kp, per, err);
-    LENTILS_CHECK_LAUNCH("conv gemm (split-K)");
-    return LENTILS_OK;
+    return conv_gemm_launch<N>(la, lb, ep, mtiles, kp, per, nz, pipe, err, s);
 }
 
 template <class LA, class EP>
 static int conv_gemm_n(int N, const LA &la, const tc::RowMajorLoader &lb, const EP &ep, int M,
-                       int K, int *err, cudaStream_t s)
+                       int K, bool pipe, int *err, cudaStream_t s)
 {
     switch (N) {
-    case 32: return conv_gemm<32>(la, lb, ep, M, K, err, s);
-    case 64: return conv_gemm<64>(la, lb, ep, M, K, err, s);
-    case 128: return conv_gemm<128>(la, lb, ep, M, K, err, s);
+    case 32: return conv_gemm<32>(la, lb, ep, M, K, pipe, err, s);
+    case 64: return conv_gemm<64>(la, lb, ep, M, K, pipe, err, s);
+    case 128: return conv_gemm<128>(la, lb, ep, M, K, pipe, err, s);
     }
     return set_error(LENTILS_ERR_UNSUPPORTED, "conv gemm N=%d", N);
+}
+
+// pixels (in pieces of 8) per CTA of the pipelined weight-gradient GEMM
+constexpr int kWgradPieces = 512;
+
+template <int N>
+static int wgrad_launch(const ConvWgXT &la, const ConvWgDyT &lb, const EpiAtomicF32T &ep,
+                        int mtiles, int kpieces, int per, int nz, int *err, cudaStream_t s)
+{
+    auto kern = tc::gemm_pipe_kernel<N, kConvStages, ConvWgXT, ConvWgDyT, EpiAtomicF32T>;
+    LENTILS_CUDA_TRY((gemm_pipe_smem_attr<N, ConvWgXT, ConvWgDyT, EpiAtomicF32T>()));
+    kern<<<dim3(mtiles, 1, nz), tc::kPipeThreads, tc::PipeSmem<N, kConvStages>::kBytes, s>>>(
+        la, lb, ep, kpieces, per, err);
+    LENTILS_CHECK_LAUNCH("weight gradient gemm (pipelined)");
+    return LENTILS_OK;
 }
 
 static int level_dims(const lentils_unet *net, int level, int &H, int &W)
@@ -613,9 +777,10 @@ static int layer_forward(lentils_unet *net, int l, const bf16 *x, void *y, int B
     const int K = c.ks * c.ks * c.cin_p;
     ConvFwdA la{x, npix, H, W, c.cin_p, c.ks};
     tc::RowMajorLoader lb{net->wf[l], c.cout_p, K, K};
+    const bool pipe = net->gemm_form == 0;
     if (l == kNumLayers - 1) {
         EpiOut ep{(float *)y, net->b32[l], npix};
-        return conv_gemm_n(c.cout_p, la, lb, ep, npix, K, net->err, s);
+        return conv_gemm_n(c.cout_p, la, lb, ep, npix, K, net->gemm_form == 0, net->err, s);
     }
     const int mtiles = (npix + 127) / 128;
     const int kp = (K + 7) / 8, nchunks = (kp + 7) / 8;
@@ -627,9 +792,9 @@ static int layer_forward(lentils_unet *net, int l, const bf16 *x, void *y, int B
         EpiPartialF32 ep{net->splitk, npix, c.cout_p};
         int st = LENTILS_OK;
         switch (c.cout_p) {
-        case 32: st = conv_gemm_split<32>(la, lb, ep, mtiles, kp, per, nz, net->err, s); break;
-        case 64: st = conv_gemm_split<64>(la, lb, ep, mtiles, kp, per, nz, net->err, s); break;
-        case 128: st = conv_gemm_split<128>(la, lb, ep, mtiles, kp, per, nz, net->err, s); break;
+        case 32: st = conv_gemm_split<32>(la, lb, ep, mtiles, kp, per, nz, pipe, net->err, s); break;
+        case 64: st = conv_gemm_split<64>(la, lb, ep, mtiles, kp, per, nz, pipe, net->err, s); break;
+        case 128: st = conv_gemm_split<128>(la, lb, ep, mtiles, kp, per, nz, pipe, net->err, s); break;
         default: return set_error(LENTILS_ERR_UNSUPPORTED, "split-K N=%d", c.cout_p);
         }
         if (st) return st;
@@ -639,7 +804,7 @@ static int layer_forward(lentils_unet *net, int l, const bf16 *x, void *y, int B
         return LENTILS_OK;
     }
     EpiAct ep{(bf16 *)y, net->b32[l], npix, c.cout_p, c.relu};
-    return conv_gemm_n(c.cout_p, la, lb, ep, npix, K, net->err, s);
+    return conv_gemm_n(c.cout_p, la, lb, ep, npix, K, pipe, net->err, s);
 }
 
 // backward of layer l: dy (gradient of its output, before the ReLU mask), y (its output, for
@@ -656,6 +821,44 @@ static int layer_backward(lentils_unet *net, int l, const bf16 *dy, const bf16 *
     // bias gradient
     bias_grad_kernel<<<std::min(npix, 1024), c.cout_p, 0, s>>>(dy, mask, net->gb[l], npix, c.cout_p, c.cout);
     LENTILS_CHECK_LAUNCH("bias_grad_kernel");
+    // the transposed weight-gradient operands take 8 pixels of one image row per piece
+    const bool pipe = net->gemm_form == 0 && c.cout_p <= 128 && c.cin_p <= 128 && (W % 8) == 0;
+    if (pipe) {
+        // masked gradient (pixel-major and transposed) and the shifted transposed input
+        const int blocks = (npix + 63) / 64;
+        grad_prep_kernel<<<blocks, 256, 0, s>>>(dy, mask, net->dym, net->dyT, npix, c.cout_p);
+        LENTILS_CHECK_LAUNCH("grad_prep_kernel");
+        shift_transpose_kernel<<<blocks, 256, 0, s>>>(x, net->xT, npix, W, c.cin_p,
+                                                      c.ks == 3 ? 3 : 1);
+        LENTILS_CHECK_LAUNCH("shift_transpose_kernel");
+        // weight gradient: rows = taps * cin_p, columns = cout_p, K = pixels split over CTAs
+        const int Kw = taps * c.cin_p;
+        ConvWgXT la{net->xT, npix, H, W, c.cin_p, c.ks};
+        ConvWgDyT lb{net->dyT, npix, c.cout_p};
+        EpiAtomicF32T ep{net->gw_pad[l], Kw, c.cout_p};
+        const int kpieces = npix / 8;  // npix is a multiple of 8 (W is)
+        const int per = kWgradPieces;
+        const int nz = (kpieces + per - 1) / per;
+        const int mtiles = (Kw + 127) / 128;
+        int st = LENTILS_OK;
+        switch (c.cout_p) {
+        case 32: st = wgrad_launch<32>(la, lb, ep, mtiles, kpieces, per, nz, net->err, s); break;
+        case 64: st = wgrad_launch<64>(la, lb, ep, mtiles, kpieces, per, nz, net->err, s); break;
+        case 128: st = wgrad_launch<128>(la, lb, ep, mtiles, kpieces, per, nz, net->err, s); break;
+        default: return set_error(LENTILS_ERR_UNSUPPORTED, "weight gradient N=%d", c.cout_p);
+        }
+        if (st) return st;
+        if (dx) {  // data gradient from the masked copy: plain gathers, pipelined
+            const int K = taps * c.cout_p;
+            ConvBwdDataA lad{net->dym, nullptr, npix, H, W, c.cout_p, c.ks};
+            tc::RowMajorLoader lbd{net->wb[l], c.cin_p, K, K};
+            EpiStoreBf16 epd{dx, npix, c.cin_p};
+            if (int st2 = conv_gemm_n(std::max(32, c.cin_p), lad, lbd, epd, npix, K, true,
+                                      net->err, s))
+                return st2;
+        }
+        return LENTILS_OK;
+    }
     // weight gradient: M = cout_p (one tile), N = taps * cin_p in tiles of <= 256, K = pixels
     {
         const int Kw = taps * c.cin_p;
@@ -689,7 +892,9 @@ static int layer_backward(lentils_unet *net, int l, const bf16 *dy, const bf16 *
         ConvBwdDataA la{dy, mask, npix, H, W, c.cout_p, c.ks};
         tc::RowMajorLoader lb{net->wb[l], c.cin_p, K, K};
         EpiStoreBf16 ep{dx, npix, c.cin_p};
-        if (int st = conv_gemm_n(std::max(32, c.cin_p), la, lb, ep, npix, K, net->err, s)) return st;
+        if (int st = conv_gemm_n(std::max(32, c.cin_p), la, lb, ep, npix, K,
+                                 net->gemm_form == 0 && !mask, net->err, s))
+            return st;
     }
     return LENTILS_OK;
 }
@@ -923,6 +1128,18 @@ int lentils_unet_create(lentils_unet **out, int H, int W, int max_batch, const f
     add((void **)&net->d_e2, b2 * np0 / 4 * 64);
     add((void **)&net->d_p1, b2 * np0 / 4 * 32);
     add((void **)&net->d_e1, b2 * np0 * 32);
+    {
+        size_t dmax = 0, xmax = 0;  // largest npix * cout_p and 3 * npix * cin_p over the layers
+        for (int l = 0; l < kNumLayers; ++l) {
+            const ConvSpec &c = kLayers[l];
+            const size_t np = (size_t)np0 >> (2 * c.level);
+            dmax = std::max(dmax, np * c.cout_p);
+            xmax = std::max(xmax, np * c.cin_p * (c.ks == 3 ? 3 : 1));
+        }
+        add((void **)&net->dym, b2 * dmax);
+        add((void **)&net->dyT, b2 * dmax);
+        add((void **)&net->xT, b2 * xmax);
+    }
     add((void **)&net->loss, sizeof(float));
     add((void **)&net->pscale, sizeof(float));
     add((void **)&net->splitk, sizeof(float) * kSplitSlabPix * 128);
@@ -1066,6 +1283,14 @@ int lentils_unet_backward(lentils_unet *net, const float *dout, int Bn, float lr
         LENTILS_CUDA_TRY(cudaStreamSynchronize(s));
     }
     if (lr > 0.f && (st = adam_update(net, lr, s))) return st;
+    return LENTILS_OK;
+}
+
+int lentils_unet_set_gemm_form(lentils_unet *net, int form)
+{
+    clear_error();
+    if (!net || form < 0 || form > 1) return set_error(LENTILS_ERR_INVALID, "unet_set_gemm_form");
+    net->gemm_form = form;
     return LENTILS_OK;
 }
 

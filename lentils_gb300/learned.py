@@ -191,6 +191,10 @@ class UNet:
                                                   _ptr(z), self._sp()))
         return z
 
+    def set_gemm_form(self, form):
+        """Convolution GEMM kernel (lentils_unet_set_gemm_form): 0 pipelined, 1 staged."""
+        N.check(N.lib().lentils_unet_set_gemm_form(self._h, int(form)))
+
     def set_jacobi_weight(self, gamma):
         N.check(N.lib().lentils_unet_set_jacobi_weight(self._h, float(gamma)))
 

@@ -70,9 +70,9 @@ class BatchedSweep:
     Per sample s: grid_in[s] (2n x (n+1) complex64 half plane), vis_in[s] (plan-order
     complex64), and after run(): vis_out[s] = degrid(grid_in[s]), grid_out[s] =
     grid(vis_in[s]), beta_out[s] (n*n, 2) float32 source-plane positions of the pixel centres
-    (x-major)."""
+    (x-major). form selects the sweep kernel's item functions (lentils_sweep_create flags)."""
 
-    def __init__(self, samples, tuner=None, seed=1):
+    def __init__(self, samples, tuner=None, seed=1, form=0):
         from .spaces import ImageSpace
         from .synthetic import padded_fourier_space, synth_uv
         self.samples = list(samples)
@@ -122,7 +122,8 @@ class BatchedSweep:
                 c.dx = c.dy = dx
                 c.beta_out = _ptr(bo)
             self._h = ctypes.c_void_p()
-            N.check(N.lib().lentils_sweep_create(ctypes.byref(self._h), cs, len(self.samples), 0,
+            N.check(N.lib().lentils_sweep_create(ctypes.byref(self._h), cs, len(self.samples),
+                                                 int(form),
                                                  ctypes.c_void_p(self.stream.cuda_stream)))
         self.stream.synchronize()
 

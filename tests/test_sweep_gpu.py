@@ -69,6 +69,29 @@ def test_sweep_matches_per_sample_entry_points(sweep, use_graph):
         assert torch.allclose(sw.beta_out[k], b_ref, rtol=0, atol=2e-6), k
 
 
+@pytest.mark.parametrize("form", [1, 2])
+def test_sweep_kernel_forms(sweep, form):
+    """The other item forms of the sweep kernel (column-pair gridder; same-cell chunk or
+    per-visibility degridding) on the same samples, plans and inputs: visibilities identical,
+    grids within FP32 summation order, deflections identical."""
+    from lentils_gb300.autotune import Autotuner
+    from lentils_gb300.sweep import BatchedSweep
+    sw, _, path = sweep
+    sw.run(use_graph=True)
+    sw.stream.synchronize()
+    tuner = Autotuner(path=path, tiles=(8, 16), chunks=(256, 1024), mode="batched")
+    other = BatchedSweep(_samples(np.random.default_rng(11)), tuner=tuner, form=form)
+    assert tuner.tuned == 0
+    other.run(use_graph=True)
+    other.stream.synchronize()
+    for k in range(len(sw.samples)):
+        assert torch.equal(other.grid_in[k], sw.grid_in[k]) and torch.equal(other.vis_in[k], sw.vis_in[k])
+        assert torch.equal(other.vis_out[k], sw.vis_out[k]), k
+        rel = float((other.grid_out[k] - sw.grid_out[k]).abs().norm() / sw.grid_out[k].abs().norm())
+        assert rel < 1e-6, (k, rel)
+        assert torch.equal(other.beta_out[k], sw.beta_out[k]), k
+
+
 def test_sweep_against_oracle(sweep):
     """Two samples (one per KB width) in user row order against the FP64 CPU oracle."""
     from lentils_gb300.lens_models import GlobalLensModel

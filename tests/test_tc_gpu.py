@@ -8,10 +8,11 @@ import torch
 pytestmark = pytest.mark.gpu
 
 
+@pytest.mark.parametrize("form", [0, 1])
 @pytest.mark.parametrize("M,N,K", [(128, 64, 64), (256, 64, 192), (384, 128, 576),
                                    (128, 32, 64), (200, 256, 128), (1000, 128, 1152),
-                                   (128, 32, 72), (256, 64, 200)])
-def test_tc_gemm_bf16(native, M, N, K):
+                                   (128, 32, 72), (256, 64, 200), (512, 32, 8), (640, 128, 4096)])
+def test_tc_gemm_bf16(native, M, N, K, form):
     L = native.lib()
     g = torch.Generator(device="cuda").manual_seed(M * 7 + N + K)
     A = torch.randn(M, K, device="cuda", generator=g).to(torch.bfloat16)
@@ -19,7 +20,7 @@ def test_tc_gemm_bf16(native, M, N, K):
     C = torch.full((M, N), float("nan"), device="cuda")
     err = torch.zeros(1, dtype=torch.int32, device="cuda")
     st = L.lentils_tc_gemm_bf16(ctypes.c_void_p(A.data_ptr()), ctypes.c_void_p(B.data_ptr()),
-                                ctypes.c_void_p(C.data_ptr()), M, N, K, 0,
+                                ctypes.c_void_p(C.data_ptr()), M, N, K, form,
                                 ctypes.c_void_p(err.data_ptr()), None)
     torch.cuda.synchronize()
     assert st == 0 and int(err.item()) == 0
@@ -36,4 +37,5 @@ def test_bounded_wait_times_out_and_context_survives(native):
     assert L.lentils_tc_timeout_selftest(ctypes.c_void_p(err.data_ptr()), 1000, None) == 0
     torch.cuda.synchronize()
     assert int(err.item()) == 1
-    test_tc_gemm_bf16(native, 128, 64, 64)
+    test_tc_gemm_bf16(native, 128, 64, 64, 0)
+    test_tc_gemm_bf16(native, 128, 64, 64, 1)

