@@ -453,8 +453,10 @@ int lentils_dot64(const double *a, const double *b, int n, double *out, void *st
  * {32, 64, 128, 256}, K a multiple of 8. The core of the learned preconditioner's kernels,
  * exposed for testing. form 0: the threads stage each K chunk and then the tensor core runs it
  * (double-buffered); form 1: the pipelined kernel (operands copied by cp.async into a ring of
- * chunks, the MMAs issued by a thread of a fifth warp). *err_dev (device int) is set to 1 if a
- * bounded wait on the tensor core gave up (the result is then invalid).
+ * chunks, the MMAs issued by a thread of a fifth warp); form 2: operands loaded by TMA
+ * (tensor maps, 128-byte swizzled shared-memory tiles; A and B 16-byte aligned). *err_dev
+ * (device int) is set to 1 if a bounded wait on the tensor core gave up (the result is then
+ * invalid).
  * ---------------------------------------------------------------------------------------- */
 int lentils_tc_gemm_bf16(const void *A, const void *B, float *C, int M, int N, int K,
                          int form, int *err_dev, void *stream);

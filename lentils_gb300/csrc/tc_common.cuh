@@ -113,6 +113,87 @@ __device__ __forceinline__ uint64_t smem_desc(uint32_t saddr, uint32_t lbo_bytes
     return d;                // base offset 0, LBO mode 0, layout type 0 (no swizzle)
 }
 
+// Shared-memory matrix descriptor for a K-major operand in the 128-byte swizzled layout that a
+// TMA load with CU_TENSOR_MAP_SWIZZLE_128B writes: rows of 64 BF16 values (128 bytes), groups
+// of 8 rows 1024 bytes apart (SBO), 16-byte chunks permuted within each row by the row index
+// modulo 8. The group base must be 1024-byte aligned; a K step of 16 values advances the start
+// address by 32 bytes. LBO is unused in this layout (encoded as 1).
+__device__ __forceinline__ uint64_t smem_desc_sw128(uint32_t saddr)
+{
+    uint64_t d = 0;
+    d |= (uint64_t)((saddr >> 4) & 0x3FFFu);
+    d |= (uint64_t)1 << 16;                     // LBO (unused)
+    d |= (uint64_t)(1024 >> 4) << 32;           // SBO: 8 rows x 128 bytes
+    d |= (uint64_t)1 << 46;                     // descriptor version
+    d |= (uint64_t)2 << 61;                     // layout: 128-byte swizzle
+    return d;
+}
+
+// The same for rows of 32 BF16 values (64 bytes) in the 64-byte swizzled layout
+// (CU_TENSOR_MAP_SWIZZLE_64B): groups of 8 rows 512 bytes apart; a K step of 16 values advances
+// the start address by 32 bytes.
+__device__ __forceinline__ uint64_t smem_desc_sw64(uint32_t saddr)
+{
+    uint64_t d = 0;
+    d |= (uint64_t)((saddr >> 4) & 0x3FFFu);
+    d |= (uint64_t)1 << 16;                     // LBO (unused)
+    d |= (uint64_t)(512 >> 4) << 32;            // SBO: 8 rows x 64 bytes
+    d |= (uint64_t)1 << 46;                     // descriptor version
+    d |= (uint64_t)4 << 61;                     // layout: 64-byte swizzle
+    return d;
+}
+
+template <int SWZ>
+__device__ __forceinline__ uint64_t smem_desc_swz(uint32_t saddr)
+{
+    static_assert(SWZ == 64 || SWZ == 128, "swizzle");
+    if constexpr (SWZ == 128) return smem_desc_sw128(saddr);
+    else return smem_desc_sw64(saddr);
+}
+
+// -- TMA --------------------------------------------------------------------------------------
+// mbarrier arrival that also expects `bytes` of asynchronous copies to complete on it
+__device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t *bar, uint32_t bytes)
+{
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)),
+                 "r"(bytes)
+                 : "memory");
+}
+// 3-D tiled TMA load of the box at (x, y, z) (x innermost)
+__device__ __forceinline__ void tma_load_3d(void *dst, const void *map, int x, int y, int z,
+                                            uint64_t *bar)
+{
+    asm volatile(
+        "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes "
+        "[%0], [%1, {%2, %3, %4}], [%5];" ::"r"(smem_u32(dst)),
+        "l"(map), "r"(x), "r"(y), "r"(z), "r"(smem_u32(bar))
+        : "memory");
+}
+
+// 4-D tiled TMA load of the box at (x, y, z, w) (x innermost; coordinates may be negative or
+// past the end, which reads zeros)
+__device__ __forceinline__ void tma_load_4d(void *dst, const void *map, int x, int y, int z, int w,
+                                            uint64_t *bar)
+{
+    asm volatile(
+        "cp.async.bulk.tensor.4d.shared::cluster.global.tile.mbarrier::complete_tx::bytes "
+        "[%0], [%1, {%2, %3, %4, %5}], [%6];" ::"r"(smem_u32(dst)),
+        "l"(map), "r"(x), "r"(y), "r"(z), "r"(w), "r"(smem_u32(bar))
+        : "memory");
+}
+
+// 2-D tiled TMA load of the box at (x, y) (x innermost, in elements) into shared memory;
+// completion is signalled on `bar` as transaction bytes. `map` is the generic address of a
+// CUtensorMap in parameter (__grid_constant__), constant or global memory.
+__device__ __forceinline__ void tma_load_2d(void *dst, const void *map, int x, int y, uint64_t *bar)
+{
+    asm volatile(
+        "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes "
+        "[%0], [%1, {%2, %3}], [%4];" ::"r"(smem_u32(dst)),
+        "l"(map), "r"(x), "r"(y), "r"(smem_u32(bar))
+        : "memory");
+}
+
 // Instruction descriptor for kind::f16 with BF16 A and B, FP32 accumulation, both operands
 // K-major, shape M x N.
 __host__ __device__ constexpr uint32_t idesc_bf16_f32(int M, int N)

@@ -3,6 +3,7 @@
 //   C[M x N] (f32, row-major) = A[M x K] (bf16, row-major) * B[N x K]^T (bf16, row-major)
 #include "common.cuh"
 #include "tc_gemm.cuh"
+#include "tma.cuh"
 
 namespace lentils {
 
@@ -16,6 +17,22 @@ static int launch_tc_gemm(const void *A, const void *B, float *C, int M, int K, 
     StoreF32 ep{C, M, N, N};
     const int kpieces = (K + 7) / 8;
     dim3 grid((M + 127) / 128, 1, 1);
+    if (form == 2) {
+        constexpr int kStages = 4;
+        TmaRowMajor<128> ta;
+        TmaRowMajor<N> tb;
+        const uint64_t da[2] = {(uint64_t)K, (uint64_t)M}, db[2] = {(uint64_t)K, (uint64_t)N};
+        const uint64_t stride[1] = {(uint64_t)K * 2};
+        const uint32_t ba[2] = {64, 128}, bb[2] = {64, (uint32_t)N};
+        if (int st = tma_map_bf16(&ta.map, A, 2, da, stride, ba)) return st;
+        if (int st = tma_map_bf16(&tb.map, B, 2, db, stride, bb)) return st;
+        const size_t smem = TmaSmem<N, kStages>::kBytes;
+        auto kern = gemm_tma_kernel<N, kStages, TmaRowMajor<128>, TmaRowMajor<N>, StoreF32>;
+        LENTILS_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        kern<<<grid, kPipeThreads, smem, s>>>(ta, tb, ep, kpieces, kpieces, err);
+        LENTILS_CHECK_LAUNCH("tc gemm_tma_kernel");
+        return LENTILS_OK;
+    }
     if (form == 1) {
         constexpr int kStages = 3;
         const size_t smem = PipeSmem<N, kStages>::kBytes;
@@ -77,7 +94,7 @@ int lentils_tc_gemm_bf16(const void *A, const void *B, float *C, int M, int N, i
                          int form, int *err_dev, void *stream)
 {
     clear_error();
-    if (!A || !B || !C || !err_dev || M < 1 || K < 8 || (K % 8) != 0 || form < 0 || form > 1)
+    if (!A || !B || !C || !err_dev || M < 1 || K < 8 || (K % 8) != 0 || form < 0 || form > 2)
         return set_error(LENTILS_ERR_INVALID, "tc_gemm_bf16: bad arguments");
     cudaStream_t s = (cudaStream_t)stream;
     switch (N) {

@@ -15,6 +15,8 @@
 // kernel still frees its tensor memory.
 #pragma once
 
+#include <cuda.h>
+
 #include "tc_common.cuh"
 
 namespace lentils {
@@ -341,6 +343,160 @@ __global__ void __launch_bounds__(kPipeThreads)
     __syncthreads();
     if (warp == 4) tmem_dealloc(tmem, ncols);
 }
+
+// -- TMA form ------------------------------------------------------------------------------------
+// The GEMM fed by TMA: operands are functors `void LA::load(void *dst, uint64_t *bar, int row0,
+// int kp0) const` that issue the tensor-map loads of one K chunk (kChunk values starting at
+// piece kp0, in the swizzled layout of kSwz-byte rows: 64 values with 128-byte swizzle or 32
+// with 64-byte) of rows row0 .. row0 + 127 (A; LB: N rows) onto the mbarrier `bar`, with
+// `static constexpr uint32_t kBytes` the bytes they deliver. One thread issues every load (the
+// operands must be passed as __grid_constant__ so that their tensor maps have parameter-space
+// addresses), one thread of warp 4 issues the MMAs, warps 0-3 run the epilogue. STAGES chunks
+// are in flight; `full` expects the chunk's bytes, `empty` is the MMAs' commit.
+template <int N, int STAGES, int KCH = 64>
+struct TmaSmem {
+    static constexpr int kATile = 128 * KCH * 2;
+    static constexpr int kStageBytes = kATile + N * KCH * 2;
+    static constexpr int kBytes = STAGES * kStageBytes + 1024;  // + alignment slack
+};
+
+template <int N, int STAGES, class LA, class LB, class EP>
+__global__ void __launch_bounds__(kPipeThreads)
+    gemm_tma_kernel(const __grid_constant__ LA la, const __grid_constant__ LB lb, const EP ep,
+                    int kpieces, int kp_per_split, int *err)
+{
+    static_assert(N % 16 == 0 && N >= 32 && N <= 256, "N");
+    constexpr int KCH = LA::kChunk, SWZ = LA::kSwz;
+    static_assert(LB::kChunk == KCH && LB::kSwz == SWZ && KCH * 2 == SWZ, "operand layouts");
+    constexpr int kATile = TmaSmem<N, STAGES, KCH>::kATile;
+    constexpr int kPieces = KCH / 8;  // pieces of 8 values per chunk
+    static_assert(LA::kBytes == (uint32_t)kATile && LB::kBytes == (uint32_t)(N * KCH * 2),
+                  "operand bytes");
+    extern __shared__ __align__(1024) unsigned char smem_raw[];
+    __shared__ uint64_t full[STAGES], empty[STAGES], done;
+    __shared__ uint32_t tmem_base;
+    __shared__ int abort_flag;
+    // 128-byte swizzle atoms need 1024-byte aligned tiles
+    unsigned char *smem = smem_raw + ((1024 - (smem_u32(smem_raw) & 1023)) & 1023);
+    constexpr uint32_t ncols = (N <= 32) ? 32 : (N <= 64) ? 64 : (N <= 128) ? 128 : 256;
+    constexpr int kStage = TmaSmem<N, STAGES, KCH>::kStageBytes;
+    const int m0 = blockIdx.x * 128;
+    const int n0 = blockIdx.y * N;
+    const int kp_begin = blockIdx.z * kp_per_split;
+    const int kp_end = min(kpieces, kp_begin + kp_per_split);
+    const int warp = threadIdx.x >> 5;
+    const int nchunks = (kp_end > kp_begin) ? (kp_end - kp_begin + kPieces - 1) / kPieces : 0;
+
+    if (warp == 4) {
+        tmem_alloc(&tmem_base, ncols);
+        tmem_relinquish();
+    }
+    if (threadIdx.x == 0) {
+        for (int i = 0; i < STAGES; ++i) {
+            mbar_init(&full[i], 1);
+            mbar_init(&empty[i], 1);
+        }
+        mbar_init(&done, 1);
+        abort_flag = 0;
+        fence_mbar_init();
+    }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = tmem_base;
+    int last[STAGES];  // producer: the last chunk loaded into each stage (-1: none)
+#pragma unroll
+    for (int i = 0; i < STAGES; ++i) last[i] = -1;
+
+    if (threadIdx.x == 0) {  // the TMA producer
+        for (int ch = 0; ch < nchunks; ++ch) {
+            const int st = ch % STAGES;
+            if (ch >= STAGES && !mbar_wait(&empty[st], ((ch / STAGES) - 1) & 1)) {
+                atomicExch(&abort_flag, 1);
+                break;
+            }
+            if (*(volatile int *)&abort_flag) break;
+            unsigned char *sa = smem + st * kStage;
+            const int kp0 = kp_begin + ch * kPieces;
+            mbar_arrive_expect_tx(&full[st], LA::kBytes + LB::kBytes);
+            la.load(sa, &full[st], m0, kp0);
+            lb.load(sa + kATile, &full[st], n0, kp0);
+            last[st] = ch;
+        }
+    } else if (threadIdx.x == 128) {  // the MMA issuer
+        constexpr uint32_t idesc = idesc_bf16_f32(128, N);
+        for (int ch = 0; ch < nchunks; ++ch) {
+            const int st = ch % STAGES;
+            if (!mbar_wait(&full[st], (ch / STAGES) & 1) || *(volatile int *)&abort_flag) {
+                atomicExch(&abort_flag, 1);
+                break;
+            }
+            tc_fence_after();
+            const uint32_t sa = smem_u32(smem + st * kStage);
+            const uint32_t sb = sa + kATile;
+#pragma unroll
+            for (int k = 0; k < KCH / 16; ++k)
+                mma_bf16(tmem, smem_desc_swz<SWZ>(sa + 32 * k), smem_desc_swz<SWZ>(sb + 32 * k),
+                         idesc, (ch > 0 || k > 0) ? 1u : 0u);
+            mma_commit(&empty[st]);
+        }
+        mma_commit(&done);
+    }
+    const bool fin = mbar_wait(&done, 0);
+    if (threadIdx.x == 0) {
+        // every load has landed before shared memory is reused or the CTA exits (the MMAs
+        // waited for each chunk they read; after an abort a chunk may not have been read)
+#pragma unroll
+        for (int i = 0; i < STAGES; ++i)
+            if (last[i] >= 0 && !mbar_wait(&full[i], (last[i] / STAGES) & 1)) atomicExch(&abort_flag, 1);
+    }
+    tc_fence_after();
+    __syncthreads();
+    const bool bad = !fin || *(volatile int *)&abort_flag;
+    if (threadIdx.x == 0 && bad) atomicExch(err, 1);
+    if (!bad && nchunks > 0 && warp < 4) {
+        const int lane = threadIdx.x & 31;
+        const uint32_t taddr = tmem + ((uint32_t)(warp * 32) << 16);
+        if constexpr (row_per_lane<EP>::value || N % 32 != 0) {
+            for (int c0 = 0; c0 < N; c0 += 8) {
+                float v[8];
+                tmem_ld8(taddr + c0, v);
+#pragma unroll
+                for (int j = 0; j < 8; ++j) ep(m0 + warp * 32 + lane, n0 + c0 + j, v[j]);
+            }
+        } else {
+            float *tr = reinterpret_cast<float *>(smem) + warp * (32 * 33);
+            for (int c0 = 0; c0 < N; c0 += 32) {
+#pragma unroll
+                for (int j = 0; j < 32; j += 8) {
+                    float v[8];
+                    tmem_ld8(taddr + c0 + j, v);
+#pragma unroll
+                    for (int i = 0; i < 8; ++i) tr[lane * 33 + j + i] = v[i];
+                }
+                __syncwarp();
+#pragma unroll 4
+                for (int r = 0; r < 32; ++r) ep(m0 + warp * 32 + r, n0 + c0 + lane, tr[r * 33 + lane]);
+                __syncwarp();
+            }
+        }
+    }
+    tc_fence_before();
+    __syncthreads();
+    if (warp == 4) tmem_dealloc(tmem, ncols);
+}
+
+// A row-major [rows][K] BF16 operand through a 2-D tensor map (K innermost, box 64 x ROWS).
+template <int ROWS>
+struct TmaRowMajor {
+    static constexpr int kChunk = 64, kSwz = 128;
+    static constexpr uint32_t kBytes = ROWS * 128;
+    CUtensorMap map;
+    __device__ __forceinline__ void load(void *dst, uint64_t *bar, int row0, int kp0) const
+    {
+        tma_load_2d(dst, &map, kp0 * 8, row0, bar);
+    }
+};
 
 // -- loaders / epilogues for plain row-major GEMMs ----------------------------------------------
 struct RowMajorLoader {  // rows x K bf16, leading dimension ld (multiple of 8)

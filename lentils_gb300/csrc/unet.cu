@@ -30,6 +30,7 @@
 
 #include "common.cuh"
 #include "tc_gemm.cuh"
+#include "tma.cuh"
 #include "unet.cuh"
 
 namespace lentils {
@@ -183,25 +184,27 @@ struct ConvBwdWB {
     }
 };
 
-// Weight gradient on transposed operands (the pipelined form): the GEMM rows are the (tap,
+// Weight gradient on transposed operands (the pipelined forms): the GEMM rows are the (tap,
 // input channel) pairs and the columns the output channels, K runs over pixels, and both
-// operands are read as 16-byte pieces of 8 consecutive pixels from pixel-major copies made per
-// layer: xT[s][c][p] = x[p + s - 1][c] within the image row (zero across its ends), for the
-// three column shifts s of a 3 x 3 tap (one copy, s = 1, for 1 x 1), and dyT[co][p] = the
-// ReLU-masked output gradient. A tap's row shift is then a whole-row pixel offset, so a piece
-// is one aligned 16-byte load, or zero when the shifted row leaves the image.
+// operands are read as pieces of consecutive pixels from channel-major copies made per layer:
+// xT[s][c][q] = x[p + s - 1][c] within the image row (zero across its ends), for the three
+// column shifts s of a 3 x 3 tap (one copy, s = 1, for 1 x 1), in a row-padded layout with a
+// zero row above and below each image (shift_transpose_kernel), and dyT[co][p] = the
+// ReLU-masked output gradient. A tap's row shift is then a whole-row offset, and a 16-byte
+// piece of 8 pixels is one aligned load.
 struct ConvWgXT {
-    const bf16 *xT;  // [3 or 1][C][npix]
+    const bf16 *xT;  // [3 or 1][C][qtot]
     int npix, H, W, C, ks;
+    long long qtot;
     __device__ __forceinline__ const void *ptr(int kk, int kp) const
     {
         const int t = kk / C, c = kk - t * C;
         const int p0 = kp * 8;
         if (t >= ks * ks || p0 >= npix) return nullptr;
         const int dh = t / ks - ks / 2, dw = t % ks - ks / 2;
-        const int h = (p0 / W) % H;
-        if (h + dh < 0 || h + dh >= H) return nullptr;
-        return xT + ((size_t)(dw + ks / 2) * C + c) * npix + p0 + dh * W;
+        const int hw = H * W, n = p0 / hw, r = p0 - n * hw, h = r / W, w = r - h * W;
+        const long long q = ((long long)n * (H + 2) + h + 1 + dh) * W + w;
+        return xT + ((size_t)(dw + ks / 2) * C + c) * qtot + q;
     }
     __device__ __forceinline__ const void *base() const { return xT; }
 };
@@ -216,6 +219,124 @@ struct ConvWgDyT {
         return dyT + (size_t)co * npix + p0;
     }
     __device__ __forceinline__ const void *base() const { return dyT; }
+};
+
+// The same operands loaded by TMA (tc::gemm_tma_kernel): xT in the row-padded layout of
+// shift_transpose_kernel as a 2-D tensor (padded pixel position innermost, (shift, channel)
+// rows), one box of 64 positions x C rows per tap of the row tile (a tap past the kernel's
+// reads rows past the tensor: zeros); dyT as a 2-D tensor (pixel innermost, output-channel
+// rows). A K chunk is 64 pixels of one image (H W is a multiple of 64), contiguous in both.
+struct ConvWgXTTma {
+    static constexpr int kChunk = 64, kSwz = 128;
+    static constexpr uint32_t kBytes = 128 * 128;
+    CUtensorMap map;
+    int C, ks, H, W, rows;  // rows = (number of shifts) * C
+    __device__ __forceinline__ void load(void *dst, uint64_t *bar, int m0, int kp0) const
+    {
+        const int p0 = kp0 * 8, hw = H * W;
+        const int n = p0 / hw, r = p0 - n * hw, h = r / W, w = r - h * W;
+        const int q0 = (n * (H + 2) + h + 1) * W + w;
+        const int t0 = m0 / C;
+        for (int j = 0; j < 128 / C; ++j) {
+            const int t = t0 + j;
+            unsigned char *d = static_cast<unsigned char *>(dst) + j * C * 128;
+            if (t < ks * ks) {
+                const int dh = t / ks - ks / 2, dw = t % ks - ks / 2;
+                tc::tma_load_2d(d, &map, q0 + dh * W, (dw + ks / 2) * C, bar);
+            } else {
+                tc::tma_load_2d(d, &map, q0, rows, bar);  // past the last row: zeros
+            }
+        }
+    }
+};
+
+template <int N>
+struct ConvWgDyTTma {
+    static constexpr int kChunk = 64, kSwz = 128;
+    static constexpr uint32_t kBytes = N * 128;
+    CUtensorMap map;
+    __device__ __forceinline__ void load(void *dst, uint64_t *bar, int n0, int kp0) const
+    {
+        tc::tma_load_2d(dst, &map, kp0 * 8, n0, bar);
+    }
+};
+
+// The same operands in the blocked layouts (W a multiple of 64): a tap's rows for a 64-pixel
+// chunk are one contiguous run of C x 128 bytes, loaded as a 3-D box (64, C, 1).
+struct ConvWgXTTmaBlk {
+    static constexpr int kChunk = 64, kSwz = 128;
+    static constexpr uint32_t kBytes = 128 * 128;
+    CUtensorMap map;  // (64, C, nshift * qtot / 64)
+    int C, ks, H, W, nblk;  // nblk = qtot / 64
+    __device__ __forceinline__ void load(void *dst, uint64_t *bar, int m0, int kp0) const
+    {
+        const int p0 = kp0 * 8, hw = H * W;
+        const int n = p0 / hw, r = p0 - n * hw, h = r / W, w = r - h * W;
+        const int q0 = (n * (H + 2) + h + 1) * W + w;  // a multiple of 64
+        const int t0 = m0 / C;
+        for (int j = 0; j < 128 / C; ++j) {
+            const int t = t0 + j;
+            unsigned char *d = static_cast<unsigned char *>(dst) + j * C * 128;
+            if (t < ks * ks) {
+                const int dh = t / ks - ks / 2, dw = t % ks - ks / 2;
+                tc::tma_load_3d(d, &map, 0, 0, (dw + ks / 2) * nblk + (q0 + dh * W) / 64, bar);
+            } else {
+                tc::tma_load_3d(d, &map, 0, 0, (ks == 3 ? 3 : 1) * nblk, bar);  // zeros
+            }
+        }
+    }
+};
+
+template <int N>
+struct ConvWgDyTTmaBlk {
+    static constexpr int kChunk = 64, kSwz = 128;
+    static constexpr uint32_t kBytes = N * 128;
+    CUtensorMap map;  // (64, N, npix / 64)
+    __device__ __forceinline__ void load(void *dst, uint64_t *bar, int n0, int kp0) const
+    {
+        tc::tma_load_3d(dst, &map, 0, n0, kp0 / 8, bar);
+    }
+};
+
+// A operand of a convolution over NHWC activations (forward: the input, taps as they are; data
+// gradient: the masked output gradient, taps flipped) through a 4-D tensor map (C, W, H, B)
+// with box (CB, WB, HB, 1): a row tile is 128 consecutive pixels of one image (WB HB = 128),
+// a K chunk is CB channels of one tap (K = tap C + c). The box is placed at the tap's pixel
+// offset, and the tensor map reads zeros where it leaves the image: the zero padding of the
+// convolution. CB = 64 (128-byte rows, 128-byte swizzle) or 32 (64-byte).
+template <int CB>
+struct ConvTmaA {
+    static constexpr int kChunk = CB, kSwz = 2 * CB;
+    static constexpr uint32_t kBytes = 128 * CB * 2;
+    CUtensorMap map;
+    int C, ks, H, W, flip;
+    __device__ __forceinline__ void load(void *dst, uint64_t *bar, int m0, int kp0) const
+    {
+        const int k = kp0 * 8, t = k / C, c0 = k - t * C;
+        const int hw = H * W, n = m0 / hw, r = m0 - n * hw, h = r / W, w = r - h * W;
+        if (t >= ks * ks) {  // past the last tap: a box past the channels reads zeros
+            tc::tma_load_4d(dst, &map, C, w, h, n, bar);
+            return;
+        }
+        int dh = t / ks - ks / 2, dw = t % ks - ks / 2;
+        if (flip) {
+            dh = -dh;
+            dw = -dw;
+        }
+        tc::tma_load_4d(dst, &map, c0, w + dw, h + dh, n, bar);
+    }
+};
+
+// B operand: row-major [N][K] BF16 weights through a 2-D tensor map, box (CB, N).
+template <int CB, int N>
+struct ConvTmaB {
+    static constexpr int kChunk = CB, kSwz = 2 * CB;
+    static constexpr uint32_t kBytes = N * CB * 2;
+    CUtensorMap map;
+    __device__ __forceinline__ void load(void *dst, uint64_t *bar, int n0, int kp0) const
+    {
+        tc::tma_load_2d(dst, &map, kp0 * 8, n0, bar);
+    }
 };
 
 // -- epilogues -------------------------------------------------------------------------------------
@@ -462,54 +583,91 @@ __global__ void bias_grad_kernel(const bf16 *__restrict__ dy, const bf16 *__rest
 }
 
 // Operands of the pipelined backward pass of a layer, from its output gradient dy and output y
-// (ReLU mask; null: none), C channels, pixels p0 .. p0 + 63 per block of 256 threads:
-// dym[p][c] = masked dy (pixel-major, for the data gradient) and dyT[c][p] (for the weight
-// gradient). C <= 128.
+// (ReLU mask; null: none), C channels (a multiple of 8, <= 128), 64 pixels per block of 256
+// threads: dym[p][c] = the masked gradient (pixel-major, for the data gradient), dyT[c][p]
+// (channel-major, for the weight gradient), and the bias gradient db[c] += sum over the
+// block's pixels (c < creal). 16-byte loads and stores; the transpose goes through shared
+// memory with rows padded to C + 8 values.
+// blocked: dyT in 64-pixel blocks, dyT[(p / 64) C + c][p % 64], so that a block's C rows are
+// one contiguous 128 C-byte run.
 __global__ void __launch_bounds__(256)
     grad_prep_kernel(const bf16 *__restrict__ dy, const bf16 *__restrict__ y,
-                     bf16 *__restrict__ dym, bf16 *__restrict__ dyT, int npix, int C)
+                     bf16 *__restrict__ dym, bf16 *__restrict__ dyT, float *__restrict__ db,
+                     int npix, int C, int creal, int blocked)
 {
-    __shared__ bf16 tile[64][129];
+    __shared__ __align__(16) bf16 tile[64][136];
     const int p0 = blockIdx.x * 64;
-    for (int e = threadIdx.x; e < 64 * C; e += blockDim.x) {
-        const int i = e / C, c = e - i * C, p = p0 + i;
-        bf16 v = __float2bfloat16(0.f);
+    const int cv = C / 8;
+    for (int e = threadIdx.x; e < 64 * cv; e += blockDim.x) {
+        const int i = e / cv, c8 = (e - i * cv) * 8, p = p0 + i;
+        uint4 v = make_uint4(0, 0, 0, 0);
         if (p < npix) {
-            const size_t o = (size_t)p * C + c;
-            v = dy[o];
-            if (y && !(bf(y[o]) > 0.f)) v = __float2bfloat16(0.f);
-            dym[o] = v;
+            const size_t o = (size_t)p * C + c8;
+            v = *reinterpret_cast<const uint4 *>(dy + o);
+            if (y) v = relu_mask(v, *reinterpret_cast<const uint4 *>(y + o));
+            *reinterpret_cast<uint4 *>(dym + o) = v;
         }
-        tile[i][c] = v;
+        *reinterpret_cast<uint4 *>(&tile[i][c8]) = v;
     }
     __syncthreads();
-    for (int e = threadIdx.x; e < 64 * C; e += blockDim.x) {
-        const int c = e / 64, i = e - c * 64, p = p0 + i;
-        if (p < npix) dyT[(size_t)c * npix + p] = tile[i][c];
+    if (threadIdx.x < creal) {
+        float acc = 0.f;
+        for (int i = 0; i < 64; ++i) acc += bf(tile[i][threadIdx.x]);
+        atomicAdd(&db[threadIdx.x], acc);
+    }
+    for (int e = threadIdx.x; e < 8 * C; e += blockDim.x) {  // 8 runs of 8 pixels per channel
+        const int c = e / 8, j = (e - c * 8) * 8;
+        if (p0 + j >= npix) continue;  // npix is a multiple of 8
+        bf16 r[8];
+#pragma unroll
+        for (int k = 0; k < 8; ++k) r[k] = tile[j + k][c];
+        const size_t o = blocked ? ((size_t)blockIdx.x * C + c) * 64 + j : (size_t)c * npix + p0 + j;
+        *reinterpret_cast<uint4 *>(dyT + o) = *reinterpret_cast<uint4 *>(r);
     }
 }
 
-// xT[s][c][p] = x[p + s - shift0][c] when that pixel is in p's image row, else 0, for the
-// nshift column shifts s (3 for a 3 x 3 kernel: -1, 0, +1; 1 for 1 x 1: 0). C <= 128.
+// xT[s][c][q] = x[p + s - nshift / 2][c] when that pixel is in p's image row, else 0, for the
+// nshift column shifts s (3 for a 3 x 3 kernel: -1, 0, +1; 1 for 1 x 1: 0). q is p's position
+// in the row-padded layout, q = (n (H + 2) + h + 1) W + w, with a zero row above and below each
+// image (written here too), so that a tap's row shift is a whole-row offset that reads zeros at
+// the image's edges. qtot = B (H + 2) W. C a multiple of 8, <= 128; 64 pixels per block.
+// blocked (W a multiple of 64): xT in 64-position blocks of the padded layout,
+// xT[(s qtot / 64 + q / 64) C + c][q % 64].
 __global__ void __launch_bounds__(256)
-    shift_transpose_kernel(const bf16 *__restrict__ x, bf16 *__restrict__ xT, int npix, int W,
-                           int C, int nshift)
+    shift_transpose_kernel(const bf16 *__restrict__ x, bf16 *__restrict__ xT, int npix, int H,
+                           int W, int C, int nshift, long long qtot, int blocked)
 {
-    __shared__ bf16 tile[66][129];  // pixels p0 - 1 .. p0 + 64
+    __shared__ __align__(16) bf16 tile[66][136];  // pixels p0 - 1 .. p0 + 64
     const int p0 = blockIdx.x * 64;
-    for (int e = threadIdx.x; e < 66 * C; e += blockDim.x) {
-        const int i = e / C, c = e - i * C, p = p0 - 1 + i;
-        tile[i][c] = (p >= 0 && p < npix) ? x[(size_t)p * C + c] : __float2bfloat16(0.f);
+    const int cv = C / 8;
+    for (int e = threadIdx.x; e < 66 * cv; e += blockDim.x) {
+        const int i = e / cv, c8 = (e - i * cv) * 8, p = p0 - 1 + i;
+        uint4 v = make_uint4(0, 0, 0, 0);
+        if (p >= 0 && p < npix) v = *reinterpret_cast<const uint4 *>(x + (size_t)p * C + c8);
+        *reinterpret_cast<uint4 *>(&tile[i][c8]) = v;
     }
     __syncthreads();
-    const int half = nshift / 2;
-    for (int e = threadIdx.x; e < nshift * 64 * C; e += blockDim.x) {
-        const int sc = e / 64, i = e - sc * 64;  // sc = shift * C + c
-        const int sh = sc / C, c = sc - sh * C, p = p0 + i;
-        if (p >= npix) continue;
-        const int dw = sh - half, w = p % W;
-        const bf16 v = (w + dw >= 0 && w + dw < W) ? tile[i + 1 + dw][c] : __float2bfloat16(0.f);
-        xT[((size_t)sh * C + c) * npix + p] = v;
+    const int half = nshift / 2, hw = H * W;
+    for (int e = threadIdx.x; e < nshift * 8 * C; e += blockDim.x) {
+        const int sc = e / 8, j = (e - sc * 8) * 8;  // sc = shift * C + c
+        const int sh = sc / C, c = sc - sh * C, p = p0 + j;
+        if (p >= npix) continue;  // npix is a multiple of 8 and W of 8: a run stays in one row
+        const int dw = sh - half;
+        const int n = p / hw, r = p - n * hw, h = r / W, w0 = r - h * W;
+        bf16 v[8];
+#pragma unroll
+        for (int k = 0; k < 8; ++k) {
+            const int w = w0 + k;
+            v[k] = (w + dw >= 0 && w + dw < W) ? tile[j + k + 1 + dw][c] : __float2bfloat16(0.f);
+        }
+        const long long q = ((long long)n * (H + 2) + h + 1) * W + w0;
+        auto at = [&](long long qq) {
+            return blocked ? xT + (((size_t)sh * (qtot / 64) + qq / 64) * C + c) * 64 + qq % 64
+                           : xT + (size_t)sc * qtot + qq;
+        };
+        *reinterpret_cast<uint4 *>(at(q)) = *reinterpret_cast<uint4 *>(v);
+        if (h == 0) *reinterpret_cast<uint4 *>(at(q - W)) = make_uint4(0, 0, 0, 0);
+        if (h == H - 1) *reinterpret_cast<uint4 *>(at(q + W)) = make_uint4(0, 0, 0, 0);
     }
 }
 
@@ -686,6 +844,9 @@ static cudaError_t gemm_smem_attr()
 
 // stages of the pipelined convolution GEMM (tc::gemm_pipe_kernel)
 constexpr int kConvStages = 3;
+// forward layers with fewer row tiles than this run the pipelined GEMM (measured at batch 32
+// on 128^2: faster for 64 and 256 tiles, slower for 1024 and 4096)
+constexpr int kPipeMaxTiles = 512;
 
 template <int N, class LA, class LB, class EP>
 static cudaError_t gemm_pipe_smem_attr()
@@ -745,8 +906,28 @@ static int conv_gemm_n(int N, const LA &la, const tc::RowMajorLoader &lb, const 
     return set_error(LENTILS_ERR_UNSUPPORTED, "conv gemm N=%d", N);
 }
 
-// pixels (in pieces of 8) per CTA of the pipelined weight-gradient GEMM
-constexpr int kWgradPieces = 512;
+// the weight-gradient GEMM splits its pixel reduction so that about kWgradCtas CTAs run, each
+// over at least kWgradMinPieces pieces of 8 pixels
+constexpr int kWgradCtas = 320;
+constexpr int kWgradMinPieces = 64;
+constexpr int kTmaStages = 4;
+
+template <int N>
+static int wgrad_tma_launch(const ConvWgXTTma &la, const bf16 *dyT, const uint64_t *db,
+                            const uint64_t *sb, const uint32_t *bb, const EpiAtomicF32T &ep,
+                            int mtiles, int kpieces, int per, int nz, int *err, cudaStream_t s)
+{
+    ConvWgDyTTma<N> lb;
+    if (int st = tma_map_bf16(&lb.map, dyT, 2, db, sb, bb)) return st;
+    auto kern = tc::gemm_tma_kernel<N, kTmaStages, ConvWgXTTma, ConvWgDyTTma<N>, EpiAtomicF32T>;
+    static const cudaError_t attr = cudaFuncSetAttribute(
+        kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tc::TmaSmem<N, kTmaStages>::kBytes);
+    LENTILS_CUDA_TRY(attr);
+    kern<<<dim3(mtiles, 1, nz), tc::kPipeThreads, tc::TmaSmem<N, kTmaStages>::kBytes, s>>>(
+        la, lb, ep, kpieces, per, err);
+    LENTILS_CHECK_LAUNCH("weight gradient gemm (TMA)");
+    return LENTILS_OK;
+}
 
 template <int N>
 static int wgrad_launch(const ConvWgXT &la, const ConvWgDyT &lb, const EpiAtomicF32T &ep,
@@ -757,6 +938,89 @@ static int wgrad_launch(const ConvWgXT &la, const ConvWgDyT &lb, const EpiAtomic
     kern<<<dim3(mtiles, 1, nz), tc::kPipeThreads, tc::PipeSmem<N, kConvStages>::kBytes, s>>>(
         la, lb, ep, kpieces, per, err);
     LENTILS_CHECK_LAUNCH("weight gradient gemm (pipelined)");
+    return LENTILS_OK;
+}
+
+// A convolution GEMM with TMA operands: activations act (NHWC, C channels, Bn images of
+// H x W; flip: data gradient), weights wt (row-major [N][K], K = ks^2 C), rows = pixels,
+// split over nz CTAs of kp_per_split pieces along K.
+template <int CB, int N, class EP>
+static int conv_tma_launch(const bf16 *act, int C, int ks, int Bn, int H, int W, int flip,
+                           const bf16 *wt, int K, const EP &ep, int nz, int kp_per_split,
+                           int *err, cudaStream_t s)
+{
+    constexpr int kStages = (CB == 64 && N == 128) ? 3 : 4;
+    ConvTmaA<CB> la;
+    la.C = C;
+    la.ks = ks;
+    la.H = H;
+    la.W = W;
+    la.flip = flip;
+    const int WB = std::min(W, 128), HB = 128 / WB;
+    const uint64_t da[4] = {(uint64_t)C, (uint64_t)W, (uint64_t)H, (uint64_t)Bn};
+    const uint64_t sa[3] = {(uint64_t)C * 2, (uint64_t)W * C * 2, (uint64_t)H * W * C * 2};
+    const uint32_t ba[4] = {(uint32_t)CB, (uint32_t)WB, (uint32_t)HB, 1};
+    if (int st = tma_map_bf16(&la.map, act, 4, da, sa, ba, 2 * CB)) return st;
+    ConvTmaB<CB, N> lb;
+    const uint64_t db[2] = {(uint64_t)K, (uint64_t)N};
+    const uint64_t sb[1] = {(uint64_t)K * 2};
+    const uint32_t bb[2] = {(uint32_t)CB, (uint32_t)N};
+    if (int st = tma_map_bf16(&lb.map, wt, 2, db, sb, bb, 2 * CB)) return st;
+    auto kern = tc::gemm_tma_kernel<N, kStages, ConvTmaA<CB>, ConvTmaB<CB, N>, EP>;
+    constexpr int smem = tc::TmaSmem<N, kStages, CB>::kBytes;
+    static const cudaError_t attr =
+        cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    LENTILS_CUDA_TRY(attr);
+    const int mtiles = Bn * H * W / 128;
+    kern<<<dim3(mtiles, 1, nz), tc::kPipeThreads, smem, s>>>(la, lb, ep, K / 8, kp_per_split, err);
+    LENTILS_CHECK_LAUNCH("convolution gemm (TMA)");
+    return LENTILS_OK;
+}
+
+// whether a layer's convolution can take the TMA operands: row tiles of 128 pixels inside one
+// image, CB-channel chunks, N in {32, 64, 128}
+static bool conv_tma_ok(int C, int N, int H, int W)
+{
+    return (C == 32 || C == 64 || C == 128) && (N == 32 || N == 64 || N == 128) &&
+           (H * W) % 128 == 0 && (W >= 128 ? W % 128 == 0 : 128 % W == 0);
+}
+
+template <class EP>
+static int conv_tma(const bf16 *act, int C, int ks, int Bn, int H, int W, int flip,
+                    const bf16 *wt, int N, const EP &ep, int nz, int kp_per_split, int *err,
+                    cudaStream_t s)
+{
+    const int K = ks * ks * C;
+    if (C == 32) {
+        switch (N) {
+        case 32: return conv_tma_launch<32, 32>(act, C, ks, Bn, H, W, flip, wt, K, ep, nz, kp_per_split, err, s);
+        case 64: return conv_tma_launch<32, 64>(act, C, ks, Bn, H, W, flip, wt, K, ep, nz, kp_per_split, err, s);
+        case 128: return conv_tma_launch<32, 128>(act, C, ks, Bn, H, W, flip, wt, K, ep, nz, kp_per_split, err, s);
+        }
+    } else {
+        switch (N) {
+        case 32: return conv_tma_launch<64, 32>(act, C, ks, Bn, H, W, flip, wt, K, ep, nz, kp_per_split, err, s);
+        case 64: return conv_tma_launch<64, 64>(act, C, ks, Bn, H, W, flip, wt, K, ep, nz, kp_per_split, err, s);
+        case 128: return conv_tma_launch<64, 128>(act, C, ks, Bn, H, W, flip, wt, K, ep, nz, kp_per_split, err, s);
+        }
+    }
+    return set_error(LENTILS_ERR_UNSUPPORTED, "conv_tma: C=%d N=%d", C, N);
+}
+
+template <int N>
+static int wgrad_tma_blk(const ConvWgXTTmaBlk &la, const bf16 *dyT, const uint64_t *db,
+                         const uint64_t *sb, const uint32_t *bb, const EpiAtomicF32T &ep,
+                         int mtiles, int kpieces, int per, int nz, int *err, cudaStream_t s)
+{
+    ConvWgDyTTmaBlk<N> lb;
+    if (int st = tma_map_bf16(&lb.map, dyT, 3, db, sb, bb)) return st;
+    auto kern = tc::gemm_tma_kernel<N, kTmaStages, ConvWgXTTmaBlk, ConvWgDyTTmaBlk<N>, EpiAtomicF32T>;
+    static const cudaError_t attr = cudaFuncSetAttribute(
+        kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tc::TmaSmem<N, kTmaStages>::kBytes);
+    LENTILS_CUDA_TRY(attr);
+    kern<<<dim3(mtiles, 1, nz), tc::kPipeThreads, tc::TmaSmem<N, kTmaStages>::kBytes, s>>>(
+        la, lb, ep, kpieces, per, err);
+    LENTILS_CHECK_LAUNCH("weight gradient gemm (TMA, blocked)");
     return LENTILS_OK;
 }
 
@@ -777,9 +1041,14 @@ static int layer_forward(lentils_unet *net, int l, const bf16 *x, void *y, int B
     const int K = c.ks * c.ks * c.cin_p;
     ConvFwdA la{x, npix, H, W, c.cin_p, c.ks};
     tc::RowMajorLoader lb{net->wf[l], c.cout_p, K, K};
-    const bool pipe = net->gemm_form == 0;
+    // the pipelined GEMM wins where a layer has few row tiles (the deep layers); with many
+    // CTAs the staged GEMM keeps more of them resident and hides its loads by occupancy
+    const int mt = (npix + 127) / 128;
+    const bool pipe = net->gemm_form == 0 && mt < kPipeMaxTiles;
+    const bool tma = net->gemm_form == 0 && conv_tma_ok(c.cin_p, c.cout_p, H, W);
     if (l == kNumLayers - 1) {
         EpiOut ep{(float *)y, net->b32[l], npix};
+        if (tma) return conv_tma(x, c.cin_p, c.ks, Bn, H, W, 0, net->wf[l], c.cout_p, ep, 1, K / 8, net->err, s);
         return conv_gemm_n(c.cout_p, la, lb, ep, npix, K, net->gemm_form == 0, net->err, s);
     }
     const int mtiles = (npix + 127) / 128;
@@ -791,7 +1060,8 @@ static int layer_forward(lentils_unet *net, int l, const bf16 *x, void *y, int B
     if (npix < kSplitMaxPix && nz > 1 && nz * n <= (long long)kSplitSlabPix * 128) {
         EpiPartialF32 ep{net->splitk, npix, c.cout_p};
         int st = LENTILS_OK;
-        switch (c.cout_p) {
+        if (tma) st = conv_tma(x, c.cin_p, c.ks, Bn, H, W, 0, net->wf[l], c.cout_p, ep, nz, per, net->err, s);
+        else switch (c.cout_p) {
         case 32: st = conv_gemm_split<32>(la, lb, ep, mtiles, kp, per, nz, pipe, net->err, s); break;
         case 64: st = conv_gemm_split<64>(la, lb, ep, mtiles, kp, per, nz, pipe, net->err, s); break;
         case 128: st = conv_gemm_split<128>(la, lb, ep, mtiles, kp, per, nz, pipe, net->err, s); break;
@@ -804,6 +1074,7 @@ static int layer_forward(lentils_unet *net, int l, const bf16 *x, void *y, int B
         return LENTILS_OK;
     }
     EpiAct ep{(bf16 *)y, net->b32[l], npix, c.cout_p, c.relu};
+    if (tma) return conv_tma(x, c.cin_p, c.ks, Bn, H, W, 0, net->wf[l], c.cout_p, ep, 1, K / 8, net->err, s);
     return conv_gemm_n(c.cout_p, la, lb, ep, npix, K, pipe, net->err, s);
 }
 
@@ -818,37 +1089,95 @@ static int layer_backward(lentils_unet *net, int l, const bf16 *dy, const bf16 *
     const int npix = Bn * H * W;
     const int taps = c.ks * c.ks;
     const bf16 *mask = c.relu ? y : nullptr;
-    // bias gradient
-    bias_grad_kernel<<<std::min(npix, 1024), c.cout_p, 0, s>>>(dy, mask, net->gb[l], npix, c.cout_p, c.cout);
-    LENTILS_CHECK_LAUNCH("bias_grad_kernel");
     // the transposed weight-gradient operands take 8 pixels of one image row per piece
     const bool pipe = net->gemm_form == 0 && c.cout_p <= 128 && c.cin_p <= 128 && (W % 8) == 0;
+    if (!pipe) {  // bias gradient (the pipelined form sums it in grad_prep_kernel)
+        bias_grad_kernel<<<std::min(npix, 1024), c.cout_p, 0, s>>>(dy, mask, net->gb[l], npix,
+                                                                   c.cout_p, c.cout);
+        LENTILS_CHECK_LAUNCH("bias_grad_kernel");
+    }
     if (pipe) {
         // masked gradient (pixel-major and transposed) and the shifted transposed input
         const int blocks = (npix + 63) / 64;
-        grad_prep_kernel<<<blocks, 256, 0, s>>>(dy, mask, net->dym, net->dyT, npix, c.cout_p);
+        // 64-pixel blocks (W a multiple of 64) keep a TMA box in one contiguous run
+        const bool blocked = (W % 64) == 0;
+        grad_prep_kernel<<<blocks, 256, 0, s>>>(dy, mask, net->dym, net->dyT, net->gb[l], npix,
+                                                c.cout_p, c.cout, blocked ? 1 : 0);
         LENTILS_CHECK_LAUNCH("grad_prep_kernel");
-        shift_transpose_kernel<<<blocks, 256, 0, s>>>(x, net->xT, npix, W, c.cin_p,
-                                                      c.ks == 3 ? 3 : 1);
+        const int nshift = c.ks == 3 ? 3 : 1;
+        const long long qtot = (long long)(npix / (H * W)) * (H + 2) * W;
+        shift_transpose_kernel<<<blocks, 256, 0, s>>>(x, net->xT, npix, H, W, c.cin_p, nshift,
+                                                      qtot, blocked ? 1 : 0);
         LENTILS_CHECK_LAUNCH("shift_transpose_kernel");
-        // weight gradient: rows = taps * cin_p, columns = cout_p, K = pixels split over CTAs
+        // weight gradient: rows = taps * cin_p, columns = cout_p, K = pixels split over CTAs,
+        // about kWgradCtas CTAs in all
         const int Kw = taps * c.cin_p;
-        ConvWgXT la{net->xT, npix, H, W, c.cin_p, c.ks};
-        ConvWgDyT lb{net->dyT, npix, c.cout_p};
         EpiAtomicF32T ep{net->gw_pad[l], Kw, c.cout_p};
         const int kpieces = npix / 8;  // npix is a multiple of 8 (W is)
-        const int per = kWgradPieces;
-        const int nz = (kpieces + per - 1) / per;
         const int mtiles = (Kw + 127) / 128;
+        const int want = std::max(1, kWgradCtas / mtiles);
+        int per = (kpieces + want - 1) / want;
+        per = std::max(kWgradMinPieces, (per + 7) / 8 * 8);  // whole chunks
+        const int nz = (kpieces + per - 1) / per;
         int st = LENTILS_OK;
-        switch (c.cout_p) {
-        case 32: st = wgrad_launch<32>(la, lb, ep, mtiles, kpieces, per, nz, net->err, s); break;
-        case 64: st = wgrad_launch<64>(la, lb, ep, mtiles, kpieces, per, nz, net->err, s); break;
-        case 128: st = wgrad_launch<128>(la, lb, ep, mtiles, kpieces, per, nz, net->err, s); break;
-        default: return set_error(LENTILS_ERR_UNSUPPORTED, "weight gradient N=%d", c.cout_p);
+        if (blocked) {
+            ConvWgXTTmaBlk la;
+            la.C = c.cin_p;
+            la.ks = c.ks;
+            la.H = H;
+            la.W = W;
+            la.nblk = (int)(qtot / 64);
+            const uint64_t da[3] = {64, (uint64_t)c.cin_p, (uint64_t)nshift * la.nblk};
+            const uint64_t sa[2] = {128, (uint64_t)c.cin_p * 128};
+            const uint32_t ba[3] = {64, (uint32_t)c.cin_p, 1};
+            if ((st = tma_map_bf16(&la.map, net->xT, 3, da, sa, ba))) return st;
+            const uint64_t db[3] = {64, (uint64_t)c.cout_p, (uint64_t)npix / 64};
+            const uint64_t sb[2] = {128, (uint64_t)c.cout_p * 128};
+            const uint32_t bb[3] = {64, (uint32_t)c.cout_p, 1};
+            switch (c.cout_p) {
+            case 32: st = wgrad_tma_blk<32>(la, net->dyT, db, sb, bb, ep, mtiles, kpieces, per, nz, net->err, s); break;
+            case 64: st = wgrad_tma_blk<64>(la, net->dyT, db, sb, bb, ep, mtiles, kpieces, per, nz, net->err, s); break;
+            case 128: st = wgrad_tma_blk<128>(la, net->dyT, db, sb, bb, ep, mtiles, kpieces, per, nz, net->err, s); break;
+            default: return set_error(LENTILS_ERR_UNSUPPORTED, "weight gradient N=%d", c.cout_p);
+            }
+        } else if ((H * W) % 64 == 0) {
+            ConvWgXTTma la;
+            la.C = c.cin_p;
+            la.ks = c.ks;
+            la.H = H;
+            la.W = W;
+            la.rows = nshift * c.cin_p;
+            const uint64_t da[2] = {(uint64_t)qtot, (uint64_t)la.rows};
+            const uint64_t sa[1] = {(uint64_t)qtot * 2};
+            const uint32_t ba[2] = {64, (uint32_t)c.cin_p};
+            if ((st = tma_map_bf16(&la.map, net->xT, 2, da, sa, ba))) return st;
+            const uint64_t db[2] = {(uint64_t)npix, (uint64_t)c.cout_p};
+            const uint64_t sb[1] = {(uint64_t)npix * 2};
+            const uint32_t bb[2] = {64, (uint32_t)c.cout_p};
+            switch (c.cout_p) {
+            case 32: st = wgrad_tma_launch<32>(la, net->dyT, db, sb, bb, ep, mtiles, kpieces, per, nz, net->err, s); break;
+            case 64: st = wgrad_tma_launch<64>(la, net->dyT, db, sb, bb, ep, mtiles, kpieces, per, nz, net->err, s); break;
+            case 128: st = wgrad_tma_launch<128>(la, net->dyT, db, sb, bb, ep, mtiles, kpieces, per, nz, net->err, s); break;
+            default: return set_error(LENTILS_ERR_UNSUPPORTED, "weight gradient N=%d", c.cout_p);
+            }
+        } else {
+            ConvWgXT la{net->xT, npix, H, W, c.cin_p, c.ks, qtot};
+            ConvWgDyT lb{net->dyT, npix, c.cout_p};
+            switch (c.cout_p) {
+            case 32: st = wgrad_launch<32>(la, lb, ep, mtiles, kpieces, per, nz, net->err, s); break;
+            case 64: st = wgrad_launch<64>(la, lb, ep, mtiles, kpieces, per, nz, net->err, s); break;
+            case 128: st = wgrad_launch<128>(la, lb, ep, mtiles, kpieces, per, nz, net->err, s); break;
+            default: return set_error(LENTILS_ERR_UNSUPPORTED, "weight gradient N=%d", c.cout_p);
+            }
         }
         if (st) return st;
-        if (dx) {  // data gradient from the masked copy: plain gathers, pipelined
+        if (dx && conv_tma_ok(c.cout_p, c.cin_p, H, W)) {  // data gradient, TMA operands
+            EpiStoreBf16 epd{dx, npix, c.cin_p};
+            const int K = taps * c.cout_p;
+            if (int st2 = conv_tma(net->dym, c.cout_p, c.ks, Bn, H, W, 1, net->wb[l], c.cin_p, epd,
+                                   1, K / 8, net->err, s))
+                return st2;
+        } else if (dx) {  // data gradient from the masked copy: plain gathers, pipelined
             const int K = taps * c.cout_p;
             ConvBwdDataA lad{net->dym, nullptr, npix, H, W, c.cout_p, c.ks};
             tc::RowMajorLoader lbd{net->wb[l], c.cin_p, K, K};
@@ -1133,8 +1462,11 @@ int lentils_unet_create(lentils_unet **out, int H, int W, int max_batch, const f
         for (int l = 0; l < kNumLayers; ++l) {
             const ConvSpec &c = kLayers[l];
             const size_t np = (size_t)np0 >> (2 * c.level);
+            const size_t Hl = (size_t)(H >> c.level);
             dmax = std::max(dmax, np * c.cout_p);
-            xmax = std::max(xmax, np * c.cin_p * (c.ks == 3 ? 3 : 1));
+            // row-padded: (H + 2) rows per image
+            xmax = std::max(xmax, np / std::max<size_t>(Hl, 1) * (Hl + 2) * c.cin_p *
+                                      (c.ks == 3 ? 3 : 1));
         }
         add((void **)&net->dym, b2 * dmax);
         add((void **)&net->dyT, b2 * dmax);

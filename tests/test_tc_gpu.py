@@ -8,7 +8,7 @@ import torch
 pytestmark = pytest.mark.gpu
 
 
-@pytest.mark.parametrize("form", [0, 1])
+@pytest.mark.parametrize("form", [0, 1, 2])
 @pytest.mark.parametrize("M,N,K", [(128, 64, 64), (256, 64, 192), (384, 128, 576),
                                    (128, 32, 64), (200, 256, 128), (1000, 128, 1152),
                                    (128, 32, 72), (256, 64, 200), (512, 32, 8), (640, 128, 4096)])
@@ -37,5 +37,5 @@ def test_bounded_wait_times_out_and_context_survives(native):
     assert L.lentils_tc_timeout_selftest(ctypes.c_void_p(err.data_ptr()), 1000, None) == 0
     torch.cuda.synchronize()
     assert int(err.item()) == 1
-    test_tc_gemm_bf16(native, 128, 64, 64, 0)
-    test_tc_gemm_bf16(native, 128, 64, 64, 1)
+    for form in (0, 1, 2):
+        test_tc_gemm_bf16(native, 128, 64, 64, form)
