@@ -558,6 +558,9 @@ int lentils_unet_backward(lentils_unet *net, const float *dout, int B, float lr,
 /* Tuning: 0 (default) runs the convolution GEMMs whose operands are plain gathers (forward;
  * data gradient of a layer without ReLU) on the pipelined kernel, 1 on the staged kernel. */
 int lentils_unet_set_gemm_form(lentils_unet *net, int form);
+/* Tuning: about how many CTAs a weight-gradient GEMM runs (its pixel reduction is split over
+ * them); 0 selects the built-in default. */
+int lentils_unet_set_wgrad_ctas(lentils_unet *net, int ctas);
 int lentils_unet_set_jacobi_weight(lentils_unet *net, float gamma);
 /* 1 if a bounded tensor-core wait gave up since creation (results then invalid) */
 int lentils_unet_error_flag(lentils_unet *net, int *flag);

@@ -192,6 +192,7 @@ _SIGNATURES = [
     ("lentils_unet_error_flag", c_int, [c_void_p, POINTER(c_int)]),
     ("lentils_unet_set_jacobi_weight", c_int, [c_void_p, c_float]),
     ("lentils_unet_set_gemm_form", c_int, [c_void_p, c_int]),
+    ("lentils_unet_set_wgrad_ctas", c_int, [c_void_p, c_int]),
     ("lentils_unet_backward", c_int, [c_void_p, c_void_p, c_int, c_float, c_void_p, c_void_p]),
     ("lentils_unet_features", c_int, [c_void_p, c_void_p, c_int, c_void_p]),
     ("lentils_unet_precondition", c_int, [c_void_p, c_void_p, c_void_p, c_void_p, c_void_p,

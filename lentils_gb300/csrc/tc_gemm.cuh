@@ -306,6 +306,7 @@ __global__ void __launch_bounds__(kPipeThreads)
         if (!ok) atomicExch(&abort_flag, 1);
         mma_commit(&done);  // arrives once every MMA issued above has completed
     }
+    if (warp == 4) __syncwarp();  // the issuer's warp-mates wait here, not on the mbarrier
     // every MMA has completed once `done` fires (bounded wait; on a timeout nothing is read)
     const bool fin = mbar_wait(&done, 0);
     tc_fence_after();
@@ -408,6 +409,8 @@ __global__ void __launch_bounds__(kPipeThreads)
 #pragma unroll
     for (int i = 0; i < STAGES; ++i) last[i] = -1;
 
+    // The producer and the MMA issuer are lane 0 of warps 0 and 4; the other lanes of those warps
+    // wait at __syncwarp (not polling an mbarrier, which would hold up the lane that works).
     if (threadIdx.x == 0) {  // the TMA producer
         for (int ch = 0; ch < nchunks; ++ch) {
             const int st = ch % STAGES;
@@ -442,6 +445,7 @@ __global__ void __launch_bounds__(kPipeThreads)
         }
         mma_commit(&done);
     }
+    if (warp == 0 || warp == 4) __syncwarp();
     const bool fin = mbar_wait(&done, 0);
     if (threadIdx.x == 0) {
         // every load has landed before shared memory is reused or the CTA exits (the MMAs

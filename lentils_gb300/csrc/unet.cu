@@ -448,24 +448,52 @@ __global__ void finalize_act_kernel(const float *__restrict__ part, int nz,
     }
 }
 
+// The pooling / upsampling kernels below work on 8 channels (16 bytes) per thread; C is a
+// multiple of 8. Per element the arithmetic (FP32 sums of BF16 values, one rounding) is that
+// of a one-element-per-thread form.
+__device__ __forceinline__ void bf8_load(const bf16 *p, float (&v)[8])
+{
+    const uint4 u = *reinterpret_cast<const uint4 *>(p);
+    const bf16 *b = reinterpret_cast<const bf16 *>(&u);
+#pragma unroll
+    for (int i = 0; i < 8; ++i) v[i] = bf(b[i]);
+}
+__device__ __forceinline__ void bf8_store(bf16 *p, const float (&v)[8])
+{
+    uint4 u;
+    bf16 *b = reinterpret_cast<bf16 *>(&u);
+#pragma unroll
+    for (int i = 0; i < 8; ++i) b[i] = __float2bfloat16(v[i]);
+    *reinterpret_cast<uint4 *>(p) = u;
+}
+
 // out (n, H/2, W/2, C) = mean of the 2 x 2 block
 __global__ void pool2_kernel(const bf16 *__restrict__ x, bf16 *__restrict__ y, int Bn, int H,
                              int W, int C)
 {
-    const int h2 = H / 2, w2 = W / 2;
-    const long long n = (long long)Bn * h2 * w2 * C;
+    const int h2 = H / 2, w2 = W / 2, cv = C / 8;
+    const long long n = (long long)Bn * h2 * w2 * cv;
     LENTILS_GRID_STRIDE(e, n)
     {
-        const int c = (int)(e % C);
-        long long r = e / C;
-        const int w = (int)(r % w2);
-        r /= w2;
+        const int c = (int)(e % cv) * 8;
+        const long long q = e / cv;  // output pixel
+        const int w = (int)(q % w2);
+        const long long r = q / w2;
         const int h = (int)(r % h2);
         const int b = (int)(r / h2);
         const size_t base = ((size_t)(b * H + 2 * h) * W + 2 * w) * C + c;
-        const float s = bf(x[base]) + bf(x[base + C]) + bf(x[base + (size_t)W * C]) +
-                        bf(x[base + (size_t)W * C + C]);
-        y[e] = __float2bfloat16(0.25f * s);
+        float a[8], t[8];
+        bf8_load(x + base, a);
+        bf8_load(x + base + C, t);
+#pragma unroll
+        for (int i = 0; i < 8; ++i) a[i] += t[i];
+        bf8_load(x + base + (size_t)W * C, t);
+#pragma unroll
+        for (int i = 0; i < 8; ++i) a[i] += t[i];
+        bf8_load(x + base + (size_t)W * C + C, t);
+#pragma unroll
+        for (int i = 0; i < 8; ++i) a[i] = 0.25f * (a[i] + t[i]);
+        bf8_store(y + q * C + c, a);
     }
 }
 
@@ -473,17 +501,22 @@ __global__ void pool2_kernel(const bf16 *__restrict__ x, bf16 *__restrict__ y, i
 __global__ void up2add_kernel(const bf16 *__restrict__ low, const bf16 *__restrict__ skip,
                               bf16 *__restrict__ y, int Bn, int H, int W, int C)
 {
-    const long long n = (long long)Bn * H * W * C;
+    const int cv = C / 8;
+    const long long n = (long long)Bn * H * W * cv;
     LENTILS_GRID_STRIDE(e, n)
     {
-        const int c = (int)(e % C);
-        long long r = e / C;
-        const int w = (int)(r % W);
-        r /= W;
+        const int c = (int)(e % cv) * 8;
+        const long long q = e / cv;
+        const int w = (int)(q % W);
+        const long long r = q / W;
         const int h = (int)(r % H);
         const int b = (int)(r / H);
-        const float v = bf(low[((size_t)(b * (H / 2) + h / 2) * (W / 2) + w / 2) * C + c]) + bf(skip[e]);
-        y[e] = __float2bfloat16(v);
+        float a[8], t[8];
+        bf8_load(low + ((size_t)(b * (H / 2) + h / 2) * (W / 2) + w / 2) * C + c, a);
+        bf8_load(skip + q * C + c, t);
+#pragma unroll
+        for (int i = 0; i < 8; ++i) a[i] += t[i];
+        bf8_store(y + q * C + c, a);
     }
 }
 
@@ -491,20 +524,29 @@ __global__ void up2add_kernel(const bf16 *__restrict__ low, const bf16 *__restri
 __global__ void sum4_kernel(const bf16 *__restrict__ dy, bf16 *__restrict__ dlow, int Bn, int H,
                             int W, int C)
 {
-    const int h2 = H / 2, w2 = W / 2;
-    const long long n = (long long)Bn * h2 * w2 * C;
+    const int h2 = H / 2, w2 = W / 2, cv = C / 8;
+    const long long n = (long long)Bn * h2 * w2 * cv;
     LENTILS_GRID_STRIDE(e, n)
     {
-        const int c = (int)(e % C);
-        long long r = e / C;
-        const int w = (int)(r % w2);
-        r /= w2;
+        const int c = (int)(e % cv) * 8;
+        const long long q = e / cv;
+        const int w = (int)(q % w2);
+        const long long r = q / w2;
         const int h = (int)(r % h2);
         const int b = (int)(r / h2);
         const size_t base = ((size_t)(b * H + 2 * h) * W + 2 * w) * C + c;
-        const float s = bf(dy[base]) + bf(dy[base + C]) + bf(dy[base + (size_t)W * C]) +
-                        bf(dy[base + (size_t)W * C + C]);
-        dlow[e] = __float2bfloat16(s);
+        float a[8], t[8];
+        bf8_load(dy + base, a);
+        bf8_load(dy + base + C, t);
+#pragma unroll
+        for (int i = 0; i < 8; ++i) a[i] += t[i];
+        bf8_load(dy + base + (size_t)W * C, t);
+#pragma unroll
+        for (int i = 0; i < 8; ++i) a[i] += t[i];
+        bf8_load(dy + base + (size_t)W * C + C, t);
+#pragma unroll
+        for (int i = 0; i < 8; ++i) a[i] += t[i];
+        bf8_store(dlow + q * C + c, a);
     }
 }
 
@@ -512,17 +554,22 @@ __global__ void sum4_kernel(const bf16 *__restrict__ dy, bf16 *__restrict__ dlow
 __global__ void add_pool_grad_kernel(const bf16 *__restrict__ a, const bf16 *__restrict__ dp,
                                      bf16 *__restrict__ d, int Bn, int H, int W, int C)
 {
-    const long long n = (long long)Bn * H * W * C;
+    const int cv = C / 8;
+    const long long n = (long long)Bn * H * W * cv;
     LENTILS_GRID_STRIDE(e, n)
     {
-        const int c = (int)(e % C);
-        long long r = e / C;
-        const int w = (int)(r % W);
-        r /= W;
+        const int c = (int)(e % cv) * 8;
+        const long long q = e / cv;
+        const int w = (int)(q % W);
+        const long long r = q / W;
         const int h = (int)(r % H);
         const int b = (int)(r / H);
-        const float v = bf(a[e]) + 0.25f * bf(dp[((size_t)(b * (H / 2) + h / 2) * (W / 2) + w / 2) * C + c]);
-        d[e] = __float2bfloat16(v);
+        float v[8], t[8];
+        bf8_load(a + q * C + c, v);
+        bf8_load(dp + ((size_t)(b * (H / 2) + h / 2) * (W / 2) + w / 2) * C + c, t);
+#pragma unroll
+        for (int i = 0; i < 8; ++i) v[i] += 0.25f * t[i];
+        bf8_store(d + q * C + c, v);
     }
 }
 
@@ -800,6 +847,7 @@ __global__ void __launch_bounds__(1024)
 struct lentils_unet {
     int H, W, maxB;
     int gemm_form;        // 0: pipelined convolution GEMMs (cp.async ring), 1: synchronous staging
+    int wgrad_ctas;       // CTAs of a weight-gradient GEMM (its pixel reduction is split to fill them)
     float jacobi_weight;  // gamma of the preconditioner form
     long long nparams;
     // per layer
@@ -908,7 +956,7 @@ static int conv_gemm_n(int N, const LA &la, const tc::RowMajorLoader &lb, const 
 
 // the weight-gradient GEMM splits its pixel reduction so that about kWgradCtas CTAs run, each
 // over at least kWgradMinPieces pieces of 8 pixels
-constexpr int kWgradCtas = 320;
+constexpr int kWgradCtas = 1024;
 constexpr int kWgradMinPieces = 64;
 constexpr int kTmaStages = 4;
 
@@ -1115,7 +1163,7 @@ static int layer_backward(lentils_unet *net, int l, const bf16 *dy, const bf16 *
         EpiAtomicF32T ep{net->gw_pad[l], Kw, c.cout_p};
         const int kpieces = npix / 8;  // npix is a multiple of 8 (W is)
         const int mtiles = (Kw + 127) / 128;
-        const int want = std::max(1, kWgradCtas / mtiles);
+        const int want = std::max(1, (net->wgrad_ctas > 0 ? net->wgrad_ctas : kWgradCtas) / mtiles);
         int per = (kpieces + want - 1) / want;
         per = std::max(kWgradMinPieces, (per + 7) / 8 * 8);  // whole chunks
         const int nz = (kpieces + per - 1) / per;
@@ -1615,6 +1663,14 @@ int lentils_unet_backward(lentils_unet *net, const float *dout, int Bn, float lr
         LENTILS_CUDA_TRY(cudaStreamSynchronize(s));
     }
     if (lr > 0.f && (st = adam_update(net, lr, s))) return st;
+    return LENTILS_OK;
+}
+
+int lentils_unet_set_wgrad_ctas(lentils_unet *net, int ctas)
+{
+    clear_error();
+    if (!net || ctas < 0 || ctas > 1 << 16) return set_error(LENTILS_ERR_INVALID, "unet_set_wgrad_ctas");
+    net->wgrad_ctas = ctas;
     return LENTILS_OK;
 }
 
