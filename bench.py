@@ -394,6 +394,8 @@ def run_ours(args):
             line["cg"] = run_cg_bench(cpu=not (args.no_cpu_baseline or args.no_cpu_cg))
         if not args.no_sweep:
             line["sweep"] = run_sweep_bench(peak, args.sweep_samples)
+        if not args.no_unet:
+            line["unet"] = run_unet_bench()
         if not args.no_cpu_baseline:
             line["cpu_baseline"] = cpu_baseline(four, uvw)
         print(json.dumps(line))
@@ -896,6 +898,53 @@ def run_sweep_bench(peak, nsamples=256, steps=10, warmup=3, form=SWEEP_FORM):
             "kernel_form": form, "setup_s": setup_s, "autotuned_classes": sw.tuner.tuned}
 
 
+def run_unet_bench(steps=20, warmup=3):
+    """The learned preconditioner's network (128^2 source grid, 276,545 parameters, BF16 on the
+    tcgen05 tensor cores): forward at batch 1 (as the solver applies it) and 32, one training
+    step (forward, backward, Adam) at batch 32, and the preconditioner application, with CUDA
+    events on the current stream. Random weights and inputs (seeded); the forward FLOPs are
+    2 * pixels * K * N summed over the convolutions."""
+    import torch
+    from lentils_gb300 import learned
+    H = W = 128
+    net = learned.UNet(H, W, max_batch=32, seed=3)
+    g = torch.Generator(device="cuda").manual_seed(5)
+    x, f, t = (torch.randn(32, H, W, device="cuda", generator=g) for _ in range(3))
+    r = x[0].reshape(-1)
+    d = torch.rand(H * W, device="cuda", generator=g) + 0.5
+    ft = f[0].reshape(-1)
+    s = torch.cuda.current_stream()
+
+    def timed(fn, n):
+        for _ in range(warmup):
+            fn()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        e0.record(s)
+        for _ in range(n):
+            fn()
+        e1.record(s)
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / n
+
+    fwd_flop = 0
+    for ci, co, k, _, level in learned.LAYERS:
+        npix = 32 * (H >> level) * (W >> level)
+        fwd_flop += 2 * npix * k * k * ci * co
+    out = {"workload": "U-Net 2->32->64->128->128 (3x3, 1x1 convolutions), 128^2 source grid, "
+                       "BF16 tcgen05 GEMMs with FP32 accumulation; random weights and inputs",
+           "forward_b1_ms": timed(lambda: net.forward(x[:1], f[:1]), steps),
+           "forward_b32_ms": timed(lambda: net.forward(x, f), steps),
+           "train_step_b32_ms": timed(lambda: net.train_step(x, f, t, 0.0), max(3, steps // 2)),
+           "precondition_ms": timed(lambda: net.precondition(r, d, ft), steps),
+           "forward_b32_gflop": fwd_flop / 1e9}
+    out["forward_b32_tflops"] = fwd_flop / (out["forward_b32_ms"] * 1e-3) / 1e12
+    out["train_step_b32_tflops"] = 3 * fwd_flop / (out["train_step_b32_ms"] * 1e-3) / 1e12
+    if net.error_flag():
+        raise RuntimeError("a tensor-core wait gave up in the U-Net section")
+    return out
+
+
 def _omp_threads(n):
     """Set the OpenMP thread count of this (calling) thread for the CPU gridder's parallel
     loops (libgomp, which the compiled gridder links)."""
@@ -944,10 +993,16 @@ def main():
     ap.add_argument("--no-deflect", action="store_true")
     ap.add_argument("--no-dropin", action="store_true")
     ap.add_argument("--no-cpu-cg", action="store_true")
+    ap.add_argument("--no-unet", action="store_true")
+    ap.add_argument("--unet-only", action="store_true",
+                    help="print only the U-Net section's JSON (for profiling its kernels)")
     args = ap.parse_args()
     os.environ.setdefault("OMP_NUM_THREADS", str(os.cpu_count() or 1))
     if args.impl == "reference":
         return run_reference(args)
+    if args.unet_only:
+        print(json.dumps({"unet": run_unet_bench(steps=args.steps, warmup=max(3, args.warmup))}))
+        return 0
     return run_ours(args)
 
 
