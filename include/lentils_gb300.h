@@ -555,8 +555,13 @@ int lentils_unet_train_step(lentils_unet *net, const float *r, const float *d, c
 int lentils_unet_backward(lentils_unet *net, const float *dout, int B, float lr,
                           float *grad_host, void *stream);
 /* gamma of the preconditioner form (default 0) */
-/* Tuning: 0 (default) runs the convolution GEMMs whose operands are plain gathers (forward;
- * data gradient of a layer without ReLU) on the pipelined kernel, 1 on the staged kernel. */
+/* Tuning, the convolution kernels: 0 (default) runs the forward convolutions with TMA operands
+ * on the persistent GEMM (one wave of CTAs, accumulators double buffered in tensor memory), the
+ * first layer with its input packing and pooling as one CUDA-core kernel, and the last hidden
+ * layer with the 1 x 1 output layer (and, for lentils_unet_precondition, the combination) in
+ * one GEMM epilogue; 2 runs every layer as its own per-tile TMA or cp.async-ring GEMM; 1 runs
+ * the GEMMs whose operands are plain gathers on the staged kernel. The forms agree up to FP32
+ * summation order and the BF16 roundings it can flip. */
 int lentils_unet_set_gemm_form(lentils_unet *net, int form);
 /* Tuning: about how many CTAs a weight-gradient GEMM runs (its pixel reduction is split over
  * them); 0 selects the built-in default. */

@@ -490,6 +490,194 @@ __global__ void __launch_bounds__(kPipeThreads)
     if (warp == 4) tmem_dealloc(tmem, ncols);
 }
 
+// -- persistent TMA form -----------------------------------------------------------------------
+// The TMA-fed GEMM as a persistent kernel: each CTA takes row tiles blockIdx.x, blockIdx.x +
+// gridDim.x, ... over the whole K (no split). The accumulator is double buffered in tensor
+// memory (2 x N columns), so the epilogue of one tile runs while the MMAs of the next fill the
+// other buffer, and the TMA ring runs on across tile boundaries. Six warps: warps 0-3 the
+// epilogue (warp w reads TMEM lanes 32w .. 32w + 31, one row per thread), lane 0 of warp 4 the
+// TMA producer, warp 5 allocates tensor memory and its lane 0 issues the MMAs.
+//   full[s]   : the chunk in stage s has landed (TMA transaction bytes)
+//   empty[s]  : the MMAs that read stage s have completed (tcgen05.commit)
+//   tfull[b]  : the last MMA of the tile in accumulator b has completed
+//   tempty[b] : the four epilogue warps have read accumulator b
+// Operands walk K with cursors: `typename L::Cursor L::begin(int row0) const` at the start of a
+// tile and `void L::next(void *dst, uint64_t *bar, Cursor &) const`, which issues the loads of
+// the next chunk and advances (the producer is one thread, so per-chunk address arithmetic is
+// on the critical path). Row epilogues are functors with
+//   `void prepare(float *sh, int tid) const` (tid 0..127: stage constants in the 1 KB shared
+//   scratch sh, once per CTA),
+//   `void row(int m, int n0, const float (&v)[32], float &acc, const float *sh) const`
+//   (columns n0 .. n0 + 31 of row m, for n0 = 0, 32, ..., N - 32 in order; acc starts at 0),
+//   `void row_end(int m, float acc, const float *sh) const`.
+// Every wait is bounded; after a timeout *err is set, each role stops, the producer waits for
+// the copies it issued, and the tensor memory is freed.
+constexpr int kPersistThreads = 192;
+
+__device__ __forceinline__ void prefetch_tensormap(const void *map)
+{
+    asm volatile("prefetch.tensormap [%0];" ::"l"(map) : "memory");
+}
+
+template <int N, int STAGES, class LA, class LB, class EP>
+__global__ void __launch_bounds__(kPersistThreads, 1)
+    gemm_tma_persist_kernel(const __grid_constant__ LA la, const __grid_constant__ LB lb,
+                            const EP ep, int mtiles, int kpieces, int *err)
+{
+    static_assert(N % 32 == 0 && N >= 32 && N <= 128, "N");
+    constexpr int KCH = LA::kChunk, SWZ = LA::kSwz;
+    static_assert(LB::kChunk == KCH && LB::kSwz == SWZ && KCH * 2 == SWZ, "operand layouts");
+    constexpr int kATile = TmaSmem<N, STAGES, KCH>::kATile;
+    constexpr int kStage = TmaSmem<N, STAGES, KCH>::kStageBytes;
+    constexpr int kPieces = KCH / 8;
+    static_assert(LA::kBytes == (uint32_t)kATile && LB::kBytes == (uint32_t)(N * KCH * 2),
+                  "operand bytes");
+    extern __shared__ __align__(1024) unsigned char smem_raw[];
+    __shared__ uint64_t full[STAGES], empty[STAGES], tfull[2], tempty[2], mdone;
+    __shared__ uint32_t tmem_base;
+    __shared__ int abort_flag;
+    __shared__ float scratch[256];
+    unsigned char *smem = smem_raw + ((1024 - (smem_u32(smem_raw) & 1023)) & 1023);
+    constexpr uint32_t ncols = (2 * N <= 64) ? 64 : (2 * N <= 128) ? 128 : 256;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int nchunks = (kpieces + kPieces - 1) / kPieces;
+    const int ntiles =
+        (mtiles > (int)blockIdx.x) ? (mtiles - (int)blockIdx.x + (int)gridDim.x - 1) / (int)gridDim.x : 0;
+
+    if (warp == 5) {
+        tmem_alloc(&tmem_base, ncols);
+        tmem_relinquish();
+    }
+    if (threadIdx.x == 0) {
+        for (int i = 0; i < STAGES; ++i) {
+            mbar_init(&full[i], 1);
+            mbar_init(&empty[i], 1);
+        }
+        for (int i = 0; i < 2; ++i) {
+            mbar_init(&tfull[i], 1);
+            mbar_init(&tempty[i], 4);
+        }
+        mbar_init(&mdone, 1);
+        abort_flag = 0;
+        fence_mbar_init();
+    }
+    if (threadIdx.x == 128) {
+        prefetch_tensormap(&la.map);
+        prefetch_tensormap(&lb.map);
+    }
+    if (warp < 4) ep.prepare(scratch, threadIdx.x);
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = tmem_base;
+
+    if (warp == 4) {
+        if (lane == 0) {  // the TMA producer
+            int it = 0;
+            for (int j = 0; j < ntiles; ++j) {
+                typename LA::Cursor ca = la.begin(((int)blockIdx.x + j * (int)gridDim.x) * 128);
+                typename LB::Cursor cb = lb.begin(0);
+                int ch = 0;
+                for (; ch < nchunks; ++ch, ++it) {
+                    const int st = it % STAGES;
+                    if (it >= STAGES && !mbar_wait(&empty[st], ((it / STAGES) - 1) & 1)) {
+                        atomicExch(&abort_flag, 1);
+                        break;
+                    }
+                    unsigned char *sa = smem + st * kStage;
+                    mbar_arrive_expect_tx(&full[st], LA::kBytes + LB::kBytes);
+                    la.next(sa, &full[st], ca);
+                    lb.next(sa + kATile, &full[st], cb);
+                }
+                if (ch < nchunks) break;
+            }
+            // every copy has landed before the CTA exits: stage i last took chunk
+            // i + STAGES q for the largest q with that below it
+#pragma unroll
+            for (int i = 0; i < STAGES; ++i) {
+                if (i >= it) continue;
+                const int last = i + ((it - 1 - i) / STAGES) * STAGES;
+                if (!mbar_wait(&full[i], (last / STAGES) & 1)) atomicExch(&abort_flag, 1);
+            }
+        }
+        __syncwarp();
+    } else if (warp == 5) {
+        if (lane == 0) {  // the MMA issuer
+            constexpr uint32_t idesc = idesc_bf16_f32(128, N);
+            int it = 0;
+            bool ok = true;
+            for (int j = 0; j < ntiles && ok; ++j) {
+                const int buf = j & 1;
+                if (j >= 2 && !mbar_wait(&tempty[buf], ((j >> 1) - 1) & 1)) {
+                    atomicExch(&abort_flag, 1);
+                    break;
+                }
+                tc_fence_after();
+                const uint32_t acc = tmem + (uint32_t)(buf * N);
+                for (int ch = 0; ch < nchunks; ++ch, ++it) {
+                    const int st = it % STAGES;
+                    if (!mbar_wait(&full[st], (it / STAGES) & 1)) {
+                        atomicExch(&abort_flag, 1);
+                        ok = false;
+                        break;
+                    }
+                    tc_fence_after();
+                    const uint32_t sa = smem_u32(smem + st * kStage);
+                    const uint32_t sb = sa + kATile;
+#pragma unroll
+                    for (int k = 0; k < KCH / 16; ++k)
+                        mma_bf16(acc, smem_desc_swz<SWZ>(sa + 32 * k), smem_desc_swz<SWZ>(sb + 32 * k),
+                                 idesc, (ch > 0 || k > 0) ? 1u : 0u);
+                    mma_commit(&empty[st]);
+                }
+                if (ok) mma_commit(&tfull[buf]);
+            }
+            // every MMA has completed before the tensor memory is freed
+            mma_commit(&mdone);
+            if (!mbar_wait(&mdone, 0)) atomicExch(&abort_flag, 1);
+        }
+        __syncwarp();
+    } else {  // the epilogue warps
+        const uint32_t lane_base = (uint32_t)(warp * 32) << 16;
+        for (int j = 0; j < ntiles; ++j) {
+            const int buf = j & 1;
+            // lane 0 polls; the warp takes one decision (tcgen05.ld needs the whole warp)
+            int go = 0;
+            if (lane == 0)
+                go = mbar_wait(&tfull[buf], (j >> 1) & 1) && !*(volatile int *)&abort_flag;
+            go = __shfl_sync(0xffffffffu, go, 0);
+            if (!go) {
+                if (lane == 0) atomicExch(&abort_flag, 1);
+                break;
+            }
+            tc_fence_after();
+            const int m = ((int)blockIdx.x + j * (int)gridDim.x) * 128 + warp * 32 + lane;
+            const uint32_t taddr = tmem + lane_base + (uint32_t)(buf * N);
+            float acc = 0.f;
+#pragma unroll 1
+            for (int n0 = 0; n0 < N; n0 += 32) {
+                uint32_t r[32];
+                tmem_ld32(taddr + n0, r);
+                tmem_wait_ld();
+                if (n0 + 32 == N) {  // the accumulator is free for the tile after next
+                    tc_fence_before();
+                    __syncwarp();
+                    if (lane == 0) mbar_arrive(&tempty[buf]);
+                }
+                float v[32];
+#pragma unroll
+                for (int i = 0; i < 32; ++i) v[i] = __uint_as_float(r[i]);
+                ep.row(m, n0, v, acc, scratch);
+            }
+            ep.row_end(m, acc, scratch);
+        }
+    }
+    tc_fence_before();
+    __syncthreads();
+    if (threadIdx.x == 0 && *(volatile int *)&abort_flag) atomicExch(err, 1);
+    if (warp == 5) tmem_dealloc(tmem, ncols);
+}
+
 // A row-major [rows][K] BF16 operand through a 2-D tensor map (K innermost, box 64 x ROWS).
 template <int ROWS>
 struct TmaRowMajor {

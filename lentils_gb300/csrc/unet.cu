@@ -325,6 +325,35 @@ struct ConvTmaA {
         }
         tc::tma_load_4d(dst, &map, c0, w + dw, h + dh, n, bar);
     }
+    // The persistent GEMM walks the chunks of a tile with a cursor: the tile's pixel is split
+    // once, and each chunk steps the channel offset and the tap with adds and compares (the
+    // single producer thread otherwise spends most of a chunk's time in integer divisions).
+    // K = ks^2 C exactly (C a multiple of CB).
+    struct Cursor {
+        int c0, ky, kx, w, h, n;
+    };
+    __device__ __forceinline__ Cursor begin(int m0) const
+    {
+        const int hw = H * W, n = m0 / hw, r = m0 - n * hw, h = r / W;
+        return Cursor{0, 0, 0, r - h * W, h, n};
+    }
+    __device__ __forceinline__ void next(void *dst, uint64_t *bar, Cursor &c) const
+    {
+        int dh = c.ky - ks / 2, dw = c.kx - ks / 2;
+        if (flip) {
+            dh = -dh;
+            dw = -dw;
+        }
+        tc::tma_load_4d(dst, &map, c.c0, c.w + dw, c.h + dh, c.n, bar);
+        c.c0 += CB;
+        if (c.c0 == C) {
+            c.c0 = 0;
+            if (++c.kx == ks) {
+                c.kx = 0;
+                ++c.ky;
+            }
+        }
+    }
 };
 
 // B operand: row-major [N][K] BF16 weights through a 2-D tensor map, box (CB, N).
@@ -336,6 +365,15 @@ struct ConvTmaB {
     __device__ __forceinline__ void load(void *dst, uint64_t *bar, int n0, int kp0) const
     {
         tc::tma_load_2d(dst, &map, kp0 * 8, n0, bar);
+    }
+    struct Cursor {
+        int k, n0;
+    };
+    __device__ __forceinline__ Cursor begin(int n0) const { return Cursor{0, n0}; }
+    __device__ __forceinline__ void next(void *dst, uint64_t *bar, Cursor &c) const
+    {
+        tc::tma_load_2d(dst, &map, c.k, c.n0, bar);
+        c.k += CB;
     }
 };
 
@@ -400,6 +438,92 @@ struct EpiPartialF32 {  // slab blockIdx.z of g: g[z][row][col] = v (split-K par
     }
 };
 
+// Row epilogues of the persistent GEMM (tc::gemm_tma_persist_kernel): one thread per output
+// pixel, 32 channels per call, BF16 rows written 16 bytes at a time. prepare() copies the
+// per-channel constants into the kernel's shared scratch `sh` (the 128 epilogue threads, tid
+// 0..127) once per CTA; row() reads them from there.
+__device__ __forceinline__ void act32_bf16(const float (&v)[32], const float *sb, int relu,
+                                           uint4 (&u)[4])
+{
+    bf16 *b = reinterpret_cast<bf16 *>(u);
+#pragma unroll
+    for (int i = 0; i < 32; ++i) {
+        float t = v[i] + sb[i];
+        if (relu) t = fmaxf(t, 0.f);
+        b[i] = __float2bfloat16(t);
+    }
+}
+
+struct RowAct {  // y[pixel][n0 + i] = bf16(relu?(v + bias)), C channels per pixel
+    bf16 *y;
+    const float *bias;
+    int npix, C, relu;
+    __device__ __forceinline__ void prepare(float *sh, int tid) const
+    {
+        for (int i = tid; i < C; i += 128) sh[i] = bias[i];
+    }
+    __device__ __forceinline__ void row(int m, int n0, const float (&v)[32], float &,
+                                        const float *sh) const
+    {
+        if (m >= npix) return;
+        uint4 u[4];
+        act32_bf16(v, sh + n0, relu, u);
+        uint4 *dst = reinterpret_cast<uint4 *>(y + (size_t)m * C + n0);
+#pragma unroll
+        for (int i = 0; i < 4; ++i) dst[i] = u[i];
+    }
+    __device__ __forceinline__ void row_end(int, float, const float *) const {}
+};
+
+// The last hidden layer (32 channels, ReLU) fused with the 1 x 1 output layer: y as RowAct (not
+// stored when y is null), then out = sum_c wo[c] * y[c] + bo over the BF16 values of y in
+// channel order. With z set, the preconditioner's combination z = s * out + gamma * dinv * r
+// is written instead of out.
+struct RowActOut {
+    bf16 *y;
+    const float *bias;
+    int npix;
+    const bf16 *wo;   // output-layer weights, 32 values
+    const float *bo;  // output-layer bias
+    float *out;
+    float *z;
+    const float *r, *dinv, *scale;
+    float gamma;
+    // sh: [0, 32) bias, [32, 64) output weights, 64 output bias, 65 s
+    __device__ __forceinline__ void prepare(float *sh, int tid) const
+    {
+        if (tid < 32) {
+            sh[tid] = bias[tid];
+            sh[32 + tid] = bf(wo[tid]);
+        } else if (tid == 32) {
+            sh[64] = bo[0];
+            sh[65] = z ? scale[0] : 0.f;
+        }
+    }
+    __device__ __forceinline__ void row(int m, int n0, const float (&v)[32], float &acc,
+                                        const float *sh) const
+    {
+        if (m >= npix) return;
+        uint4 u[4];
+        act32_bf16(v, sh + n0, 1, u);
+        const bf16 *b = reinterpret_cast<const bf16 *>(u);
+#pragma unroll
+        for (int i = 0; i < 32; ++i) acc = fmaf(bf(b[i]), sh[32 + n0 + i], acc);
+        if (y) {
+            uint4 *dst = reinterpret_cast<uint4 *>(y + (size_t)m * 32 + n0);
+#pragma unroll
+            for (int i = 0; i < 4; ++i) dst[i] = u[i];
+        }
+    }
+    __device__ __forceinline__ void row_end(int m, float acc, const float *sh) const
+    {
+        if (m >= npix) return;
+        const float o = acc + sh[64];
+        if (z) z[m] = fmaf(sh[65], o, gamma * dinv[m] * r[m]);
+        else out[m] = o;
+    }
+};
+
 // A forward layer whose output has fewer than kSplitMaxPix pixels (fewer than 64 row tiles of
 // 128) splits its K reduction over CTAs: each split writes an FP32 partial slab, and a second
 // kernel sums the slabs in a fixed order and applies bias / ReLU / BF16, so the result does not
@@ -414,6 +538,13 @@ static int blocks_n(long long n)
 {
     long long b = (n + 255) / 256;
     return (int)std::max(1LL, std::min(b, 152LL * 16));
+}
+
+// blocks of 64 threads for n work items (the small batch-1 kernels: more SMs, fewer threads each)
+static int blocks_small(long long n)
+{
+    long long b = (n + 63) / 64;
+    return (int)std::max(1LL, std::min(b, 152LL * 32));
 }
 
 #define LENTILS_GRID_STRIDE(i, n)                                                              \
@@ -465,6 +596,249 @@ __device__ __forceinline__ void bf8_store(bf16 *p, const float (&v)[8])
 #pragma unroll
     for (int i = 0; i < 8; ++i) b[i] = __float2bfloat16(v[i]);
     *reinterpret_cast<uint4 *>(p) = u;
+}
+
+// First layer (2 -> 32 channels, 3 x 3, ReLU) on the CUDA cores, fused with the input packing
+// and the 2 x 2 pooling that follows it: a GEMM over K = 9 taps x 2 channels would leave the
+// tensor core and its operand staging mostly idle. One thread computes a 2 x 2 block of
+// output pixels, 16 channels at a time, from the 4 x 4 input patch around it:
+//   channel 0 = bf16(a * a2 * inv) (a2, inv optional: a2 = dinv and inv = 1 / scale for the
+//   preconditioner), channel 1 = bf16(b); x0 (optional) = the packed 8-channel input,
+//   y = bf16(relu(conv + bias)), yp = the 2 x 2 mean of y with pool2_kernel's arithmetic.
+// The products are exact in FP32; their sum is taken in tap order (the GEMM's order is the
+// tensor core's), so y can differ from the GEMM form by the BF16 rounding of an FP32 ulp.
+__global__ void __launch_bounds__(128)
+    e1_direct_kernel(const float *__restrict__ a, const float *__restrict__ a2,
+                     const float *__restrict__ scale, const float *__restrict__ b,
+                     const bf16 *__restrict__ wf, const float *__restrict__ bias,
+                     bf16 *__restrict__ x0, bf16 *__restrict__ y, bf16 *__restrict__ yp, int Bn,
+                     int H, int W, int nh)
+{
+    __shared__ __align__(16) float ws[18][32];  // [tap * 2 + ci][co]
+    __shared__ float bs[32];
+    for (int i = threadIdx.x; i < 18 * 32; i += blockDim.x) {
+        const int co = i / 18, r = i - co * 18, t = r >> 1, ci = r & 1;
+        ws[r][co] = bf(wf[co * 72 + t * 8 + ci]);
+    }
+    if (threadIdx.x < 32) bs[threadIdx.x] = bias[threadIdx.x];
+    __syncthreads();
+    const float inv = scale ? 1.f / scale[0] : 1.f;
+    const int h2 = H / 2, w2 = W / 2;
+    const long long nblk = (long long)Bn * h2 * w2;
+    // nh = 2: two threads per block of pixels, one for each half of the channels
+    LENTILS_GRID_STRIDE(item, nblk * nh)
+    {
+        const long long q = item / nh;
+        const int half0 = nh == 2 ? (int)(item & 1) : 0, half1 = nh == 2 ? half0 + 1 : 2;
+        const int ww = (int)(q % w2);
+        const long long rq = q / w2;
+        const int hh = (int)(rq % h2);
+        const int n = (int)(rq / h2);
+        const int h0 = 2 * hh, w0 = 2 * ww;
+        const size_t img = (size_t)n * H * W;
+        float in0[4][4], in1[4][4];
+#pragma unroll
+        for (int dy = 0; dy < 4; ++dy) {
+#pragma unroll
+            for (int dx = 0; dx < 4; ++dx) {
+                const int h = h0 - 1 + dy, w = w0 - 1 + dx;
+                float v0 = 0.f, v1 = 0.f;
+                if (h >= 0 && h < H && w >= 0 && w < W) {
+                    const size_t p = img + (size_t)h * W + w;
+                    float x = a[p];
+                    if (a2) x = a2[p] * x;
+                    if (scale) x = x * inv;
+                    v0 = bf(__float2bfloat16(x));
+                    v1 = bf(__float2bfloat16(b[p]));
+                }
+                in0[dy][dx] = v0;
+                in1[dy][dx] = v1;
+            }
+        }
+        if (x0 && half0 == 0) {
+#pragma unroll
+            for (int py = 0; py < 2; ++py)
+#pragma unroll
+                for (int px = 0; px < 2; ++px) {
+                    bf16 v[8];
+                    v[0] = __float2bfloat16(in0[py + 1][px + 1]);
+                    v[1] = __float2bfloat16(in1[py + 1][px + 1]);
+#pragma unroll
+                    for (int i = 2; i < 8; ++i) v[i] = __float2bfloat16(0.f);
+                    const size_t p = img + (size_t)(h0 + py) * W + w0 + px;
+                    *reinterpret_cast<uint4 *>(x0 + p * 8) = *reinterpret_cast<const uint4 *>(v);
+                }
+        }
+#pragma unroll 1
+        for (int half = half0; half < half1; ++half) {
+            float acc[4][16];
+#pragma unroll
+            for (int k = 0; k < 4; ++k)
+#pragma unroll
+                for (int c = 0; c < 16; ++c) acc[k][c] = 0.f;
+#pragma unroll
+            for (int t = 0; t < 9; ++t) {
+                const int ky = t / 3, kx = t % 3;
+#pragma unroll
+                for (int ci = 0; ci < 2; ++ci) {
+#pragma unroll
+                    for (int c4 = 0; c4 < 4; ++c4) {
+                        const float4 wv =
+                            *reinterpret_cast<const float4 *>(&ws[t * 2 + ci][half * 16 + c4 * 4]);
+#pragma unroll
+                        for (int py = 0; py < 2; ++py)
+#pragma unroll
+                            for (int px = 0; px < 2; ++px) {
+                                const float xv =
+                                    ci ? in1[py + ky][px + kx] : in0[py + ky][px + kx];
+                                float *ac = &acc[py * 2 + px][c4 * 4];
+                                ac[0] = fmaf(xv, wv.x, ac[0]);
+                                ac[1] = fmaf(xv, wv.y, ac[1]);
+                                ac[2] = fmaf(xv, wv.z, ac[2]);
+                                ac[3] = fmaf(xv, wv.w, ac[3]);
+                            }
+                    }
+                }
+            }
+            float yv[4][16];
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {
+                const int py = k >> 1, px = k & 1;
+                uint4 u[2];
+                bf16 *ub = reinterpret_cast<bf16 *>(u);
+#pragma unroll
+                for (int c = 0; c < 16; ++c) {
+                    const bf16 r = __float2bfloat16(fmaxf(acc[k][c] + bs[half * 16 + c], 0.f));
+                    ub[c] = r;
+                    yv[k][c] = bf(r);
+                }
+                const size_t p = img + (size_t)(h0 + py) * W + w0 + px;
+                uint4 *dst = reinterpret_cast<uint4 *>(y + p * 32 + half * 16);
+                dst[0] = u[0];
+                dst[1] = u[1];
+            }
+            uint4 u[2];
+            bf16 *ub = reinterpret_cast<bf16 *>(u);
+#pragma unroll
+            for (int c = 0; c < 16; ++c) {
+                float s = yv[0][c] + yv[1][c];
+                s += yv[2][c];
+                ub[c] = __float2bfloat16(0.25f * (s + yv[3][c]));
+            }
+            uint4 *dst = reinterpret_cast<uint4 *>(yp + ((size_t)n * h2 * w2 + (size_t)hh * w2 + ww) * 32 + half * 16);
+            dst[0] = u[0];
+            dst[1] = u[1];
+        }
+    }
+}
+
+// Sum of the split-K slabs part[z][o .. o + 7], z = 0, 1, ... in order, plus bias, ReLU
+__device__ __forceinline__ void finalize8(const float *__restrict__ part, int nz, long long slab,
+                                          size_t o, const float *__restrict__ bias, int relu,
+                                          float (&v)[8])
+{
+    const float4 *p = reinterpret_cast<const float4 *>(part + o);
+    float4 a = __ldg(p), b = __ldg(p + 1);
+    v[0] = a.x, v[1] = a.y, v[2] = a.z, v[3] = a.w, v[4] = b.x, v[5] = b.y, v[6] = b.z, v[7] = b.w;
+#pragma unroll 4
+    for (int z = 1; z < nz; ++z) {
+        const float4 *q = reinterpret_cast<const float4 *>(part + (size_t)z * slab + o);
+        a = __ldg(q);
+        b = __ldg(q + 1);
+        v[0] += a.x, v[1] += a.y, v[2] += a.z, v[3] += a.w;
+        v[4] += b.x, v[5] += b.y, v[6] += b.z, v[7] += b.w;
+    }
+#pragma unroll
+    for (int i = 0; i < 8; ++i) {
+        float t = v[i] + bias[i];
+        if (relu) t = fmaxf(t, 0.f);
+        v[i] = t;
+    }
+}
+
+// finalize_act_kernel fused with the 2 x 2 pooling of its output: one thread per pixel and 8
+// channels, the four pixels of a pooling block in four consecutive lanes (the pooled value is
+// gathered by shuffles into the first); y (Bn, H, W, C) and yp (Bn, H/2, W/2, C) are both
+// written, with the arithmetic of finalize_act_kernel and pool2_kernel. The thread count
+// Bn H W C / 8 is a multiple of 32 (H and W are multiples of 8), so whole warps run each
+// iteration.
+__global__ void finalize_pool_kernel(const float *__restrict__ part, int nz,
+                                     const float *__restrict__ bias, bf16 *__restrict__ y,
+                                     bf16 *__restrict__ yp, int Bn, int H, int W, int C, int relu)
+{
+    const int h2 = H / 2, w2 = W / 2, cv = C / 8;
+    const long long n = (long long)Bn * H * W * cv;
+    const long long slab = (long long)Bn * H * W * C;
+    LENTILS_GRID_STRIDE(e, n)
+    {
+        const int k = (int)(e & 3);
+        const long long rest = e >> 2;
+        const int c = (int)(rest % cv) * 8;
+        const long long q = rest / cv;  // pooled pixel
+        const int w = (int)(q % w2);
+        const long long r = q / w2;
+        const int h = (int)(r % h2);
+        const int b = (int)(r / h2);
+        const size_t p = (size_t)(b * H + 2 * h + (k >> 1)) * W + 2 * w + (k & 1);
+        const size_t o = p * C + c;
+        float v[8];
+        finalize8(part, nz, slab, o, bias + c, relu, v);
+        bf8_store(y + o, v);
+        float s[8];
+        const int lane = threadIdx.x & 31, src = lane & ~3;
+#pragma unroll
+        for (int i = 0; i < 8; ++i) {
+            const float yv = bf(__float2bfloat16(v[i]));  // the stored value, as pool2 reads it
+            const float y1 = __shfl_sync(0xffffffffu, yv, src + 1);
+            const float y2 = __shfl_sync(0xffffffffu, yv, src + 2);
+            const float y3 = __shfl_sync(0xffffffffu, yv, src + 3);
+            s[i] = 0.25f * (((yv + y1) + y2) + y3);
+        }
+        if (k == 0) bf8_store(yp + q * C + c, s);
+    }
+}
+
+// finalize_act_kernel fused with up2add_kernel: y (Bn, H, W, C) is the layer output at low
+// resolution; u (Bn, 2H, 2W, C) = up2(y) + skip. One thread per low-resolution pixel and 8
+// channels.
+__global__ void finalize_up_kernel(const float *__restrict__ part, int nz,
+                                   const float *__restrict__ bias, bf16 *__restrict__ y,
+                                   const bf16 *__restrict__ skip, bf16 *__restrict__ u, int Bn,
+                                   int H, int W, int C, int relu)
+{
+    const int cv = C / 8;
+    const long long n = (long long)Bn * H * W * cv;
+    const long long slab = (long long)Bn * H * W * C;
+    LENTILS_GRID_STRIDE(e, n)
+    {
+        const int c = (int)(e % cv) * 8;
+        const long long q = e / cv;
+        const int w = (int)(q % W);
+        const long long r = q / W;
+        const int h = (int)(r % H);
+        const int b = (int)(r / H);
+        const size_t o = q * C + c;
+        float t[4][8];
+        size_t ph[4];
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {  // the skip values, loaded ahead of the slab sums
+            ph[k] = ((size_t)(b * 2 * H + 2 * h + (k >> 1)) * (2 * W) + 2 * w + (k & 1)) * C + c;
+            bf8_load(skip + ph[k], t[k]);
+        }
+        float v[8];
+        finalize8(part, nz, slab, o, bias + c, relu, v);
+        bf8_store(y + o, v);
+        float lo[8];
+#pragma unroll
+        for (int i = 0; i < 8; ++i) lo[i] = bf(__float2bfloat16(v[i]));
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            float s[8];
+#pragma unroll
+            for (int i = 0; i < 8; ++i) s[i] = lo[i] + t[k][i];
+            bf8_store(u + ph[k], s);
+        }
+    }
 }
 
 // out (n, H/2, W/2, C) = mean of the 2 x 2 block
@@ -846,7 +1220,8 @@ __global__ void __launch_bounds__(1024)
 // ------------------------------------------------------------------------------------------------
 struct lentils_unet {
     int H, W, maxB;
-    int gemm_form;        // 0: pipelined convolution GEMMs (cp.async ring), 1: synchronous staging
+    int gemm_form;        // 0: persistent TMA convolutions with fused first / last layers,
+                          // 1: synchronous staging, 2: per-tile TMA / cp.async-ring GEMMs
     int wgrad_ctas;       // CTAs of a weight-gradient GEMM (its pixel reduction is split to fill them)
     float jacobi_weight;  // gamma of the preconditioner form
     long long nparams;
@@ -1025,6 +1400,126 @@ static int conv_tma_launch(const bf16 *act, int C, int ks, int Bn, int H, int W,
     return LENTILS_OK;
 }
 
+static int num_sms()
+{
+    static const int n = [] {
+        int dev = 0, v = 0;
+        if (cudaGetDevice(&dev) != cudaSuccess ||
+            cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
+            return 0;
+        return v;
+    }();
+    return n;
+}
+
+// CTAs per SM of a persistent GEMM instantiation: as many as the SM's shared memory, registers
+// and threads hold, and at most as many as fit their tensor memory (2 N columns each, 512 per
+// SM). Counted from the kernel's attributes (the occupancy query reported one CTA per SM for
+// these kernels where the hardware holds two or three).
+struct PersistShape {
+    cudaError_t err;
+    int per_sm;
+};
+template <class Kern>
+static PersistShape persist_shape(Kern kern, int smem, int tmem_cols)
+{
+    PersistShape r{cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem), 1};
+    if (r.err == cudaSuccess)
+        r.err = cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout,
+                                     (int)cudaSharedmemCarveoutMaxShared);
+    cudaFuncAttributes fa;
+    int dev = 0, smem_sm = 0, reserved = 0, regs_sm = 0;
+    if (r.err == cudaSuccess) r.err = cudaFuncGetAttributes(&fa, kern);
+    if (r.err == cudaSuccess) r.err = cudaGetDevice(&dev);
+    if (r.err == cudaSuccess)
+        r.err = cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev);
+    if (r.err == cudaSuccess)
+        r.err = cudaDeviceGetAttribute(&reserved, cudaDevAttrReservedSharedMemoryPerBlock, dev);
+    if (r.err == cudaSuccess)
+        r.err = cudaDeviceGetAttribute(&regs_sm, cudaDevAttrMaxRegistersPerMultiprocessor, dev);
+    if (r.err != cudaSuccess) return r;
+    const int by_smem = smem_sm / (smem + (int)fa.sharedSizeBytes + reserved);
+    // registers are allocated per warp in units of 256
+    const int warp_regs = ((fa.numRegs * 32 + 255) / 256) * 256;
+    const int by_regs = regs_sm / (warp_regs * (tc::kPersistThreads / 32));
+    const int by_threads = 2048 / tc::kPersistThreads;
+    r.per_sm = std::max(1, std::min(std::min(by_smem, by_regs), std::min(by_threads, 512 / tmem_cols)));
+    return r;
+}
+
+template <int CB>
+constexpr int persist_stages(int N)
+{
+    return CB == 32 ? 6 : (N == 128 ? 3 : 4);
+}
+
+// shared-memory limit and CTAs per SM of one persistent convolution instantiation (set up once
+// per process)
+template <int CB, int N, class EP>
+static const PersistShape &conv_persist_shape()
+{
+    constexpr int kStages = persist_stages<CB>(N);
+    static const PersistShape shape = persist_shape(
+        tc::gemm_tma_persist_kernel<N, kStages, ConvTmaA<CB>, ConvTmaB<CB, N>, EP>,
+        tc::TmaSmem<N, kStages, CB>::kBytes, 2 * N <= 64 ? 64 : 2 * N);
+    return shape;
+}
+
+// The convolution GEMM with TMA operands as a persistent kernel (whole K per tile, row
+// epilogue), one wave of CTAs over all row tiles.
+template <int CB, int N, class EP>
+static int conv_persist_launch(const bf16 *act, int C, int ks, int Bn, int H, int W,
+                               const bf16 *wt, int K, const EP &ep, int *err, cudaStream_t s)
+{
+    constexpr int kStages = persist_stages<CB>(N);
+    ConvTmaA<CB> la;
+    la.C = C;
+    la.ks = ks;
+    la.H = H;
+    la.W = W;
+    la.flip = 0;
+    const int WB = std::min(W, 128), HB = 128 / WB;
+    const uint64_t da[4] = {(uint64_t)C, (uint64_t)W, (uint64_t)H, (uint64_t)Bn};
+    const uint64_t sa[3] = {(uint64_t)C * 2, (uint64_t)W * C * 2, (uint64_t)H * W * C * 2};
+    const uint32_t ba[4] = {(uint32_t)CB, (uint32_t)WB, (uint32_t)HB, 1};
+    if (int st = tma_map_bf16(&la.map, act, 4, da, sa, ba, 2 * CB)) return st;
+    ConvTmaB<CB, N> lb;
+    const uint64_t db[2] = {(uint64_t)K, (uint64_t)N};
+    const uint64_t sb[1] = {(uint64_t)K * 2};
+    const uint32_t bb[2] = {(uint32_t)CB, (uint32_t)N};
+    if (int st = tma_map_bf16(&lb.map, wt, 2, db, sb, bb, 2 * CB)) return st;
+    auto kern = tc::gemm_tma_persist_kernel<N, kStages, ConvTmaA<CB>, ConvTmaB<CB, N>, EP>;
+    constexpr int smem = tc::TmaSmem<N, kStages, CB>::kBytes;
+    const PersistShape &shape = conv_persist_shape<CB, N, EP>();
+    LENTILS_CUDA_TRY(shape.err);
+    const int mtiles = Bn * H * W / 128;
+    const int grid = std::min(mtiles, std::max(1, num_sms() * shape.per_sm));
+    kern<<<grid, tc::kPersistThreads, smem, s>>>(la, lb, ep, mtiles, K / 8, err);
+    LENTILS_CHECK_LAUNCH("convolution gemm (TMA, persistent)");
+    return LENTILS_OK;
+}
+
+template <class EP>
+static int conv_persist(const bf16 *act, int C, int ks, int Bn, int H, int W, const bf16 *wt,
+                        int N, const EP &ep, int *err, cudaStream_t s)
+{
+    const int K = ks * ks * C;
+    if (C == 32) {
+        switch (N) {
+        case 32: return conv_persist_launch<32, 32>(act, C, ks, Bn, H, W, wt, K, ep, err, s);
+        case 64: return conv_persist_launch<32, 64>(act, C, ks, Bn, H, W, wt, K, ep, err, s);
+        case 128: return conv_persist_launch<32, 128>(act, C, ks, Bn, H, W, wt, K, ep, err, s);
+        }
+    } else {
+        switch (N) {
+        case 32: return conv_persist_launch<64, 32>(act, C, ks, Bn, H, W, wt, K, ep, err, s);
+        case 64: return conv_persist_launch<64, 64>(act, C, ks, Bn, H, W, wt, K, ep, err, s);
+        case 128: return conv_persist_launch<64, 128>(act, C, ks, Bn, H, W, wt, K, ep, err, s);
+        }
+    }
+    return set_error(LENTILS_ERR_UNSUPPORTED, "conv_persist: C=%d N=%d", C, N);
+}
+
 // whether a layer's convolution can take the TMA operands: row tiles of 128 pixels inside one
 // image, CB-channel chunks, N in {32, 64, 128}
 static bool conv_tma_ok(int C, int N, int H, int W)
@@ -1079,8 +1574,30 @@ static int level_dims(const lentils_unet *net, int level, int &H, int &W)
     return LENTILS_OK;
 }
 
-// forward of layer l: y = act(conv(x))
-static int layer_forward(lentils_unet *net, int l, const bf16 *x, void *y, int Bn, cudaStream_t s)
+// What follows a hidden layer in the forward pass: a 2 x 2 pooling of its output into pool, or
+// an upsampling of it added to skip into up (the next level's input), or nothing.
+struct FwdPost {
+    bf16 *pool = nullptr;
+    const bf16 *skip = nullptr;
+    bf16 *up = nullptr;
+};
+
+static int run_post(lentils_unet *net, const ConvSpec &c, const bf16 *y, const FwdPost &post,
+                    int Bn, int H, int W, cudaStream_t s)
+{
+    const long long npix = (long long)Bn * H * W;
+    if (post.pool)
+        pool2_kernel<<<blocks_n(npix / 4 * c.cout_p / 8), 256, 0, s>>>(y, post.pool, Bn, H, W, c.cout_p);
+    else if (post.up)
+        up2add_kernel<<<blocks_n(npix * 4 * c.cout_p / 8), 256, 0, s>>>(y, post.skip, post.up, Bn,
+                                                                       2 * H, 2 * W, c.cout_p);
+    LENTILS_CHECK_LAUNCH("pool2 / up2add");
+    return LENTILS_OK;
+}
+
+// forward of layer l: y = act(conv(x)), then the post step
+static int layer_forward(lentils_unet *net, int l, const bf16 *x, void *y, int Bn, cudaStream_t s,
+                         const FwdPost &post = FwdPost())
 {
     const ConvSpec &c = kLayers[l];
     int H, W;
@@ -1092,12 +1609,14 @@ static int layer_forward(lentils_unet *net, int l, const bf16 *x, void *y, int B
     // the pipelined GEMM wins where a layer has few row tiles (the deep layers); with many
     // CTAs the staged GEMM keeps more of them resident and hides its loads by occupancy
     const int mt = (npix + 127) / 128;
-    const bool pipe = net->gemm_form == 0 && mt < kPipeMaxTiles;
-    const bool tma = net->gemm_form == 0 && conv_tma_ok(c.cin_p, c.cout_p, H, W);
+    const bool fast = net->gemm_form != 1;
+    const bool pipe = fast && mt < kPipeMaxTiles;
+    const bool tma = fast && conv_tma_ok(c.cin_p, c.cout_p, H, W);
+    const bool persist = net->gemm_form == 0 && tma;
     if (l == kNumLayers - 1) {
         EpiOut ep{(float *)y, net->b32[l], npix};
         if (tma) return conv_tma(x, c.cin_p, c.ks, Bn, H, W, 0, net->wf[l], c.cout_p, ep, 1, K / 8, net->err, s);
-        return conv_gemm_n(c.cout_p, la, lb, ep, npix, K, net->gemm_form == 0, net->err, s);
+        return conv_gemm_n(c.cout_p, la, lb, ep, npix, K, fast, net->err, s);
     }
     const int mtiles = (npix + 127) / 128;
     const int kp = (K + 7) / 8, nchunks = (kp + 7) / 8;
@@ -1116,14 +1635,50 @@ static int layer_forward(lentils_unet *net, int l, const bf16 *x, void *y, int B
         default: return set_error(LENTILS_ERR_UNSUPPORTED, "split-K N=%d", c.cout_p);
         }
         if (st) return st;
-        finalize_act_kernel<<<blocks_n(n), 256, 0, s>>>(net->splitk, nz, net->b32[l], (bf16 *)y,
-                                                        n, c.cout_p, c.relu);
-        LENTILS_CHECK_LAUNCH("finalize_act_kernel");
+        // the slabs are summed together with the post step
+        if (post.pool)
+            finalize_pool_kernel<<<blocks_small(n / 8), 64, 0, s>>>(net->splitk, nz, net->b32[l], (bf16 *)y,
+                                                                    post.pool, Bn, H, W, c.cout_p, c.relu);
+        else if (post.up)
+            finalize_up_kernel<<<blocks_small(n / 8), 64, 0, s>>>(net->splitk, nz, net->b32[l], (bf16 *)y,
+                                                                  post.skip, post.up, Bn, H, W, c.cout_p, c.relu);
+        else
+            finalize_act_kernel<<<blocks_n(n), 256, 0, s>>>(net->splitk, nz, net->b32[l], (bf16 *)y,
+                                                            n, c.cout_p, c.relu);
+        LENTILS_CHECK_LAUNCH("finalize kernel");
         return LENTILS_OK;
     }
-    EpiAct ep{(bf16 *)y, net->b32[l], npix, c.cout_p, c.relu};
-    if (tma) return conv_tma(x, c.cin_p, c.ks, Bn, H, W, 0, net->wf[l], c.cout_p, ep, 1, K / 8, net->err, s);
-    return conv_gemm_n(c.cout_p, la, lb, ep, npix, K, pipe, net->err, s);
+    int st;
+    if (persist) {
+        RowAct ep{(bf16 *)y, net->b32[l], npix, c.cout_p, c.relu};
+        st = conv_persist(x, c.cin_p, c.ks, Bn, H, W, net->wf[l], c.cout_p, ep, net->err, s);
+    } else {
+        EpiAct ep{(bf16 *)y, net->b32[l], npix, c.cout_p, c.relu};
+        st = tma ? conv_tma(x, c.cin_p, c.ks, Bn, H, W, 0, net->wf[l], c.cout_p, ep, 1, K / 8, net->err, s)
+                 : conv_gemm_n(c.cout_p, la, lb, ep, npix, K, pipe, net->err, s);
+    }
+    if (st) return st;
+    return run_post(net, c, (const bf16 *)y, post, Bn, H, W, s);
+}
+
+// The last hidden layer (c1) fused with the output layer on the persistent GEMM, when c1 takes
+// that path; returns 1 (nothing run) otherwise. y (c1's output) may be null; with z set the
+// preconditioner's combination is written instead of out.
+static int fused_c1_out(lentils_unet *net, const bf16 *x, bf16 *y, float *out, float *z,
+                        const float *r, const float *dinv, int Bn, cudaStream_t s)
+{
+    const int l = kNumLayers - 2;
+    const ConvSpec &c = kLayers[l];
+    int H, W;
+    level_dims(net, c.level, H, W);
+    const int npix = Bn * H * W;
+    if (net->gemm_form != 0 || !conv_tma_ok(c.cin_p, c.cout_p, H, W) || c.cout_p != 32 ||
+        c.cin_p != 32 || npix < kSplitMaxPix)
+        return 1;
+    RowActOut ep{y, net->b32[l], npix, net->wf[l + 1], net->b32[l + 1], out, z, r, dinv,
+                 net->pscale, net->jacobi_weight};
+    return conv_persist_launch<32, 32>(x, c.cin_p, c.ks, Bn, H, W, net->wf[l], c.ks * c.ks * c.cin_p,
+                                       ep, net->err, s);
 }
 
 // backward of layer l: dy (gradient of its output, before the ReLU mask), y (its output, for
@@ -1138,7 +1693,7 @@ static int layer_backward(lentils_unet *net, int l, const bf16 *dy, const bf16 *
     const int taps = c.ks * c.ks;
     const bf16 *mask = c.relu ? y : nullptr;
     // the transposed weight-gradient operands take 8 pixels of one image row per piece
-    const bool pipe = net->gemm_form == 0 && c.cout_p <= 128 && c.cin_p <= 128 && (W % 8) == 0;
+    const bool pipe = net->gemm_form != 1 && c.cout_p <= 128 && c.cin_p <= 128 && (W % 8) == 0;
     if (!pipe) {  // bias gradient (the pipelined form sums it in grad_prep_kernel)
         bias_grad_kernel<<<std::min(npix, 1024), c.cout_p, 0, s>>>(dy, mask, net->gb[l], npix,
                                                                    c.cout_p, c.cout);
@@ -1270,41 +1825,80 @@ static int layer_backward(lentils_unet *net, int l, const bf16 *dy, const bf16 *
         tc::RowMajorLoader lb{net->wb[l], c.cin_p, K, K};
         EpiStoreBf16 ep{dx, npix, c.cin_p};
         if (int st = conv_gemm_n(std::max(32, c.cin_p), la, lb, ep, npix, K,
-                                 net->gemm_form == 0 && !mask, net->err, s))
+                                 net->gemm_form != 1 && !mask, net->err, s))
             return st;
     }
     return LENTILS_OK;
 }
 
 // all layers, from the packed input x0 to out
-static int net_layers_forward(lentils_unet *net, int Bn, cudaStream_t s)
+// Input of a forward pass: channel 0 = a (times a2 and 1 / scale where those are given),
+// channel 1 = b. With z set (the preconditioner: a = r, a2 = dinv, b = feat) the result is the
+// combination z = s * out + gamma * dinv * r, and the activations that only a backward pass
+// reads (the packed input, c1) are not written where the fused kernels can skip them.
+struct FwdIn {
+    const float *a, *a2, *scale, *b;
+    float *z;
+};
+
+static int net_forward_in(lentils_unet *net, const FwdIn &in, int Bn, cudaStream_t s)
 {
     const int H = net->H, W = net->W;
     const long long np0 = (long long)Bn * H * W;
+    const bool pre = in.z != nullptr;
     int st;
-    if ((st = layer_forward(net, 0, net->x0, net->e1, Bn, s))) return st;
-    pool2_kernel<<<blocks_n(np0 / 4 * 32), 256, 0, s>>>(net->e1, net->p1, Bn, H, W, 32);
-    if ((st = layer_forward(net, 1, net->p1, net->e2, Bn, s))) return st;
-    pool2_kernel<<<blocks_n(np0 / 16 * 64), 256, 0, s>>>(net->e2, net->p2, Bn, H / 2, W / 2, 64);
-    if ((st = layer_forward(net, 2, net->p2, net->e3, Bn, s))) return st;
-    pool2_kernel<<<blocks_n(np0 / 64 * 128), 256, 0, s>>>(net->e3, net->p3, Bn, H / 4, W / 4, 128);
-    if ((st = layer_forward(net, 3, net->p3, net->b, Bn, s))) return st;
-    up2add_kernel<<<blocks_n(np0 / 16 * 128), 256, 0, s>>>(net->b, net->e3, net->u3, Bn, H / 4, W / 4, 128);
-    if ((st = layer_forward(net, 4, net->u3, net->c3, Bn, s))) return st;
-    up2add_kernel<<<blocks_n(np0 / 4 * 64), 256, 0, s>>>(net->c3, net->e2, net->u2, Bn, H / 2, W / 2, 64);
-    if ((st = layer_forward(net, 5, net->u2, net->c2, Bn, s))) return st;
-    up2add_kernel<<<blocks_n(np0 * 32), 256, 0, s>>>(net->c2, net->e1, net->u1, Bn, H, W, 32);
-    if ((st = layer_forward(net, 6, net->u1, net->c1, Bn, s))) return st;
-    if ((st = layer_forward(net, 7, net->c1, net->out, Bn, s))) return st;
+    if (net->gemm_form == 0) {
+        // below about two waves of blocks, each thread takes half the channels
+        const long long nblk = np0 / 4;
+        const int nh = nblk < 152LL * 256 ? 2 : 1;
+        const int blocks = (int)std::max(1LL, std::min((nblk * nh + 127) / 128, 152LL * 16));
+        e1_direct_kernel<<<blocks, 128, 0, s>>>(in.a, in.a2, in.scale, in.b, net->wf[0],
+                                                net->b32[0], pre ? nullptr : net->x0, net->e1,
+                                                net->p1, Bn, H, W, nh);
+        LENTILS_CHECK_LAUNCH("e1_direct_kernel");
+    } else {
+        if (pre)
+            precond_input_kernel<<<blocks_n(np0), 256, 0, s>>>(in.a, in.a2, in.b, in.scale, net->x0,
+                                                               (int)np0);
+        else
+            make_input_kernel<<<blocks_n(np0), 256, 0, s>>>(in.a, in.b, net->x0, np0);
+        FwdPost p0;
+        p0.pool = net->p1;
+        if ((st = layer_forward(net, 0, net->x0, net->e1, Bn, s, p0))) return st;
+    }
+    FwdPost p1, p2, p3, p4, p5;
+    p1.pool = net->p2;
+    p2.pool = net->p3;
+    p3.skip = net->e3;
+    p3.up = net->u3;
+    p4.skip = net->e2;
+    p4.up = net->u2;
+    p5.skip = net->e1;
+    p5.up = net->u1;
+    if ((st = layer_forward(net, 1, net->p1, net->e2, Bn, s, p1))) return st;
+    if ((st = layer_forward(net, 2, net->p2, net->e3, Bn, s, p2))) return st;
+    if ((st = layer_forward(net, 3, net->p3, net->b, Bn, s, p3))) return st;
+    if ((st = layer_forward(net, 4, net->u3, net->c3, Bn, s, p4))) return st;
+    if ((st = layer_forward(net, 5, net->u2, net->c2, Bn, s, p5))) return st;
+    st = fused_c1_out(net, net->u1, pre ? nullptr : net->c1, net->out, in.z, in.a, in.a2, Bn, s);
+    if (st == 1) {
+        if ((st = layer_forward(net, 6, net->u1, net->c1, Bn, s))) return st;
+        if ((st = layer_forward(net, 7, net->c1, net->out, Bn, s))) return st;
+        if (pre) {
+            precond_combine_kernel<<<blocks_n(np0), 256, 0, s>>>(in.a, in.a2, net->out, net->pscale,
+                                                                 net->jacobi_weight, in.z, (int)np0);
+            LENTILS_CHECK_LAUNCH("precond_combine_kernel");
+        }
+    } else if (st) {
+        return st;
+    }
     LENTILS_CHECK_LAUNCH("unet forward");
     return LENTILS_OK;
 }
 
 static int net_forward(lentils_unet *net, const float *r, const float *d, int Bn, cudaStream_t s)
 {
-    const long long np0 = (long long)Bn * net->H * net->W;
-    make_input_kernel<<<blocks_n(np0), 256, 0, s>>>(r, d, net->x0, np0);
-    return net_layers_forward(net, Bn, s);
+    return net_forward_in(net, FwdIn{r, nullptr, nullptr, d, nullptr}, Bn, s);
 }
 
 // parameter gradients (forward must have run for this batch): of the mean squared error
@@ -1373,7 +1967,14 @@ static int prepare_forward()
     LENTILS_CUDA_TRY((gemm_smem_attr<32, ConvFwdA, tc::RowMajorLoader, EpiPartialF32>()));
     LENTILS_CUDA_TRY((gemm_smem_attr<64, ConvFwdA, tc::RowMajorLoader, EpiPartialF32>()));
     LENTILS_CUDA_TRY((gemm_smem_attr<128, ConvFwdA, tc::RowMajorLoader, EpiPartialF32>()));
-    return LENTILS_OK;
+    LENTILS_CUDA_TRY((conv_persist_shape<32, 32, RowAct>().err));
+    LENTILS_CUDA_TRY((conv_persist_shape<32, 64, RowAct>().err));
+    LENTILS_CUDA_TRY((conv_persist_shape<32, 128, RowAct>().err));
+    LENTILS_CUDA_TRY((conv_persist_shape<64, 32, RowAct>().err));
+    LENTILS_CUDA_TRY((conv_persist_shape<64, 64, RowAct>().err));
+    LENTILS_CUDA_TRY((conv_persist_shape<64, 128, RowAct>().err));
+    LENTILS_CUDA_TRY((conv_persist_shape<32, 32, RowActOut>().err));
+    return num_sms() > 0 ? LENTILS_OK : set_error(LENTILS_ERR_CUDA, "SM count");
 }
 
 int unet_precondition(lentils_unet *net, const float *r, const float *dinv, const float *feat,
@@ -1381,13 +1982,8 @@ int unet_precondition(lentils_unet *net, const float *r, const float *dinv, cons
 {
     const int n = net->H * net->W;
     precond_scale_kernel<<<1, 1024, 0, s>>>(r, dinv, n, net->pscale);
-    precond_input_kernel<<<blocks_n(n), 256, 0, s>>>(r, dinv, feat, net->pscale, net->x0, n);
-    LENTILS_CHECK_LAUNCH("precond input");
-    if (int st = net_layers_forward(net, 1, s)) return st;
-    precond_combine_kernel<<<blocks_n(n), 256, 0, s>>>(r, dinv, net->out, net->pscale,
-                                                       net->jacobi_weight, z, n);
-    LENTILS_CHECK_LAUNCH("precond_combine_kernel");
-    return LENTILS_OK;
+    LENTILS_CHECK_LAUNCH("precond_scale_kernel");
+    return net_forward_in(net, FwdIn{r, dinv, net->pscale, feat, z}, 1, s);
 }
 
 int unet_prepare(lentils_unet *net) { return net ? prepare_forward() : LENTILS_OK; }
@@ -1677,7 +2273,7 @@ int lentils_unet_set_wgrad_ctas(lentils_unet *net, int ctas)
 int lentils_unet_set_gemm_form(lentils_unet *net, int form)
 {
     clear_error();
-    if (!net || form < 0 || form > 1) return set_error(LENTILS_ERR_INVALID, "unet_set_gemm_form");
+    if (!net || form < 0 || form > 2) return set_error(LENTILS_ERR_INVALID, "unet_set_gemm_form");
     net->gemm_form = form;
     return LENTILS_OK;
 }

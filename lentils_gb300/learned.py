@@ -192,7 +192,8 @@ class UNet:
         return z
 
     def set_gemm_form(self, form):
-        """Convolution GEMM kernel (lentils_unet_set_gemm_form): 0 pipelined, 1 staged."""
+        """Convolution kernels (lentils_unet_set_gemm_form): 0 persistent TMA GEMMs with the
+        first and output layers fused, 1 staged GEMMs, 2 per-tile TMA / pipelined GEMMs."""
         N.check(N.lib().lentils_unet_set_gemm_form(self._h, int(form)))
 
     def set_jacobi_weight(self, gamma):

@@ -98,27 +98,29 @@ def test_unet_gradients_match_oracle(native, B, H, W):
 
 
 def test_unet_gemm_forms_agree(native):
-    """The pipelined convolution GEMMs (cp.async ring; transposed weight-gradient operands)
-    and the staged ones give the same forward output and gradients on the 128^2 grid, up to
-    FP32 summation order and the BF16 rounding it can flip."""
+    """The persistent TMA convolutions with the fused first and output layers (form 0), the
+    per-tile TMA / pipelined GEMMs (form 2) and the staged ones (form 1) give the same forward
+    output and gradients on the 128^2 grid, up to FP32 summation order and the BF16 rounding it
+    can flip."""
     from lentils_gb300 import learned
     p, x, f, t = _problem(77, 2, 128, 128)
     net = learned.UNet(128, 128, max_batch=2, params=p)
     xc, fc, tc = _cuda(x, f, t)
     res = {}
-    for form in (1, 0):
+    for form in (1, 2, 0):
         net.set_gemm_form(form)
         out = net.forward(xc, fc)
         g, loss = net.gradients(xc, fc, tc)
         res[form] = (out.cpu().numpy(), g, loss)
     assert net.error_flag() == 0
-    assert _rel(res[0][0], res[1][0]) < 1e-3
-    o = 0
-    for li, (ci, co, k, _, _) in enumerate(learned.LAYERS):
-        n = co * k * k * ci
-        assert _rel(res[0][1][o:o + n], res[1][1][o:o + n]) < 1e-2, li
-        o += n + co
-    assert abs(res[0][2] - res[1][2]) <= 1e-4 * abs(res[1][2])
+    for form in (0, 2):
+        assert _rel(res[form][0], res[1][0]) < 1e-3, form
+        o = 0
+        for li, (ci, co, k, _, _) in enumerate(learned.LAYERS):
+            n = co * k * k * ci
+            assert _rel(res[form][1][o:o + n], res[1][1][o:o + n]) < 1e-2, (form, li)
+            o += n + co
+        assert abs(res[form][2] - res[1][2]) <= 1e-4 * abs(res[1][2]), form
 
 
 def test_unet_adam_overfits_one_batch(native):
@@ -138,9 +140,12 @@ def test_unet_adam_overfits_one_batch(native):
     assert l1 < 0.1 * l0, (l0, l1)
 
 
-def test_unet_precondition_form(native):
+# 32 x 32: every hidden layer split over K; 128 x 128: the first layer, c1 and the output layer
+# and the combination fused (persistent GEMM epilogue)
+@pytest.mark.parametrize("H", [32, 128])
+def test_unet_precondition_form(native, H):
     from lentils_gb300 import learned
-    H = W = 32
+    W = H
     rng = np.random.default_rng(7)
     net = learned.UNet(H, W, max_batch=1, params=learned.init_params(2, out_scale=1.0))
     r = torch.as_tensor(rng.normal(size=(H, W)).astype(np.float32)).cuda()
