@@ -901,8 +901,9 @@ def run_sweep_bench(peak, nsamples=256, steps=10, warmup=3, form=SWEEP_FORM):
 def run_unet_bench(steps=20, warmup=3):
     """The learned preconditioner's network (128^2 source grid, 276,545 parameters, BF16 on the
     tcgen05 tensor cores): forward at batch 1 (as the solver applies it) and 32, one training
-    step (forward, backward, Adam) at batch 32, and the preconditioner application, with CUDA
-    events on the current stream. Random weights and inputs (seeded); the forward FLOPs are
+    step (forward, backward, Adam) at batch 32, and the preconditioner application (called from
+    Python, and replayed from a CUDA graph as the solver applies it), with CUDA events on the
+    current stream. Random weights and inputs (seeded); the forward FLOPs are
     2 * pixels * K * N summed over the convolutions."""
     import torch
     from lentils_gb300 import learned
@@ -927,6 +928,19 @@ def run_unet_bench(steps=20, warmup=3):
         torch.cuda.synchronize()
         return e0.elapsed_time(e1) / n
 
+    def graphed(fn, n):
+        # the call captured once into a CUDA graph and replayed, as the solver applies it
+        side = torch.cuda.Stream()
+        side.wait_stream(torch.cuda.current_stream())
+        with torch.cuda.stream(side):
+            for _ in range(warmup):
+                fn()
+        torch.cuda.current_stream().wait_stream(side)
+        gr = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(gr):
+            fn()
+        return timed(gr.replay, n)
+
     fwd_flop = 0
     for ci, co, k, _, level in learned.LAYERS:
         npix = 32 * (H >> level) * (W >> level)
@@ -937,6 +951,7 @@ def run_unet_bench(steps=20, warmup=3):
            "forward_b32_ms": timed(lambda: net.forward(x, f), steps),
            "train_step_b32_ms": timed(lambda: net.train_step(x, f, t, 0.0), max(3, steps // 2)),
            "precondition_ms": timed(lambda: net.precondition(r, d, ft), steps),
+           "precondition_graph_ms": graphed(lambda: net.precondition(r, d, ft), steps),
            "forward_b32_gflop": fwd_flop / 1e9}
     out["forward_b32_tflops"] = fwd_flop / (out["forward_b32_ms"] * 1e-3) / 1e12
     out["train_step_b32_tflops"] = 3 * fwd_flop / (out["train_step_b32_ms"] * 1e-3) / 1e12

@@ -83,6 +83,15 @@ __device__ __forceinline__ void fence_async_smem()
 __device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
 __device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
 
+// -- programmatic dependent launch ------------------------------------------------------------
+// A kernel launched with programmatic stream serialization may start while the kernel before it
+// in the stream is still running; pdl_wait() blocks until that kernel has completed and its
+// memory is visible (a no-op for a kernel launched without the attribute), pdl_trigger() lets
+// the next such kernel start once every CTA of this grid has triggered or exited. Everything
+// before pdl_wait() must neither read what the previous kernel writes nor write what it reads.
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+__device__ __forceinline__ void pdl_trigger() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
+
 // -- TMEM allocation (one full warp) ----------------------------------------------------------
 __device__ __forceinline__ void tmem_alloc(uint32_t *dst_smem, uint32_t ncols)
 {

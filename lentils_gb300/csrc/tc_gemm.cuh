@@ -401,9 +401,11 @@ __global__ void __launch_bounds__(kPipeThreads)
         abort_flag = 0;
         fence_mbar_init();
     }
+    pdl_wait();
     tc_fence_before();
     __syncthreads();
     tc_fence_after();
+    pdl_trigger();
     const uint32_t tmem = tmem_base;
     int last[STAGES];  // producer: the last chunk loaded into each stage (-1: none)
 #pragma unroll
@@ -565,10 +567,12 @@ __global__ void __launch_bounds__(kPersistThreads, 1)
         prefetch_tensormap(&la.map);
         prefetch_tensormap(&lb.map);
     }
+    pdl_wait();
     if (warp < 4) ep.prepare(scratch, threadIdx.x);
     tc_fence_before();
     __syncthreads();
     tc_fence_after();
+    pdl_trigger();
     const uint32_t tmem = tmem_base;
 
     if (warp == 4) {

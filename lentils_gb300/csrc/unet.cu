@@ -475,6 +475,25 @@ struct RowAct {  // y[pixel][n0 + i] = bf16(relu?(v + bias)), C channels per pix
     __device__ __forceinline__ void row_end(int, float, const float *) const {}
 };
 
+struct RowStore {  // dx[pixel][n0 + i] = bf16(v), C channels per pixel (a data gradient)
+    bf16 *y;
+    int npix, C;
+    __device__ __forceinline__ void prepare(float *, int) const {}
+    __device__ __forceinline__ void row(int m, int n0, const float (&v)[32], float &,
+                                        const float *) const
+    {
+        if (m >= npix) return;
+        uint4 u[4];
+        bf16 *b = reinterpret_cast<bf16 *>(u);
+#pragma unroll
+        for (int i = 0; i < 32; ++i) b[i] = __float2bfloat16(v[i]);
+        uint4 *dst = reinterpret_cast<uint4 *>(y + (size_t)m * C + n0);
+#pragma unroll
+        for (int i = 0; i < 4; ++i) dst[i] = u[i];
+    }
+    __device__ __forceinline__ void row_end(int, float, const float *) const {}
+};
+
 // The last hidden layer (32 channels, ReLU) fused with the 1 x 1 output layer: y as RowAct (not
 // stored when y is null), then out = sum_c wo[c] * y[c] + bo over the BF16 values of y in
 // channel order. With z set, the preconditioner's combination z = s * out + gamma * dinv * r
@@ -554,6 +573,8 @@ static int blocks_small(long long n)
 __global__ void make_input_kernel(const float *__restrict__ r, const float *__restrict__ d,
                                   bf16 *__restrict__ x0, long long npix)
 {
+    tc::pdl_wait();
+    tc::pdl_trigger();
     LENTILS_GRID_STRIDE(p, npix)
     {
         bf16 v[8];
@@ -569,6 +590,8 @@ __global__ void finalize_act_kernel(const float *__restrict__ part, int nz,
                                     const float *__restrict__ bias, bf16 *__restrict__ y,
                                     long long n, int C, int relu)
 {
+    tc::pdl_wait();
+    tc::pdl_trigger();
     LENTILS_GRID_STRIDE(e, n)
     {
         float acc = part[e];
@@ -614,6 +637,8 @@ __global__ void __launch_bounds__(128)
                      bf16 *__restrict__ x0, bf16 *__restrict__ y, bf16 *__restrict__ yp, int Bn,
                      int H, int W, int nh)
 {
+    tc::pdl_wait();
+    tc::pdl_trigger();
     __shared__ __align__(16) float ws[18][32];  // [tap * 2 + ci][co]
     __shared__ float bs[32];
     for (int i = threadIdx.x; i < 18 * 32; i += blockDim.x) {
@@ -766,6 +791,8 @@ __global__ void finalize_pool_kernel(const float *__restrict__ part, int nz,
                                      const float *__restrict__ bias, bf16 *__restrict__ y,
                                      bf16 *__restrict__ yp, int Bn, int H, int W, int C, int relu)
 {
+    tc::pdl_wait();
+    tc::pdl_trigger();
     const int h2 = H / 2, w2 = W / 2, cv = C / 8;
     const long long n = (long long)Bn * H * W * cv;
     const long long slab = (long long)Bn * H * W * C;
@@ -806,6 +833,8 @@ __global__ void finalize_up_kernel(const float *__restrict__ part, int nz,
                                    const bf16 *__restrict__ skip, bf16 *__restrict__ u, int Bn,
                                    int H, int W, int C, int relu)
 {
+    tc::pdl_wait();
+    tc::pdl_trigger();
     const int cv = C / 8;
     const long long n = (long long)Bn * H * W * cv;
     const long long slab = (long long)Bn * H * W * C;
@@ -845,6 +874,8 @@ __global__ void finalize_up_kernel(const float *__restrict__ part, int nz,
 __global__ void pool2_kernel(const bf16 *__restrict__ x, bf16 *__restrict__ y, int Bn, int H,
                              int W, int C)
 {
+    tc::pdl_wait();
+    tc::pdl_trigger();
     const int h2 = H / 2, w2 = W / 2, cv = C / 8;
     const long long n = (long long)Bn * h2 * w2 * cv;
     LENTILS_GRID_STRIDE(e, n)
@@ -875,6 +906,8 @@ __global__ void pool2_kernel(const bf16 *__restrict__ x, bf16 *__restrict__ y, i
 __global__ void up2add_kernel(const bf16 *__restrict__ low, const bf16 *__restrict__ skip,
                               bf16 *__restrict__ y, int Bn, int H, int W, int C)
 {
+    tc::pdl_wait();
+    tc::pdl_trigger();
     const int cv = C / 8;
     const long long n = (long long)Bn * H * W * cv;
     LENTILS_GRID_STRIDE(e, n)
@@ -1047,6 +1080,166 @@ __global__ void __launch_bounds__(256)
     }
 }
 
+// The output layer's backward pass fused with grad_prep_kernel of the layer below it (c1, 32
+// channels, ReLU). The output layer is 1 x 1 from 32 channels to 1, so its data gradient is
+// the outer product dx[p][c] = bf16(g[p] wo[c]) of the output gradient g (channel 0 of dyo)
+// and its weights (exact in FP32, as the GEMM form gives it), and its weight and bias gradients
+// are gw_out[c] += sum_p g[p] x[p][c], gb_out += sum_p g[p], with x = y = c1, the layer's input.
+// dx is masked by c1's ReLU and written as grad_prep_kernel writes it (dym, dyT, db of c1).
+// 64 pixels per block of 256 threads.
+__global__ void __launch_bounds__(256)
+    out_grad_prep_kernel(const bf16 *__restrict__ dyo, const bf16 *__restrict__ wo,
+                         const bf16 *__restrict__ y, bf16 *__restrict__ dym,
+                         bf16 *__restrict__ dyT, float *__restrict__ db,
+                         float *__restrict__ gw_out, float *__restrict__ gb_out, int npix,
+                         int blocked)
+{
+    constexpr int C = 32;
+    __shared__ __align__(16) bf16 tile[64][C + 8];
+    __shared__ __align__(16) bf16 ytile[64][C + 8];
+    __shared__ float g[64];
+    const int p0 = blockIdx.x * 64;
+    if (threadIdx.x < 64) {
+        const int p = p0 + threadIdx.x;
+        g[threadIdx.x] = p < npix ? bf(dyo[(size_t)p * 32]) : 0.f;
+    }
+    __syncthreads();
+    for (int e = threadIdx.x; e < 64 * (C / 8); e += blockDim.x) {
+        const int i = e / (C / 8), c8 = (e % (C / 8)) * 8, p = p0 + i;
+        uint4 v = make_uint4(0, 0, 0, 0), yv = make_uint4(0, 0, 0, 0);
+        if (p < npix) {
+            const size_t o = (size_t)p * C + c8;
+            yv = *reinterpret_cast<const uint4 *>(y + o);
+            uint4 d;
+            bf16 *dv = reinterpret_cast<bf16 *>(&d);
+#pragma unroll
+            for (int k = 0; k < 8; ++k) dv[k] = __float2bfloat16(g[i] * bf(wo[c8 + k]));
+            v = relu_mask(d, yv);
+            *reinterpret_cast<uint4 *>(dym + o) = v;
+        }
+        *reinterpret_cast<uint4 *>(&tile[i][c8]) = v;
+        *reinterpret_cast<uint4 *>(&ytile[i][c8]) = yv;
+    }
+    __syncthreads();
+    if (threadIdx.x < C) {
+        float acc = 0.f, accw = 0.f;
+        for (int i = 0; i < 64; ++i) {
+            acc += bf(tile[i][threadIdx.x]);
+            accw = fmaf(g[i], bf(ytile[i][threadIdx.x]), accw);
+        }
+        atomicAdd(&db[threadIdx.x], acc);
+        atomicAdd(&gw_out[threadIdx.x], accw);
+    } else if (threadIdx.x == C) {
+        float acc = 0.f;
+        for (int i = 0; i < 64; ++i) acc += g[i];
+        atomicAdd(gb_out, acc);
+    }
+    for (int e = threadIdx.x; e < 8 * C; e += blockDim.x) {  // 8 runs of 8 pixels per channel
+        const int c = e / 8, j = (e - c * 8) * 8;
+        if (p0 + j >= npix) continue;  // npix is a multiple of 8
+        bf16 r[8];
+#pragma unroll
+        for (int k = 0; k < 8; ++k) r[k] = tile[j + k][c];
+        const size_t o = blocked ? ((size_t)blockIdx.x * C + c) * 64 + j : (size_t)c * npix + p0 + j;
+        *reinterpret_cast<uint4 *>(dyT + o) = *reinterpret_cast<uint4 *>(r);
+    }
+}
+
+// Weight and bias gradients of the first layer (2 -> 32 channels, 3 x 3, ReLU) on the CUDA
+// cores: gw[co][t][ci] += sum_p m[p][co] x0[p + off(t)][ci] and gb[co] += sum_p m[p][co], with
+// m = dy masked by y > 0 (dy, y: (Bn, H, W, 32) BF16), x0 the packed 8-channel input (channels
+// 0 and 1), gw in the padded [co][tap][8] layout, taps t = (dh + 1) 3 + dw + 1. A GEMM over
+// K = pixels would leave the tensor core idle behind transposed copies of dy and x0. A thread
+// owns two output channels and walks runs of kE1Run pixels along a row with the 3 x 3 x 2 input
+// window in registers (3 new input pairs per pixel); each block sums its threads in shared
+// memory and adds to gw / gb atomically. W is a multiple of kE1Run.
+constexpr int kE1Run = 16;
+__global__ void __launch_bounds__(256)
+    e1_wgrad_kernel(const bf16 *__restrict__ dy, const bf16 *__restrict__ y,
+                    const bf16 *__restrict__ x0, float *__restrict__ gw, float *__restrict__ gb,
+                    int Bn, int H, int W)
+{
+    __shared__ float red[16][16][38];  // [run slot][channel pair][2 x 18 taps, 2 biases]
+    const int cp = threadIdx.x & 15, slot = threadIdx.x >> 4;
+    float acc[2][18], accb[2] = {0.f, 0.f};
+#pragma unroll
+    for (int q = 0; q < 2; ++q)
+#pragma unroll
+        for (int k = 0; k < 18; ++k) acc[q][k] = 0.f;
+    const int wr = W / kE1Run;
+    const long long nruns = (long long)Bn * H * wr;
+    for (long long run = (long long)blockIdx.x * 16 + slot; run < nruns; run += (long long)gridDim.x * 16) {
+        const int w0 = (int)(run % wr) * kE1Run;
+        const long long rh = run / wr;
+        const int h = (int)(rh % H), n = (int)(rh / H);
+        // loads at clamped addresses, zeroed outside the image, so that they do not depend on
+        // branches and the unrolled loop can issue them early
+        auto ld = [&](int hh, int ww, float (&v)[2]) {
+            const bool ok = hh >= 0 && hh < H && ww >= 0 && ww < W;
+            const size_t idx = ok ? ((size_t)(n * H + hh) * W + ww) * 8 : 0;
+            const __nv_bfloat162 t = *reinterpret_cast<const __nv_bfloat162 *>(x0 + idx);
+            v[0] = ok ? __low2float(t) : 0.f;
+            v[1] = ok ? __high2float(t) : 0.f;
+        };
+        float xw[3][3][2];  // rows h - 1 .. h + 1, columns w - 1 .. w + 1, 2 channels
+#pragma unroll
+        for (int dh = 0; dh < 3; ++dh) {
+            ld(h - 1 + dh, w0 - 1, xw[dh][0]);
+            ld(h - 1 + dh, w0, xw[dh][1]);
+        }
+        const size_t o0 = ((size_t)(n * H + h) * W + w0) * 32 + 2 * cp;
+#pragma unroll
+        for (int k = 0; k < kE1Run; ++k) {
+            const int w = w0 + k;
+#pragma unroll
+            for (int dh = 0; dh < 3; ++dh) ld(h - 1 + dh, w + 1, xw[dh][2]);
+            const __nv_bfloat162 d = *reinterpret_cast<const __nv_bfloat162 *>(dy + o0 + k * 32);
+            const __nv_bfloat162 yy = *reinterpret_cast<const __nv_bfloat162 *>(y + o0 + k * 32);
+            const float m0 = __low2float(yy) > 0.f ? __low2float(d) : 0.f;
+            const float m1 = __high2float(yy) > 0.f ? __high2float(d) : 0.f;
+            accb[0] += m0;
+            accb[1] += m1;
+#pragma unroll
+            for (int dh = 0; dh < 3; ++dh)
+#pragma unroll
+                for (int dx = 0; dx < 3; ++dx)
+#pragma unroll
+                    for (int ci = 0; ci < 2; ++ci) {
+                        const int t = (dh * 3 + dx) * 2 + ci;
+                        acc[0][t] = fmaf(m0, xw[dh][dx][ci], acc[0][t]);
+                        acc[1][t] = fmaf(m1, xw[dh][dx][ci], acc[1][t]);
+                    }
+#pragma unroll
+            for (int dh = 0; dh < 3; ++dh) {
+#pragma unroll
+                for (int ci = 0; ci < 2; ++ci) {
+                    xw[dh][0][ci] = xw[dh][1][ci];
+                    xw[dh][1][ci] = xw[dh][2][ci];
+                }
+            }
+        }
+    }
+#pragma unroll
+    for (int k = 0; k < 18; ++k) {
+        red[slot][cp][k] = acc[0][k];
+        red[slot][cp][18 + k] = acc[1][k];
+    }
+    red[slot][cp][36] = accb[0];
+    red[slot][cp][37] = accb[1];
+    __syncthreads();
+    for (int e = threadIdx.x; e < 16 * 38; e += blockDim.x) {
+        const int c = e / 38, k = e - c * 38;
+        float t = 0.f;
+        for (int sl = 0; sl < 16; ++sl) t += red[sl][c][k];
+        if (k < 36) {
+            const int co = 2 * c + k / 18, tk = k % 18, tap = tk / 2, ci = tk % 2;
+            atomicAdd(&gw[co * 72 + tap * 8 + ci], t);
+        } else {
+            atomicAdd(&gb[2 * c + (k - 36)], t);
+        }
+    }
+}
+
 // xT[s][c][q] = x[p + s - nshift / 2][c] when that pixel is in p's image row, else 0, for the
 // nshift column shifts s (3 for a 3 x 3 kernel: -1, 0, +1; 1 for 1 x 1: 0). q is p's position
 // in the row-padded layout, q = (n (H + 2) + h + 1) W + w, with a zero row above and below each
@@ -1150,6 +1343,8 @@ __global__ void __launch_bounds__(1024)
     precond_scale_kernel(const float *__restrict__ r, const float *__restrict__ dinv, int n,
                          float *__restrict__ scale)
 {
+    tc::pdl_wait();
+    tc::pdl_trigger();
     __shared__ double sh[32];
     double acc = 0.0;
     for (int i = threadIdx.x; i < n; i += blockDim.x) {
@@ -1173,6 +1368,8 @@ __global__ void precond_input_kernel(const float *__restrict__ r, const float *_
                                      const float *__restrict__ feat,
                                      const float *__restrict__ scale, bf16 *__restrict__ x0, int n)
 {
+    tc::pdl_wait();
+    tc::pdl_trigger();
     const float inv = 1.f / scale[0];
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         bf16 v[8];
@@ -1188,6 +1385,8 @@ __global__ void precond_combine_kernel(const float *__restrict__ r, const float 
                                        const float *__restrict__ scale, float gamma,
                                        float *__restrict__ z, int n)
 {
+    tc::pdl_wait();
+    tc::pdl_trigger();
     const float s = scale[0];
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
         z[i] = fmaf(s, out[i], gamma * dinv[i] * r[i]);
@@ -1395,9 +1594,30 @@ static int conv_tma_launch(const bf16 *act, int C, int ks, int Bn, int H, int W,
         cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
     LENTILS_CUDA_TRY(attr);
     const int mtiles = Bn * H * W / 128;
-    kern<<<dim3(mtiles, 1, nz), tc::kPipeThreads, smem, s>>>(la, lb, ep, K / 8, kp_per_split, err);
+    LENTILS_CUDA_TRY(pdl_launch(kern, dim3(mtiles, 1, nz), dim3(tc::kPipeThreads), smem, s, la, lb, ep,
+                                K / 8, kp_per_split, err));
     LENTILS_CHECK_LAUNCH("convolution gemm (TMA)");
     return LENTILS_OK;
+}
+
+// Launches kern with programmatic stream serialization: it may start while the kernel before
+// it in the stream finishes, and waits for it (tc::pdl_wait) before touching its results. Used
+// for the kernels of the forward pass, all of which call tc::pdl_wait first.
+template <class... KArgs, class... Args>
+static cudaError_t pdl_launch(void (*kern)(KArgs...), dim3 grid, dim3 block, size_t smem,
+                              cudaStream_t s, Args &&...args)
+{
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = grid;
+    cfg.blockDim = block;
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = s;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, kern, std::forward<Args>(args)...);
 }
 
 static int num_sms()
@@ -1468,7 +1688,7 @@ static const PersistShape &conv_persist_shape()
 // The convolution GEMM with TMA operands as a persistent kernel (whole K per tile, row
 // epilogue), one wave of CTAs over all row tiles.
 template <int CB, int N, class EP>
-static int conv_persist_launch(const bf16 *act, int C, int ks, int Bn, int H, int W,
+static int conv_persist_launch(const bf16 *act, int C, int ks, int Bn, int H, int W, int flip,
                                const bf16 *wt, int K, const EP &ep, int *err, cudaStream_t s)
 {
     constexpr int kStages = persist_stages<CB>(N);
@@ -1477,7 +1697,7 @@ static int conv_persist_launch(const bf16 *act, int C, int ks, int Bn, int H, in
     la.ks = ks;
     la.H = H;
     la.W = W;
-    la.flip = 0;
+    la.flip = flip;
     const int WB = std::min(W, 128), HB = 128 / WB;
     const uint64_t da[4] = {(uint64_t)C, (uint64_t)W, (uint64_t)H, (uint64_t)Bn};
     const uint64_t sa[3] = {(uint64_t)C * 2, (uint64_t)W * C * 2, (uint64_t)H * W * C * 2};
@@ -1494,27 +1714,29 @@ static int conv_persist_launch(const bf16 *act, int C, int ks, int Bn, int H, in
     LENTILS_CUDA_TRY(shape.err);
     const int mtiles = Bn * H * W / 128;
     const int grid = std::min(mtiles, std::max(1, num_sms() * shape.per_sm));
-    kern<<<grid, tc::kPersistThreads, smem, s>>>(la, lb, ep, mtiles, K / 8, err);
+    LENTILS_CUDA_TRY(pdl_launch(kern, dim3(grid), dim3(tc::kPersistThreads), smem, s, la, lb, ep,
+                                mtiles, K / 8, err));
     LENTILS_CHECK_LAUNCH("convolution gemm (TMA, persistent)");
     return LENTILS_OK;
 }
 
+// flip: the data gradient (taps mirrored; act = the masked output gradient)
 template <class EP>
-static int conv_persist(const bf16 *act, int C, int ks, int Bn, int H, int W, const bf16 *wt,
-                        int N, const EP &ep, int *err, cudaStream_t s)
+static int conv_persist(const bf16 *act, int C, int ks, int Bn, int H, int W, int flip,
+                        const bf16 *wt, int N, const EP &ep, int *err, cudaStream_t s)
 {
     const int K = ks * ks * C;
     if (C == 32) {
         switch (N) {
-        case 32: return conv_persist_launch<32, 32>(act, C, ks, Bn, H, W, wt, K, ep, err, s);
-        case 64: return conv_persist_launch<32, 64>(act, C, ks, Bn, H, W, wt, K, ep, err, s);
-        case 128: return conv_persist_launch<32, 128>(act, C, ks, Bn, H, W, wt, K, ep, err, s);
+        case 32: return conv_persist_launch<32, 32>(act, C, ks, Bn, H, W, flip, wt, K, ep, err, s);
+        case 64: return conv_persist_launch<32, 64>(act, C, ks, Bn, H, W, flip, wt, K, ep, err, s);
+        case 128: return conv_persist_launch<32, 128>(act, C, ks, Bn, H, W, flip, wt, K, ep, err, s);
         }
     } else {
         switch (N) {
-        case 32: return conv_persist_launch<64, 32>(act, C, ks, Bn, H, W, wt, K, ep, err, s);
-        case 64: return conv_persist_launch<64, 64>(act, C, ks, Bn, H, W, wt, K, ep, err, s);
-        case 128: return conv_persist_launch<64, 128>(act, C, ks, Bn, H, W, wt, K, ep, err, s);
+        case 32: return conv_persist_launch<64, 32>(act, C, ks, Bn, H, W, flip, wt, K, ep, err, s);
+        case 64: return conv_persist_launch<64, 64>(act, C, ks, Bn, H, W, flip, wt, K, ep, err, s);
+        case 128: return conv_persist_launch<64, 128>(act, C, ks, Bn, H, W, flip, wt, K, ep, err, s);
         }
     }
     return set_error(LENTILS_ERR_UNSUPPORTED, "conv_persist: C=%d N=%d", C, N);
@@ -1587,10 +1809,11 @@ static int run_post(lentils_unet *net, const ConvSpec &c, const bf16 *y, const F
 {
     const long long npix = (long long)Bn * H * W;
     if (post.pool)
-        pool2_kernel<<<blocks_n(npix / 4 * c.cout_p / 8), 256, 0, s>>>(y, post.pool, Bn, H, W, c.cout_p);
+        LENTILS_CUDA_TRY(pdl_launch(pool2_kernel, dim3(blocks_n(npix / 4 * c.cout_p / 8)), dim3(256), 0, s,
+                                    y, post.pool, Bn, H, W, c.cout_p));
     else if (post.up)
-        up2add_kernel<<<blocks_n(npix * 4 * c.cout_p / 8), 256, 0, s>>>(y, post.skip, post.up, Bn,
-                                                                       2 * H, 2 * W, c.cout_p);
+        LENTILS_CUDA_TRY(pdl_launch(up2add_kernel, dim3(blocks_n(npix * 4 * c.cout_p / 8)), dim3(256), 0, s,
+                                    y, post.skip, post.up, Bn, 2 * H, 2 * W, c.cout_p));
     LENTILS_CHECK_LAUNCH("pool2 / up2add");
     return LENTILS_OK;
 }
@@ -1636,22 +1859,24 @@ static int layer_forward(lentils_unet *net, int l, const bf16 *x, void *y, int B
         }
         if (st) return st;
         // the slabs are summed together with the post step
+        const float *part = net->splitk;
         if (post.pool)
-            finalize_pool_kernel<<<blocks_small(n / 8), 64, 0, s>>>(net->splitk, nz, net->b32[l], (bf16 *)y,
-                                                                    post.pool, Bn, H, W, c.cout_p, c.relu);
+            LENTILS_CUDA_TRY(pdl_launch(finalize_pool_kernel, dim3(blocks_small(n / 8)), dim3(64), 0, s, part,
+                                        nz, net->b32[l], (bf16 *)y, post.pool, Bn, H, W, c.cout_p, c.relu));
         else if (post.up)
-            finalize_up_kernel<<<blocks_small(n / 8), 64, 0, s>>>(net->splitk, nz, net->b32[l], (bf16 *)y,
-                                                                  post.skip, post.up, Bn, H, W, c.cout_p, c.relu);
+            LENTILS_CUDA_TRY(pdl_launch(finalize_up_kernel, dim3(blocks_small(n / 8)), dim3(64), 0, s, part,
+                                        nz, net->b32[l], (bf16 *)y, post.skip, post.up, Bn, H, W, c.cout_p,
+                                        c.relu));
         else
-            finalize_act_kernel<<<blocks_n(n), 256, 0, s>>>(net->splitk, nz, net->b32[l], (bf16 *)y,
-                                                            n, c.cout_p, c.relu);
+            LENTILS_CUDA_TRY(pdl_launch(finalize_act_kernel, dim3(blocks_n(n)), dim3(256), 0, s, part, nz,
+                                        net->b32[l], (bf16 *)y, n, c.cout_p, c.relu));
         LENTILS_CHECK_LAUNCH("finalize kernel");
         return LENTILS_OK;
     }
     int st;
     if (persist) {
         RowAct ep{(bf16 *)y, net->b32[l], npix, c.cout_p, c.relu};
-        st = conv_persist(x, c.cin_p, c.ks, Bn, H, W, net->wf[l], c.cout_p, ep, net->err, s);
+        st = conv_persist(x, c.cin_p, c.ks, Bn, H, W, 0, net->wf[l], c.cout_p, ep, net->err, s);
     } else {
         EpiAct ep{(bf16 *)y, net->b32[l], npix, c.cout_p, c.relu};
         st = tma ? conv_tma(x, c.cin_p, c.ks, Bn, H, W, 0, net->wf[l], c.cout_p, ep, 1, K / 8, net->err, s)
@@ -1677,14 +1902,16 @@ static int fused_c1_out(lentils_unet *net, const bf16 *x, bf16 *y, float *out, f
         return 1;
     RowActOut ep{y, net->b32[l], npix, net->wf[l + 1], net->b32[l + 1], out, z, r, dinv,
                  net->pscale, net->jacobi_weight};
-    return conv_persist_launch<32, 32>(x, c.cin_p, c.ks, Bn, H, W, net->wf[l], c.ks * c.ks * c.cin_p,
-                                       ep, net->err, s);
+    return conv_persist_launch<32, 32>(x, c.cin_p, c.ks, Bn, H, W, 0, net->wf[l],
+                                       c.ks * c.ks * c.cin_p, ep, net->err, s);
 }
 
 // backward of layer l: dy (gradient of its output, before the ReLU mask), y (its output, for
-// the mask; null for the output layer), x (its input); accumulates gw/gb, writes dx (optional)
+// the mask; null for the output layer), x (its input); accumulates gw/gb, writes dx (optional).
+// prepared: the masked gradient operands (dym, dyT) and the bias gradient have been written
+// already (out_grad_prep_kernel); dy is then unused.
 static int layer_backward(lentils_unet *net, int l, const bf16 *dy, const bf16 *y, const bf16 *x,
-                          bf16 *dx, int Bn, cudaStream_t s)
+                          bf16 *dx, int Bn, cudaStream_t s, bool prepared = false)
 {
     const ConvSpec &c = kLayers[l];
     int H, W;
@@ -1694,6 +1921,7 @@ static int layer_backward(lentils_unet *net, int l, const bf16 *dy, const bf16 *
     const bf16 *mask = c.relu ? y : nullptr;
     // the transposed weight-gradient operands take 8 pixels of one image row per piece
     const bool pipe = net->gemm_form != 1 && c.cout_p <= 128 && c.cin_p <= 128 && (W % 8) == 0;
+    if (prepared && !pipe) return set_error(LENTILS_ERR_UNSUPPORTED, "prepared backward, layer %d", l);
     if (!pipe) {  // bias gradient (the pipelined form sums it in grad_prep_kernel)
         bias_grad_kernel<<<std::min(npix, 1024), c.cout_p, 0, s>>>(dy, mask, net->gb[l], npix,
                                                                    c.cout_p, c.cout);
@@ -1704,9 +1932,11 @@ static int layer_backward(lentils_unet *net, int l, const bf16 *dy, const bf16 *
         const int blocks = (npix + 63) / 64;
         // 64-pixel blocks (W a multiple of 64) keep a TMA box in one contiguous run
         const bool blocked = (W % 64) == 0;
-        grad_prep_kernel<<<blocks, 256, 0, s>>>(dy, mask, net->dym, net->dyT, net->gb[l], npix,
-                                                c.cout_p, c.cout, blocked ? 1 : 0);
-        LENTILS_CHECK_LAUNCH("grad_prep_kernel");
+        if (!prepared) {
+            grad_prep_kernel<<<blocks, 256, 0, s>>>(dy, mask, net->dym, net->dyT, net->gb[l], npix,
+                                                    c.cout_p, c.cout, blocked ? 1 : 0);
+            LENTILS_CHECK_LAUNCH("grad_prep_kernel");
+        }
         const int nshift = c.ks == 3 ? 3 : 1;
         const long long qtot = (long long)(npix / (H * W)) * (H + 2) * W;
         shift_transpose_kernel<<<blocks, 256, 0, s>>>(x, net->xT, npix, H, W, c.cin_p, nshift,
@@ -1775,11 +2005,17 @@ static int layer_backward(lentils_unet *net, int l, const bf16 *dy, const bf16 *
         }
         if (st) return st;
         if (dx && conv_tma_ok(c.cout_p, c.cin_p, H, W)) {  // data gradient, TMA operands
-            EpiStoreBf16 epd{dx, npix, c.cin_p};
-            const int K = taps * c.cout_p;
-            if (int st2 = conv_tma(net->dym, c.cout_p, c.ks, Bn, H, W, 1, net->wb[l], c.cin_p, epd,
-                                   1, K / 8, net->err, s))
-                return st2;
+            int st2;
+            if (net->gemm_form == 0) {
+                st2 = conv_persist(net->dym, c.cout_p, c.ks, Bn, H, W, 1, net->wb[l], c.cin_p,
+                                   RowStore{dx, npix, c.cin_p}, net->err, s);
+            } else {
+                EpiStoreBf16 epd{dx, npix, c.cin_p};
+                const int K = taps * c.cout_p;
+                st2 = conv_tma(net->dym, c.cout_p, c.ks, Bn, H, W, 1, net->wb[l], c.cin_p, epd, 1,
+                               K / 8, net->err, s);
+            }
+            if (st2) return st2;
         } else if (dx) {  // data gradient from the masked copy: plain gathers, pipelined
             const int K = taps * c.cout_p;
             ConvBwdDataA lad{net->dym, nullptr, npix, H, W, c.cout_p, c.ks};
@@ -1852,16 +2088,17 @@ static int net_forward_in(lentils_unet *net, const FwdIn &in, int Bn, cudaStream
         const long long nblk = np0 / 4;
         const int nh = nblk < 152LL * 256 ? 2 : 1;
         const int blocks = (int)std::max(1LL, std::min((nblk * nh + 127) / 128, 152LL * 16));
-        e1_direct_kernel<<<blocks, 128, 0, s>>>(in.a, in.a2, in.scale, in.b, net->wf[0],
-                                                net->b32[0], pre ? nullptr : net->x0, net->e1,
-                                                net->p1, Bn, H, W, nh);
+        LENTILS_CUDA_TRY(pdl_launch(e1_direct_kernel, dim3(blocks), dim3(128), 0, s, in.a, in.a2, in.scale,
+                                    in.b, (const bf16 *)net->wf[0], (const float *)net->b32[0],
+                                    pre ? nullptr : net->x0, net->e1, net->p1, Bn, H, W, nh));
         LENTILS_CHECK_LAUNCH("e1_direct_kernel");
     } else {
         if (pre)
-            precond_input_kernel<<<blocks_n(np0), 256, 0, s>>>(in.a, in.a2, in.b, in.scale, net->x0,
-                                                               (int)np0);
+            LENTILS_CUDA_TRY(pdl_launch(precond_input_kernel, dim3(blocks_n(np0)), dim3(256), 0, s, in.a,
+                                        in.a2, in.b, in.scale, net->x0, (int)np0));
         else
-            make_input_kernel<<<blocks_n(np0), 256, 0, s>>>(in.a, in.b, net->x0, np0);
+            LENTILS_CUDA_TRY(pdl_launch(make_input_kernel, dim3(blocks_n(np0)), dim3(256), 0, s, in.a, in.b,
+                                        net->x0, np0));
         FwdPost p0;
         p0.pool = net->p1;
         if ((st = layer_forward(net, 0, net->x0, net->e1, Bn, s, p0))) return st;
@@ -1885,8 +2122,9 @@ static int net_forward_in(lentils_unet *net, const FwdIn &in, int Bn, cudaStream
         if ((st = layer_forward(net, 6, net->u1, net->c1, Bn, s))) return st;
         if ((st = layer_forward(net, 7, net->c1, net->out, Bn, s))) return st;
         if (pre) {
-            precond_combine_kernel<<<blocks_n(np0), 256, 0, s>>>(in.a, in.a2, net->out, net->pscale,
-                                                                 net->jacobi_weight, in.z, (int)np0);
+            LENTILS_CUDA_TRY(pdl_launch(precond_combine_kernel, dim3(blocks_n(np0)), dim3(256), 0, s, in.a,
+                                        in.a2, (const float *)net->out, (const float *)net->pscale,
+                                        net->jacobi_weight, in.z, (int)np0));
             LENTILS_CHECK_LAUNCH("precond_combine_kernel");
         }
     } else if (st) {
@@ -1920,8 +2158,17 @@ static int net_backward(lentils_unet *net, const float *tgt, const float *dout, 
     else
         mse_kernel<<<blocks_n(np0), 256, 0, s>>>(net->out, tgt, net->dy_out, np0, net->loss);
     int st;
-    if ((st = layer_backward(net, 7, net->dy_out, nullptr, net->c1, net->d_c1, Bn, s))) return st;
-    if ((st = layer_backward(net, 6, net->d_c1, net->c1, net->u1, net->d_u1, Bn, s))) return st;
+    if (net->gemm_form == 0 && kLayers[6].cout_p == 32 && (W % 8) == 0) {
+        // the output layer's whole backward pass in c1's gradient preparation
+        out_grad_prep_kernel<<<(int)((np0 + 63) / 64), 256, 0, s>>>(
+            net->dy_out, net->wf[7], net->c1, net->dym, net->dyT, net->gb[6], net->gw_pad[7],
+            net->gb[7], (int)np0, (W % 64) == 0 ? 1 : 0);
+        LENTILS_CHECK_LAUNCH("out_grad_prep_kernel");
+        if ((st = layer_backward(net, 6, nullptr, net->c1, net->u1, net->d_u1, Bn, s, true))) return st;
+    } else {
+        if ((st = layer_backward(net, 7, net->dy_out, nullptr, net->c1, net->d_c1, Bn, s))) return st;
+        if ((st = layer_backward(net, 6, net->d_c1, net->c1, net->u1, net->d_u1, Bn, s))) return st;
+    }
     // u1 = up2(c2) + e1
     sum4_kernel<<<blocks_n(np0 / 4 * 32), 256, 0, s>>>(net->d_u1, net->d_c2, Bn, H, W, 32);
     if ((st = layer_backward(net, 5, net->d_c2, net->c2, net->u2, net->d_u2, Bn, s))) return st;
@@ -1935,7 +2182,15 @@ static int net_backward(lentils_unet *net, const float *tgt, const float *dout, 
     add_pool_grad_kernel<<<blocks_n(np0 / 4 * 64), 256, 0, s>>>(net->d_u2, net->d_p2, net->d_e2, Bn, H / 2, W / 2, 64);
     if ((st = layer_backward(net, 1, net->d_e2, net->e2, net->p1, net->d_p1, Bn, s))) return st;
     add_pool_grad_kernel<<<blocks_n(np0 * 32), 256, 0, s>>>(net->d_u1, net->d_p1, net->d_e1, Bn, H, W, 32);
-    if ((st = layer_backward(net, 0, net->d_e1, net->e1, net->x0, nullptr, Bn, s))) return st;
+    if (net->gemm_form == 0 && W % kE1Run == 0) {
+        const long long items = np0 / kE1Run / 16;  // block iterations of 16 runs
+        const int blocks = (int)std::max(1LL, std::min(items, 152LL * 4));
+        e1_wgrad_kernel<<<blocks, 256, 0, s>>>(net->d_e1, net->e1, net->x0, net->gw_pad[0],
+                                               net->gb[0], Bn, H, W);
+        LENTILS_CHECK_LAUNCH("e1_wgrad_kernel");
+    } else if ((st = layer_backward(net, 0, net->d_e1, net->e1, net->x0, nullptr, Bn, s))) {
+        return st;
+    }
     for (int l = 0; l < kNumLayers; ++l) {
         const ConvSpec &c = kLayers[l];
         gather_wgrad_kernel<<<blocks_n(layer_wcount(l)), 256, 0, s>>>(
@@ -1981,7 +2236,7 @@ int unet_precondition(lentils_unet *net, const float *r, const float *dinv, cons
                       float *z, cudaStream_t s)
 {
     const int n = net->H * net->W;
-    precond_scale_kernel<<<1, 1024, 0, s>>>(r, dinv, n, net->pscale);
+    LENTILS_CUDA_TRY(pdl_launch(precond_scale_kernel, dim3(1), dim3(1024), 0, s, r, dinv, n, net->pscale));
     LENTILS_CHECK_LAUNCH("precond_scale_kernel");
     return net_forward_in(net, FwdIn{r, dinv, net->pscale, feat, z}, 1, s);
 }
