@@ -152,6 +152,21 @@ __device__ __forceinline__ uint64_t smem_desc_sw64(uint32_t saddr)
     return d;
 }
 
+// Shared-memory matrix descriptor for an MN-major operand in the 64-byte swizzled layout: each
+// K row holds 32 consecutive M (or N) values (64 bytes), 8 K rows form a 512-byte swizzle atom,
+// atoms adjacent along K are sbo bytes apart and atoms adjacent along M (N) lbo bytes apart. A
+// K step of 16 values advances the start address by 2 sbo.
+__device__ __forceinline__ uint64_t smem_desc_mn_sw64(uint32_t saddr, uint32_t lbo, uint32_t sbo)
+{
+    uint64_t d = 0;
+    d |= (uint64_t)((saddr >> 4) & 0x3FFFu);
+    d |= (uint64_t)((lbo >> 4) & 0x3FFFu) << 16;
+    d |= (uint64_t)((sbo >> 4) & 0x3FFFu) << 32;
+    d |= (uint64_t)1 << 46;  // descriptor version
+    d |= (uint64_t)4 << 61;  // layout: 64-byte swizzle
+    return d;
+}
+
 template <int SWZ>
 __device__ __forceinline__ uint64_t smem_desc_swz(uint32_t saddr)
 {
@@ -212,6 +227,12 @@ __host__ __device__ constexpr uint32_t idesc_bf16_f32(int M, int N)
            | (1u << 10)                    // B format: BF16
            | ((uint32_t)(N >> 3) << 17)    // N / 8
            | ((uint32_t)(M >> 4) << 24);   // M / 16
+}
+
+// The same with both operands MN-major (the instruction's transpose bits for A and B)
+__host__ __device__ constexpr uint32_t idesc_bf16_f32_mn(int M, int N)
+{
+    return idesc_bf16_f32(M, N) | (1u << 15) | (1u << 16);
 }
 
 // D[tmem] (+)= A[smem] * B[smem]^T, issued by one thread

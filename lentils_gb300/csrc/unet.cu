@@ -1043,7 +1043,7 @@ __global__ void bias_grad_kernel(const bf16 *__restrict__ dy, const bf16 *__rest
 // block's pixels (c < creal). 16-byte loads and stores; the transpose goes through shared
 // memory with rows padded to C + 8 values.
 // blocked: dyT in 64-pixel blocks, dyT[(p / 64) C + c][p % 64], so that a block's C rows are
-// one contiguous 128 C-byte run.
+// one contiguous 128 C-byte run. dyT null: no transposed copy (the MN-major weight gradient).
 __global__ void __launch_bounds__(256)
     grad_prep_kernel(const bf16 *__restrict__ dy, const bf16 *__restrict__ y,
                      bf16 *__restrict__ dym, bf16 *__restrict__ dyT, float *__restrict__ db,
@@ -1069,7 +1069,7 @@ __global__ void __launch_bounds__(256)
         for (int i = 0; i < 64; ++i) acc += bf(tile[i][threadIdx.x]);
         atomicAdd(&db[threadIdx.x], acc);
     }
-    for (int e = threadIdx.x; e < 8 * C; e += blockDim.x) {  // 8 runs of 8 pixels per channel
+    for (int e = threadIdx.x; dyT && e < 8 * C; e += blockDim.x) {  // 8 runs of 8 pixels per channel
         const int c = e / 8, j = (e - c * 8) * 8;
         if (p0 + j >= npix) continue;  // npix is a multiple of 8
         bf16 r[8];
@@ -1085,7 +1085,8 @@ __global__ void __launch_bounds__(256)
 // the outer product dx[p][c] = bf16(g[p] wo[c]) of the output gradient g (channel 0 of dyo)
 // and its weights (exact in FP32, as the GEMM form gives it), and its weight and bias gradients
 // are gw_out[c] += sum_p g[p] x[p][c], gb_out += sum_p g[p], with x = y = c1, the layer's input.
-// dx is masked by c1's ReLU and written as grad_prep_kernel writes it (dym, dyT, db of c1).
+// dx is masked by c1's ReLU and written as grad_prep_kernel writes it (dym, dyT unless null,
+// db of c1).
 // 64 pixels per block of 256 threads.
 __global__ void __launch_bounds__(256)
     out_grad_prep_kernel(const bf16 *__restrict__ dyo, const bf16 *__restrict__ wo,
@@ -1134,7 +1135,7 @@ __global__ void __launch_bounds__(256)
         for (int i = 0; i < 64; ++i) acc += g[i];
         atomicAdd(gb_out, acc);
     }
-    for (int e = threadIdx.x; e < 8 * C; e += blockDim.x) {  // 8 runs of 8 pixels per channel
+    for (int e = threadIdx.x; dyT && e < 8 * C; e += blockDim.x) {  // 8 runs of 8 pixels per channel
         const int c = e / 8, j = (e - c * 8) * 8;
         if (p0 + j >= npix) continue;  // npix is a multiple of 8
         bf16 r[8];
@@ -1528,6 +1529,212 @@ static int conv_gemm_n(int N, const LA &la, const tc::RowMajorLoader &lb, const 
     return set_error(LENTILS_ERR_UNSUPPORTED, "conv gemm N=%d", N);
 }
 
+// Weight gradient of a convolution layer as a GEMM whose operands are both MN-major, read
+// straight from the pixel-major (NHWC) activations and gradients, with no transposed copies:
+//   D[(t, ci)][co] = sum_p x[p + off(t)][ci] dym[p][co],   rows (t, ci) = t C + ci,
+// K = pixels in chunks of 64 (consecutive in raster order, inside one image), one 128-row tile
+// per blockIdx.x, the chunks split over blockIdx.y. An A tile is four boxes of 32 channels x 64
+// pixels of x, each at its tap's pixel offset (the tensor map reads zeros outside the image,
+// the convolution's padding); a B tile is N / 32 such boxes of dym at the chunk itself. With
+// 64-byte rows and the 64-byte swizzle, a box is one 32-wide MN atom column: K groups of 8
+// pixels 512 bytes apart (SBO), boxes 4096 bytes apart (LBO). Row tiles past the last tap
+// leave their boxes unloaded; those rows of D are not written. The epilogue adds each row's N
+// values to g[co][rows] with atomics (the per-split partial sums). Warps: 0-3 epilogue, lane 0
+// of 4 the TMA producer, 5 TMEM and the MMA issuer. Waits are bounded (*err on a timeout).
+constexpr int kWgMnThreads = 192;
+constexpr int kWgMnStages = 4;
+
+template <int N>
+struct WgMnSmem {
+    static constexpr int kA = 4 * 4096, kB = N / 32 * 4096, kStage = kA + kB;
+    static constexpr int kBytes = kWgMnStages * kStage + 1024;
+};
+
+template <int N>
+__global__ void __launch_bounds__(kWgMnThreads, 1)
+    wgrad_mn_kernel(const __grid_constant__ CUtensorMap mx, const __grid_constant__ CUtensorMap mdy,
+                    float *__restrict__ g, int C, int ks, int H, int W, int rows, int nchunks,
+                    int per_cta, int *err)
+{
+    constexpr int S = kWgMnStages;
+    constexpr int kA = WgMnSmem<N>::kA, kStage = WgMnSmem<N>::kStage;
+    constexpr uint32_t ncols = N < 32 ? 32 : N;
+    extern __shared__ __align__(1024) unsigned char smem_raw[];
+    __shared__ uint64_t full[S], empty[S], done;
+    __shared__ uint32_t tmem_base;
+    __shared__ int abort_flag;
+    unsigned char *smem = smem_raw + ((1024 - (tc::smem_u32(smem_raw) & 1023)) & 1023);
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int mt = blockIdx.x;
+    const int c0 = blockIdx.y * per_cta, c1 = min(nchunks, c0 + per_cta);
+    const int nch = c1 > c0 ? c1 - c0 : 0;
+    if (warp == 5) {
+        tc::tmem_alloc(&tmem_base, ncols);
+        tc::tmem_relinquish();
+    }
+    if (threadIdx.x == 0) {
+        for (int i = 0; i < S; ++i) {
+            tc::mbar_init(&full[i], 1);
+            tc::mbar_init(&empty[i], 1);
+        }
+        tc::mbar_init(&done, 1);
+        abort_flag = 0;
+        tc::fence_mbar_init();
+    }
+    if (threadIdx.x == 128) {
+        tc::prefetch_tensormap(&mx);
+        tc::prefetch_tensormap(&mdy);
+    }
+    tc::tc_fence_before();
+    __syncthreads();
+    tc::tc_fence_after();
+    const uint32_t tmem = tmem_base;
+
+    if (warp == 4) {
+        if (lane == 0) {  // the TMA producer
+            // the tile's four boxes: tap offset and first channel (fixed for the CTA)
+            int bdh[4], bdw[4], bci[4], nvalid = 0;
+#pragma unroll
+            for (int b = 0; b < 4; ++b) {
+                const int r0 = mt * 128 + 32 * b, t = r0 / C;
+                bci[b] = r0 - t * C;
+                bdh[b] = t / ks - ks / 2;
+                bdw[b] = t % ks - ks / 2;
+                if (r0 < rows) nvalid = b + 1;
+            }
+            const uint32_t bytes = (uint32_t)nvalid * 4096u + (uint32_t)N / 32u * 4096u;
+            // the first chunk's pixel, then 64 pixels per chunk
+            const int hw = H * W;
+            const long long p0 = (long long)c0 * 64;
+            int n = (int)(p0 / hw), r = (int)(p0 - (long long)n * hw), h = r / W, w0 = r - h * W;
+            const int hstep = W >= 64 ? 0 : 64 / W;
+            int it = 0;
+            for (; it < nch; ++it) {
+                const int st = it % S;
+                if (it >= S && !tc::mbar_wait(&empty[st], ((it / S) - 1) & 1)) {
+                    atomicExch(&abort_flag, 1);
+                    break;
+                }
+                unsigned char *sa = smem + st * kStage;
+                tc::mbar_arrive_expect_tx(&full[st], bytes);
+#pragma unroll
+                for (int b = 0; b < 4; ++b)
+                    if (b < nvalid)
+                        tc::tma_load_4d(sa + 4096 * b, &mx, bci[b], w0 + bdw[b], h + bdh[b], n, &full[st]);
+#pragma unroll
+                for (int b = 0; b < N / 32; ++b)
+                    tc::tma_load_4d(sa + kA + 4096 * b, &mdy, 32 * b, w0, h, n, &full[st]);
+                if (hstep == 0) {
+                    w0 += 64;
+                    if (w0 == W) {
+                        w0 = 0;
+                        if (++h == H) {
+                            h = 0;
+                            ++n;
+                        }
+                    }
+                } else {
+                    h += hstep;
+                    if (h >= H) {
+                        h -= H;
+                        ++n;
+                    }
+                }
+            }
+#pragma unroll
+            for (int i = 0; i < S; ++i) {
+                if (i >= it) continue;
+                const int last = i + ((it - 1 - i) / S) * S;
+                if (!tc::mbar_wait(&full[i], (last / S) & 1)) atomicExch(&abort_flag, 1);
+            }
+        }
+        __syncwarp();
+    } else if (warp == 5) {
+        if (lane == 0) {  // the MMA issuer
+            constexpr uint32_t idesc = tc::idesc_bf16_f32_mn(128, N);
+            for (int it = 0; it < nch; ++it) {
+                const int st = it % S;
+                if (!tc::mbar_wait(&full[st], (it / S) & 1)) {
+                    atomicExch(&abort_flag, 1);
+                    break;
+                }
+                tc::tc_fence_after();
+                const uint32_t sa = tc::smem_u32(smem + st * kStage), sb = sa + kA;
+#pragma unroll
+                for (int k = 0; k < 4; ++k)
+                    tc::mma_bf16(tmem, tc::smem_desc_mn_sw64(sa + 1024 * k, 4096, 512),
+                                 tc::smem_desc_mn_sw64(sb + 1024 * k, 4096, 512), idesc,
+                                 (it > 0 || k > 0) ? 1u : 0u);
+                tc::mma_commit(&empty[st]);
+            }
+            tc::mma_commit(&done);
+        }
+        __syncwarp();
+    }
+    const bool fin = tc::mbar_wait(&done, 0);
+    tc::tc_fence_after();
+    __syncthreads();
+    const bool bad = !fin || *(volatile int *)&abort_flag;
+    if (threadIdx.x == 0 && bad) atomicExch(err, 1);
+    if (!bad && nch > 0 && warp < 4) {
+        const int r = mt * 128 + warp * 32 + lane;
+        const uint32_t taddr = tmem + ((uint32_t)(warp * 32) << 16);
+#pragma unroll 1
+        for (int n0 = 0; n0 < N; n0 += 32) {
+            uint32_t v[32];
+            tc::tmem_ld32(taddr + n0, v);
+            tc::tmem_wait_ld();
+            if (r < rows) {
+#pragma unroll
+                for (int i = 0; i < 32; ++i) {
+                    const float f = __uint_as_float(v[i]);
+                    if (f != 0.f) atomicAdd(&g[(size_t)(n0 + i) * rows + r], f);
+                }
+            }
+        }
+    }
+    tc::tc_fence_before();
+    __syncthreads();
+    if (warp == 5) tc::tmem_dealloc(tmem, ncols);
+}
+
+// Launches wgrad_mn_kernel for layer input x (C channels) and masked output gradient dym
+// (N = cout_p channels), Bn images of H x W, accumulating into g (padded [co][t][ci] layout).
+template <int N>
+static int wgrad_mn_launch(const bf16 *x, const bf16 *dym, float *g, int C, int ks, int Bn, int H,
+                           int W, int ctas_want, int *err, cudaStream_t s)
+{
+    const int WB = std::min(W, 64), HB = 64 / WB;
+    CUtensorMap mx, mdy;
+    const uint64_t dx[4] = {(uint64_t)C, (uint64_t)W, (uint64_t)H, (uint64_t)Bn};
+    const uint64_t sx[3] = {(uint64_t)C * 2, (uint64_t)W * C * 2, (uint64_t)H * W * C * 2};
+    const uint32_t bx[4] = {32, (uint32_t)WB, (uint32_t)HB, 1};
+    if (int st = tma_map_bf16(&mx, x, 4, dx, sx, bx, 64)) return st;
+    const uint64_t dd[4] = {(uint64_t)N, (uint64_t)W, (uint64_t)H, (uint64_t)Bn};
+    const uint64_t sd[3] = {(uint64_t)N * 2, (uint64_t)W * N * 2, (uint64_t)H * W * N * 2};
+    if (int st = tma_map_bf16(&mdy, dym, 4, dd, sd, bx, 64)) return st;
+    const int rows = ks * ks * C, mtiles = (rows + 127) / 128;
+    const int nchunks = Bn * H * W / 64;
+    const int want = std::max(1, ctas_want / mtiles);
+    const int per = std::max(8, (nchunks + want - 1) / want);
+    const int nsplit = (nchunks + per - 1) / per;
+    auto kern = wgrad_mn_kernel<N>;
+    static const cudaError_t attr = cudaFuncSetAttribute(
+        kern, cudaFuncAttributeMaxDynamicSharedMemorySize, WgMnSmem<N>::kBytes);
+    LENTILS_CUDA_TRY(attr);
+    kern<<<dim3(mtiles, nsplit), kWgMnThreads, WgMnSmem<N>::kBytes, s>>>(mx, mdy, g, C, ks, H, W,
+                                                                         rows, nchunks, per, err);
+    LENTILS_CHECK_LAUNCH("weight gradient gemm (MN-major operands)");
+    return LENTILS_OK;
+}
+
+// whether wgrad_mn_kernel takes a layer: 32-channel boxes, 64-pixel chunks inside an image
+static bool wgrad_mn_ok(int C, int N, int H, int W)
+{
+    return C % 32 == 0 && C <= 128 && (N == 32 || N == 64 || N == 128) && (H * W) % 64 == 0 &&
+           (W >= 64 ? W % 64 == 0 : (64 % W == 0 && H % (64 / W) == 0));
+}
+
 // the weight-gradient GEMM splits its pixel reduction so that about kWgradCtas CTAs run, each
 // over at least kWgradMinPieces pieces of 8 pixels
 constexpr int kWgradCtas = 1024;
@@ -1906,6 +2113,13 @@ static int fused_c1_out(lentils_unet *net, const bf16 *x, bf16 *y, float *out, f
                                        c.ks * c.ks * c.cin_p, ep, net->err, s);
 }
 
+// whether layer l's weight gradient runs on wgrad_mn_kernel (form 0, shapes it takes)
+static bool wgrad_mn_uses(const lentils_unet *net, int l)
+{
+    const ConvSpec &c = kLayers[l];
+    return net->gemm_form == 0 && wgrad_mn_ok(c.cin_p, c.cout_p, net->H >> c.level, net->W >> c.level);
+}
+
 // backward of layer l: dy (gradient of its output, before the ReLU mask), y (its output, for
 // the mask; null for the output layer), x (its input); accumulates gw/gb, writes dx (optional).
 // prepared: the masked gradient operands (dym, dyT) and the bias gradient have been written
@@ -1932,16 +2146,32 @@ static int layer_backward(lentils_unet *net, int l, const bf16 *dy, const bf16 *
         const int blocks = (npix + 63) / 64;
         // 64-pixel blocks (W a multiple of 64) keep a TMA box in one contiguous run
         const bool blocked = (W % 64) == 0;
+        // form 0: the weight gradient reads x and dym as they are (MN-major operands)
+        const bool mn = wgrad_mn_uses(net, l);
         if (!prepared) {
-            grad_prep_kernel<<<blocks, 256, 0, s>>>(dy, mask, net->dym, net->dyT, net->gb[l], npix,
-                                                    c.cout_p, c.cout, blocked ? 1 : 0);
+            grad_prep_kernel<<<blocks, 256, 0, s>>>(dy, mask, net->dym, mn ? nullptr : net->dyT,
+                                                    net->gb[l], npix, c.cout_p, c.cout,
+                                                    blocked ? 1 : 0);
             LENTILS_CHECK_LAUNCH("grad_prep_kernel");
+        }
+        int st = LENTILS_OK;
+        if (mn) {
+            const int ctas = net->wgrad_ctas > 0 ? net->wgrad_ctas : kWgradCtas;
+            switch (c.cout_p) {
+            case 32: st = wgrad_mn_launch<32>(x, net->dym, net->gw_pad[l], c.cin_p, c.ks, Bn, H, W, ctas, net->err, s); break;
+            case 64: st = wgrad_mn_launch<64>(x, net->dym, net->gw_pad[l], c.cin_p, c.ks, Bn, H, W, ctas, net->err, s); break;
+            case 128: st = wgrad_mn_launch<128>(x, net->dym, net->gw_pad[l], c.cin_p, c.ks, Bn, H, W, ctas, net->err, s); break;
+            default: return set_error(LENTILS_ERR_UNSUPPORTED, "weight gradient N=%d", c.cout_p);
+            }
+            if (st) return st;
         }
         const int nshift = c.ks == 3 ? 3 : 1;
         const long long qtot = (long long)(npix / (H * W)) * (H + 2) * W;
-        shift_transpose_kernel<<<blocks, 256, 0, s>>>(x, net->xT, npix, H, W, c.cin_p, nshift,
-                                                      qtot, blocked ? 1 : 0);
-        LENTILS_CHECK_LAUNCH("shift_transpose_kernel");
+        if (!mn) {
+            shift_transpose_kernel<<<blocks, 256, 0, s>>>(x, net->xT, npix, H, W, c.cin_p, nshift,
+                                                          qtot, blocked ? 1 : 0);
+            LENTILS_CHECK_LAUNCH("shift_transpose_kernel");
+        }
         // weight gradient: rows = taps * cin_p, columns = cout_p, K = pixels split over CTAs,
         // about kWgradCtas CTAs in all
         const int Kw = taps * c.cin_p;
@@ -1952,8 +2182,9 @@ static int layer_backward(lentils_unet *net, int l, const bf16 *dy, const bf16 *
         int per = (kpieces + want - 1) / want;
         per = std::max(kWgradMinPieces, (per + 7) / 8 * 8);  // whole chunks
         const int nz = (kpieces + per - 1) / per;
-        int st = LENTILS_OK;
-        if (blocked) {
+        if (mn) {
+            // done above
+        } else if (blocked) {
             ConvWgXTTmaBlk la;
             la.C = c.cin_p;
             la.ks = c.ks;
@@ -2161,7 +2392,8 @@ static int net_backward(lentils_unet *net, const float *tgt, const float *dout, 
     if (net->gemm_form == 0 && kLayers[6].cout_p == 32 && (W % 8) == 0) {
         // the output layer's whole backward pass in c1's gradient preparation
         out_grad_prep_kernel<<<(int)((np0 + 63) / 64), 256, 0, s>>>(
-            net->dy_out, net->wf[7], net->c1, net->dym, net->dyT, net->gb[6], net->gw_pad[7],
+            net->dy_out, net->wf[7], net->c1, net->dym, wgrad_mn_uses(net, 6) ? nullptr : net->dyT,
+            net->gb[6], net->gw_pad[7],
             net->gb[7], (int)np0, (W % 64) == 0 ? 1 : 0);
         LENTILS_CHECK_LAUNCH("out_grad_prep_kernel");
         if ((st = layer_backward(net, 6, nullptr, net->c1, net->u1, net->d_u1, Bn, s, true))) return st;
