@@ -550,6 +550,8 @@ struct RowActOut {
 // chunks on 2-8 CTAs) into a few chunks on many CTAs. The number of splits is at most
 // max(2, 128 / row tiles), so the slabs hold at most kSplitSlabPix pixels x 128 channels.
 constexpr int kSplitMaxPix = 64 * 128;
+// at most this many splits: each adds an FP32 slab that the finalize kernel reads
+constexpr int kSplitMax = 8;
 constexpr int kSplitSlabPix = 2 * kSplitMaxPix;
 
 // -- elementwise kernels ----------------------------------------------------------------------------
@@ -1347,21 +1349,35 @@ __global__ void __launch_bounds__(1024)
     tc::pdl_wait();
     tc::pdl_trigger();
     __shared__ double sh[32];
-    double acc = 0.0;
-    for (int i = threadIdx.x; i < n; i += blockDim.x) {
-        const double u = (double)dinv[i] * (double)r[i];
-        acc += u * u;
+    __shared__ float shm[32];
+    // FP64 arithmetic is slow on this part: the sum of squares is taken in FP32 on values scaled
+    // by the largest |u| (no overflow or underflow of the squares that matter), FP64 across
+    // threads
+    float m = 0.f;
+    for (int i = threadIdx.x; i < n; i += blockDim.x) m = fmaxf(m, fabsf(dinv[i] * r[i]));
+    for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+    if ((threadIdx.x & 31) == 0) shm[threadIdx.x >> 5] = m;
+    __syncthreads();
+    m = 0.f;
+    for (int i = 0; i < (int)(blockDim.x >> 5); ++i) m = fmaxf(m, shm[i]);
+    if (!(m > 0.f) || !(m < INFINITY)) {  // zero, NaN or infinite
+        if (threadIdx.x == 0) scale[0] = 1.f;
+        return;
     }
+    const float inv = 1.f / m;
+    float part = 0.f;
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+        const float u = dinv[i] * r[i] * inv;
+        part = fmaf(u, u, part);
+    }
+    double acc = part;
     for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
     if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = acc;
     __syncthreads();
     if (threadIdx.x < 32) {
         double t = (threadIdx.x < (blockDim.x >> 5)) ? sh[threadIdx.x] : 0.0;
         for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
-        if (threadIdx.x == 0) {
-            const double rms = sqrt(t / (double)n);
-            scale[0] = (rms > 0.0 && rms < 1e300) ? (float)rms : 1.f;
-        }
+        if (threadIdx.x == 0) scale[0] = (float)((double)m * sqrt(t / (double)n));
     }
 }
 
@@ -2050,7 +2066,7 @@ static int layer_forward(lentils_unet *net, int l, const bf16 *x, void *y, int B
     }
     const int mtiles = (npix + 127) / 128;
     const int kp = (K + 7) / 8, nchunks = (kp + 7) / 8;
-    const int split = std::min(nchunks, std::max(2, 128 / mtiles));
+    const int split = std::min(nchunks, std::max(2, std::min(kSplitMax, 128 / mtiles)));
     const int per = ((nchunks + split - 1) / split) * 8;  // pieces per split (whole chunks)
     const int nz = (kp + per - 1) / per;
     const long long n = (long long)npix * c.cout_p;
