@@ -950,6 +950,8 @@ def run_unet_bench(steps=20, warmup=3):
            "forward_b1_ms": timed(lambda: net.forward(x[:1], f[:1]), steps),
            "forward_b32_ms": timed(lambda: net.forward(x, f), steps),
            "train_step_b32_ms": timed(lambda: net.train_step(x, f, t, 0.0), max(3, steps // 2)),
+           "forward_b32_graph_ms": graphed(lambda: net.forward(x, f), steps),
+           "train_step_b32_graph_ms": graphed(lambda: net.train_step(x, f, t, 0.0), max(3, steps // 2)),
            "precondition_ms": timed(lambda: net.precondition(r, d, ft), steps),
            "precondition_graph_ms": graphed(lambda: net.precondition(r, d, ft), steps),
            "forward_b32_gflop": fwd_flop / 1e9}

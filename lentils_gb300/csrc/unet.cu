@@ -930,11 +930,38 @@ __global__ void up2add_kernel(const bf16 *__restrict__ low, const bf16 *__restri
 }
 
 // dlow (n, H/2, W/2, C) = sum of the 2 x 2 children of dy (gradient of up2)
-__global__ void sum4_kernel(const bf16 *__restrict__ dy, bf16 *__restrict__ dlow, int Bn, int H,
-                            int W, int C)
+// With y set, the result is also masked by y > 0 (the ReLU of the layer whose output gradient
+// it is: grad_prep_kernel's dym) and db[c] += its sum over pixels (that layer's bias gradient).
+// The grid-stride step is a multiple of C / 8, so a thread keeps its 8 channels.
+__device__ __forceinline__ void mask8(float (&v)[8], const bf16 *y)
 {
+    float t[8];
+    bf8_load(y, t);
+#pragma unroll
+    for (int i = 0; i < 8; ++i) v[i] = t[i] > 0.f ? bf(__float2bfloat16(v[i])) : 0.f;
+}
+
+__device__ __forceinline__ void db_flush(const float (&acc)[8], int c, int C, float *sdb,
+                                         float *__restrict__ db)
+{
+#pragma unroll
+    for (int i = 0; i < 8; ++i) atomicAdd(&sdb[c + i], acc[i]);
+    __syncthreads();
+    for (int i = threadIdx.x; i < C; i += blockDim.x) atomicAdd(&db[i], sdb[i]);
+}
+
+__global__ void sum4_kernel(const bf16 *__restrict__ dy, bf16 *__restrict__ dlow, int Bn, int H,
+                            int W, int C, const bf16 *__restrict__ y, float *__restrict__ db)
+{
+    __shared__ float sdb[128];
     const int h2 = H / 2, w2 = W / 2, cv = C / 8;
     const long long n = (long long)Bn * h2 * w2 * cv;
+    if (db) {
+        for (int i = threadIdx.x; i < C; i += blockDim.x) sdb[i] = 0.f;
+        __syncthreads();
+    }
+    float acc[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+    const int cthr = (int)((blockIdx.x * (long long)blockDim.x + threadIdx.x) % cv) * 8;
     LENTILS_GRID_STRIDE(e, n)
     {
         const int c = (int)(e % cv) * 8;
@@ -955,16 +982,31 @@ __global__ void sum4_kernel(const bf16 *__restrict__ dy, bf16 *__restrict__ dlow
         bf8_load(dy + base + (size_t)W * C + C, t);
 #pragma unroll
         for (int i = 0; i < 8; ++i) a[i] += t[i];
+        if (y) {
+            mask8(a, y + q * C + c);
+#pragma unroll
+            for (int i = 0; i < 8; ++i) acc[i] += a[i];
+        }
         bf8_store(dlow + q * C + c, a);
     }
+    if (db) db_flush(acc, cthr, C, sdb, db);
 }
 
 // d (n, H, W, C) = a + 0.25 * up2(dp) (gradient through pool2 added to another gradient)
+// (y, db: masked, with the bias gradient, as sum4_kernel)
 __global__ void add_pool_grad_kernel(const bf16 *__restrict__ a, const bf16 *__restrict__ dp,
-                                     bf16 *__restrict__ d, int Bn, int H, int W, int C)
+                                     bf16 *__restrict__ d, int Bn, int H, int W, int C,
+                                     const bf16 *__restrict__ y, float *__restrict__ db)
 {
+    __shared__ float sdb[128];
     const int cv = C / 8;
     const long long n = (long long)Bn * H * W * cv;
+    if (db) {
+        for (int i = threadIdx.x; i < C; i += blockDim.x) sdb[i] = 0.f;
+        __syncthreads();
+    }
+    float acc[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+    const int cthr = (int)((blockIdx.x * (long long)blockDim.x + threadIdx.x) % cv) * 8;
     LENTILS_GRID_STRIDE(e, n)
     {
         const int c = (int)(e % cv) * 8;
@@ -978,8 +1020,14 @@ __global__ void add_pool_grad_kernel(const bf16 *__restrict__ a, const bf16 *__r
         bf8_load(dp + ((size_t)(b * (H / 2) + h / 2) * (W / 2) + w / 2) * C + c, t);
 #pragma unroll
         for (int i = 0; i < 8; ++i) v[i] += 0.25f * t[i];
+        if (y) {
+            mask8(v, y + q * C + c);
+#pragma unroll
+            for (int i = 0; i < 8; ++i) acc[i] += v[i];
+        }
         bf8_store(d + q * C + c, v);
     }
+    if (db) db_flush(acc, cthr, C, sdb, db);
 }
 
 // loss = mean((out - tgt)^2); dy[pixel][0..31] = (2/npix (out - tgt), 0, ...)
@@ -1304,40 +1352,59 @@ __global__ void adam_kernel(float *__restrict__ w, const float *__restrict__ g,
     }
 }
 
-// BF16 copies of one layer's weights: fwd[co][tap*cin_p + ci], bwd[ci][tap*cout_p + co]
-__global__ void refresh_weights_kernel(const float *__restrict__ w, bf16 *__restrict__ fwd,
-                                       bf16 *__restrict__ bwd, int cin, int cout, int cin_p,
-                                       int cout_p, int taps)
+// Every layer's weight refresh (after an Adam step) or gradient gather in one launch: the
+// layers' index spaces are concatenated (off[l] .. off[l + 1]).
+struct AllLayers {
+    const float *src[kNumLayers];
+    float *dst32[kNumLayers];
+    bf16 *fwd[kNumLayers], *bwd[kNumLayers];
+    int cin[kNumLayers], cout[kNumLayers], cin_p[kNumLayers], cout_p[kNumLayers], taps[kNumLayers];
+    long long off[kNumLayers + 1];
+};
+
+__device__ __forceinline__ int layer_of(const AllLayers &P, long long e)
 {
-    const long long n = (long long)cout_p * taps * cin_p;
-    LENTILS_GRID_STRIDE(e, n)
+    int l = 0;
+    while (l < kNumLayers - 1 && e >= P.off[l + 1]) ++l;
+    return l;
+}
+
+// BF16 copies of the FP32 weights src: fwd[co][tap cin_p + ci], bwd[ci][tap cout_p + co] (zero in
+// the padding); index space cout_p taps cin_p
+__global__ void refresh_all_kernel(const AllLayers P)
+{
+    LENTILS_GRID_STRIDE(e, P.off[kNumLayers])
     {
-        const int ci = (int)(e % cin_p);
-        long long r = e / cin_p;
-        const int t = (int)(r % taps);
-        const int co = (int)(r / taps);
+        const int l = layer_of(P, e);
+        const long long k = e - P.off[l];
+        const int cin_p = P.cin_p[l], taps = P.taps[l];
+        const int ci = (int)(k % cin_p);
+        const long long r = k / cin_p;
+        const int t = (int)(r % taps), co = (int)(r / taps);
         float v = 0.f;
-        if (co < cout && ci < cin) v = w[((size_t)co * taps + t) * cin + ci];
+        if (co < P.cout[l] && ci < P.cin[l]) v = P.src[l][((size_t)co * taps + t) * P.cin[l] + ci];
         const bf16 b = __float2bfloat16(v);
-        fwd[((size_t)co * taps + t) * cin_p + ci] = b;
-        bwd[((size_t)ci * taps + t) * cout_p + co] = b;
+        P.fwd[l][((size_t)co * taps + t) * cin_p + ci] = b;
+        P.bwd[l][((size_t)ci * taps + t) * P.cout_p[l] + co] = b;
     }
 }
 
-// gather padded FP32 weight gradients [cout_p][taps*cin_p] into the flat layout [cout][taps][cin]
-__global__ void gather_wgrad_kernel(const float *__restrict__ gp, float *__restrict__ g, int cin,
-                                    int cout, int cin_p, int taps)
+// the padded FP32 weight gradients src [cout_p][taps cin_p] gathered into the flat parameter
+// layout dst32 [cout][taps][cin]; index space cout taps cin
+__global__ void gather_all_kernel(const AllLayers P)
 {
-    const long long n = (long long)cout * taps * cin;
-    LENTILS_GRID_STRIDE(e, n)
+    LENTILS_GRID_STRIDE(e, P.off[kNumLayers])
     {
-        const int ci = (int)(e % cin);
-        long long r = e / cin;
-        const int t = (int)(r % taps);
-        const int co = (int)(r / taps);
-        g[e] = gp[(size_t)co * taps * cin_p + (size_t)t * cin_p + ci];
+        const int l = layer_of(P, e);
+        const long long k = e - P.off[l];
+        const int cin = P.cin[l], taps = P.taps[l];
+        const int ci = (int)(k % cin);
+        const long long r = k / cin;
+        const int t = (int)(r % taps), co = (int)(r / taps);
+        P.dst32[l][k] = P.src[l][(size_t)co * taps * P.cin_p[l] + (size_t)t * P.cin_p[l] + ci];
     }
 }
+
 
 // Preconditioner pieces (one sample of n = H * W values):
 //   u = dinv * r, s = rms(u) (1 where u = 0), x0 = (u / s, feat, 0...),
@@ -1965,6 +2032,236 @@ static int conv_persist(const bf16 *act, int C, int ks, int Bn, int H, int W, in
     return set_error(LENTILS_ERR_UNSUPPORTED, "conv_persist: C=%d N=%d", C, N);
 }
 
+// 3 x 3 convolution from 32 to 32 channels on a grid 128 pixels wide (c1's forward and data
+// gradient) with input-row reuse. A row tile is one image row; the implicit GEMM of the
+// persistent kernel loads each input row nine times (three taps in each of three output rows,
+// 64-byte box rows), and that L2 -> SM traffic bounds it. Here a CTA takes bands of kRowBand
+// consecutive output rows of one image; each input row of the band (kRowBand + 2 of them) is
+// loaded once, as three boxes shifted by -1, 0, +1 columns (the zero fill at the image edge is
+// the padding), into a ring of kRowSlots slots; the output tile of row h reads its nine A
+// operands from the slots of rows h - 1, h, h + 1, and the slot of row h - 1 is released (MMA
+// commit) after it. The 9 x 32 x 32 weights stay in shared memory. Accumulators double
+// buffered in TMEM and the row epilogues as in tc::gemm_tma_persist_kernel. flip: taps mirrored
+// (data gradient). Warps: 0-3 epilogue, lane 0 of 4 TMA, 5 TMEM + MMA.
+constexpr int kRowBand = 4;
+constexpr int kRowSlots = 6;
+struct RowsSmem {
+    static constexpr int kB = 9 * 2048, kVar = 8192, kSlot = 3 * kVar;
+    static constexpr int kBytes = kB + kRowSlots * kSlot + 1024;
+};
+
+template <class EP>
+__global__ void __launch_bounds__(tc::kPersistThreads, 1)
+    conv3_rows_kernel(const __grid_constant__ CUtensorMap ma, const __grid_constant__ CUtensorMap mb,
+                      const EP ep, int Bn, int H, int flip, int *err)
+{
+    constexpr int S = kRowSlots, R = kRowBand;
+    constexpr int kB = RowsSmem::kB, kVar = RowsSmem::kVar, kSlot = RowsSmem::kSlot;
+    constexpr uint32_t ncols = 64;
+    extern __shared__ __align__(1024) unsigned char smem_raw[];
+    __shared__ uint64_t bfull, sfull[S], sempty[S], tfull[2], tempty[2], mdone;
+    __shared__ uint32_t tmem_base;
+    __shared__ int abort_flag;
+    __shared__ float scratch[256];
+    unsigned char *smem = smem_raw + ((1024 - (tc::smem_u32(smem_raw) & 1023)) & 1023);
+    unsigned char *bres = smem, *slots = smem + kB;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int bpi = (H + R - 1) / R, nbands = Bn * bpi;
+
+    if (warp == 5) {
+        tc::tmem_alloc(&tmem_base, ncols);
+        tc::tmem_relinquish();
+    }
+    if (threadIdx.x == 0) {
+        tc::mbar_init(&bfull, 1);
+        for (int i = 0; i < S; ++i) {
+            tc::mbar_init(&sfull[i], 1);
+            tc::mbar_init(&sempty[i], 1);
+        }
+        for (int i = 0; i < 2; ++i) {
+            tc::mbar_init(&tfull[i], 1);
+            tc::mbar_init(&tempty[i], 4);
+        }
+        tc::mbar_init(&mdone, 1);
+        abort_flag = 0;
+        tc::fence_mbar_init();
+    }
+    if (threadIdx.x == 128) {
+        tc::prefetch_tensormap(&ma);
+        tc::prefetch_tensormap(&mb);
+    }
+    tc::pdl_wait();
+    if (warp < 4) ep.prepare(scratch, threadIdx.x);
+    tc::tc_fence_before();
+    __syncthreads();
+    tc::tc_fence_after();
+    tc::pdl_trigger();
+    const uint32_t tmem = tmem_base;
+
+    if (warp == 4) {
+        if (lane == 0) {  // the TMA producer: the weights once, then each band's input rows
+            tc::mbar_arrive_expect_tx(&bfull, 9 * 2048);
+            for (int t = 0; t < 9; ++t) tc::tma_load_2d(bres + t * 2048, &mb, t * 32, 0, &bfull);
+            int L = 0;
+            bool ok = true;
+            for (int b = blockIdx.x; b < nbands && ok; b += gridDim.x) {
+                const int n = b / bpi, h0 = (b - n * bpi) * R, h1 = min(H, h0 + R);
+                for (int r = h0 - 1; r <= h1; ++r, ++L) {
+                    const int sl = L % S;
+                    if (L >= S && !tc::mbar_wait(&sempty[sl], ((L / S) - 1) & 1)) {
+                        atomicExch(&abort_flag, 1);
+                        ok = false;
+                        break;
+                    }
+                    unsigned char *dst = slots + sl * kSlot;
+                    tc::mbar_arrive_expect_tx(&sfull[sl], 3 * kVar);
+#pragma unroll
+                    for (int v = 0; v < 3; ++v) tc::tma_load_4d(dst + v * kVar, &ma, 0, v - 1, r, n, &sfull[sl]);
+                }
+            }
+            if (!tc::mbar_wait(&bfull, 0)) atomicExch(&abort_flag, 1);
+#pragma unroll 1
+            for (int i = 0; i < S; ++i) {
+                if (i >= L) continue;
+                const int last = i + ((L - 1 - i) / S) * S;
+                if (!tc::mbar_wait(&sfull[i], (last / S) & 1)) atomicExch(&abort_flag, 1);
+            }
+        }
+        __syncwarp();
+    } else if (warp == 5) {
+        if (lane == 0) {  // the MMA issuer
+            constexpr uint32_t idesc = tc::idesc_bf16_f32(128, 32);
+            bool ok = tc::mbar_wait(&bfull, 0);
+            tc::tc_fence_after();
+            int L = 0, j = 0;
+            for (int b = blockIdx.x; b < nbands && ok; b += gridDim.x) {
+                const int n = b / bpi, h0 = (b - n * bpi) * R, h1 = min(H, h0 + R);
+                (void)n;
+                const int nrows = h1 - h0 + 2;
+                int ready = 0;  // loads of this band known to have landed
+                for (int h = h0; h < h1 && ok; ++h, ++j) {
+                    const int buf = j & 1;
+                    if (j >= 2 && !tc::mbar_wait(&tempty[buf], ((j >> 1) - 1) & 1)) {
+                        ok = false;
+                        break;
+                    }
+                    while (ok && ready <= h - h0 + 2) {
+                        const int Lr = L + ready;
+                        ok = tc::mbar_wait(&sfull[Lr % S], (Lr / S) & 1);
+                        ++ready;
+                    }
+                    if (!ok) break;
+                    tc::tc_fence_after();
+                    const uint32_t acc = tmem + (uint32_t)(buf * 32);
+#pragma unroll
+                    for (int t = 0; t < 9; ++t) {
+                        int dh = t / 3 - 1, dw = t % 3 - 1;
+                        if (flip) {
+                            dh = -dh;
+                            dw = -dw;
+                        }
+                        const int Lr = L + (h + dh) - (h0 - 1);
+                        const uint32_t a = tc::smem_u32(slots + (Lr % S) * kSlot + (dw + 1) * kVar);
+                        const uint32_t bb = tc::smem_u32(bres + t * 2048);
+#pragma unroll
+                        for (int k = 0; k < 2; ++k)
+                            tc::mma_bf16(acc, tc::smem_desc_sw64(a + 32 * k), tc::smem_desc_sw64(bb + 32 * k),
+                                         idesc, (t > 0 || k > 0) ? 1u : 0u);
+                    }
+                    tc::mma_commit(&tfull[buf]);
+                    tc::mma_commit(&sempty[(L + h - h0) % S]);  // row h - 1: no later tile reads it
+                }
+                if (!ok) break;
+                tc::mma_commit(&sempty[(L + nrows - 2) % S]);
+                tc::mma_commit(&sempty[(L + nrows - 1) % S]);
+                L += nrows;
+            }
+            if (!ok) atomicExch(&abort_flag, 1);
+            tc::mma_commit(&mdone);
+            if (!tc::mbar_wait(&mdone, 0)) atomicExch(&abort_flag, 1);
+        }
+        __syncwarp();
+    } else {  // the epilogue warps
+        const uint32_t lane_base = (uint32_t)(warp * 32) << 16;
+        int j = 0;
+        bool go_on = true;
+        for (int b = blockIdx.x; b < nbands && go_on; b += gridDim.x) {
+            const int n = b / bpi, h0 = (b - n * bpi) * R, h1 = min(H, h0 + R);
+            for (int h = h0; h < h1; ++h, ++j) {
+                const int buf = j & 1;
+                int go = 0;
+                if (lane == 0)
+                    go = tc::mbar_wait(&tfull[buf], (j >> 1) & 1) && !*(volatile int *)&abort_flag;
+                go = __shfl_sync(0xffffffffu, go, 0);
+                if (!go) {
+                    if (lane == 0) atomicExch(&abort_flag, 1);
+                    go_on = false;
+                    break;
+                }
+                tc::tc_fence_after();
+                const int m = ((n * H + h) << 7) + warp * 32 + lane;
+                uint32_t r[32];
+                tc::tmem_ld32(tmem + lane_base + (uint32_t)(buf * 32), r);
+                tc::tmem_wait_ld();
+                tc::tc_fence_before();
+                __syncwarp();
+                if (lane == 0) tc::mbar_arrive(&tempty[buf]);
+                float v[32], acc = 0.f;
+#pragma unroll
+                for (int i = 0; i < 32; ++i) v[i] = __uint_as_float(r[i]);
+                ep.row(m, 0, v, acc, scratch);
+                ep.row_end(m, acc, scratch);
+            }
+        }
+    }
+    tc::tc_fence_before();
+    __syncthreads();
+    if (threadIdx.x == 0 && *(volatile int *)&abort_flag) atomicExch(err, 1);
+    if (warp == 5) tc::tmem_dealloc(tmem, ncols);
+}
+
+template <class EP>
+static const PersistShape &conv3_rows_shape()
+{
+    static const PersistShape shape = persist_shape(conv3_rows_kernel<EP>, RowsSmem::kBytes, 64);
+    return shape;
+}
+
+// c1's convolution (32 -> 32 channels, 3 x 3, W = 128) on conv3_rows_kernel: act NHWC BF16,
+// wt [32][288] BF16 (K = tap 32 + channel)
+template <class EP>
+static int conv3_rows_launch(const bf16 *act, int Bn, int H, int flip, const bf16 *wt, const EP &ep,
+                             int *err, cudaStream_t s)
+{
+    constexpr int W = 128, C = 32;
+    CUtensorMap ma, mb;
+    const uint64_t da[4] = {(uint64_t)C, (uint64_t)W, (uint64_t)H, (uint64_t)Bn};
+    const uint64_t sa[3] = {(uint64_t)C * 2, (uint64_t)W * C * 2, (uint64_t)H * W * C * 2};
+    const uint32_t ba[4] = {32, 128, 1, 1};
+    if (int st = tma_map_bf16(&ma, act, 4, da, sa, ba, 64)) return st;
+    const uint64_t db[2] = {288, 32};
+    const uint64_t sb[1] = {288 * 2};
+    const uint32_t bb[2] = {32, 32};
+    if (int st = tma_map_bf16(&mb, wt, 2, db, sb, bb, 64)) return st;
+    const PersistShape &shape = conv3_rows_shape<EP>();
+    LENTILS_CUDA_TRY(shape.err);
+    const int nbands = Bn * ((H + kRowBand - 1) / kRowBand);
+    const int grid = std::min(nbands, std::max(1, num_sms() * shape.per_sm));
+    LENTILS_CUDA_TRY(pdl_launch(conv3_rows_kernel<EP>, dim3(grid), dim3(tc::kPersistThreads),
+                                (size_t)RowsSmem::kBytes, s, ma, mb, ep, Bn, H, flip, err));
+    LENTILS_CHECK_LAUNCH("conv3_rows_kernel");
+    return LENTILS_OK;
+}
+
+// the band kernel for a convolution of Bn images of H x W: the shape it takes, and enough bands
+// (kRowBand rows each) to give every SM one; with fewer (batch 1) the persistent GEMM's
+// row tiles spread wider
+static bool conv3_rows_ok(int C, int N, int ks, int W, int Bn, int H)
+{
+    return C == 32 && N == 32 && ks == 3 && W == 128 &&
+           (long long)Bn * ((H + kRowBand - 1) / kRowBand) >= num_sms();
+}
+
 // whether a layer's convolution can take the TMA operands: row tiles of 128 pixels inside one
 // image, CB-channel chunks, N in {32, 64, 128}
 static bool conv_tma_ok(int C, int N, int H, int W)
@@ -2099,7 +2396,9 @@ static int layer_forward(lentils_unet *net, int l, const bf16 *x, void *y, int B
     int st;
     if (persist) {
         RowAct ep{(bf16 *)y, net->b32[l], npix, c.cout_p, c.relu};
-        st = conv_persist(x, c.cin_p, c.ks, Bn, H, W, 0, net->wf[l], c.cout_p, ep, net->err, s);
+        st = conv3_rows_ok(c.cin_p, c.cout_p, c.ks, W, Bn, H)
+                 ? conv3_rows_launch(x, Bn, H, 0, net->wf[l], ep, net->err, s)
+                 : conv_persist(x, c.cin_p, c.ks, Bn, H, W, 0, net->wf[l], c.cout_p, ep, net->err, s);
     } else {
         EpiAct ep{(bf16 *)y, net->b32[l], npix, c.cout_p, c.relu};
         st = tma ? conv_tma(x, c.cin_p, c.ks, Bn, H, W, 0, net->wf[l], c.cout_p, ep, 1, K / 8, net->err, s)
@@ -2125,6 +2424,8 @@ static int fused_c1_out(lentils_unet *net, const bf16 *x, bf16 *y, float *out, f
         return 1;
     RowActOut ep{y, net->b32[l], npix, net->wf[l + 1], net->b32[l + 1], out, z, r, dinv,
                  net->pscale, net->jacobi_weight};
+    if (conv3_rows_ok(c.cin_p, c.cout_p, c.ks, W, Bn, H))
+        return conv3_rows_launch(x, Bn, H, 0, net->wf[l], ep, net->err, s);
     return conv_persist_launch<32, 32>(x, c.cin_p, c.ks, Bn, H, W, 0, net->wf[l],
                                        c.ks * c.ks * c.cin_p, ep, net->err, s);
 }
@@ -2253,7 +2554,10 @@ static int layer_backward(lentils_unet *net, int l, const bf16 *dy, const bf16 *
         if (st) return st;
         if (dx && conv_tma_ok(c.cout_p, c.cin_p, H, W)) {  // data gradient, TMA operands
             int st2;
-            if (net->gemm_form == 0) {
+            if (net->gemm_form == 0 && conv3_rows_ok(c.cout_p, c.cin_p, c.ks, W, Bn, H)) {
+                st2 = conv3_rows_launch(net->dym, Bn, H, 1, net->wb[l], RowStore{dx, npix, c.cin_p},
+                                        net->err, s);
+            } else if (net->gemm_form == 0) {
                 st2 = conv_persist(net->dym, c.cout_p, c.ks, Bn, H, W, 1, net->wb[l], c.cin_p,
                                    RowStore{dx, npix, c.cin_p}, net->err, s);
             } else {
@@ -2386,6 +2690,23 @@ static int net_forward(lentils_unet *net, const float *r, const float *d, int Bn
     return net_forward_in(net, FwdIn{r, nullptr, nullptr, d, nullptr}, Bn, s);
 }
 
+// the per-layer shapes and BF16 weight copies of all layers (src, dst32 and off left to the caller)
+static AllLayers all_layers(const lentils_unet *net)
+{
+    AllLayers P{};
+    for (int l = 0; l < kNumLayers; ++l) {
+        const ConvSpec &c = kLayers[l];
+        P.fwd[l] = net->wf[l];
+        P.bwd[l] = net->wb[l];
+        P.cin[l] = c.cin;
+        P.cout[l] = c.cout;
+        P.cin_p[l] = c.cin_p;
+        P.cout_p[l] = c.cout_p;
+        P.taps[l] = c.ks * c.ks;
+    }
+    return P;
+}
+
 // parameter gradients (forward must have run for this batch): of the mean squared error
 // against tgt, or, with dout, for the given gradient of the output
 static int net_backward(lentils_unet *net, const float *tgt, const float *dout, int Bn,
@@ -2417,19 +2738,38 @@ static int net_backward(lentils_unet *net, const float *tgt, const float *dout, 
         if ((st = layer_backward(net, 7, net->dy_out, nullptr, net->c1, net->d_c1, Bn, s))) return st;
         if ((st = layer_backward(net, 6, net->d_c1, net->c1, net->u1, net->d_u1, Bn, s))) return st;
     }
+    // The gradient of each hidden layer's output comes from the adjoint of the upsampling (sum4)
+    // or of the pooling plus the skip (add_pool_grad); where the layer's weight gradient takes
+    // the MN-major form, that kernel also applies the layer's ReLU mask and sums its bias
+    // gradient, writing the operand (dym) that layer_backward then uses as prepared.
+    auto adj_sum4 = [&](int l, const bf16 *dhi, bf16 *dlow, const bf16 *y, int h, int w, int C) {
+        const bool mn = wgrad_mn_uses(net, l);
+        sum4_kernel<<<blocks_n((long long)Bn * h / 2 * (w / 2) * C / 8), 256, 0, s>>>(
+            dhi, mn ? net->dym : dlow, Bn, h, w, C, mn ? y : nullptr, mn ? net->gb[l] : nullptr);
+        return mn;
+    };
+    auto adj_pool = [&](int l, const bf16 *a, const bf16 *dp, bf16 *d, const bf16 *y, int h, int w,
+                        int C) {
+        const bool mn = wgrad_mn_uses(net, l);
+        add_pool_grad_kernel<<<blocks_n((long long)Bn * h * w * C / 8), 256, 0, s>>>(
+            a, dp, mn ? net->dym : d, Bn, h, w, C, mn ? y : nullptr, mn ? net->gb[l] : nullptr);
+        return mn;
+    };
+    bool prep;
     // u1 = up2(c2) + e1
-    sum4_kernel<<<blocks_n(np0 / 4 * 32), 256, 0, s>>>(net->d_u1, net->d_c2, Bn, H, W, 32);
-    if ((st = layer_backward(net, 5, net->d_c2, net->c2, net->u2, net->d_u2, Bn, s))) return st;
-    sum4_kernel<<<blocks_n(np0 / 16 * 64), 256, 0, s>>>(net->d_u2, net->d_c3, Bn, H / 2, W / 2, 64);
-    if ((st = layer_backward(net, 4, net->d_c3, net->c3, net->u3, net->d_u3, Bn, s))) return st;
-    sum4_kernel<<<blocks_n(np0 / 64 * 128), 256, 0, s>>>(net->d_u3, net->d_b, Bn, H / 4, W / 4, 128);
-    if ((st = layer_backward(net, 3, net->d_b, net->b, net->p3, net->d_p3, Bn, s))) return st;
+    prep = adj_sum4(5, net->d_u1, net->d_c2, net->c2, H, W, 32);
+    if ((st = layer_backward(net, 5, net->d_c2, net->c2, net->u2, net->d_u2, Bn, s, prep))) return st;
+    prep = adj_sum4(4, net->d_u2, net->d_c3, net->c3, H / 2, W / 2, 64);
+    if ((st = layer_backward(net, 4, net->d_c3, net->c3, net->u3, net->d_u3, Bn, s, prep))) return st;
+    prep = adj_sum4(3, net->d_u3, net->d_b, net->b, H / 4, W / 4, 128);
+    if ((st = layer_backward(net, 3, net->d_b, net->b, net->p3, net->d_p3, Bn, s, prep))) return st;
     // e3 feeds u3 (skip) and p3 (pool)
-    add_pool_grad_kernel<<<blocks_n(np0 / 16 * 128), 256, 0, s>>>(net->d_u3, net->d_p3, net->d_e3, Bn, H / 4, W / 4, 128);
-    if ((st = layer_backward(net, 2, net->d_e3, net->e3, net->p2, net->d_p2, Bn, s))) return st;
-    add_pool_grad_kernel<<<blocks_n(np0 / 4 * 64), 256, 0, s>>>(net->d_u2, net->d_p2, net->d_e2, Bn, H / 2, W / 2, 64);
-    if ((st = layer_backward(net, 1, net->d_e2, net->e2, net->p1, net->d_p1, Bn, s))) return st;
-    add_pool_grad_kernel<<<blocks_n(np0 * 32), 256, 0, s>>>(net->d_u1, net->d_p1, net->d_e1, Bn, H, W, 32);
+    prep = adj_pool(2, net->d_u3, net->d_p3, net->d_e3, net->e3, H / 4, W / 4, 128);
+    if ((st = layer_backward(net, 2, net->d_e3, net->e3, net->p2, net->d_p2, Bn, s, prep))) return st;
+    prep = adj_pool(1, net->d_u2, net->d_p2, net->d_e2, net->e2, H / 2, W / 2, 64);
+    if ((st = layer_backward(net, 1, net->d_e2, net->e2, net->p1, net->d_p1, Bn, s, prep))) return st;
+    add_pool_grad_kernel<<<blocks_n(np0 * 32), 256, 0, s>>>(net->d_u1, net->d_p1, net->d_e1, Bn, H, W, 32,
+                                                            nullptr, nullptr);
     if (net->gemm_form == 0 && W % kE1Run == 0) {
         const long long items = np0 / kE1Run / 16;  // block iterations of 16 runs
         const int blocks = (int)std::max(1LL, std::min(items, 152LL * 4));
@@ -2439,10 +2779,15 @@ static int net_backward(lentils_unet *net, const float *tgt, const float *dout, 
     } else if ((st = layer_backward(net, 0, net->d_e1, net->e1, net->x0, nullptr, Bn, s))) {
         return st;
     }
-    for (int l = 0; l < kNumLayers; ++l) {
-        const ConvSpec &c = kLayers[l];
-        gather_wgrad_kernel<<<blocks_n(layer_wcount(l)), 256, 0, s>>>(
-            net->gw_pad[l], net->gw[l], c.cin, c.cout, c.cin_p, c.ks * c.ks);
+    {
+        AllLayers P = all_layers(net);
+        P.off[0] = 0;
+        for (int l = 0; l < kNumLayers; ++l) {
+            P.src[l] = net->gw_pad[l];
+            P.dst32[l] = net->gw[l];
+            P.off[l + 1] = P.off[l] + layer_wcount(l);
+        }
+        gather_all_kernel<<<blocks_n(P.off[kNumLayers]), 256, 0, s>>>(P);
     }
     LENTILS_CHECK_LAUNCH("unet backward");
     return LENTILS_OK;
@@ -2450,12 +2795,15 @@ static int net_backward(lentils_unet *net, const float *tgt, const float *dout, 
 
 static int refresh_all(lentils_unet *net, cudaStream_t s)
 {
+    AllLayers P = all_layers(net);
+    P.off[0] = 0;
     for (int l = 0; l < kNumLayers; ++l) {
         const ConvSpec &c = kLayers[l];
-        refresh_weights_kernel<<<blocks_n((long long)c.cout_p * c.ks * c.ks * c.cin_p), 256, 0, s>>>(
-            net->w32[l], net->wf[l], net->wb[l], c.cin, c.cout, c.cin_p, c.cout_p, c.ks * c.ks);
+        P.src[l] = net->w32[l];
+        P.off[l + 1] = P.off[l] + (long long)c.cout_p * c.ks * c.ks * c.cin_p;
     }
-    LENTILS_CHECK_LAUNCH("refresh_weights_kernel");
+    refresh_all_kernel<<<blocks_n(P.off[kNumLayers]), 256, 0, s>>>(P);
+    LENTILS_CHECK_LAUNCH("refresh_all_kernel");
     return LENTILS_OK;
 }
 
@@ -2477,6 +2825,8 @@ static int prepare_forward()
     LENTILS_CUDA_TRY((conv_persist_shape<64, 64, RowAct>().err));
     LENTILS_CUDA_TRY((conv_persist_shape<64, 128, RowAct>().err));
     LENTILS_CUDA_TRY((conv_persist_shape<32, 32, RowActOut>().err));
+    LENTILS_CUDA_TRY((conv3_rows_shape<RowAct>().err));
+    LENTILS_CUDA_TRY((conv3_rows_shape<RowActOut>().err));
     return num_sms() > 0 ? LENTILS_OK : set_error(LENTILS_ERR_CUDA, "SM count");
 }
 

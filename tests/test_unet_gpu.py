@@ -43,8 +43,10 @@ def _cuda(*a):
 
 # (1, 16, 16) ... (2, 32, 48) run every layer through the split-K form (FP32 partial slabs summed
 # in order), (3, 64, 64) the full-resolution layers through the unsplit form, (1, 128, 128) is
-# the 128 x 128 source at batch 1 as the solver applies it (deep layers split, top ones not).
-@pytest.mark.parametrize("B,H,W", [(1, 16, 16), (2, 32, 48), (3, 64, 64), (1, 128, 128)])
+# the 128 x 128 source at batch 1 as the solver applies it (deep layers split, top ones not),
+# (5, 128, 128) has enough 4-row bands for c1's band kernel.
+@pytest.mark.parametrize("B,H,W", [(1, 16, 16), (2, 32, 48), (3, 64, 64), (1, 128, 128),
+                                   (5, 128, 128)])
 def test_unet_forward_matches_oracle(native, B, H, W):
     from lentils_gb300 import learned
     p, x, f, _ = _problem(10 + H, B, H, W)
@@ -101,10 +103,11 @@ def test_unet_gemm_forms_agree(native):
     """The persistent TMA convolutions with the fused first and output layers (form 0), the
     per-tile TMA / pipelined GEMMs (form 2) and the staged ones (form 1) give the same forward
     output and gradients on the 128^2 grid, up to FP32 summation order and the BF16 rounding it
-    can flip."""
+    can flip. Batch 5 gives c1 160 bands of 4 rows, enough for its band kernel (forward and
+    data gradient)."""
     from lentils_gb300 import learned
-    p, x, f, t = _problem(77, 2, 128, 128)
-    net = learned.UNet(128, 128, max_batch=2, params=p)
+    p, x, f, t = _problem(77, 5, 128, 128)
+    net = learned.UNet(128, 128, max_batch=5, params=p)
     xc, fc, tc = _cuda(x, f, t)
     res = {}
     for form in (1, 2, 0):
@@ -114,7 +117,11 @@ def test_unet_gemm_forms_agree(native):
         res[form] = (out.cpu().numpy(), g, loss)
     assert net.error_flag() == 0
     for form in (0, 2):
-        assert _rel(res[form][0], res[1][0]) < 1e-3, form
+        # the first layer and the output layer sum in another order in form 0; a wrong tile or
+        # band would show as a local error of the output's size
+        assert _rel(res[form][0], res[1][0]) < 2e-3, form
+        err = np.max(np.abs(res[form][0] - res[1][0]))
+        assert err < 0.02 * np.max(np.abs(res[1][0])), (form, err)
         o = 0
         for li, (ci, co, k, _, _) in enumerate(learned.LAYERS):
             n = co * k * k * ci
