@@ -626,13 +626,13 @@ __device__ __forceinline__ void bf8_store(bf16 *p, const float (&v)[8])
 // First layer (2 -> 32 channels, 3 x 3, ReLU) on the CUDA cores, fused with the input packing
 // and the 2 x 2 pooling that follows it: a GEMM over K = 9 taps x 2 channels would leave the
 // tensor core and its operand staging mostly idle. One thread computes a 2 x 2 block of
-// output pixels, 16 channels at a time, from the 4 x 4 input patch around it:
+// output pixels, 8 channels at a time, from the 4 x 4 input patch around it:
 //   channel 0 = bf16(a * a2 * inv) (a2, inv optional: a2 = dinv and inv = 1 / scale for the
 //   preconditioner), channel 1 = bf16(b); x0 (optional) = the packed 8-channel input,
 //   y = bf16(relu(conv + bias)), yp = the 2 x 2 mean of y with pool2_kernel's arithmetic.
 // The products are exact in FP32; their sum is taken in tap order (the GEMM's order is the
 // tensor core's), so y can differ from the GEMM form by the BF16 rounding of an FP32 ulp.
-__global__ void __launch_bounds__(128)
+__global__ void __launch_bounds__(128, 5)
     e1_direct_kernel(const float *__restrict__ a, const float *__restrict__ a2,
                      const float *__restrict__ scale, const float *__restrict__ b,
                      const bf16 *__restrict__ wf, const float *__restrict__ bias,
@@ -697,21 +697,21 @@ __global__ void __launch_bounds__(128)
                 }
         }
 #pragma unroll 1
-        for (int half = half0; half < half1; ++half) {
-            float acc[4][16];
+        for (int g = 2 * half0; g < 2 * half1; ++g) {  // 8 channels at a time: 8 g .. 8 g + 7
+            float acc[4][8];
 #pragma unroll
             for (int k = 0; k < 4; ++k)
 #pragma unroll
-                for (int c = 0; c < 16; ++c) acc[k][c] = 0.f;
+                for (int c = 0; c < 8; ++c) acc[k][c] = 0.f;
 #pragma unroll
             for (int t = 0; t < 9; ++t) {
                 const int ky = t / 3, kx = t % 3;
 #pragma unroll
                 for (int ci = 0; ci < 2; ++ci) {
 #pragma unroll
-                    for (int c4 = 0; c4 < 4; ++c4) {
+                    for (int c4 = 0; c4 < 2; ++c4) {
                         const float4 wv =
-                            *reinterpret_cast<const float4 *>(&ws[t * 2 + ci][half * 16 + c4 * 4]);
+                            *reinterpret_cast<const float4 *>(&ws[t * 2 + ci][g * 8 + c4 * 4]);
 #pragma unroll
                         for (int py = 0; py < 2; ++py)
 #pragma unroll
@@ -727,34 +727,26 @@ __global__ void __launch_bounds__(128)
                     }
                 }
             }
-            float yv[4][16];
+            float ps[8];  // the pooling sum, in pool2_kernel's order ((y0 + y1) + y2) + y3
 #pragma unroll
             for (int k = 0; k < 4; ++k) {
                 const int py = k >> 1, px = k & 1;
-                uint4 u[2];
-                bf16 *ub = reinterpret_cast<bf16 *>(u);
+                uint4 u;
+                bf16 *ub = reinterpret_cast<bf16 *>(&u);
 #pragma unroll
-                for (int c = 0; c < 16; ++c) {
-                    const bf16 r = __float2bfloat16(fmaxf(acc[k][c] + bs[half * 16 + c], 0.f));
+                for (int c = 0; c < 8; ++c) {
+                    const bf16 r = __float2bfloat16(fmaxf(acc[k][c] + bs[g * 8 + c], 0.f));
                     ub[c] = r;
-                    yv[k][c] = bf(r);
+                    ps[c] = k == 0 ? bf(r) : ps[c] + bf(r);
                 }
                 const size_t p = img + (size_t)(h0 + py) * W + w0 + px;
-                uint4 *dst = reinterpret_cast<uint4 *>(y + p * 32 + half * 16);
-                dst[0] = u[0];
-                dst[1] = u[1];
+                *reinterpret_cast<uint4 *>(y + p * 32 + g * 8) = u;
             }
-            uint4 u[2];
-            bf16 *ub = reinterpret_cast<bf16 *>(u);
+            uint4 u;
+            bf16 *ub = reinterpret_cast<bf16 *>(&u);
 #pragma unroll
-            for (int c = 0; c < 16; ++c) {
-                float s = yv[0][c] + yv[1][c];
-                s += yv[2][c];
-                ub[c] = __float2bfloat16(0.25f * (s + yv[3][c]));
-            }
-            uint4 *dst = reinterpret_cast<uint4 *>(yp + ((size_t)n * h2 * w2 + (size_t)hh * w2 + ww) * 32 + half * 16);
-            dst[0] = u[0];
-            dst[1] = u[1];
+            for (int c = 0; c < 8; ++c) ub[c] = __float2bfloat16(0.25f * ps[c]);
+            *reinterpret_cast<uint4 *>(yp + ((size_t)n * h2 * w2 + (size_t)hh * w2 + ww) * 32 + g * 8) = u;
         }
     }
 }
@@ -1201,25 +1193,28 @@ __global__ void __launch_bounds__(256)
 // m = dy masked by y > 0 (dy, y: (Bn, H, W, 32) BF16), x0 the packed 8-channel input (channels
 // 0 and 1), gw in the padded [co][tap][8] layout, taps t = (dh + 1) 3 + dw + 1. A GEMM over
 // K = pixels would leave the tensor core idle behind transposed copies of dy and x0. A thread
-// owns two output channels and walks runs of kE1Run pixels along a row with the 3 x 3 x 2 input
-// window in registers (3 new input pairs per pixel); each block sums its threads in shared
-// memory and adds to gw / gb atomically. W is a multiple of kE1Run.
+// owns four output channels (72 products per pixel from one 8-byte gradient load and three new
+// input pairs) and walks runs of kE1Run pixels along a row with the 3 x 3 x 2 input window in
+// registers; the four threads of a warp that share a channel quad are summed by shuffles, the
+// warps in shared memory, and each block adds to gw / gb atomically. W is a multiple of kE1Run.
 constexpr int kE1Run = 16;
-__global__ void __launch_bounds__(256)
+__global__ void __launch_bounds__(256, 2)
     e1_wgrad_kernel(const bf16 *__restrict__ dy, const bf16 *__restrict__ y,
                     const bf16 *__restrict__ x0, float *__restrict__ gw, float *__restrict__ gb,
                     int Bn, int H, int W)
 {
-    __shared__ float red[16][16][38];  // [run slot][channel pair][2 x 18 taps, 2 biases]
-    const int cp = threadIdx.x & 15, slot = threadIdx.x >> 4;
-    float acc[2][18], accb[2] = {0.f, 0.f};
+    __shared__ float red[8][8][76];  // [warp][channel quad][4 x 18 taps, 4 biases]
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int cq = lane & 7;                      // channels 4 cq .. 4 cq + 3
+    const int slot = warp * 4 + (lane >> 3);      // 32 runs per block iteration
+    float acc[4][18], accb[4] = {0.f, 0.f, 0.f, 0.f};
 #pragma unroll
-    for (int q = 0; q < 2; ++q)
+    for (int q = 0; q < 4; ++q)
 #pragma unroll
         for (int k = 0; k < 18; ++k) acc[q][k] = 0.f;
     const int wr = W / kE1Run;
     const long long nruns = (long long)Bn * H * wr;
-    for (long long run = (long long)blockIdx.x * 16 + slot; run < nruns; run += (long long)gridDim.x * 16) {
+    for (long long run = (long long)blockIdx.x * 32 + slot; run < nruns; run += (long long)gridDim.x * 32) {
         const int w0 = (int)(run % wr) * kE1Run;
         const long long rh = run / wr;
         const int h = (int)(rh % H), n = (int)(rh / H);
@@ -1238,18 +1233,22 @@ __global__ void __launch_bounds__(256)
             ld(h - 1 + dh, w0 - 1, xw[dh][0]);
             ld(h - 1 + dh, w0, xw[dh][1]);
         }
-        const size_t o0 = ((size_t)(n * H + h) * W + w0) * 32 + 2 * cp;
-#pragma unroll
+        const size_t o0 = ((size_t)(n * H + h) * W + w0) * 32 + 4 * cq;
+#pragma unroll 2
         for (int k = 0; k < kE1Run; ++k) {
             const int w = w0 + k;
 #pragma unroll
             for (int dh = 0; dh < 3; ++dh) ld(h - 1 + dh, w + 1, xw[dh][2]);
-            const __nv_bfloat162 d = *reinterpret_cast<const __nv_bfloat162 *>(dy + o0 + k * 32);
-            const __nv_bfloat162 yy = *reinterpret_cast<const __nv_bfloat162 *>(y + o0 + k * 32);
-            const float m0 = __low2float(yy) > 0.f ? __low2float(d) : 0.f;
-            const float m1 = __high2float(yy) > 0.f ? __high2float(d) : 0.f;
-            accb[0] += m0;
-            accb[1] += m1;
+            const uint2 dd = *reinterpret_cast<const uint2 *>(dy + o0 + k * 32);
+            const uint2 yy = *reinterpret_cast<const uint2 *>(y + o0 + k * 32);
+            const bf16 *dv = reinterpret_cast<const bf16 *>(&dd);
+            const bf16 *yv = reinterpret_cast<const bf16 *>(&yy);
+            float m[4];
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                m[q] = bf(yv[q]) > 0.f ? bf(dv[q]) : 0.f;
+                accb[q] += m[q];
+            }
 #pragma unroll
             for (int dh = 0; dh < 3; ++dh)
 #pragma unroll
@@ -1257,8 +1256,8 @@ __global__ void __launch_bounds__(256)
 #pragma unroll
                     for (int ci = 0; ci < 2; ++ci) {
                         const int t = (dh * 3 + dx) * 2 + ci;
-                        acc[0][t] = fmaf(m0, xw[dh][dx][ci], acc[0][t]);
-                        acc[1][t] = fmaf(m1, xw[dh][dx][ci], acc[1][t]);
+#pragma unroll
+                        for (int q = 0; q < 4; ++q) acc[q][t] = fmaf(m[q], xw[dh][dx][ci], acc[q][t]);
                     }
 #pragma unroll
             for (int dh = 0; dh < 3; ++dh) {
@@ -1270,23 +1269,32 @@ __global__ void __launch_bounds__(256)
             }
         }
     }
+    // lanes cq, cq + 8, cq + 16, cq + 24 hold the same channels
 #pragma unroll
-    for (int k = 0; k < 18; ++k) {
-        red[slot][cp][k] = acc[0][k];
-        red[slot][cp][18 + k] = acc[1][k];
+    for (int q = 0; q < 4; ++q) {
+#pragma unroll
+        for (int k = 0; k < 18; ++k) {
+            float v = acc[q][k];
+            v += __shfl_xor_sync(0xffffffffu, v, 8);
+            v += __shfl_xor_sync(0xffffffffu, v, 16);
+            if (lane < 8) red[warp][cq][q * 18 + k] = v;
+        }
+        float b = accb[q];
+        b += __shfl_xor_sync(0xffffffffu, b, 8);
+        b += __shfl_xor_sync(0xffffffffu, b, 16);
+        if (lane < 8) red[warp][cq][72 + q] = b;
     }
-    red[slot][cp][36] = accb[0];
-    red[slot][cp][37] = accb[1];
     __syncthreads();
-    for (int e = threadIdx.x; e < 16 * 38; e += blockDim.x) {
-        const int c = e / 38, k = e - c * 38;
+    for (int e = threadIdx.x; e < 8 * 76; e += blockDim.x) {
+        const int c = e / 76, k = e - c * 76;
         float t = 0.f;
-        for (int sl = 0; sl < 16; ++sl) t += red[sl][c][k];
-        if (k < 36) {
-            const int co = 2 * c + k / 18, tk = k % 18, tap = tk / 2, ci = tk % 2;
+#pragma unroll
+        for (int wv = 0; wv < 8; ++wv) t += red[wv][c][k];
+        if (k < 72) {
+            const int co = 4 * c + k / 18, tk = k % 18, tap = tk / 2, ci = tk % 2;
             atomicAdd(&gw[co * 72 + tap * 8 + ci], t);
         } else {
-            atomicAdd(&gb[2 * c + (k - 36)], t);
+            atomicAdd(&gb[4 * c + (k - 72)], t);
         }
     }
 }
@@ -2771,8 +2779,8 @@ static int net_backward(lentils_unet *net, const float *tgt, const float *dout, 
     add_pool_grad_kernel<<<blocks_n(np0 * 32), 256, 0, s>>>(net->d_u1, net->d_p1, net->d_e1, Bn, H, W, 32,
                                                             nullptr, nullptr);
     if (net->gemm_form == 0 && W % kE1Run == 0) {
-        const long long items = np0 / kE1Run / 16;  // block iterations of 16 runs
-        const int blocks = (int)std::max(1LL, std::min(items, 152LL * 4));
+        const long long items = np0 / kE1Run / 32;  // block iterations of 32 runs
+        const int blocks = (int)std::max(1LL, std::min(items, 152LL * 2));
         e1_wgrad_kernel<<<blocks, 256, 0, s>>>(net->d_e1, net->e1, net->x0, net->gw_pad[0],
                                                net->gb[0], Bn, H, W);
         LENTILS_CHECK_LAUNCH("e1_wgrad_kernel");
