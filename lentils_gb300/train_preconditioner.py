@@ -362,10 +362,31 @@ def main(argv=None):
                          "flexible-CG trajectories with the trained network in the loop")
     ap.add_argument("--refine-steps", type=int, default=3000)
     ap.add_argument("--refine-lr", type=float, default=3e-4)
+    ap.add_argument("--reevaluate", action="store_true",
+                    help="no training: measure the deployment policy of the weights in --out "
+                         "again (network period 1, 2, 4, 8 with gamma 0 on the workload "
+                         "inversion) and store it, keeping the previous evaluation")
     a = ap.parse_args(argv)
 
     def log(msg):
         print(msg, flush=True)
+
+    if a.reevaluate:
+        params, meta = load(a.out)
+        inv, _, _ = workloads.inversion()
+        pnet = learned.UNet(workloads.SRC, workloads.SRC, max_batch=1, params=params)
+        ev = evaluate(pnet, inv, repeats=3, gammas=(0.0,), windows=(8,), every=(1, 2, 4, 8))
+        if "evaluation" in meta:
+            meta.setdefault("evaluation_history", []).append(
+                {"evaluation": meta["evaluation"], "deploy": meta.get("deploy", {})})
+        meta["evaluation"] = ev
+        meta["deploy"] = ev["best"]
+        log(json.dumps({k: ev[k] for k in ("best", "iteration_ratio", "time_ratio")}))
+        log(json.dumps({k: (v["inner_total"], round(v["seconds"], 5)) for k, v in ev["learned"].items()}))
+        log(json.dumps({k: (v["inner_total"], round(v["seconds"], 5)) for k, v in ev["jacobi_fcg"].items()}))
+        save(a.out, params, meta)
+        log(f"saved {a.out}")
+        return 0
 
     from .operators import NUFFTOperator
     vs, ims, srcs, uvw, _ = workloads.geometry()
