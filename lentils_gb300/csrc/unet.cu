@@ -945,6 +945,8 @@ __device__ __forceinline__ void db_flush(const float (&acc)[8], int c, int C, fl
 __global__ void sum4_kernel(const bf16 *__restrict__ dy, bf16 *__restrict__ dlow, int Bn, int H,
                             int W, int C, const bf16 *__restrict__ y, float *__restrict__ db)
 {
+    tc::pdl_wait();
+    tc::pdl_trigger();
     __shared__ float sdb[128];
     const int h2 = H / 2, w2 = W / 2, cv = C / 8;
     const long long n = (long long)Bn * h2 * w2 * cv;
@@ -990,6 +992,8 @@ __global__ void add_pool_grad_kernel(const bf16 *__restrict__ a, const bf16 *__r
                                      bf16 *__restrict__ d, int Bn, int H, int W, int C,
                                      const bf16 *__restrict__ y, float *__restrict__ db)
 {
+    tc::pdl_wait();
+    tc::pdl_trigger();
     __shared__ float sdb[128];
     const int cv = C / 8;
     const long long n = (long long)Bn * H * W * cv;
@@ -1026,6 +1030,8 @@ __global__ void add_pool_grad_kernel(const bf16 *__restrict__ a, const bf16 *__r
 __global__ void mse_kernel(const float *__restrict__ out, const float *__restrict__ tgt,
                            bf16 *__restrict__ dy, long long npix, float *__restrict__ loss)
 {
+    tc::pdl_wait();
+    tc::pdl_trigger();
     __shared__ float sh[256];
     float acc = 0.f;
     const float scale = 2.f / (float)npix;
@@ -1053,6 +1059,8 @@ __global__ void mse_kernel(const float *__restrict__ out, const float *__restric
 __global__ void pack_dout_kernel(const float *__restrict__ dout, bf16 *__restrict__ dy,
                                  long long npix)
 {
+    tc::pdl_wait();
+    tc::pdl_trigger();
     LENTILS_GRID_STRIDE(p, npix)
     {
         bf16 v[8];
@@ -1091,6 +1099,8 @@ __global__ void __launch_bounds__(256)
                      bf16 *__restrict__ dym, bf16 *__restrict__ dyT, float *__restrict__ db,
                      int npix, int C, int creal, int blocked)
 {
+    tc::pdl_wait();
+    tc::pdl_trigger();
     __shared__ __align__(16) bf16 tile[64][136];
     const int p0 = blockIdx.x * 64;
     const int cv = C / 8;
@@ -1137,6 +1147,8 @@ __global__ void __launch_bounds__(256)
                          float *__restrict__ gw_out, float *__restrict__ gb_out, int npix,
                          int blocked)
 {
+    tc::pdl_wait();
+    tc::pdl_trigger();
     constexpr int C = 32;
     __shared__ __align__(16) bf16 tile[64][C + 8];
     __shared__ __align__(16) bf16 ytile[64][C + 8];
@@ -1203,6 +1215,8 @@ __global__ void __launch_bounds__(256, 2)
                     const bf16 *__restrict__ x0, float *__restrict__ gw, float *__restrict__ gb,
                     int Bn, int H, int W)
 {
+    tc::pdl_wait();
+    tc::pdl_trigger();
     __shared__ float red[8][8][76];  // [warp][channel quad][4 x 18 taps, 4 biases]
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int cq = lane & 7;                      // channels 4 cq .. 4 cq + 3
@@ -1349,6 +1363,8 @@ __global__ void adam_kernel(float *__restrict__ w, const float *__restrict__ g,
                             float *__restrict__ m, float *__restrict__ v, long long n, float lr,
                             float b1, float b2, float eps, float c1, float c2)
 {
+    tc::pdl_wait();
+    tc::pdl_trigger();
     LENTILS_GRID_STRIDE(i, n)
     {
         const float gi = g[i];
@@ -1357,6 +1373,24 @@ __global__ void adam_kernel(float *__restrict__ w, const float *__restrict__ g,
         m[i] = mi;
         v[i] = vi;
         w[i] -= lr * (mi / c1) / (sqrtf(vi / c2) + eps);
+    }
+}
+
+// Zeroes up to 16 FP32 buffers in one launch (the gradient accumulators of a backward pass)
+struct ZeroList {
+    float *p[16];
+    long long off[17];
+    int count;
+};
+__global__ void zero_kernel(const ZeroList L)
+{
+    tc::pdl_wait();
+    tc::pdl_trigger();
+    LENTILS_GRID_STRIDE(e, L.off[L.count])
+    {
+        int b = 0;
+        while (b < L.count - 1 && e >= L.off[b + 1]) ++b;
+        L.p[b][e - L.off[b]] = 0.f;
     }
 }
 
@@ -1381,6 +1415,8 @@ __device__ __forceinline__ int layer_of(const AllLayers &P, long long e)
 // the padding); index space cout_p taps cin_p
 __global__ void refresh_all_kernel(const AllLayers P)
 {
+    tc::pdl_wait();
+    tc::pdl_trigger();
     LENTILS_GRID_STRIDE(e, P.off[kNumLayers])
     {
         const int l = layer_of(P, e);
@@ -1401,6 +1437,8 @@ __global__ void refresh_all_kernel(const AllLayers P)
 // layout dst32 [cout][taps][cin]; index space cout taps cin
 __global__ void gather_all_kernel(const AllLayers P)
 {
+    tc::pdl_wait();
+    tc::pdl_trigger();
     LENTILS_GRID_STRIDE(e, P.off[kNumLayers])
     {
         const int l = layer_of(P, e);
@@ -1620,6 +1658,26 @@ static int conv_gemm_n(int N, const LA &la, const tc::RowMajorLoader &lb, const 
     return set_error(LENTILS_ERR_UNSUPPORTED, "conv gemm N=%d", N);
 }
 
+// Launches kern with programmatic stream serialization: it may start while the kernel before
+// it in the stream finishes, and waits for it (tc::pdl_wait) before touching its results. Used
+// for the kernels of the forward and backward passes, all of which call tc::pdl_wait first.
+template <class... KArgs, class... Args>
+static cudaError_t pdl_launch(void (*kern)(KArgs...), dim3 grid, dim3 block, size_t smem,
+                              cudaStream_t s, Args &&...args)
+{
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = grid;
+    cfg.blockDim = block;
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = s;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, kern, std::forward<Args>(args)...);
+}
+
 // Weight gradient of a convolution layer as a GEMM whose operands are both MN-major, read
 // straight from the pixel-major (NHWC) activations and gradients, with no transposed copies:
 //   D[(t, ci)][co] = sum_p x[p + off(t)][ci] dym[p][co],   rows (t, ci) = t C + ci,
@@ -1676,9 +1734,11 @@ __global__ void __launch_bounds__(kWgMnThreads, 1)
         tc::prefetch_tensormap(&mx);
         tc::prefetch_tensormap(&mdy);
     }
+    tc::pdl_wait();
     tc::tc_fence_before();
     __syncthreads();
     tc::tc_fence_after();
+    tc::pdl_trigger();
     const uint32_t tmem = tmem_base;
 
     if (warp == 4) {
@@ -1813,8 +1873,9 @@ static int wgrad_mn_launch(const bf16 *x, const bf16 *dym, float *g, int C, int 
     static const cudaError_t attr = cudaFuncSetAttribute(
         kern, cudaFuncAttributeMaxDynamicSharedMemorySize, WgMnSmem<N>::kBytes);
     LENTILS_CUDA_TRY(attr);
-    kern<<<dim3(mtiles, nsplit), kWgMnThreads, WgMnSmem<N>::kBytes, s>>>(mx, mdy, g, C, ks, H, W,
-                                                                         rows, nchunks, per, err);
+    LENTILS_CUDA_TRY(pdl_launch(kern, dim3(mtiles, nsplit), dim3(kWgMnThreads),
+                                (size_t)WgMnSmem<N>::kBytes, s, mx, mdy, g, C, ks, H, W, rows,
+                                nchunks, per, err));
     LENTILS_CHECK_LAUNCH("weight gradient gemm (MN-major operands)");
     return LENTILS_OK;
 }
@@ -1896,26 +1957,6 @@ static int conv_tma_launch(const bf16 *act, int C, int ks, int Bn, int H, int W,
                                 K / 8, kp_per_split, err));
     LENTILS_CHECK_LAUNCH("convolution gemm (TMA)");
     return LENTILS_OK;
-}
-
-// Launches kern with programmatic stream serialization: it may start while the kernel before
-// it in the stream finishes, and waits for it (tc::pdl_wait) before touching its results. Used
-// for the kernels of the forward pass, all of which call tc::pdl_wait first.
-template <class... KArgs, class... Args>
-static cudaError_t pdl_launch(void (*kern)(KArgs...), dim3 grid, dim3 block, size_t smem,
-                              cudaStream_t s, Args &&...args)
-{
-    cudaLaunchConfig_t cfg = {};
-    cfg.gridDim = grid;
-    cfg.blockDim = block;
-    cfg.dynamicSmemBytes = smem;
-    cfg.stream = s;
-    cudaLaunchAttribute attr[1];
-    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
-    attr[0].val.programmaticStreamSerializationAllowed = 1;
-    cfg.attrs = attr;
-    cfg.numAttrs = 1;
-    return cudaLaunchKernelEx(&cfg, kern, std::forward<Args>(args)...);
 }
 
 static int num_sms()
@@ -2722,24 +2763,35 @@ static int net_backward(lentils_unet *net, const float *tgt, const float *dout, 
 {
     const int H = net->H, W = net->W;
     const long long np0 = (long long)Bn * H * W;
-    LENTILS_CUDA_TRY(cudaMemsetAsync(net->grads, 0, sizeof(float) * net->nparams, s));
-    for (int l = 0; l < kNumLayers; ++l) {
-        const ConvSpec &c = kLayers[l];
-        LENTILS_CUDA_TRY(cudaMemsetAsync(net->gw_pad[l], 0,
-                                         sizeof(float) * c.cout_p * c.ks * c.ks * c.cin_p, s));
+    {
+        ZeroList Z{};
+        auto add = [&](float *p, long long n) {
+            Z.p[Z.count] = p;
+            Z.off[Z.count + 1] = Z.off[Z.count] + n;
+            ++Z.count;
+        };
+        add(net->grads, net->nparams);
+        for (int l = 0; l < kNumLayers; ++l) {
+            const ConvSpec &c = kLayers[l];
+            add(net->gw_pad[l], (long long)c.cout_p * c.ks * c.ks * c.cin_p);
+        }
+        add(net->loss, 1);
+        LENTILS_CUDA_TRY(pdl_launch(zero_kernel, dim3(blocks_n(Z.off[Z.count])), dim3(256), 0, s, Z));
     }
-    LENTILS_CUDA_TRY(cudaMemsetAsync(net->loss, 0, sizeof(float), s));
     if (dout)
-        pack_dout_kernel<<<blocks_n(np0), 256, 0, s>>>(dout, net->dy_out, np0);
+        LENTILS_CUDA_TRY(pdl_launch(pack_dout_kernel, dim3(blocks_n(np0)), dim3(256), 0, s, dout,
+                                    net->dy_out, np0));
     else
-        mse_kernel<<<blocks_n(np0), 256, 0, s>>>(net->out, tgt, net->dy_out, np0, net->loss);
+        LENTILS_CUDA_TRY(pdl_launch(mse_kernel, dim3(blocks_n(np0)), dim3(256), 0, s,
+                                    (const float *)net->out, tgt, net->dy_out, np0, net->loss));
     int st;
     if (net->gemm_form == 0 && kLayers[6].cout_p == 32 && (W % 8) == 0) {
         // the output layer's whole backward pass in c1's gradient preparation
-        out_grad_prep_kernel<<<(int)((np0 + 63) / 64), 256, 0, s>>>(
-            net->dy_out, net->wf[7], net->c1, net->dym, wgrad_mn_uses(net, 6) ? nullptr : net->dyT,
-            net->gb[6], net->gw_pad[7],
-            net->gb[7], (int)np0, (W % 64) == 0 ? 1 : 0);
+        LENTILS_CUDA_TRY(pdl_launch(
+            out_grad_prep_kernel, dim3((int)((np0 + 63) / 64)), dim3(256), 0, s,
+            (const bf16 *)net->dy_out, (const bf16 *)net->wf[7], (const bf16 *)net->c1, net->dym,
+            wgrad_mn_uses(net, 6) ? nullptr : net->dyT, net->gb[6], net->gw_pad[7], net->gb[7],
+            (int)np0, (W % 64) == 0 ? 1 : 0));
         LENTILS_CHECK_LAUNCH("out_grad_prep_kernel");
         if ((st = layer_backward(net, 6, nullptr, net->c1, net->u1, net->d_u1, Bn, s, true))) return st;
     } else {
@@ -2750,39 +2802,48 @@ static int net_backward(lentils_unet *net, const float *tgt, const float *dout, 
     // or of the pooling plus the skip (add_pool_grad); where the layer's weight gradient takes
     // the MN-major form, that kernel also applies the layer's ReLU mask and sums its bias
     // gradient, writing the operand (dym) that layer_backward then uses as prepared.
-    auto adj_sum4 = [&](int l, const bf16 *dhi, bf16 *dlow, const bf16 *y, int h, int w, int C) {
+    auto adj_sum4 = [&](int l, const bf16 *dhi, bf16 *dlow, const bf16 *y, int h, int w, int C) -> int {
         const bool mn = wgrad_mn_uses(net, l);
-        sum4_kernel<<<blocks_n((long long)Bn * h / 2 * (w / 2) * C / 8), 256, 0, s>>>(
-            dhi, mn ? net->dym : dlow, Bn, h, w, C, mn ? y : nullptr, mn ? net->gb[l] : nullptr);
-        return mn;
+        const cudaError_t e = pdl_launch(sum4_kernel, dim3(blocks_n((long long)Bn * h / 2 * (w / 2) * C / 8)),
+                                         dim3(256), 0, s, dhi, mn ? net->dym : dlow, Bn, h, w, C,
+                                         mn ? y : nullptr, mn ? net->gb[l] : nullptr);
+        return e == cudaSuccess ? (mn ? 1 : 0) : -1;
     };
     auto adj_pool = [&](int l, const bf16 *a, const bf16 *dp, bf16 *d, const bf16 *y, int h, int w,
-                        int C) {
+                        int C) -> int {
         const bool mn = wgrad_mn_uses(net, l);
-        add_pool_grad_kernel<<<blocks_n((long long)Bn * h * w * C / 8), 256, 0, s>>>(
-            a, dp, mn ? net->dym : d, Bn, h, w, C, mn ? y : nullptr, mn ? net->gb[l] : nullptr);
-        return mn;
+        const cudaError_t e = pdl_launch(add_pool_grad_kernel, dim3(blocks_n((long long)Bn * h * w * C / 8)),
+                                         dim3(256), 0, s, a, dp, mn ? net->dym : d, Bn, h, w, C,
+                                         mn ? y : nullptr, mn ? net->gb[l] : nullptr);
+        return e == cudaSuccess ? (mn ? 1 : 0) : -1;
     };
-    bool prep;
+    int prep;  // 1: dym prepared, 0: not, -1: the launch failed
     // u1 = up2(c2) + e1
     prep = adj_sum4(5, net->d_u1, net->d_c2, net->c2, H, W, 32);
-    if ((st = layer_backward(net, 5, net->d_c2, net->c2, net->u2, net->d_u2, Bn, s, prep))) return st;
+    if (prep < 0) return set_error(LENTILS_ERR_CUDA, "gradient adjoint launch");
+    if ((st = layer_backward(net, 5, net->d_c2, net->c2, net->u2, net->d_u2, Bn, s, prep == 1))) return st;
     prep = adj_sum4(4, net->d_u2, net->d_c3, net->c3, H / 2, W / 2, 64);
-    if ((st = layer_backward(net, 4, net->d_c3, net->c3, net->u3, net->d_u3, Bn, s, prep))) return st;
+    if (prep < 0) return set_error(LENTILS_ERR_CUDA, "gradient adjoint launch");
+    if ((st = layer_backward(net, 4, net->d_c3, net->c3, net->u3, net->d_u3, Bn, s, prep == 1))) return st;
     prep = adj_sum4(3, net->d_u3, net->d_b, net->b, H / 4, W / 4, 128);
-    if ((st = layer_backward(net, 3, net->d_b, net->b, net->p3, net->d_p3, Bn, s, prep))) return st;
+    if (prep < 0) return set_error(LENTILS_ERR_CUDA, "gradient adjoint launch");
+    if ((st = layer_backward(net, 3, net->d_b, net->b, net->p3, net->d_p3, Bn, s, prep == 1))) return st;
     // e3 feeds u3 (skip) and p3 (pool)
     prep = adj_pool(2, net->d_u3, net->d_p3, net->d_e3, net->e3, H / 4, W / 4, 128);
-    if ((st = layer_backward(net, 2, net->d_e3, net->e3, net->p2, net->d_p2, Bn, s, prep))) return st;
+    if (prep < 0) return set_error(LENTILS_ERR_CUDA, "gradient adjoint launch");
+    if ((st = layer_backward(net, 2, net->d_e3, net->e3, net->p2, net->d_p2, Bn, s, prep == 1))) return st;
     prep = adj_pool(1, net->d_u2, net->d_p2, net->d_e2, net->e2, H / 2, W / 2, 64);
-    if ((st = layer_backward(net, 1, net->d_e2, net->e2, net->p1, net->d_p1, Bn, s, prep))) return st;
-    add_pool_grad_kernel<<<blocks_n(np0 * 32), 256, 0, s>>>(net->d_u1, net->d_p1, net->d_e1, Bn, H, W, 32,
-                                                            nullptr, nullptr);
+    if (prep < 0) return set_error(LENTILS_ERR_CUDA, "gradient adjoint launch");
+    if ((st = layer_backward(net, 1, net->d_e2, net->e2, net->p1, net->d_p1, Bn, s, prep == 1))) return st;
+    LENTILS_CUDA_TRY(pdl_launch(add_pool_grad_kernel, dim3(blocks_n(np0 * 4)), dim3(256), 0, s,
+                                (const bf16 *)net->d_u1, (const bf16 *)net->d_p1, net->d_e1, Bn, H, W,
+                                32, (const bf16 *)nullptr, (float *)nullptr));
     if (net->gemm_form == 0 && W % kE1Run == 0) {
         const long long items = np0 / kE1Run / 32;  // block iterations of 32 runs
         const int blocks = (int)std::max(1LL, std::min(items, 152LL * 2));
-        e1_wgrad_kernel<<<blocks, 256, 0, s>>>(net->d_e1, net->e1, net->x0, net->gw_pad[0],
-                                               net->gb[0], Bn, H, W);
+        LENTILS_CUDA_TRY(pdl_launch(e1_wgrad_kernel, dim3(blocks), dim3(256), 0, s,
+                                    (const bf16 *)net->d_e1, (const bf16 *)net->e1,
+                                    (const bf16 *)net->x0, net->gw_pad[0], net->gb[0], Bn, H, W));
         LENTILS_CHECK_LAUNCH("e1_wgrad_kernel");
     } else if ((st = layer_backward(net, 0, net->d_e1, net->e1, net->x0, nullptr, Bn, s))) {
         return st;
@@ -2795,7 +2856,8 @@ static int net_backward(lentils_unet *net, const float *tgt, const float *dout, 
             P.dst32[l] = net->gw[l];
             P.off[l + 1] = P.off[l] + layer_wcount(l);
         }
-        gather_all_kernel<<<blocks_n(P.off[kNumLayers]), 256, 0, s>>>(P);
+        LENTILS_CUDA_TRY(pdl_launch(gather_all_kernel, dim3(blocks_n(P.off[kNumLayers])), dim3(256), 0,
+                                    s, P));
     }
     LENTILS_CHECK_LAUNCH("unet backward");
     return LENTILS_OK;
@@ -2810,7 +2872,7 @@ static int refresh_all(lentils_unet *net, cudaStream_t s)
         P.src[l] = net->w32[l];
         P.off[l + 1] = P.off[l] + (long long)c.cout_p * c.ks * c.ks * c.cin_p;
     }
-    refresh_all_kernel<<<blocks_n(P.off[kNumLayers]), 256, 0, s>>>(P);
+    LENTILS_CUDA_TRY(pdl_launch(refresh_all_kernel, dim3(blocks_n(P.off[kNumLayers])), dim3(256), 0, s, P));
     LENTILS_CHECK_LAUNCH("refresh_all_kernel");
     return LENTILS_OK;
 }
@@ -2862,9 +2924,9 @@ static int adam_update(lentils_unet *net, float lr, cudaStream_t s)
     net->step += 1;
     const float b1 = 0.9f, b2 = 0.999f;
     const float c1 = 1.f - powf(b1, (float)net->step), c2 = 1.f - powf(b2, (float)net->step);
-    adam_kernel<<<blocks_n(net->nparams), 256, 0, s>>>(net->params, net->grads, net->adam_m,
-                                                       net->adam_v, net->nparams, lr, b1, b2,
-                                                       1e-8f, c1, c2);
+    LENTILS_CUDA_TRY(pdl_launch(adam_kernel, dim3(blocks_n(net->nparams)), dim3(256), 0, s, net->params,
+                                (const float *)net->grads, net->adam_m, net->adam_v, net->nparams,
+                                lr, b1, b2, 1e-8f, c1, c2));
     LENTILS_CHECK_LAUNCH("adam_kernel");
     return refresh_all(net, s);
 }
