@@ -1027,8 +1027,25 @@ __global__ void add_pool_grad_kernel(const bf16 *__restrict__ a, const bf16 *__r
 }
 
 // loss = mean((out - tgt)^2); dy[pixel][0..31] = (2/npix (out - tgt), 0, ...)
+// compact: dy[pixel] = the gradient alone (the output layer's fused backward pass reads only
+// channel 0), else the 32-channel row the GEMM forms read
+__device__ __forceinline__ void store_out_grad(bf16 *dy, long long p, float g, int compact)
+{
+    if (compact) {
+        dy[p] = __float2bfloat16(g);
+        return;
+    }
+    bf16 v[8];
+    v[0] = __float2bfloat16(g);
+    for (int i = 1; i < 8; ++i) v[i] = __float2bfloat16(0.f);
+    uint4 *dst = reinterpret_cast<uint4 *>(dy + p * 32);
+    dst[0] = *reinterpret_cast<uint4 *>(v);
+    dst[1] = dst[2] = dst[3] = make_uint4(0, 0, 0, 0);
+}
+
 __global__ void mse_kernel(const float *__restrict__ out, const float *__restrict__ tgt,
-                           bf16 *__restrict__ dy, long long npix, float *__restrict__ loss)
+                           bf16 *__restrict__ dy, long long npix, float *__restrict__ loss,
+                           int compact)
 {
     tc::pdl_wait();
     tc::pdl_trigger();
@@ -1039,12 +1056,7 @@ __global__ void mse_kernel(const float *__restrict__ out, const float *__restric
     {
         const float e = out[p] - tgt[p];
         acc += e * e;
-        bf16 v[8];
-        v[0] = __float2bfloat16(scale * e);
-        for (int i = 1; i < 8; ++i) v[i] = __float2bfloat16(0.f);
-        uint4 *dst = reinterpret_cast<uint4 *>(dy + p * 32);
-        dst[0] = *reinterpret_cast<uint4 *>(v);
-        dst[1] = dst[2] = dst[3] = make_uint4(0, 0, 0, 0);
+        store_out_grad(dy, p, scale * e, compact);
     }
     sh[threadIdx.x] = acc;
     __syncthreads();
@@ -1055,21 +1067,14 @@ __global__ void mse_kernel(const float *__restrict__ out, const float *__restric
     if (threadIdx.x == 0) atomicAdd(loss, sh[0] / (float)npix);
 }
 
-// dy[pixel][0..31] = (dout[pixel], 0, ...): an external gradient of the output
+// dy[pixel][0..31] = (dout[pixel], 0, ...), or dy[pixel] = dout[pixel] (compact): an external
+// gradient of the output
 __global__ void pack_dout_kernel(const float *__restrict__ dout, bf16 *__restrict__ dy,
-                                 long long npix)
+                                 long long npix, int compact)
 {
     tc::pdl_wait();
     tc::pdl_trigger();
-    LENTILS_GRID_STRIDE(p, npix)
-    {
-        bf16 v[8];
-        v[0] = __float2bfloat16(dout[p]);
-        for (int i = 1; i < 8; ++i) v[i] = __float2bfloat16(0.f);
-        uint4 *dst = reinterpret_cast<uint4 *>(dy + p * 32);
-        dst[0] = *reinterpret_cast<uint4 *>(v);
-        dst[1] = dst[2] = dst[3] = make_uint4(0, 0, 0, 0);
-    }
+    LENTILS_GRID_STRIDE(p, npix) store_out_grad(dy, p, dout[p], compact);
 }
 
 // db[co] += sum_pixel dy'[pixel][co]
@@ -1137,6 +1142,7 @@ __global__ void __launch_bounds__(256)
 // the outer product dx[p][c] = bf16(g[p] wo[c]) of the output gradient g (channel 0 of dyo)
 // and its weights (exact in FP32, as the GEMM form gives it), and its weight and bias gradients
 // are gw_out[c] += sum_p g[p] x[p][c], gb_out += sum_p g[p], with x = y = c1, the layer's input.
+// dyo is the compact output gradient (one value per pixel).
 // dx is masked by c1's ReLU and written as grad_prep_kernel writes it (dym, dyT unless null,
 // db of c1).
 // 64 pixels per block of 256 threads.
@@ -1156,7 +1162,7 @@ __global__ void __launch_bounds__(256)
     const int p0 = blockIdx.x * 64;
     if (threadIdx.x < 64) {
         const int p = p0 + threadIdx.x;
-        g[threadIdx.x] = p < npix ? bf(dyo[(size_t)p * 32]) : 0.f;
+        g[threadIdx.x] = p < npix ? bf(dyo[p]) : 0.f;
     }
     __syncthreads();
     for (int e = threadIdx.x; e < 64 * (C / 8); e += blockDim.x) {
@@ -2778,14 +2784,17 @@ static int net_backward(lentils_unet *net, const float *tgt, const float *dout, 
         add(net->loss, 1);
         LENTILS_CUDA_TRY(pdl_launch(zero_kernel, dim3(blocks_n(Z.off[Z.count])), dim3(256), 0, s, Z));
     }
+    // the fused output-layer backward pass (form 0) reads a compact gradient
+    const bool fuse_out = net->gemm_form == 0 && kLayers[6].cout_p == 32 && (W % 8) == 0;
     if (dout)
         LENTILS_CUDA_TRY(pdl_launch(pack_dout_kernel, dim3(blocks_n(np0)), dim3(256), 0, s, dout,
-                                    net->dy_out, np0));
+                                    net->dy_out, np0, fuse_out ? 1 : 0));
     else
         LENTILS_CUDA_TRY(pdl_launch(mse_kernel, dim3(blocks_n(np0)), dim3(256), 0, s,
-                                    (const float *)net->out, tgt, net->dy_out, np0, net->loss));
+                                    (const float *)net->out, tgt, net->dy_out, np0, net->loss,
+                                    fuse_out ? 1 : 0));
     int st;
-    if (net->gemm_form == 0 && kLayers[6].cout_p == 32 && (W % 8) == 0) {
+    if (fuse_out) {
         // the output layer's whole backward pass in c1's gradient preparation
         LENTILS_CUDA_TRY(pdl_launch(
             out_grad_prep_kernel, dim3((int)((np0 + 63) / 64)), dim3(256), 0, s,
