@@ -1472,8 +1472,21 @@ __global__ void __launch_bounds__(1024)
     // FP64 arithmetic is slow on this part: the sum of squares is taken in FP32 on values scaled
     // by the largest |u| (no overflow or underflow of the squares that matter), FP64 across
     // threads
+    // 16-byte loads, four per array in flight per thread at 128^2, where the pointers allow
+    const bool vec = ((reinterpret_cast<uintptr_t>(r) | reinterpret_cast<uintptr_t>(dinv)) & 15) == 0 &&
+                     (n & 3) == 0;
+    const float4 *r4 = reinterpret_cast<const float4 *>(r);
+    const float4 *d4 = reinterpret_cast<const float4 *>(dinv);
     float m = 0.f;
-    for (int i = threadIdx.x; i < n; i += blockDim.x) m = fmaxf(m, fabsf(dinv[i] * r[i]));
+    if (vec) {
+#pragma unroll 4
+        for (int i = threadIdx.x; i < n / 4; i += blockDim.x) {
+            const float4 a = r4[i], b = d4[i];
+            m = fmaxf(fmaxf(m, fabsf(b.x * a.x)), fmaxf(fabsf(b.y * a.y), fmaxf(fabsf(b.z * a.z), fabsf(b.w * a.w))));
+        }
+    } else {
+        for (int i = threadIdx.x; i < n; i += blockDim.x) m = fmaxf(m, fabsf(dinv[i] * r[i]));
+    }
     for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
     if ((threadIdx.x & 31) == 0) shm[threadIdx.x >> 5] = m;
     __syncthreads();
@@ -1485,9 +1498,22 @@ __global__ void __launch_bounds__(1024)
     }
     const float inv = 1.f / m;
     float part = 0.f;
-    for (int i = threadIdx.x; i < n; i += blockDim.x) {
-        const float u = dinv[i] * r[i] * inv;
-        part = fmaf(u, u, part);
+    if (vec) {
+#pragma unroll 4
+        for (int i = threadIdx.x; i < n / 4; i += blockDim.x) {
+            const float4 a = r4[i], b = d4[i];
+            const float u0 = b.x * a.x * inv, u1 = b.y * a.y * inv, u2 = b.z * a.z * inv,
+                        u3 = b.w * a.w * inv;
+            part = fmaf(u0, u0, part);
+            part = fmaf(u1, u1, part);
+            part = fmaf(u2, u2, part);
+            part = fmaf(u3, u3, part);
+        }
+    } else {
+        for (int i = threadIdx.x; i < n; i += blockDim.x) {
+            const float u = dinv[i] * r[i] * inv;
+            part = fmaf(u, u, part);
+        }
     }
     double acc = part;
     for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
