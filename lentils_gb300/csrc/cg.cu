@@ -83,6 +83,7 @@ template <typename R>
 __global__ void rtr_kernel(const R *__restrict__ s, R *__restrict__ out, int nx, int ny, R idx2,
                            R idy2, R lam, int accumulate)
 {
+    pdl_entry();
     const long long n = (long long)nx * ny;
     for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < n;
          e += (long long)gridDim.x * blockDim.x) {
@@ -118,6 +119,7 @@ __global__ void __launch_bounds__(256)
     dot_partial_kernel(const A *__restrict__ a, const B *__restrict__ b, long long n,
                        double *__restrict__ partial)
 {
+    pdl_entry();
     __shared__ double sh[8];
     double acc = 0.0;
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
@@ -130,6 +132,7 @@ __global__ void __launch_bounds__(256)
 __global__ void sum_partials_kernel(const double *__restrict__ partial, int np,
                                     double *__restrict__ out)
 {
+    pdl_entry();
     __shared__ double sh[8];
     double acc = 0.0;
     for (int i = threadIdx.x; i < np; i += blockDim.x) acc += partial[i];
@@ -144,6 +147,7 @@ struct CGScalars {
 
 __global__ void cg_alpha_kernel(const double *__restrict__ partial, int np, CGScalars *sc)
 {
+    pdl_entry();
     __shared__ double sh[8];
     double acc = 0.0;
     for (int i = threadIdx.x; i < np; i += blockDim.x) acc += partial[i];
@@ -161,6 +165,7 @@ __global__ void __launch_bounds__(256)
                      const float *__restrict__ minv, const CGScalars *__restrict__ sc, int n,
                      double *__restrict__ partial)
 {
+    pdl_entry();
     __shared__ double sh[8];
     const float alpha = (float)sc->alpha;
     double rz = 0.0, rr = 0.0;
@@ -183,6 +188,7 @@ __global__ void __launch_bounds__(256)
 
 __global__ void cg_beta_kernel(const double *__restrict__ partial, int np, CGScalars *sc)
 {
+    pdl_entry();
     __shared__ double sh[8];
     double a = 0.0, b = 0.0;
     for (int i = threadIdx.x; i < np; i += blockDim.x) {
@@ -202,6 +208,7 @@ __global__ void cg_beta_kernel(const double *__restrict__ partial, int np, CGSca
 __global__ void cg_p_kernel(float *__restrict__ p, const float *__restrict__ z,
                             const CGScalars *__restrict__ sc, int n)
 {
+    pdl_entry();
     const float beta = (float)sc->beta;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
         p[i] = fmaf(beta, p[i], z[i]);
@@ -213,6 +220,7 @@ __global__ void cg_start_kernel(const double *__restrict__ r64, float *__restric
                                 float *__restrict__ p, const float *__restrict__ minv, int n,
                                 double *__restrict__ partial)
 {
+    pdl_entry();
     __shared__ double sh[8];
     double rz = 0.0, rr = 0.0;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
@@ -235,6 +243,7 @@ __global__ void cg_start_kernel(const double *__restrict__ r64, float *__restric
 
 __global__ void cg_start_finish_kernel(const double *__restrict__ partial, int np, CGScalars *sc)
 {
+    pdl_entry();
     __shared__ double sh[8];
     double a = 0.0, b = 0.0;
     for (int i = threadIdx.x; i < np; i += blockDim.x) {
@@ -253,6 +262,7 @@ __global__ void cg_start_finish_kernel(const double *__restrict__ partial, int n
 // x64 += e32 ; r64 = b - ax64 handled separately
 __global__ void add_f32_to_f64_kernel(double *__restrict__ x, const float *__restrict__ e, int n)
 {
+    pdl_entry();
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
         x[i] += (double)e[i];
 }
@@ -260,6 +270,7 @@ __global__ void add_f32_to_f64_kernel(double *__restrict__ x, const float *__res
 __global__ void sub_kernel(const double *__restrict__ b, const double *__restrict__ a,
                            double *__restrict__ r, int n)
 {
+    pdl_entry();
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
         r[i] = b[i] - a[i];
 }
@@ -286,6 +297,7 @@ struct FCGScalars {
 
 __global__ void fcg_rr_kernel(const double *__restrict__ partial, int np, FCGScalars *sc, int start)
 {
+    pdl_entry();
     __shared__ double sh[8];
     double a = 0.0;
     for (int i = threadIdx.x; i < np; i += blockDim.x) a += partial[i];
@@ -312,6 +324,7 @@ __global__ void __launch_bounds__(256)
                      float *__restrict__ p, float *__restrict__ ap, int n,
                      double *__restrict__ partial)
 {
+    pdl_entry();
     __shared__ double sh[8];
     double rr = 0.0;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
@@ -358,6 +371,7 @@ __global__ void __launch_bounds__(256)
                            const float *__restrict__ r, int n, double *__restrict__ part,
                            unsigned *__restrict__ counter, FCGScalars *__restrict__ sc)
 {
+    pdl_entry();
     __shared__ double sh[8];
     __shared__ int last;
     double a = 0.0, b = 0.0;
@@ -407,6 +421,7 @@ __global__ void __launch_bounds__(256)
                             FCGWindow *__restrict__ win, double *__restrict__ part,
                             unsigned *__restrict__ counter, int with_dir)
 {
+    pdl_entry();
     __shared__ double sh[8];
     __shared__ int last;
     const float alpha = (float)sc->alpha;
@@ -460,6 +475,7 @@ __global__ void __launch_bounds__(256)
                             FCGScalars *__restrict__ sc, FCGWindow *__restrict__ win,
                             double *__restrict__ part, unsigned *__restrict__ counter, int first)
 {
+    pdl_entry();
     __shared__ double sh[8];
     __shared__ int last;
     const int valid = first ? 0 : min(win->count + 1, win->m);
@@ -518,6 +534,7 @@ __global__ void __launch_bounds__(256)
                        const float *__restrict__ P, const FCGScalars *__restrict__ sc,
                        const FCGWindow *__restrict__ win, int n)
 {
+    pdl_entry();
     __shared__ float beta[kMaxWindow];
     const int m = win->m;
     if (threadIdx.x < kMaxWindow) beta[threadIdx.x] = (threadIdx.x < m) ? (float)win->beta[threadIdx.x] : 0.f;
@@ -533,8 +550,8 @@ __global__ void __launch_bounds__(256)
 static double host_dot64(const double *a, const double *b, int n, double *partial, double *out,
                          cudaStream_t s)
 {
-    dot_partial_kernel<double, double><<<kRedBlocks, 256, 0, s>>>(a, b, n, partial);
-    sum_partials_kernel<<<1, 256, 0, s>>>(partial, kRedBlocks, out);
+    LENTILS_CUDA_TRY(pdl_launch(dot_partial_kernel<double, double>, dim3(kRedBlocks), dim3(256), 0, s, a, b, n, partial));
+    LENTILS_CUDA_TRY(pdl_launch(sum_partials_kernel, dim3(1), dim3(256), 0, s, partial, kRedBlocks, out));
     double h = 0.0;
     cudaMemcpyAsync(&h, out, sizeof(double), cudaMemcpyDeviceToHost, s);
     cudaStreamSynchronize(s);
@@ -552,7 +569,7 @@ static int initial_residual(lentils_normal_op *op, const double *b, const double
         return LENTILS_OK;
     }
     if (int st = lentils_normal_op_apply64(op, x, ax64, s)) return st;
-    sub_kernel<<<nb(n), 256, 0, s>>>(b, ax64, r64, n);
+    LENTILS_CUDA_TRY(pdl_launch(sub_kernel, dim3(nb(n)), dim3(256), 0, s, b, ax64, r64, n));
     LENTILS_CHECK_LAUNCH("sub_kernel");
     return LENTILS_OK;
 }
@@ -717,8 +734,8 @@ int lentils_normal_op_apply(lentils_normal_op *op, const float *s_in, float *out
             return st;
     }
     if ((st = lentils_lensop_apply_t(op->L, op->img32b, out, stream))) return st;
-    rtr_kernel<float><<<nb(op->nsrc), 256, 0, s>>>(s_in, out, op->nsx, op->nsy, (float)op->idx2,
-                                                   (float)op->idy2, (float)op->lambda, 1);
+    LENTILS_CUDA_TRY(pdl_launch(rtr_kernel<float>, dim3(nb(op->nsrc)), dim3(256), 0, s, s_in, out, op->nsx, op->nsy, (float)op->idx2,
+                                                   (float)op->idy2, (float)op->lambda, 1));
     LENTILS_CHECK_LAUNCH("rtr_kernel");
     return LENTILS_OK;
 }
@@ -741,8 +758,8 @@ int lentils_normal_op_apply64(lentils_normal_op *op, const double *s_in, double 
             return st;
     }
     if ((st = lentils_lensop_apply_t64(op->L, op->img64b, out, stream))) return st;
-    rtr_kernel<double><<<nb(op->nsrc), 256, 0, s>>>(s_in, out, op->nsx, op->nsy, op->idx2,
-                                                    op->idy2, op->lambda, 1);
+    LENTILS_CUDA_TRY(pdl_launch(rtr_kernel<double>, dim3(nb(op->nsrc)), dim3(256), 0, s, s_in, out, op->nsx, op->nsy, op->idx2,
+                                                    op->idy2, op->lambda, 1));
     LENTILS_CHECK_LAUNCH("rtr_kernel");
     return LENTILS_OK;
 }
@@ -821,12 +838,12 @@ int lentils_cg_solve(lentils_normal_op *op, const double *b, double *x, const fl
     auto inner_iteration = [&]() -> int {
         int q = lentils_normal_op_apply(op, p32, ap32, s);
         if (q) return q;
-        dot_partial_kernel<float, float><<<kRedBlocks, 256, 0, s>>>(p32, ap32, n, partial);
-        cg_alpha_kernel<<<1, 256, 0, s>>>(partial, kRedBlocks, sc);
-        cg_update_kernel<<<kRedBlocks, 256, 0, s>>>(e32, r32, z32, p32, ap32, inv_diag32, sc, n,
-                                                   partial);
-        cg_beta_kernel<<<1, 256, 0, s>>>(partial, kRedBlocks, sc);
-        cg_p_kernel<<<nb(n), 256, 0, s>>>(p32, z32, sc, n);
+        LENTILS_CUDA_TRY(pdl_launch(dot_partial_kernel<float, float>, dim3(kRedBlocks), dim3(256), 0, s, p32, ap32, n, partial));
+        LENTILS_CUDA_TRY(pdl_launch(cg_alpha_kernel, dim3(1), dim3(256), 0, s, partial, kRedBlocks, sc));
+        LENTILS_CUDA_TRY(pdl_launch(cg_update_kernel, dim3(kRedBlocks), dim3(256), 0, s, e32, r32, z32, p32, ap32, inv_diag32, sc, n,
+                                                   partial));
+        LENTILS_CUDA_TRY(pdl_launch(cg_beta_kernel, dim3(1), dim3(256), 0, s, partial, kRedBlocks, sc));
+        LENTILS_CUDA_TRY(pdl_launch(cg_p_kernel, dim3(nb(n)), dim3(256), 0, s, p32, z32, sc, n));
         cudaError_t le = cudaGetLastError();
         return le == cudaSuccess ? LENTILS_OK : cuda_status(le, "cg inner iteration");
     };
@@ -860,8 +877,8 @@ int lentils_cg_solve(lentils_normal_op *op, const double *b, double *x, const fl
     const int check = std::max(1, opt->check_every);
     while (!st && rel > opt->tol && outer < opt->max_outer) {
         ++outer;
-        cg_start_kernel<<<kRedBlocks, 256, 0, s>>>(r64, r32, e32, z32, p32, inv_diag32, n, partial);
-        cg_start_finish_kernel<<<1, 256, 0, s>>>(partial, kRedBlocks, sc);
+        LENTILS_CUDA_TRY(pdl_launch(cg_start_kernel, dim3(kRedBlocks), dim3(256), 0, s, r64, r32, e32, z32, p32, inv_diag32, n, partial));
+        LENTILS_CUDA_TRY(pdl_launch(cg_start_finish_kernel, dim3(1), dim3(256), 0, s, partial, kRedBlocks, sc));
         CGScalars hs;
         int k = 0;
         while (k < opt->max_inner) {
@@ -891,9 +908,9 @@ int lentils_cg_solve(lentils_normal_op *op, const double *b, double *x, const fl
         }
         inner_total += k;
         if (st) break;
-        add_f32_to_f64_kernel<<<nb(n), 256, 0, s>>>(x, e32, n);
+        LENTILS_CUDA_TRY(pdl_launch(add_f32_to_f64_kernel, dim3(nb(n)), dim3(256), 0, s, x, e32, n));
         if ((st = lentils_normal_op_apply64(op, x, ax64, s))) break;
-        sub_kernel<<<nb(n), 256, 0, s>>>(b, ax64, r64, n);
+        LENTILS_CUDA_TRY(pdl_launch(sub_kernel, dim3(nb(n)), dim3(256), 0, s, b, ax64, r64, n));
         rel = (bnorm > 0) ? sqrt(host_dot64(r64, r64, n, partial, scal, s)) / bnorm : 0.0;
     }
     if (!st) {
@@ -986,9 +1003,9 @@ int lentils_fcg_solve(lentils_normal_op *op, const double *b, double *x, const f
         float *zdir = with_net ? z32 : nullptr;
         if (with_net)
             if (int q = unet_precondition(net, r32, inv_diag32, feat, z32, s)) return q;
-        fcg_select_fused_kernel<<<kRedBlocks, 256, 0, s>>>(zdir, r32, inv_diag32, Qw, n, sc, win,
-                                                            fpart, counter, first ? 1 : 0);
-        fcg_p_fused_kernel<<<nb(n), 256, 0, s>>>(p32, zdir, r32, inv_diag32, Pw, sc, win, n);
+        LENTILS_CUDA_TRY(pdl_launch(fcg_select_fused_kernel, dim3(kRedBlocks), dim3(256), 0, s, zdir, r32, inv_diag32, Qw, n, sc, win,
+                                                            fpart, counter, first ? 1 : 0));
+        LENTILS_CUDA_TRY(pdl_launch(fcg_p_fused_kernel, dim3(nb(n)), dim3(256), 0, s, p32, zdir, r32, inv_diag32, Pw, sc, win, n));
         cudaError_t le = cudaGetLastError();
         return le == cudaSuccess ? LENTILS_OK : cuda_status(le, "fcg direction");
     };
@@ -997,12 +1014,12 @@ int lentils_fcg_solve(lentils_normal_op *op, const double *b, double *x, const f
     auto inner_iteration = [&](bool with_net) -> int {
         int q = lentils_normal_op_apply(op, p32, ap32, s);
         if (q) return q;
-        fcg_alpha_fused_kernel<<<kRedBlocks, 256, 0, s>>>(p32, ap32, r32, n, fpart, counter, sc);
-        fcg_update_fused_kernel<<<kRedBlocks, 256, 0, s>>>(e32, r32, p32, ap32, Pw, Qw,
+        LENTILS_CUDA_TRY(pdl_launch(fcg_alpha_fused_kernel, dim3(kRedBlocks), dim3(256), 0, s, p32, ap32, r32, n, fpart, counter, sc));
+        LENTILS_CUDA_TRY(pdl_launch(fcg_update_fused_kernel, dim3(kRedBlocks), dim3(256), 0, s, e32, r32, p32, ap32, Pw, Qw,
                                                             inv_diag32, n, sc, win, fpart,
-                                                            counter, with_net ? 0 : 1);
+                                                            counter, with_net ? 0 : 1));
         if (with_net) return direction(false, true);
-        fcg_p_fused_kernel<<<nb(n), 256, 0, s>>>(p32, nullptr, r32, inv_diag32, Pw, sc, win, n);
+        LENTILS_CUDA_TRY(pdl_launch(fcg_p_fused_kernel, dim3(nb(n)), dim3(256), 0, s, p32, nullptr, r32, inv_diag32, Pw, sc, win, n));
         cudaError_t le = cudaGetLastError();
         return le == cudaSuccess ? LENTILS_OK : cuda_status(le, "fcg step");
     };
@@ -1045,8 +1062,8 @@ int lentils_fcg_solve(lentils_normal_op *op, const double *b, double *x, const f
     const int stall_checks = 20;
     while (!st && rel > opt->tol && outer < opt->max_outer) {
         ++outer;
-        fcg_start_kernel<<<kRedBlocks, 256, 0, s>>>(r64, r32, e32, p32, ap32, n, partial);
-        fcg_rr_kernel<<<1, 256, 0, s>>>(partial, kRedBlocks, sc, 1);
+        LENTILS_CUDA_TRY(pdl_launch(fcg_start_kernel, dim3(kRedBlocks), dim3(256), 0, s, r64, r32, e32, p32, ap32, n, partial));
+        LENTILS_CUDA_TRY(pdl_launch(fcg_rr_kernel, dim3(1), dim3(256), 0, s, partial, kRedBlocks, sc, 1));
         if ((st = direction(true, use_net))) break;
         FCGScalars hs;
         int k = 0;
@@ -1091,9 +1108,9 @@ int lentils_fcg_solve(lentils_normal_op *op, const double *b, double *x, const f
         }
         inner_total += k;
         if (st) break;
-        add_f32_to_f64_kernel<<<nb(n), 256, 0, s>>>(x, e32, n);
+        LENTILS_CUDA_TRY(pdl_launch(add_f32_to_f64_kernel, dim3(nb(n)), dim3(256), 0, s, x, e32, n));
         if ((st = lentils_normal_op_apply64(op, x, ax64, s))) break;
-        sub_kernel<<<nb(n), 256, 0, s>>>(b, ax64, r64, n);
+        LENTILS_CUDA_TRY(pdl_launch(sub_kernel, dim3(nb(n)), dim3(256), 0, s, b, ax64, r64, n));
         rel = (bnorm > 0) ? sqrt(host_dot64(r64, r64, n, partial, scal, s)) / bnorm : 0.0;
     }
     if (!st) {
@@ -1149,8 +1166,7 @@ int lentils_prior_gradient_apply(const float *s_in, float *out, int nx, int ny, 
     clear_error();
     if (!s_in || !out || nx < 1 || ny < 1 || !(dx > 0) || !(dy > 0))
         return set_error(LENTILS_ERR_INVALID, "prior_gradient_apply: bad arguments");
-    rtr_kernel<float><<<nb((long long)nx * ny), 256, 0, (cudaStream_t)stream>>>(
-        s_in, out, nx, ny, (float)(1.0 / (dx * dx)), (float)(1.0 / (dy * dy)), (float)lambda, 0);
+    LENTILS_CUDA_TRY(pdl_launch(rtr_kernel<float>, dim3(nb((long long)nx * ny)), dim3(256), 0, (cudaStream_t)stream, s_in, out, nx, ny, (float)(1.0 / (dx * dx)), (float)(1.0 / (dy * dy)), (float)lambda, 0));
     LENTILS_CHECK_LAUNCH("rtr_kernel");
     return LENTILS_OK;
 }
@@ -1161,8 +1177,7 @@ int lentils_prior_gradient_apply64(const double *s_in, double *out, int nx, int 
     clear_error();
     if (!s_in || !out || nx < 1 || ny < 1 || !(dx > 0) || !(dy > 0))
         return set_error(LENTILS_ERR_INVALID, "prior_gradient_apply64: bad arguments");
-    rtr_kernel<double><<<nb((long long)nx * ny), 256, 0, (cudaStream_t)stream>>>(
-        s_in, out, nx, ny, 1.0 / (dx * dx), 1.0 / (dy * dy), lambda, 0);
+    LENTILS_CUDA_TRY(pdl_launch(rtr_kernel<double>, dim3(nb((long long)nx * ny)), dim3(256), 0, (cudaStream_t)stream, s_in, out, nx, ny, 1.0 / (dx * dx), 1.0 / (dy * dy), lambda, 0));
     LENTILS_CHECK_LAUNCH("rtr_kernel");
     return LENTILS_OK;
 }

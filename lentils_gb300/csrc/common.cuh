@@ -6,6 +6,8 @@
 #include <stdio.h>
 #include <string.h>
 
+#include <utility>
+
 #include "lentils_gb300.h"
 
 namespace lentils {
@@ -114,6 +116,35 @@ struct WorkItem {
     int begin;    // first visibility (plan order)
     int count;    // number of visibilities
 };
+
+// -- programmatic dependent launch ----------------------------------------------------------
+// A kernel launched by pdl_launch may start while the kernel before it in the stream is still
+// running. It must call pdl_entry() before it reads anything an earlier kernel writes or writes
+// anything an earlier kernel reads: griddepcontrol.wait blocks until the previous kernel has
+// completed and its memory is visible (a no-op without the launch attribute), and
+// launch_dependents lets the next such kernel start once every CTA of this grid has reached it.
+__device__ __forceinline__ void pdl_entry()
+{
+    asm volatile("griddepcontrol.wait;" ::: "memory");
+    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+}
+
+template <class... KArgs, class... Args>
+inline cudaError_t pdl_launch(void (*kern)(KArgs...), dim3 grid, dim3 block, size_t smem,
+                              cudaStream_t s, Args &&...args)
+{
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = grid;
+    cfg.blockDim = block;
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = s;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, kern, std::forward<Args>(args)...);
+}
 
 }  // namespace lentils
 

@@ -108,6 +108,7 @@ template <typename R>
 __global__ void lens_apply_kernel(const int *__restrict__ col, const R *__restrict__ val,
                                   const R *__restrict__ src, R *__restrict__ img, int nimg)
 {
+    pdl_entry();
     for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < nimg;
          p += (long long)gridDim.x * blockDim.x) {
         const int4 c = reinterpret_cast<const int4 *>(col)[p];
@@ -125,6 +126,7 @@ __global__ void lens_apply_csr_kernel(const int *__restrict__ ptr, const int *__
                                       const R *__restrict__ val, const R *__restrict__ src,
                                       R *__restrict__ img, int nimg)
 {
+    pdl_entry();
     for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < nimg;
          p += (long long)gridDim.x * blockDim.x) {
         R acc = (R)0;
@@ -173,6 +175,7 @@ __global__ void lens_apply_t_kernel(const int *__restrict__ ptr, const int *__re
                                     const R *__restrict__ val, const R *__restrict__ img,
                                     R *__restrict__ src, int nsrc)
 {
+    pdl_entry();
     const int lane = threadIdx.x & 31;
     const long long nwarps = ((long long)gridDim.x * blockDim.x) >> 5;
     for (long long j = (blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5; j < nsrc;
@@ -406,11 +409,9 @@ int lentils_lensop_apply(const lentils_lensop *op, const float *src, float *img,
     clear_error();
     if (!op || !src || !img) return set_error(LENTILS_ERR_INVALID, "lensop_apply: null argument");
     if (op->f_ptr)
-        lens_apply_csr_kernel<float><<<blocks_for(op->nimg), 256, 0, (cudaStream_t)stream>>>(
-            op->f_ptr, op->f_col, op->f_val32, src, img, op->nimg);
+        LENTILS_CUDA_TRY(pdl_launch(lens_apply_csr_kernel<float>, dim3(blocks_for(op->nimg)), dim3(256), 0, (cudaStream_t)stream, op->f_ptr, op->f_col, op->f_val32, src, img, op->nimg));
     else
-        lens_apply_kernel<float><<<blocks_for(op->nimg), 256, 0, (cudaStream_t)stream>>>(
-            op->ell_col, op->ell_val32, src, img, op->nimg);
+        LENTILS_CUDA_TRY(pdl_launch(lens_apply_kernel<float>, dim3(blocks_for(op->nimg)), dim3(256), 0, (cudaStream_t)stream, op->ell_col, op->ell_val32, src, img, op->nimg));
     LENTILS_CHECK_LAUNCH("lens_apply_kernel");
     return LENTILS_OK;
 }
@@ -419,8 +420,7 @@ int lentils_lensop_apply_t(const lentils_lensop *op, const float *img, float *sr
 {
     clear_error();
     if (!op || !src || !img) return set_error(LENTILS_ERR_INVALID, "lensop_apply_t: null argument");
-    lens_apply_t_kernel<float><<<blocks_for(32LL * op->nsrc), 256, 0, (cudaStream_t)stream>>>(
-        op->t_ptr, op->t_row, op->t_val32, img, src, op->nsrc);
+    LENTILS_CUDA_TRY(pdl_launch(lens_apply_t_kernel<float>, dim3(blocks_for(32LL * op->nsrc)), dim3(256), 0, (cudaStream_t)stream, op->t_ptr, op->t_row, op->t_val32, img, src, op->nsrc));
     LENTILS_CHECK_LAUNCH("lens_apply_t_kernel");
     return LENTILS_OK;
 }
@@ -430,11 +430,9 @@ int lentils_lensop_apply64(const lentils_lensop *op, const double *src, double *
     clear_error();
     if (!op || !src || !img) return set_error(LENTILS_ERR_INVALID, "lensop_apply64: null argument");
     if (op->f_ptr)
-        lens_apply_csr_kernel<double><<<blocks_for(op->nimg), 256, 0, (cudaStream_t)stream>>>(
-            op->f_ptr, op->f_col, op->f_val64, src, img, op->nimg);
+        LENTILS_CUDA_TRY(pdl_launch(lens_apply_csr_kernel<double>, dim3(blocks_for(op->nimg)), dim3(256), 0, (cudaStream_t)stream, op->f_ptr, op->f_col, op->f_val64, src, img, op->nimg));
     else
-        lens_apply_kernel<double><<<blocks_for(op->nimg), 256, 0, (cudaStream_t)stream>>>(
-            op->ell_col, op->ell_val64, src, img, op->nimg);
+        LENTILS_CUDA_TRY(pdl_launch(lens_apply_kernel<double>, dim3(blocks_for(op->nimg)), dim3(256), 0, (cudaStream_t)stream, op->ell_col, op->ell_val64, src, img, op->nimg));
     LENTILS_CHECK_LAUNCH("lens_apply_kernel");
     return LENTILS_OK;
 }
@@ -445,8 +443,7 @@ int lentils_lensop_apply_t64(const lentils_lensop *op, const double *img, double
     clear_error();
     if (!op || !src || !img)
         return set_error(LENTILS_ERR_INVALID, "lensop_apply_t64: null argument");
-    lens_apply_t_kernel<double><<<blocks_for(32LL * op->nsrc), 256, 0, (cudaStream_t)stream>>>(
-        op->t_ptr, op->t_row, op->t_val64, img, src, op->nsrc);
+    LENTILS_CUDA_TRY(pdl_launch(lens_apply_t_kernel<double>, dim3(blocks_for(32LL * op->nsrc)), dim3(256), 0, (cudaStream_t)stream, op->t_ptr, op->t_row, op->t_val64, img, src, op->nsrc));
     LENTILS_CHECK_LAUNCH("lens_apply_t_kernel");
     return LENTILS_OK;
 }

@@ -76,6 +76,7 @@ __global__ void apod_pad_kernel(const R *__restrict__ img, R *__restrict__ pad,
                                 const R *__restrict__ apx, const R *__restrict__ apy, int nx,
                                 int ny, int padx, int pady, int nu, int nv)
 {
+    pdl_entry();
     const long long total = (long long)nu * nv;
     for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < total;
          e += (long long)gridDim.x * blockDim.x) {
@@ -93,6 +94,7 @@ __global__ void crop_apod_kernel(const R *__restrict__ pad, R *__restrict__ img,
                                  const R *__restrict__ apx, const R *__restrict__ apy, int nx,
                                  int ny, int padx, int pady, int nv)
 {
+    pdl_entry();
     const long long total = (long long)nx * ny;
     for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < total;
          e += (long long)gridDim.x * blockDim.x) {
@@ -106,6 +108,7 @@ __global__ void crop_apod_kernel(const R *__restrict__ pad, R *__restrict__ img,
 template <typename C>
 __global__ void hermitian_edges_kernel(C *grid, int nu, int half_nv, int ncols_edge, int last)
 {
+    pdl_entry();
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     const int pairs = nu / 2 + 1;  // a = 0 .. nu/2 (a and nu-a coincide at 0 and nu/2)
     if (t >= pairs * ncols_edge) return;
@@ -283,8 +286,7 @@ int nufft_forward_scaled(lentils_nufft *op, const float *image, float *vis_plan,
     if (!op || !op->have32 || !image || !vis_plan)
         return set_error(LENTILS_ERR_INVALID, "nufft_forward: bad arguments (FP32 not created?)");
     cudaStream_t s = (cudaStream_t)stream;
-    apod_pad_kernel<float><<<nblocks((long long)op->nu * op->nv), 256, 0, s>>>(
-        image, op->pad32, op->apx32, op->apy32, op->nx, op->ny, op->padx, op->pady, op->nu, op->nv);
+    LENTILS_CUDA_TRY(pdl_launch(apod_pad_kernel<float>, dim3(nblocks((long long)op->nu * op->nv)), dim3(256), 0, s, image, op->pad32, op->apx32, op->apy32, op->nx, op->ny, op->padx, op->pady, op->nu, op->nv));
     LENTILS_CHECK_LAUNCH("apod_pad_kernel");
     LENTILS_CUFFT_TRY(cufftSetStream(op->r2c32, s));
     LENTILS_CUFFT_TRY(cufftExecR2C(op->r2c32, op->pad32, (cufftComplex *)op->grid32));
@@ -298,8 +300,7 @@ int nufft_forward_scaled64(lentils_nufft *op, const double *image, double *vis_p
     if (!op || !op->have64 || !image || !vis_plan)
         return set_error(LENTILS_ERR_INVALID, "nufft_forward64: bad arguments (FP64 not created?)");
     cudaStream_t s = (cudaStream_t)stream;
-    apod_pad_kernel<double><<<nblocks((long long)op->nu * op->nv), 256, 0, s>>>(
-        image, op->pad64, op->apx64, op->apy64, op->nx, op->ny, op->padx, op->pady, op->nu, op->nv);
+    LENTILS_CUDA_TRY(pdl_launch(apod_pad_kernel<double>, dim3(nblocks((long long)op->nu * op->nv)), dim3(256), 0, s, image, op->pad64, op->apx64, op->apy64, op->nx, op->ny, op->padx, op->pady, op->nu, op->nv));
     LENTILS_CHECK_LAUNCH("apod_pad_kernel");
     LENTILS_CUFFT_TRY(cufftSetStream(op->d2z64, s));
     LENTILS_CUFFT_TRY(cufftExecD2Z(op->d2z64, op->pad64, (cufftDoubleComplex *)op->grid64));
@@ -320,13 +321,11 @@ int lentils_nufft_adjoint(lentils_nufft *op, const float *vis_plan, float *image
     if (int st = launch_grid(op->plan, (const float2 *)vis_plan, op->grid32, s)) return st;
     const int ncols = (op->nv % 2 == 0) ? 2 : 1;
     const int pairs = op->nu / 2 + 1;
-    hermitian_edges_kernel<float2><<<(pairs * ncols + 255) / 256, 256, 0, s>>>(
-        op->grid32, op->nu, op->half_nv, ncols, op->half_nv - 1);
+    LENTILS_CUDA_TRY(pdl_launch(hermitian_edges_kernel<float2>, dim3((pairs * ncols + 255) / 256), dim3(256), 0, s, op->grid32, op->nu, op->half_nv, ncols, op->half_nv - 1));
     LENTILS_CHECK_LAUNCH("hermitian_edges_kernel");
     LENTILS_CUFFT_TRY(cufftSetStream(op->c2r32, s));
     LENTILS_CUFFT_TRY(cufftExecC2R(op->c2r32, (cufftComplex *)op->grid32, op->pad32));
-    crop_apod_kernel<float><<<nblocks((long long)op->nx * op->ny), 256, 0, s>>>(
-        op->pad32, image, op->apx32, op->apy32, op->nx, op->ny, op->padx, op->pady, op->nv);
+    LENTILS_CUDA_TRY(pdl_launch(crop_apod_kernel<float>, dim3(nblocks((long long)op->nx * op->ny)), dim3(256), 0, s, op->pad32, image, op->apx32, op->apy32, op->nx, op->ny, op->padx, op->pady, op->nv));
     LENTILS_CHECK_LAUNCH("crop_apod_kernel");
     return LENTILS_OK;
 }
@@ -342,13 +341,11 @@ int lentils_nufft_adjoint64(lentils_nufft *op, const double *vis_plan, double *i
     if (int st = launch_grid64(op->plan, (const double2 *)vis_plan, op->grid64, s)) return st;
     const int ncols = (op->nv % 2 == 0) ? 2 : 1;
     const int pairs = op->nu / 2 + 1;
-    hermitian_edges_kernel<double2><<<(pairs * ncols + 255) / 256, 256, 0, s>>>(
-        op->grid64, op->nu, op->half_nv, ncols, op->half_nv - 1);
+    LENTILS_CUDA_TRY(pdl_launch(hermitian_edges_kernel<double2>, dim3((pairs * ncols + 255) / 256), dim3(256), 0, s, op->grid64, op->nu, op->half_nv, ncols, op->half_nv - 1));
     LENTILS_CHECK_LAUNCH("hermitian_edges_kernel");
     LENTILS_CUFFT_TRY(cufftSetStream(op->z2d64, s));
     LENTILS_CUFFT_TRY(cufftExecZ2D(op->z2d64, (cufftDoubleComplex *)op->grid64, op->pad64));
-    crop_apod_kernel<double><<<nblocks((long long)op->nx * op->ny), 256, 0, s>>>(
-        op->pad64, image, op->apx64, op->apy64, op->nx, op->ny, op->padx, op->pady, op->nv);
+    LENTILS_CUDA_TRY(pdl_launch(crop_apod_kernel<double>, dim3(nblocks((long long)op->nx * op->ny)), dim3(256), 0, s, op->pad64, image, op->apx64, op->apy64, op->nx, op->ny, op->padx, op->pady, op->nv));
     LENTILS_CHECK_LAUNCH("crop_apod_kernel");
     return LENTILS_OK;
 }

@@ -1690,26 +1690,6 @@ static int conv_gemm_n(int N, const LA &la, const tc::RowMajorLoader &lb, const 
     return set_error(LENTILS_ERR_UNSUPPORTED, "conv gemm N=%d", N);
 }
 
-// Launches kern with programmatic stream serialization: it may start while the kernel before
-// it in the stream finishes, and waits for it (tc::pdl_wait) before touching its results. Used
-// for the kernels of the forward and backward passes, all of which call tc::pdl_wait first.
-template <class... KArgs, class... Args>
-static cudaError_t pdl_launch(void (*kern)(KArgs...), dim3 grid, dim3 block, size_t smem,
-                              cudaStream_t s, Args &&...args)
-{
-    cudaLaunchConfig_t cfg = {};
-    cfg.gridDim = grid;
-    cfg.blockDim = block;
-    cfg.dynamicSmemBytes = smem;
-    cfg.stream = s;
-    cudaLaunchAttribute attr[1];
-    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
-    attr[0].val.programmaticStreamSerializationAllowed = 1;
-    cfg.attrs = attr;
-    cfg.numAttrs = 1;
-    return cudaLaunchKernelEx(&cfg, kern, std::forward<Args>(args)...);
-}
-
 // Weight gradient of a convolution layer as a GEMM whose operands are both MN-major, read
 // straight from the pixel-major (NHWC) activations and gradients, with no transposed copies:
 //   D[(t, ci)][co] = sum_p x[p + off(t)][ci] dym[p][co],   rows (t, ci) = t C + ci,
