@@ -74,7 +74,9 @@ def test_unet_forward_is_deterministic(native):
     assert net.error_flag() == 0
 
 
-@pytest.mark.parametrize("B,H,W", [(1, 16, 16), (2, 32, 32)])
+# (1, 16, 16), (2, 32, 32): every weight gradient on the MN-major tensor-core kernel;
+# (1, 24, 40): no layer's grid fits its 64-pixel chunks, so the transposed-operand forms run
+@pytest.mark.parametrize("B,H,W", [(1, 16, 16), (2, 32, 32), (1, 24, 40)])
 def test_unet_gradients_match_oracle(native, B, H, W):
     from lentils_gb300 import learned
     p, x, f, t = _problem(20 + H, B, H, W)
