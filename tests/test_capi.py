@@ -77,3 +77,20 @@ def test_kb_table_rejects_bad_width(native):
     assert st == 1 and native.lib().lentils_last_error() == 1
     st = native.lib().lentils_kb_poly_table(9, 10.0, out.ctypes.data, out.size, ctypes.byref(err))
     assert st == 1
+
+
+def test_unet_entry_points_reject_bad_arguments(native):
+    """The U-Net entry points check their arguments before touching a device: sizes that are not
+    multiples of 8 (or below 16), unknown GEMM forms and null handles are LENTILS_ERR_INVALID."""
+    lib = native.lib()
+    params = np.zeros(native_param_count(lib), dtype=np.float32)
+    h = ctypes.c_void_p()
+    for H, W, B in ((12, 16, 1), (16, 20, 1), (16, 16, 0)):
+        st = lib.lentils_unet_create(ctypes.byref(h), H, W, B, params.ctypes.data, None)
+        assert st == 1 and lib.lentils_last_error() == 1, (H, W, B)
+    assert lib.lentils_unet_set_gemm_form(None, 0) == 1
+    assert lib.lentils_unet_set_gemm_form(None, 3) == 1
+
+
+def native_param_count(lib):
+    return int(lib.lentils_unet_param_count())
