@@ -61,13 +61,14 @@ def test_unet_forward_matches_oracle(native, B, H, W):
 
 
 def test_unet_forward_is_deterministic(native):
-    """Split-K layers sum their partial slabs in a fixed order: repeated forwards at batch 1
-    (and at batch 4, same weights) give bit-identical outputs."""
+    """Split-K layers sum their partial slabs in a fixed order, and no forward kernel uses
+    atomics: repeated forwards at batch 1, 4 and 5 (c1's band kernel), same weights, give
+    bit-identical outputs."""
     from lentils_gb300 import learned
-    p, x, f, _ = _problem(77, 4, 128, 128)
-    net = learned.UNet(128, 128, max_batch=4, params=p)
+    p, x, f, _ = _problem(77, 5, 128, 128)
+    net = learned.UNet(128, 128, max_batch=5, params=p)
     xc, fc = _cuda(x, f)
-    for B in (1, 4):
+    for B in (1, 4, 5):
         outs = [net.forward(xc[:B], fc[:B]) for _ in range(4)]
         for o in outs[1:]:
             assert torch.equal(o, outs[0])
