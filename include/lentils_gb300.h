@@ -533,6 +533,7 @@ int lentils_sweep_get_stats(const lentils_sweep *sweep, lentils_sweep_stats *sta
  * ---------------------------------------------------------------------------------------- */
 typedef struct lentils_unet lentils_unet;
 long long lentils_unet_param_count(void);
+/* init_params: the flat parameter vector in HOST memory */
 int lentils_unet_create(lentils_unet **out, int H, int W, int max_batch, const float *init_params,
                         void *stream);
 int lentils_unet_destroy(lentils_unet *net);
@@ -554,7 +555,6 @@ int lentils_unet_train_step(lentils_unet *net, const float *r, const float *d, c
  * and a copy of the flat parameter gradient to HOST grad_host if non-NULL (synchronising) */
 int lentils_unet_backward(lentils_unet *net, const float *dout, int B, float lr,
                           float *grad_host, void *stream);
-/* gamma of the preconditioner form (default 0) */
 /* Tuning, the convolution kernels: 0 (default) runs the forward convolutions with TMA operands
  * on the persistent GEMM (one wave of CTAs, accumulators double buffered in tensor memory), the
  * first layer with its input packing and pooling as one CUDA-core kernel, and the last hidden
@@ -566,6 +566,7 @@ int lentils_unet_set_gemm_form(lentils_unet *net, int form);
 /* Tuning: about how many CTAs a weight-gradient GEMM runs (its pixel reduction is split over
  * them); 0 selects the built-in default. */
 int lentils_unet_set_wgrad_ctas(lentils_unet *net, int ctas);
+/* gamma of the preconditioner form (default 0) */
 int lentils_unet_set_jacobi_weight(lentils_unet *net, float gamma);
 /* 1 if a bounded tensor-core wait gave up since creation (results then invalid) */
 int lentils_unet_error_flag(lentils_unet *net, int *flag);
